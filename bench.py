@@ -1,0 +1,421 @@
+"""Benchmark: lattice site-updates/s of the fused FP32 stepper on one GB300.
+
+Workload (the north-star's spin-1 configuration): spin-1 GPE on a BCC mesh of
+96^3 block cells (10,616,832 dual nodes), box [-8, 8]^3, c0 = 2000, c2 = -50,
+seeded polar state (0, 1, 0) with 1e-3 relative noise, linear Zeeman ramp
+Bz 0.5 -> -0.5 over 4000 steps plus quadrupole gradient Bq = 0.2, dt = 5e-5.
+Each psi buffer is 255 MB (FP32), larger than the 129 MB L2, so no L2 flush is
+needed between iterations.
+
+One bench "step" = 100 leapfrog steps (one fused kernel each) + one FP64
+observables pass (norm, energy, magnetisation).  value = sites * 100 * K / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+INNER = 100                 # leapfrog steps per bench step
+DIMS = (96, 96, 96)
+BOX = 16.0
+DT = 5e-5
+C0, C2 = 2000.0, -50.0
+RAMP_STEPS = 4000
+BYTES_PER_SITE_FP32 = 72    # read psi_prev (24 B) + read/write psi_next (48 B), spin-1 FP32
+BYTES_PER_SITE_FP64 = 144
+
+
+def workload(precision):
+    from spacetime_gb300 import capi, states
+
+    lat = capi.Lattice("bcc")
+    bs = BOX / (DIMS[0] * lat.block_width[0])
+    p = capi.make_params(components=3, precision=precision, dims=DIMS, block_scale=bs, dt=DT, trap_offset=100.0,
+                         c0=C0, c2=C2, lattice=lat)
+    ramp = capi.make_ramp(bq_segments=[(0.2, 1e30, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0, 0, 0.5), 0.0, capi.RAMP_CONSTANT), ((0, 0, -0.5), RAMP_STEPS * DT, capi.RAMP_LINEAR),
+                                       ((0, 0, -0.5), 1e30, capi.RAMP_CONSTANT)])
+    psi0 = states.spinor_state(lat, p, states.POLAR, seed=2, noise=1e-3)
+    return lat, p, ramp, psi0
+
+
+def config_dict():
+    return {"workload": "spin-1 GPE, BCC 96^3 block cells (10,616,832 sites), leapfrog FP32 fused + FP64 observables every 100 steps",
+            "lattice": "bcc", "cells": list(DIMS), "components": 3, "dt": DT, "c0": C0, "c2": C2,
+            "ramp": "Bz 0.5->-0.5 over 4000 steps, Bq 0.2", "inner_steps_per_step": INNER,
+            "l2": "inputs larger than L2 (255 MB per psi buffer), no flush"}
+
+
+# ------------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------- CPU baseline
+
+
+def cpu_baseline(seconds=10.0):
+    """The FP64 CPU oracle (a restatement of Spin1GpeBCC.cu:793-917; the reference
+    has no CPU spin-1 code) on the same workload, all host threads."""
+    from oracle import oracle
+    from spacetime_gb300 import capi
+
+    lat, p, ramp, psi0 = workload(capi.FP64)
+    p.precision = capi.FP64
+    threads = os.cpu_count() or 1
+    even = np.zeros_like(psi0)
+    odd = psi0.copy()
+    oracle.parabolic_step(lat, p, oracle.ramp_eval(ramp, 0.0), 0.0, oracle.EULER, even, odd, None, threads)
+    sites = lat.nodes * DIMS[0] * DIMS[1] * DIMS[2]
+    bufs = [even, odd]
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        t = (n + 1) * DT
+        oracle.parabolic_step(lat, p, oracle.ramp_eval(ramp, t), t, oracle.LEAPFROG, bufs[(n + 1) % 2], bufs[n % 2], None, threads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    return {"value": sites * n / el, "unit": "lattice-site-updates/s", "cores": threads, "kind": "port",
+            "sample": "%d leapfrog steps of the full 96^3 spin-1 BCC grid (FP64 oracle, OpenMP %d threads), %.1f s" % (n, threads, el)}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path (the reference has no
+    CPU code for spin-1, so its FP64 restatement, oracle/gpe_oracle.c) on the box's
+    host cores, bounded samples of the same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle
+    from spacetime_gb300 import capi
+
+    lat, p, ramp, psi0 = workload(capi.FP64)
+    threads = os.cpu_count() or 1
+    sites = lat.nodes * DIMS[0] * DIMS[1] * DIMS[2]
+    even = np.zeros_like(psi0)
+    odd = psi0.copy()
+    oracle.parabolic_step(lat, p, oracle.ramp_eval(ramp, 0.0), 0.0, oracle.EULER, even, odd, None, threads)
+    bufs = [even, odd]
+    per_step = 2  # leapfrog steps per bench step (bounded sample)
+    n = 0
+
+    def one():
+        nonlocal n
+        for _ in range(per_step):
+            t = (n + 1) * DT
+            oracle.parabolic_step(lat, p, oracle.ramp_eval(ramp, t), t, oracle.LEAPFROG, bufs[(n + 1) % 2], bufs[n % 2], None, threads)
+            n += 1
+
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one()
+    el = time.perf_counter() - t0
+    value = sites * per_step * args.steps / el
+    line = {"metric": "lattice-site-updates/s", "value": value, "unit": "lattice-site-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": dict(config_dict(), workload="spin-1 GPE, BCC 96^3 block cells, FP64 CPU leapfrog (2 steps per bench step)"),
+            "cpu_baseline": {"value": value, "unit": "lattice-site-updates/s", "cores": threads, "kind": "port",
+                             "sample": "%d bench steps x %d leapfrog steps of the full grid" % (args.steps, per_step)},
+            "e2e": {"value": value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+
+
+def traffic_from_profile():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        try:
+            with open(path) as f:
+                d = json.load(f)
+            return d.get("bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import ctypes as C
+
+    import torch
+    import torch.distributed as dist
+
+    from spacetime_gb300 import capi
+    from spacetime_gb300.stepper import Stepper
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    lat, p, ramp, psi0 = workload(capi.FP32)
+    stream = torch.cuda.Stream()
+    s = Stepper(lat, p)
+    s.stream = C.c_void_p(stream.cuda_stream)
+    sites = s.sites
+
+    # the newest state slot after k steps
+    def cur_slot():
+        return capi.PSI_EVEN if (s._nsteps % 2 == 0) else capi.PSI_ODD
+
+    s._nsteps = 0
+
+    def advance():
+        s.step(INNER)
+        s._nsteps += INNER
+
+    with torch.cuda.stream(stream):
+        s.upload(capi.PSI_ODD, psi0)
+        s.set_ramp(ramp, 0.0)
+        s.start()
+        for _ in range(args.warmup):
+            advance()
+            s.observe(cur_slot(), s._nsteps * DT)
+        barrier()
+        launches0 = s.launches
+        ev_start, ev_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        batch = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        obs = []
+        with ClockSampler(local) as clk:
+            ev_start.record(stream)
+            for k in range(args.steps):
+                batch[k][0].record(stream)
+                advance()
+                batch[k][1].record(stream)
+                obs.append(s.observe(cur_slot(), s._nsteps * DT))
+            ev_end.record(stream)
+            barrier()
+        clocks = clk.summary()
+        launches = s.launches - launches0
+        total_ms = ev_start.elapsed_time(ev_end)
+        step_ms = sum(a.elapsed_time(b) for a, b in batch)
+    t_ms = torch.tensor([total_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
+    total_ms = float(t_ms.item())
+    value = world * sites * INNER * args.steps / (total_ms * 1e-3)
+    launch_ms = step_ms / (INNER * args.steps)
+    algo_bytes = BYTES_PER_SITE_FP32 * sites
+    achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = traffic_from_profile()
+
+    # ---- end to end through the C ABI with host buffers: H2D of the FP64 host state
+    # (reference file layout, pinned), start + 100 leapfrog steps + FP64 observables
+    # read back, every step.
+    host = torch.from_numpy(psi0.ravel()).pin_memory()
+    host_np = host.numpy().reshape(psi0.shape)
+    e2e_steps = max(3, min(args.steps, 10))
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            s.upload(capi.PSI_ODD, host_np)
+            s.set_ramp(ramp, 0.0)
+            s.start()
+            s._nsteps = 0
+            advance()
+            s.observe(cur_slot(), s._nsteps * DT)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            s.upload(capi.PSI_ODD, host_np)
+            s.set_ramp(ramp, 0.0)
+            s.start()
+            s._nsteps = 0
+            advance()
+            s.observe(cur_slot(), s._nsteps * DT)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+    e2e_value = world * sites * INNER * e2e_steps / e2e_s
+
+    # ---- FP64 plain stepper on the same workload (the "FP64 plain GPU stepper")
+    lat64, p64, _, _ = workload(capi.FP64)
+    s64 = Stepper(lat64, p64)
+    s64.stream = C.c_void_p(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        s64.upload(capi.PSI_ODD, psi0)
+        s64.set_ramp(ramp, 0.0)
+        s64.start()
+        s64.step(20)
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s64.step(200)
+        b.record(stream)
+        barrier()
+        fp64_ms = a.elapsed_time(b) / 200
+    s64.close()
+    fp64_value = sites / (fp64_ms * 1e-3)
+
+    drift = None
+    if args.drift_steps > 0 and rank == 0:
+        drift = measure_drift(args.drift_steps, stream)
+
+    result = {
+        "metric": "lattice-site-updates/s", "value": value, "unit": "lattice-site-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(),
+        "parallelism": "replicas" if world > 1 else "single",
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "parabolic_step_kernel<float,3,LEAPFROG>", "algorithmic_bytes_per_launch": algo_bytes,
+                     "avg_launch_ms": launch_ms},
+        "e2e": {"value": e2e_value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
+                "d2h_bytes_per_step": 8 * 12, "steps": e2e_steps,
+                "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step(100) + gpe_observe"},
+        "fp64_plain": {"value": fp64_value, "unit": "lattice-site-updates/s", "ms_per_launch": fp64_ms,
+                       "speedup_fp32_fused": (sites / (launch_ms * 1e-3)) / fp64_value},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "observables_last": obs[-1] if obs else None,
+    }
+    if drift is not None:
+        result["drift"] = drift
+    if rank == 0 and args.cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    s.close()
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def measure_drift(nsteps, stream):
+    """FP32 fused vs FP64 plain from the same initial state: relative energy
+    difference every 100 steps and the max-abs psi error at the end."""
+    import ctypes as C
+
+    import torch
+
+    from spacetime_gb300 import capi
+    from spacetime_gb300.stepper import Stepper
+
+    out = {"steps": nsteps, "energy_rel_diff_max": 0.0, "norm_rel_diff_max": 0.0}
+    runs = {}
+    for prec in (capi.FP32, capi.FP64):
+        lat, p, ramp, psi0 = workload(prec)
+        st = Stepper(lat, p)
+        st.stream = C.c_void_p(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            st.upload(capi.PSI_ODD, psi0)
+            st.set_ramp(ramp, 0.0)
+            st.start()
+            e = [st.observe(capi.PSI_EVEN, 0.0)]
+            done = 0
+            while done < nsteps:
+                st.step(100)
+                done += 100
+                e.append(st.observe(capi.PSI_EVEN if done % 2 == 0 else capi.PSI_ODD, done * DT))
+            last = st.download(capi.PSI_EVEN if done % 2 == 0 else capi.PSI_ODD)
+        st.close()
+        runs[prec] = (e, last)
+    e32, l32 = runs[capi.FP32]
+    e64, l64 = runs[capi.FP64]
+    out["energy_rel_diff_max"] = max(abs(a["energy"] - b["energy"]) / abs(b["energy"]) for a, b in zip(e32, e64))
+    out["norm_rel_diff_max"] = max(abs(a["norm"] - b["norm"]) / abs(b["norm"]) for a, b in zip(e32, e64))
+    out["energy_rel_drift_fp64"] = abs(e64[-1]["energy"] - e64[0]["energy"]) / abs(e64[0]["energy"])
+    out["psi_max_abs_err"] = float(np.max(np.abs(l32 - l64)))
+    out["psi_max_abs"] = float(np.max(np.abs(l64)))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--drift-steps", type=int, default=10000)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

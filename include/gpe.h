@@ -1,0 +1,256 @@
+/*
+ * gpe.h -- C ABI of the GB300 Gross-Pitaevskii block-cell stepper (libgpe).
+ *
+ * The reference (markus-kivioja/SpaceTime) has no library API: its per-step
+ * "operator" is a __global__ kernel launched from each program's time loop.
+ * Every entry point below replaces one of those launches (or the host code
+ * around it); the comment on each names the reference code it stands in for.
+ *
+ * Conventions shared by all entry points
+ *  - One STEP advances one buffer by dt.  Leapfrog steps use
+ *    next += 2*dt*(-i H prev), as in Spin1GpeBCC/Spin1GpeBCC.cu:914-916.  The scalar
+ *    programs write next += dt_ref*(-i H prev) (GrossPitaevskiiGpuBcc/
+ *    GPUGrossPitaevskii_BCC.cu:345-346); pass dt = dt_ref/2 to reproduce them.
+ *  - State buffers keep the reference's block-cell layout: a pitched 3-D array of
+ *    cells (x fastest) with a one-cell zero halo on every side; a cell holds
+ *    V nodes x C components x (re, im) (BlockPsis, Spin1GpeBCC/utils.h:75-85),
+ *    and an edge cell E edges x C components x (re, im) (BlockEdges,
+ *    RelativisticSpin1Gpe/utils.h:91-94).  Host copies in and out use the unpadded
+ *    reference file layout ((Z+2)(Y+2)(X+2) cells, FP64), so a reference
+ *    "ground_state.dat" / "<t>.dat" dump can be loaded and written directly.
+ *  - Every call returns a gpe_status and never exits the process.  Work is
+ *    enqueued on the caller's stream; no call synchronises unless it says so.
+ *  - Handles are not thread-safe; use one handle per host thread.
+ */
+#ifndef GPE_H
+#define GPE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GPE_OK = 0,
+    GPE_ERR_INVALID_ARG = 1,  /* bad pointer, size, table or parameter */
+    GPE_ERR_OOM = 2,          /* device or host allocation failed */
+    GPE_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    GPE_ERR_TIMEOUT = 4,      /* a bounded device wait ran out */
+    GPE_ERR_NONFINITE = 5,    /* a reduction found NaN/Inf in the state */
+    GPE_ERR_UNSUPPORTED = 6,  /* combination not built (e.g. C=5 on a lattice without edges) */
+    GPE_ERR_NO_DEVICE = 7     /* no CUDA device visible */
+} gpe_status;
+
+/* ---------------------------------------------------------------- lattices */
+
+/* One node-Laplacian entry: neighbour node `node` of the cell at offset
+ * (dx,dy,dz) in {-1,0,1}^3, with DEC weight hodge = body hodge / face hodge.
+ * Replaces the int2 byte-offset table (GrossPitaevskiiGpuBcc/mesh.h:42-92) and
+ * the int4 cell-offset table (Spin1GpeBCC/mesh.h:47-100). */
+typedef struct {
+    int32_t dx, dy, dz;
+    int32_t node;
+    double hodge;
+} gpe_stencil_entry;
+
+/* One dual edge (d0 row, RelativisticSpin2Gpe/mesh.h:48-74): from node `from` of
+ * this cell to node `to` of the cell at offset (dx,dy,dz).  d0 psi = psi[to]-psi[from]. */
+typedef struct {
+    int32_t from;
+    int32_t dx, dy, dz;
+    int32_t to;
+} gpe_edge;
+
+/* One node-edge incidence (d1 row, RelativisticSpin2Gpe/mesh.h:76-133): edge
+ * `edge` of the edge cell at offset (dx,dy,dz), weight with the incidence sign
+ * folded in (RelativisticSpin2Gpe/mesh.h:185-232). */
+typedef struct {
+    int32_t dx, dy, dz;
+    int32_t edge;
+    double hodge;
+} gpe_incidence;
+
+typedef struct {
+    int32_t nodes;                      /* V (VALUES_IN_BLOCK) */
+    double block_width[3];              /* BLOCK_WIDTH in unit-block units */
+    double volume;                      /* VOLUME: dual-cell volume, unit-block units */
+    const double* pos;                  /* V*3 node positions (d_localPos) */
+    const int32_t* row_ptr;             /* V+1 CSR offsets into stencil */
+    const gpe_stencil_entry* stencil;   /* row_ptr[V] entries */
+    int32_t edges;                      /* E (EDGES_IN_BLOCK); 0 if no edge tables */
+    int32_t faces_per_node;             /* incidence entries per node (FACE_COUNT) */
+    const gpe_edge* edge_table;         /* E entries */
+    const gpe_incidence* incidence;     /* V*faces_per_node entries */
+} gpe_lattice_desc;
+
+typedef struct gpe_lattice gpe_lattice;
+
+/* Validates and copies the tables (symmetry, offsets in {-1,0,1}, node ids in
+ * range).  Replaces the host getLaplacian(...) calls, e.g. Spin1GpeBCC.cu:1156. */
+gpe_status gpe_lattice_create(const gpe_lattice_desc* desc, gpe_lattice** out);
+void gpe_lattice_destroy(gpe_lattice* lat);
+
+/* ----------------------------------------------------------------- physics */
+
+enum { GPE_SCHEME_PARABOLIC = 0, GPE_SCHEME_HYPERBOLIC = 1 };
+enum { GPE_FP32 = 0, GPE_FP64 = 1 };
+enum {
+    GPE_FLAG_THREE_BODY_LOSS = 1,     /* -i alpha rho^2 (Spin1GpeBCC.cu:877-880) */
+    GPE_FLAG_QUADRATIC_ZEEMAN = 2,    /* Spin1GpeBCC.cu:897-912 */
+    GPE_FLAG_QUADRUPOLE_OFFSET = 4,   /* Spin1GpeBCC.cu:128-137 */
+    GPE_FLAG_TRAP_OFF_AFTER = 8       /* trap() returns 0 for t >= trap_off_time (Spin1GpeBCC.cu:114) */
+};
+
+typedef struct {
+    int32_t components;      /* C: 1 (scalar), 3 (spin-1) or 5 (spin-2) */
+    int32_t scheme;          /* GPE_SCHEME_* */
+    int32_t precision;       /* GPE_FP32 (fused fast path) or GPE_FP64 (plain) */
+    int32_t flags;           /* GPE_FLAG_* */
+    uint32_t dims[3];        /* interior cells X, Y, Z */
+    double block_scale;      /* bs: physical width of a unit block / BLOCK_WIDTH */
+    double p0[3];            /* physical position of the corner of cell (0,0,0) */
+    double dt;               /* time step (code units) */
+    double trap_lambda[3];   /* V = 0.5*|lambda .* r|^2 + trap_offset (Spin1GpeBCC.cu:112-122) */
+    double trap_offset;      /* +100 in the spinor/GpuBcc programs, 0 in GPBlocks */
+    double trap_off_time;    /* with GPE_FLAG_TRAP_OFF_AFTER */
+    double c0;               /* density interaction (g for the scalar programs) */
+    double c2;               /* spin interaction (spin-1: Fz/F+-; spin-2: c2 of Spin2GpeBCC.cu:128) */
+    double c4;               /* spin-2 singlet interaction (Spin2GpeBCC.cu:129) */
+    double alpha;            /* three-body loss */
+    double sigma;            /* relativistic coefficient (RelativisticSpin2Gpe.cu:142) */
+    double quad_center[3];   /* quadrupole centre with GPE_FLAG_QUADRUPOLE_OFFSET */
+} gpe_params;
+
+/* Magnetic fields of one step (MagFields, Spin1GpeBCC/utils.h:94-100):
+ * B(r) = (Bq x + Bb.x, Bq y + Bb.y, -2 Bq z + Bb.z) (Spin1GpeBCC.cu:128-142). */
+typedef struct {
+    double bq;
+    double bb[3];
+    double bq_quad;
+    double bb_quad[3];
+} gpe_fields;
+
+/* Piecewise field ramp, the device-side form of getSignal(t)
+ * (Spin1GpeBCC/AliceRingRamps.h:74-141, KnotRamps.h:64-135).  Each channel is a
+ * list of segments (target value, duration, type); inside segment k the value
+ * goes from the previous target (0 before the first) to target k as
+ *   CONSTANT: target;  LINEAR: prev + s*(target-prev);  SQRT: prev + sqrt(s)*(target-prev)
+ * with s = time into segment / duration.  The field of step n is evaluated at
+ * ramp time tau = time_scale * (t0 + (n+1)*dt) and scaled:
+ *   Bq = bq_scale*signal.Bq, Bb = bb_scale*signal.Bb,
+ *   BqQuad = bq_quad_scale*signal.Bq, BbQuad = bb_quad_scale*signal.Bb
+ * (Spin1GpeBCC.cu:1583-1587). */
+enum { GPE_RAMP_CONSTANT = 0, GPE_RAMP_LINEAR = 1, GPE_RAMP_SQRT = 2 };
+#define GPE_RAMP_MAX_SEGMENTS 32
+typedef struct {
+    int32_t bq_segments;
+    double bq_target[GPE_RAMP_MAX_SEGMENTS];
+    double bq_duration[GPE_RAMP_MAX_SEGMENTS];
+    int32_t bq_type[GPE_RAMP_MAX_SEGMENTS];
+    int32_t bb_segments;
+    double bb_target[GPE_RAMP_MAX_SEGMENTS][3];
+    double bb_duration[GPE_RAMP_MAX_SEGMENTS];
+    int32_t bb_type[GPE_RAMP_MAX_SEGMENTS];
+    double time_scale;
+    double bq_scale, bb_scale, bq_quad_scale, bb_quad_scale;
+} gpe_ramp;
+
+/* Host evaluation of a ramp at ramp time tau (getSignal + scaling). */
+gpe_status gpe_ramp_eval(const gpe_ramp* ramp, double tau, gpe_fields* out);
+
+/* ----------------------------------------------------------------- handles */
+
+typedef struct gpe_handle gpe_handle;
+
+/* Buffer slots of a handle. */
+enum { GPE_PSI_EVEN = 0, GPE_PSI_ODD = 1, GPE_Q_EVEN = 2, GPE_Q_ODD = 3, GPE_HPSI = 4 };
+
+/* A pitched device buffer in the reference layout; ptr is the interior cell
+ * (0,0,0), one cell in from the allocation start in x, y and z (PitchedPtr,
+ * Spin1GpeBCC.cu:1145-1147).  pitch/slice_pitch in bytes. */
+typedef struct {
+    void* ptr;
+    size_t pitch;
+    size_t slice_pitch;
+} gpe_pitched;
+
+/* Creates a stepper on the current CUDA device and allocates its buffers
+ * (psi even/odd, plus q even/odd for the hyperbolic scheme), zero-filled.
+ * Replaces the cudaMalloc3D/getLaplacian/host set-up of integrateInTime
+ * (Spin1GpeBCC.cu:1105-1172, RelativisticSpin2Gpe.cu:1295-1403). */
+gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* params, gpe_handle** out);
+gpe_status gpe_destroy(gpe_handle* h);
+
+/* Describe one of the handle's device buffers (for a caller that wants to run
+ * its own kernels on it, or to hand it to another library). */
+gpe_status gpe_buffer(const gpe_handle* h, int32_t slot, gpe_pitched* out, size_t* cell_bytes);
+
+/* Host <-> device copies in the reference file layout: (Z+2)(Y+2)(X+2) cells of
+ * FP64 values, halo included (the ground_state.dat / "<t>.dat" format written at
+ * Spin1GpeBCC.cu:1690-1699).  Halo cells are ignored on upload (kept zero).
+ * count = number of doubles in host buffer.  These synchronise the stream. */
+gpe_status gpe_upload(gpe_handle* h, int32_t slot, const double* host, size_t count, void* stream);
+gpe_status gpe_download(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream);
+
+/* Install the field ramp used by gpe_step / gpe_start (device-side getSignal). */
+gpe_status gpe_set_ramp(gpe_handle* h, const gpe_ramp* ramp, double t0);
+
+/* Forward-Euler start step from PSI_ODD into PSI_EVEN at t0
+ * (forwardEuler, Spin1GpeBCC.cu:667-791, launched at :1433; hyperbolic start
+ * RelativisticSpin2Gpe.cu:1628-1630). */
+gpe_status gpe_start(gpe_handle* h, void* stream);
+
+/* n leapfrog steps, alternating odd<-even and even<-odd as the reference time loop
+ * does (Spin1GpeBCC.cu:1574-1603; GPUGrossPitaevskii_BCC.cu:883-889;
+ * hyperbolic psi+q RelativisticSpin2Gpe.cu:1859-1899, fused here into one kernel
+ * per step).  Fields follow the installed ramp.  n may be odd: the handle tracks
+ * which buffer holds the newest state. */
+gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream);
+
+/* One step with explicit fields instead of the ramp: next <- prev, the
+ * per-launch form of the reference loop (leapfrog<<<>>>(next, prev, ..., Bs, t),
+ * Spin1GpeBCC.cu:1588).  mode: 0 leapfrog, 1 forward Euler, 2 imaginary time
+ * (next = prev - dt*H prev, H prev stored in GPE_HPSI; Spin1GpeBCC.cu:554-662). */
+enum { GPE_MODE_LEAPFROG = 0, GPE_MODE_EULER = 1, GPE_MODE_ITP = 2 };
+gpe_status gpe_step_explicit(gpe_handle* h, int32_t next_slot, int32_t prev_slot,
+                             const gpe_fields* fields, double t, int32_t mode, void* stream);
+
+/* Imaginary-time ground-state iterations: itp + renormalisation to norm 1, n
+ * times, on PSI_EVEN (Spin1GpeBCC.cu:1470-1478; GPUGrossPitaevskii_BCC.cu:845-849).
+ * If mu_out != NULL it receives <psi|H psi> of the last iteration (FP64, synchronises). */
+gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* stream);
+
+/* FP64 observables of one psi slot, integrated with dv = bs^3*VOLUME
+ * (density/integrate Spin1GpeBCC.cu:191-211,328-348; innerProduct :213-233;
+ * localAvgSpinAndDensity + integrateSpinAndDensity :235-271, :992-1020;
+ * com GPUGrossPitaevskii_BCC.cu:349-413).  Synchronises the stream. */
+typedef struct {
+    double norm;            /* sum |psi|^2 dv */
+    double energy;          /* GP functional: kinetic + trap + c0/2 rho^2 + spin terms + Zeeman */
+    double h_expect;        /* <psi|H psi> dv (the reference's `energy` kernel, BCC.cu:204-226) */
+    double magnetization[3];/* sum <F> dv (unnormalised local spin times density) */
+    double spin_norm;       /* sum rho |<F>/rho| dv */
+    double com[3];          /* sum r |psi|^2 dv */
+    double max_abs;         /* max |psi_component| */
+    int32_t nonfinite;      /* number of non-finite values seen */
+} gpe_observables;
+gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream);
+
+/* Number of CUDA kernel launches this handle has issued (for accounting). */
+uint64_t gpe_launch_count(const gpe_handle* h);
+
+/* Sites (dual nodes) in the interior: V*X*Y*Z. */
+uint64_t gpe_sites(const gpe_handle* h);
+
+/* Last error text of this thread (static storage, never NULL). */
+const char* gpe_last_error(void);
+
+/* Library version string. */
+const char* gpe_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPE_H */

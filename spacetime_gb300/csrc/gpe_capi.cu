@@ -1,0 +1,730 @@
+// gpe_capi.cu -- host implementation of the libgpe C ABI (include/gpe.h).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gpe_internal.h"
+
+namespace gpe {
+template <typename R, int C>
+cudaError_t launch_parabolic(const StepArgs& a, int mode, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_observe(const StepArgs& a, double* out, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s);
+cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s);
+cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
+                            uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
+enum HyperKind {
+    HK_FUSED_LEAPFROG = 0,
+    HK_PSI_PARA_LEAPFROG,
+    HK_PSI_PARA_EULER,
+    HK_PSI_HYPER_EULER,
+    HK_PSI_PARA_ITP,
+    HK_Q_PARA,
+    HK_Q_EULER_HYPER,
+    HK_Q_HYPER
+};
+}  // namespace gpe
+
+using namespace gpe;
+
+static thread_local std::string g_last_error = "";
+
+static gpe_status fail(gpe_status st, const std::string& msg) {
+    g_last_error = msg;
+    return st;
+}
+
+static gpe_status cuda_fail(cudaError_t e, const char* where) {
+    return fail(GPE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(expr)                                    \
+    do {                                                  \
+        cudaError_t _e = (expr);                          \
+        if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
+    } while (0)
+
+struct gpe_lattice {
+    int V = 0;
+    double bw[3] = {0, 0, 0};
+    double volume = 0;
+    std::vector<double> pos;
+    std::vector<int32_t> row_ptr;
+    std::vector<gpe_stencil_entry> stencil;
+    int E = 0, F = 0;
+    std::vector<gpe_edge> edges;
+    std::vector<gpe_incidence> incidence;
+};
+
+struct gpe_handle {
+    gpe_lattice lat;
+    gpe_params p;
+    int device = 0;
+    size_t real_bytes = 4;
+    Grid g{};
+    void* alloc[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    char* interior[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t alloc_bytes[5] = {0, 0, 0, 0, 0};
+    DevTables tab{};
+    std::vector<void*> dev_tables;
+    double* partials = nullptr;
+    size_t partial_blocks = 0;
+    double* obs_out = nullptr;
+    double* stage = nullptr;   // FP64 staging for uploads/downloads (allocated on first use)
+    size_t stage_count = 0;
+    gpe_ramp ramp{};
+    bool has_ramp = false;
+    double t0 = 0;
+    int cur = 0;          // psi slot holding the newest state
+    uint64_t nstep = 0;   // leapfrog steps since gpe_start / gpe_set_ramp
+    uint64_t launches = 0;
+};
+
+extern "C" const char* gpe_last_error(void) { return g_last_error.c_str(); }
+extern "C" const char* gpe_version(void) { return "libgpe 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------ lattices
+
+extern "C" gpe_status gpe_lattice_create(const gpe_lattice_desc* d, gpe_lattice** out) {
+    if (!d || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (d->nodes <= 0 || d->nodes > kMaxNodes) return fail(GPE_ERR_INVALID_ARG, "nodes out of range");
+    if (!d->pos || !d->row_ptr || !d->stencil) return fail(GPE_ERR_INVALID_ARG, "missing table");
+    if (!(d->volume > 0) || !(d->block_width[0] > 0) || !(d->block_width[1] > 0) || !(d->block_width[2] > 0))
+        return fail(GPE_ERR_INVALID_ARG, "bad block width or volume");
+    const int V = d->nodes;
+    if (d->row_ptr[0] != 0) return fail(GPE_ERR_INVALID_ARG, "row_ptr[0] != 0");
+    for (int l = 0; l < V; ++l)
+        if (d->row_ptr[l + 1] < d->row_ptr[l]) return fail(GPE_ERR_INVALID_ARG, "row_ptr not monotone");
+    const int n = d->row_ptr[V];
+    if (n <= 0 || n > kMaxEntries) return fail(GPE_ERR_INVALID_ARG, "stencil size out of range");
+    auto off_ok = [](int a) { return a >= -1 && a <= 1; };
+    for (int f = 0; f < n; ++f) {
+        const gpe_stencil_entry& e = d->stencil[f];
+        if (!off_ok(e.dx) || !off_ok(e.dy) || !off_ok(e.dz)) return fail(GPE_ERR_INVALID_ARG, "stencil offset not in {-1,0,1}");
+        if (e.node < 0 || e.node >= V) return fail(GPE_ERR_INVALID_ARG, "stencil node out of range");
+        if (!std::isfinite(e.hodge)) return fail(GPE_ERR_INVALID_ARG, "non-finite hodge");
+    }
+    // symmetry of the neighbour graph: (l -> d, m) implies (m -> -d, l)
+    for (int l = 0; l < V; ++l)
+        for (int f = d->row_ptr[l]; f < d->row_ptr[l + 1]; ++f) {
+            const gpe_stencil_entry& e = d->stencil[f];
+            bool found = false;
+            for (int g = d->row_ptr[e.node]; g < d->row_ptr[e.node + 1] && !found; ++g) {
+                const gpe_stencil_entry& r = d->stencil[g];
+                found = r.node == l && r.dx == -e.dx && r.dy == -e.dy && r.dz == -e.dz;
+            }
+            if (!found) return fail(GPE_ERR_INVALID_ARG, "stencil is not symmetric");
+        }
+    gpe_lattice* L = new (std::nothrow) gpe_lattice();
+    if (!L) return fail(GPE_ERR_OOM, "host allocation");
+    L->V = V;
+    for (int i = 0; i < 3; ++i) L->bw[i] = d->block_width[i];
+    L->volume = d->volume;
+    L->pos.assign(d->pos, d->pos + 3 * V);
+    L->row_ptr.assign(d->row_ptr, d->row_ptr + V + 1);
+    L->stencil.assign(d->stencil, d->stencil + n);
+    if (d->edges > 0) {
+        if (d->edges > kMaxEdges || d->faces_per_node <= 0 || d->faces_per_node > kMaxFaces || !d->edge_table ||
+            !d->incidence) {
+            delete L;
+            return fail(GPE_ERR_INVALID_ARG, "bad edge tables");
+        }
+        for (int e = 0; e < d->edges; ++e) {
+            const gpe_edge& r = d->edge_table[e];
+            if (r.from < 0 || r.from >= V || r.to < 0 || r.to >= V || !off_ok(r.dx) || !off_ok(r.dy) || !off_ok(r.dz)) {
+                delete L;
+                return fail(GPE_ERR_INVALID_ARG, "edge table entry out of range");
+            }
+        }
+        for (int i = 0; i < V * d->faces_per_node; ++i) {
+            const gpe_incidence& r = d->incidence[i];
+            if (r.edge < 0 || r.edge >= d->edges || !off_ok(r.dx) || !off_ok(r.dy) || !off_ok(r.dz)) {
+                delete L;
+                return fail(GPE_ERR_INVALID_ARG, "incidence entry out of range");
+            }
+        }
+        L->E = d->edges;
+        L->F = d->faces_per_node;
+        L->edges.assign(d->edge_table, d->edge_table + d->edges);
+        L->incidence.assign(d->incidence, d->incidence + V * d->faces_per_node);
+    }
+    *out = L;
+    return GPE_OK;
+}
+
+extern "C" void gpe_lattice_destroy(gpe_lattice* lat) { delete lat; }
+
+// ------------------------------------------------------------------- ramps
+
+extern "C" gpe_status gpe_ramp_eval(const gpe_ramp* r, double tau, gpe_fields* out) {
+    if (!r || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (r->bq_segments < 0 || r->bq_segments > GPE_RAMP_MAX_SEGMENTS || r->bb_segments < 0 ||
+        r->bb_segments > GPE_RAMP_MAX_SEGMENTS)
+        return fail(GPE_ERR_INVALID_ARG, "segment count out of range");
+    // walk consecutive segment durations; inside segment k interpolate from the
+    // previous target (0 before the first) by the segment's type.
+    auto channel = [](int nseg, const double* tgt, int stride, const double* dur, const int32_t* type, double tau,
+                      double* val, int dims) {
+        for (int a = 0; a < dims; ++a) val[a] = 0;
+        if (nseg == 0) return;
+        int k = 0;
+        double t = tau;
+        while (k < nseg && t - dur[k] >= 0) {
+            t -= dur[k];
+            ++k;
+        }
+        if (k == nseg) {  // past the end: hold the last target
+            k = nseg - 1;
+            t = dur[k];
+        }
+        for (int a = 0; a < dims; ++a) {
+            const double target = tgt[k * stride + a];
+            const double prev = k > 0 ? tgt[(k - 1) * stride + a] : 0.0;
+            if (type[k] == GPE_RAMP_CONSTANT) val[a] = target;
+            else if (type[k] == GPE_RAMP_LINEAR) val[a] = prev + t * (target - prev) / dur[k];
+            else val[a] = prev + (target - prev) * std::sqrt(t / dur[k]);
+        }
+    };
+    double bq = 0, bb[3];
+    channel(r->bq_segments, r->bq_target, 1, r->bq_duration, r->bq_type, tau, &bq, 1);
+    channel(r->bb_segments, &r->bb_target[0][0], 3, r->bb_duration, r->bb_type, tau, bb, 3);
+    out->bq = r->bq_scale * bq;
+    out->bq_quad = r->bq_quad_scale * bq;
+    for (int a = 0; a < 3; ++a) {
+        out->bb[a] = r->bb_scale * bb[a];
+        out->bb_quad[a] = r->bb_quad_scale * bb[a];
+    }
+    return GPE_OK;
+}
+
+// ----------------------------------------------------------------- handles
+
+static size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+template <typename T>
+static gpe_status upload_table(gpe_handle* h, const std::vector<T>& v, T** out) {
+    *out = nullptr;
+    if (v.empty()) return GPE_OK;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, v.size() * sizeof(T));
+    if (e != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (tables)");
+    h->dev_tables.push_back(p);
+    e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (tables)");
+    *out = static_cast<T*>(p);
+    return GPE_OK;
+}
+
+static void release(gpe_handle* h) {
+    for (int i = 0; i < 5; ++i)
+        if (h->alloc[i]) cudaFree(h->alloc[i]);
+    for (void* p : h->dev_tables) cudaFree(p);
+    if (h->partials) cudaFree(h->partials);
+    if (h->obs_out) cudaFree(h->obs_out);
+    if (h->stage) cudaFree(h->stage);
+}
+
+static gpe_status build_tables(gpe_handle* h) {
+    const gpe_lattice& L = h->lat;
+    const Grid& g = h->g;
+    const double bs2 = h->p.block_scale * h->p.block_scale;
+    const size_t node_bytes = (size_t)g.C * 2 * h->real_bytes;
+    const int n = (int)L.stencil.size();
+    std::vector<int32_t> nb_off(n);
+    std::vector<double> w64(n);
+    std::vector<float> w32(n);
+    for (int f = 0; f < n; ++f) {
+        const gpe_stencil_entry& e = L.stencil[f];
+        const long long off = (long long)e.dz * (long long)g.slice + (long long)e.dy * (long long)g.pitch +
+                              (long long)e.dx * g.cell_bytes + (long long)e.node * node_bytes;
+        if (off > INT32_MAX || off < INT32_MIN) return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
+        nb_off[f] = (int32_t)off;
+        w64[f] = (-0.5 * e.hodge) / bs2;  // hodges[i] = -0.5*hodges[i]; hodge/(bs*bs) (Spin1GpeBCC.cu:1169, :859)
+        w32[f] = (float)w64[f];
+    }
+    std::vector<double> pos64(L.pos);
+    std::vector<float> pos32(L.pos.begin(), L.pos.end());
+    gpe_status st;
+    if ((st = upload_table(h, L.row_ptr, &h->tab.row_ptr))) return st;
+    if ((st = upload_table(h, nb_off, &h->tab.nb_off))) return st;
+    if ((st = upload_table(h, w64, &h->tab.w64))) return st;
+    if ((st = upload_table(h, w32, &h->tab.w32))) return st;
+    if ((st = upload_table(h, pos64, &h->tab.pos64))) return st;
+    if ((st = upload_table(h, pos32, &h->tab.pos32))) return st;
+    h->tab.entries = n;
+    if (L.E > 0) {
+        const int F = L.F;
+        std::vector<int32_t> inc_off(L.V * F), efrom(L.E), eto(L.E);
+        std::vector<double> iw64(L.V * F);
+        std::vector<float> iw32(L.V * F);
+        for (int i = 0; i < L.V * F; ++i) {
+            const gpe_incidence& r = L.incidence[i];
+            const long long off = (long long)r.dz * (long long)g.qslice + (long long)r.dy * (long long)g.qpitch +
+                                  (long long)r.dx * g.qcell_bytes + (long long)r.edge * node_bytes;
+            if (off > INT32_MAX || off < INT32_MIN) return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
+            inc_off[i] = (int32_t)off;
+            iw64[i] = (-0.5 * r.hodge) / bs2;
+            iw32[i] = (float)iw64[i];
+        }
+        for (int e = 0; e < L.E; ++e) {
+            const gpe_edge& r = L.edges[e];
+            efrom[e] = (int32_t)(r.from * node_bytes);
+            const long long off = (long long)r.dz * (long long)g.slice + (long long)r.dy * (long long)g.pitch +
+                                  (long long)r.dx * g.cell_bytes + (long long)r.to * node_bytes;
+            if (off > INT32_MAX || off < INT32_MIN) return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
+            eto[e] = (int32_t)off;
+        }
+        if ((st = upload_table(h, inc_off, &h->tab.inc_off))) return st;
+        if ((st = upload_table(h, iw64, &h->tab.inc_w64))) return st;
+        if ((st = upload_table(h, iw32, &h->tab.inc_w32))) return st;
+        if ((st = upload_table(h, efrom, &h->tab.e_from_off))) return st;
+        if ((st = upload_table(h, eto, &h->tab.e_to_off))) return st;
+        h->tab.faces = F;
+    }
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* p, gpe_handle** out) {
+    if (!lat || !p || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    if (p->components != 1 && p->components != 3 && p->components != 5)
+        return fail(GPE_ERR_INVALID_ARG, "components must be 1, 3 or 5");
+    if (p->precision != GPE_FP32 && p->precision != GPE_FP64) return fail(GPE_ERR_INVALID_ARG, "precision");
+    if (p->scheme != GPE_SCHEME_PARABOLIC && p->scheme != GPE_SCHEME_HYPERBOLIC) return fail(GPE_ERR_INVALID_ARG, "scheme");
+    if (p->dims[0] == 0 || p->dims[1] == 0 || p->dims[2] == 0) return fail(GPE_ERR_INVALID_ARG, "empty grid");
+    if (!(p->block_scale > 0) || !std::isfinite(p->dt)) return fail(GPE_ERR_INVALID_ARG, "block_scale/dt");
+    if (p->scheme == GPE_SCHEME_HYPERBOLIC && (lat->E == 0 || !(p->sigma > 0)))
+        return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme needs edge tables and sigma > 0");
+    if (p->components == 5 && (p->flags & GPE_FLAG_QUADRATIC_ZEEMAN))
+        return fail(GPE_ERR_UNSUPPORTED, "quadratic Zeeman is not built for spin-2");
+    const uint64_t sites = (uint64_t)p->dims[0] * p->dims[1] * p->dims[2] * (uint64_t)lat->V;
+    const uint64_t esites = (uint64_t)p->dims[0] * p->dims[1] * p->dims[2] * (uint64_t)lat->E;
+    if (sites >= (1ull << 32) || esites >= (1ull << 32)) return fail(GPE_ERR_INVALID_ARG, "grid exceeds 2^32 sites");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GPE_ERR_NO_DEVICE, "no CUDA device");
+
+    gpe_handle* h = new (std::nothrow) gpe_handle();
+    if (!h) return fail(GPE_ERR_OOM, "host allocation");
+    h->lat = *lat;
+    h->p = *p;
+    cudaGetDevice(&h->device);
+    h->real_bytes = p->precision == GPE_FP64 ? 8 : 4;
+    Grid& g = h->g;
+    g.X = p->dims[0];
+    g.Y = p->dims[1];
+    g.Z = p->dims[2];
+    g.V = lat->V;
+    g.C = p->components;
+    g.E = lat->E;
+    g.cell_bytes = (uint32_t)(g.V * g.C * 2 * h->real_bytes);
+    g.qcell_bytes = (uint32_t)(g.E * g.C * 2 * h->real_bytes);
+    g.pitch = round_up((size_t)(g.X + 2) * g.cell_bytes, 256);
+    g.slice = g.pitch * (g.Y + 2);
+    g.qpitch = g.E ? round_up((size_t)(g.X + 2) * g.qcell_bytes, 256) : 0;
+    g.qslice = g.qpitch * (g.Y + 2);
+
+    const bool hyper = p->scheme == GPE_SCHEME_HYPERBOLIC;
+    for (int slot = 0; slot < 5; ++slot) {
+        const bool is_q = slot == GPE_Q_EVEN || slot == GPE_Q_ODD;
+        if (is_q && !hyper) continue;
+        if (slot == GPE_HPSI) continue;  // allocated on first use (ITP)
+        const size_t bytes = (is_q ? g.qslice : g.slice) * (g.Z + 2);
+        cudaError_t e = cudaMalloc(&h->alloc[slot], bytes);
+        if (e != cudaSuccess) {
+            release(h);
+            delete h;
+            return fail(GPE_ERR_OOM, "cudaMalloc of a state buffer failed");
+        }
+        h->alloc_bytes[slot] = bytes;
+        cudaMemset(h->alloc[slot], 0, bytes);
+        h->interior[slot] = static_cast<char*>(h->alloc[slot]) + (is_q ? g.qslice + g.qpitch + g.qcell_bytes
+                                                                          : g.slice + g.pitch + g.cell_bytes);
+    }
+    gpe_status st = build_tables(h);
+    if (st != GPE_OK) {
+        release(h);
+        delete h;
+        return st;
+    }
+    h->partial_blocks = (sites + 255) / 256;
+    if (cudaMalloc(&h->partials, h->partial_blocks * OBS_COUNT * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->obs_out, OBS_COUNT * sizeof(double)) != cudaSuccess) {
+        release(h);
+        delete h;
+        return fail(GPE_ERR_OOM, "cudaMalloc of reduction scratch failed");
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        release(h);
+        delete h;
+        return cuda_fail(e, "gpe_create");
+    }
+    h->cur = GPE_PSI_ODD;  // the reference loads the initial state into the odd buffer (Spin1GpeBCC.cu:1236)
+    *out = h;
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_destroy(gpe_handle* h) {
+    if (!h) return GPE_OK;
+    release(h);
+    delete h;
+    return GPE_OK;
+}
+
+static bool slot_ok(const gpe_handle* h, int slot) { return slot >= 0 && slot < 5 && h->alloc[slot] != nullptr; }
+
+static gpe_status ensure_hpsi(gpe_handle* h) {
+    if (h->alloc[GPE_HPSI]) return GPE_OK;
+    const size_t bytes = h->g.slice * (h->g.Z + 2);
+    if (cudaMalloc(&h->alloc[GPE_HPSI], bytes) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (H psi)");
+    cudaMemset(h->alloc[GPE_HPSI], 0, bytes);
+    h->alloc_bytes[GPE_HPSI] = bytes;
+    h->interior[GPE_HPSI] = static_cast<char*>(h->alloc[GPE_HPSI]) + h->g.slice + h->g.pitch + h->g.cell_bytes;
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_buffer(const gpe_handle* h, int32_t slot, gpe_pitched* out, size_t* cell_bytes) {
+    if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (!slot_ok(h, slot)) return fail(GPE_ERR_INVALID_ARG, "slot not allocated");
+    const bool is_q = slot == GPE_Q_EVEN || slot == GPE_Q_ODD;
+    out->ptr = h->interior[slot];
+    out->pitch = is_q ? h->g.qpitch : h->g.pitch;
+    out->slice_pitch = is_q ? h->g.qslice : h->g.slice;
+    if (cell_bytes) *cell_bytes = is_q ? h->g.qcell_bytes : h->g.cell_bytes;
+    return GPE_OK;
+}
+
+static size_t host_count(const gpe_handle* h, bool is_q) {
+    const Grid& g = h->g;
+    return (size_t)(g.X + 2) * (g.Y + 2) * (g.Z + 2) * (is_q ? g.E : g.V) * g.C * 2;
+}
+
+static gpe_status ensure_stage(gpe_handle* h, size_t count) {
+    if (h->stage_count >= count) return GPE_OK;
+    if (h->stage) cudaFree(h->stage);
+    h->stage = nullptr;
+    h->stage_count = 0;
+    if (cudaMalloc(&h->stage, count * sizeof(double)) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (staging)");
+    h->stage_count = count;
+    return GPE_OK;
+}
+
+// Host FP64 (reference file layout) <-> device buffer.  The host array is copied
+// as is into a device FP64 staging buffer and converted/unpacked by a kernel, so
+// a pinned host buffer moves at full link speed and no host-side conversion pass
+// is needed.
+static gpe_status transfer(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream, bool up) {
+    if (!h || !host) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (up && slot == GPE_HPSI) {
+        gpe_status st = ensure_hpsi(h);
+        if (st) return st;
+    }
+    if (!slot_ok(h, slot)) return fail(GPE_ERR_INVALID_ARG, "slot not allocated");
+    const bool is_q = slot == GPE_Q_EVEN || slot == GPE_Q_ODD;
+    if (count != host_count(h, is_q)) return fail(GPE_ERR_INVALID_ARG, "host buffer size does not match the grid");
+    gpe_status st = ensure_stage(h, count);
+    if (st) return st;
+    const Grid& g = h->g;
+    const uint32_t vals = (uint32_t)((is_q ? g.qcell_bytes : g.cell_bytes) / h->real_bytes);
+    const size_t pitch = is_q ? g.qpitch : g.pitch;
+    const size_t slice = is_q ? g.qslice : g.slice;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (up) CUDA_TRY(cudaMemcpyAsync(h->stage, host, count * sizeof(double), cudaMemcpyHostToDevice, s));
+    cudaError_t e = launch_pack_any(h->p.precision, h->stage, static_cast<char*>(h->alloc[slot]), g.X, g.Y, g.Z, vals,
+                                    pitch, slice, up, s);
+    if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
+    h->launches += 1;
+    if (!up) CUDA_TRY(cudaMemcpyAsync(host, h->stage, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_upload(gpe_handle* h, int32_t slot, const double* host, size_t count, void* stream) {
+    return transfer(h, slot, const_cast<double*>(host), count, stream, true);
+}
+
+extern "C" gpe_status gpe_download(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream) {
+    return transfer(h, slot, host, count, stream, false);
+}
+
+extern "C" gpe_status gpe_set_ramp(gpe_handle* h, const gpe_ramp* ramp, double t0) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (ramp) {
+        gpe_fields tmp;
+        gpe_status st = gpe_ramp_eval(ramp, 0.0, &tmp);
+        if (st) return st;
+        h->ramp = *ramp;
+        h->has_ramp = true;
+    } else {
+        h->has_ramp = false;
+    }
+    h->t0 = t0;
+    h->nstep = 0;
+    return GPE_OK;
+}
+
+static gpe_fields fields_at(const gpe_handle* h, double t) {
+    gpe_fields f;
+    std::memset(&f, 0, sizeof f);
+    if (h->has_ramp) gpe_ramp_eval(&h->ramp, h->ramp.time_scale * t, &f);
+    return f;
+}
+
+static StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t) {
+    StepArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.g = h->g;
+    a.tab = h->tab;
+    const gpe_params& p = h->p;
+    for (int i = 0; i < 3; ++i) {
+        a.ph.p0[i] = p.p0[i];
+        a.ph.bw[i] = h->lat.bw[i];
+        a.ph.lambda[i] = p.trap_lambda[i];
+        a.ph.quad_center[i] = p.quad_center[i];
+    }
+    a.ph.bs = p.block_scale;
+    a.ph.dt = p.dt;
+    a.ph.trap_offset = p.trap_offset;
+    a.ph.trap_off_time = p.trap_off_time;
+    a.ph.c0 = p.c0;
+    a.ph.c2 = p.c2;
+    a.ph.c4 = p.c4;
+    a.ph.alpha = p.alpha;
+    a.ph.sigma = p.sigma;
+    a.ph.flags = p.flags;
+    a.B = B;
+    a.t = t;
+    const Grid& g = h->g;
+    a.row_items = g.X * g.V;
+    a.row_items_e = g.X * g.E;
+    a.divV = make_fastdiv(g.V);
+    a.divRow = make_fastdiv(a.row_items);
+    a.divY = make_fastdiv(g.Y);
+    a.divE = make_fastdiv(g.E ? g.E : 1);
+    a.divRowE = make_fastdiv(a.row_items_e ? a.row_items_e : 1);
+    a.total = (uint64_t)g.X * g.Y * g.Z * g.V;
+    a.partials = h->partials;
+    return a;
+}
+
+template <int C>
+static cudaError_t dispatch_parabolic_c(const gpe_handle* h, const StepArgs& a, int mode, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_parabolic<double, C>(a, mode, s) : launch_parabolic<float, C>(a, mode, s);
+}
+static cudaError_t dispatch_parabolic(const gpe_handle* h, const StepArgs& a, int mode, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_parabolic_c<1>(h, a, mode, s);
+        case 3: return dispatch_parabolic_c<3>(h, a, mode, s);
+        default: return dispatch_parabolic_c<5>(h, a, mode, s);
+    }
+}
+template <int C>
+static cudaError_t dispatch_hyper_c(const gpe_handle* h, const StepArgs& a, int kind, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_hyper<double, C>(a, kind, s) : launch_hyper<float, C>(a, kind, s);
+}
+static cudaError_t dispatch_hyper(const gpe_handle* h, const StepArgs& a, int kind, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_hyper_c<1>(h, a, kind, s);
+        case 3: return dispatch_hyper_c<3>(h, a, kind, s);
+        default: return dispatch_hyper_c<5>(h, a, kind, s);
+    }
+}
+template <int C>
+static cudaError_t dispatch_observe_c(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_observe<double, C>(a, out, s) : launch_observe<float, C>(a, out, s);
+}
+static cudaError_t dispatch_observe(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_observe_c<1>(h, a, out, s);
+        case 3: return dispatch_observe_c<3>(h, a, out, s);
+        default: return dispatch_observe_c<5>(h, a, out, s);
+    }
+}
+template <int C>
+static cudaError_t dispatch_scale_c(const gpe_handle* h, const StepArgs& a, const double* n, double dv, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_scale<double, C>(a, n, dv, s) : launch_scale<float, C>(a, n, dv, s);
+}
+static cudaError_t dispatch_scale(const gpe_handle* h, const StepArgs& a, const double* n, double dv, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_scale_c<1>(h, a, n, dv, s);
+        case 3: return dispatch_scale_c<3>(h, a, n, dv, s);
+        default: return dispatch_scale_c<5>(h, a, n, dv, s);
+    }
+}
+
+static double cell_dv(const gpe_handle* h) {
+    const double bs = h->p.block_scale;
+    return bs * bs * bs * h->lat.volume;  // volume = bs^3 * VOLUME (Spin1GpeBCC.cu:1385)
+}
+
+// psi[next] <- psi[prev] (and q when hyperbolic), one step at time t.
+static gpe_status one_step(gpe_handle* h, int next, int prev, const gpe_fields& B, double t, int mode, cudaStream_t s) {
+    StepArgs a = make_args(h, B, t);
+    a.prev = h->interior[prev];
+    a.next = h->interior[next];
+    cudaError_t e;
+    if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
+        a.hpsi = mode == GPE_MODE_ITP ? h->interior[GPE_HPSI] : nullptr;
+        e = dispatch_parabolic(h, a, mode, s);
+        h->launches += 1;
+    } else {
+        if (mode != GPE_MODE_LEAPFROG) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme: explicit steps are leapfrog only");
+        const int qprev = prev == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
+        const int qnext = next == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
+        a.q = h->interior[qprev];
+        a.qnext = h->interior[qnext];
+        e = dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
+        h->launches += 1;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_step_explicit(gpe_handle* h, int32_t next_slot, int32_t prev_slot, const gpe_fields* fields,
+                                        double t, int32_t mode, void* stream) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if ((next_slot != GPE_PSI_EVEN && next_slot != GPE_PSI_ODD) || (prev_slot != GPE_PSI_EVEN && prev_slot != GPE_PSI_ODD))
+        return fail(GPE_ERR_INVALID_ARG, "psi slots must be PSI_EVEN or PSI_ODD");
+    if (mode == GPE_MODE_LEAPFROG && next_slot == prev_slot) return fail(GPE_ERR_INVALID_ARG, "leapfrog needs two buffers");
+    if (mode < 0 || mode > 2) return fail(GPE_ERR_INVALID_ARG, "mode");
+    if (mode == GPE_MODE_ITP) {
+        gpe_status st = ensure_hpsi(h);
+        if (st) return st;
+    }
+    gpe_fields B;
+    std::memset(&B, 0, sizeof B);
+    if (fields) B = *fields;
+    return one_step(h, next_slot, prev_slot, B, t, mode, (cudaStream_t)stream);
+}
+
+extern "C" gpe_status gpe_start(gpe_handle* h, void* stream) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    cudaStream_t s = (cudaStream_t)stream;
+    const double t = h->t0;
+    const gpe_fields B = fields_at(h, t);
+    if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
+        // forwardEuler(even <- odd) at t0 (Spin1GpeBCC.cu:1428-1433)
+        gpe_status st = one_step(h, GPE_PSI_EVEN, GPE_PSI_ODD, B, t, GPE_MODE_EULER, s);
+        if (st) return st;
+    } else {
+        // q_odd = d0 psi_odd; psi_even = psi_odd + dt(-iH) (parabolic form); q_even = d0 psi_even
+        // (RelativisticSpin2Gpe.cu:1628-1630)
+        StepArgs a = make_args(h, B, t);
+        cudaError_t e;
+        a.prev = h->interior[GPE_PSI_ODD];
+        a.qnext = h->interior[GPE_Q_ODD];
+        a.q = h->interior[GPE_Q_ODD];
+        if ((e = dispatch_hyper(h, a, HK_Q_PARA, s)) != cudaSuccess) return cuda_fail(e, "q init");
+        a.next = h->interior[GPE_PSI_EVEN];
+        if ((e = dispatch_hyper(h, a, HK_PSI_PARA_EULER, s)) != cudaSuccess) return cuda_fail(e, "Euler start");
+        a.prev = h->interior[GPE_PSI_EVEN];
+        a.q = h->interior[GPE_Q_EVEN];
+        a.qnext = h->interior[GPE_Q_EVEN];
+        if ((e = dispatch_hyper(h, a, HK_Q_PARA, s)) != cudaSuccess) return cuda_fail(e, "q init");
+        h->launches += 3;
+    }
+    h->cur = GPE_PSI_EVEN;
+    h->nstep = 0;
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (n < 0) return fail(GPE_ERR_INVALID_ARG, "negative step count");
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int32_t k = 0; k < n; ++k) {
+        const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
+        const gpe_fields B = fields_at(h, t);
+        const int prev = h->cur, next = h->cur == GPE_PSI_EVEN ? GPE_PSI_ODD : GPE_PSI_EVEN;
+        gpe_status st = one_step(h, next, prev, B, t, GPE_MODE_LEAPFROG, s);
+        if (st) return st;
+        h->cur = next;
+        h->nstep++;
+    }
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream) {
+    if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (!slot_ok(h, slot) || slot == GPE_Q_EVEN || slot == GPE_Q_ODD) return fail(GPE_ERR_INVALID_ARG, "psi slot");
+    cudaStream_t s = (cudaStream_t)stream;
+    StepArgs a = make_args(h, fields_at(h, t), t);
+    a.prev = h->interior[slot];
+    cudaError_t e = dispatch_observe(h, a, h->obs_out, s);
+    if (e != cudaSuccess) return cuda_fail(e, "observe launch");
+    h->launches += 2;
+    double r[OBS_COUNT];
+    CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    const double dv = cell_dv(h);
+    std::memset(out, 0, sizeof *out);
+    out->norm = r[OBS_NORM] * dv;
+    out->h_expect = r[OBS_HEXP] * dv;
+    out->energy = (r[OBS_HEXP] - 0.5 * r[OBS_EINT]) * dv;
+    out->magnetization[0] = r[OBS_MAGX] * dv;
+    out->magnetization[1] = r[OBS_MAGY] * dv;
+    out->magnetization[2] = r[OBS_MAGZ] * dv;
+    out->spin_norm = r[OBS_SPIN] * dv;
+    out->com[0] = r[OBS_COMX] * dv;
+    out->com[1] = r[OBS_COMY] * dv;
+    out->com[2] = r[OBS_COMZ] * dv;
+    out->max_abs = r[OBS_MAXABS];
+    out->nonfinite = (int32_t)r[OBS_NONFINITE];
+    if (out->nonfinite) return fail(GPE_ERR_NONFINITE, "state holds non-finite values");
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* stream) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (h->p.scheme != GPE_SCHEME_PARABOLIC) return fail(GPE_ERR_UNSUPPORTED, "imaginary time is built for the parabolic scheme");
+    gpe_status st = ensure_hpsi(h);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    gpe_fields zero;
+    std::memset(&zero, 0, sizeof zero);
+    const double dv = cell_dv(h);
+    for (int32_t k = 0; k < n; ++k) {
+        const int prev = h->cur, next = h->cur == GPE_PSI_EVEN ? GPE_PSI_ODD : GPE_PSI_EVEN;
+        // itp(H psi, next <- prev) then normalize(next) (Spin1GpeBCC.cu:1470-1473)
+        st = one_step(h, next, prev, zero, 0.0, GPE_MODE_ITP, s);
+        if (st) return st;
+        StepArgs a = make_args(h, zero, 0.0);
+        a.prev = h->interior[next];
+        a.next = h->interior[next];
+        cudaError_t e = dispatch_observe(h, a, h->obs_out, s);
+        if (e != cudaSuccess) return cuda_fail(e, "itp norm");
+        e = dispatch_scale(h, a, h->obs_out, dv, s);
+        if (e != cudaSuccess) return cuda_fail(e, "itp scale");
+        h->launches += 3;
+        h->cur = next;
+    }
+    if (mu_out) {
+        // innerProduct(psi, H psi) + integrate (Spin1GpeBCC.cu:1481-1490)
+        StepArgs a = make_args(h, zero, 0.0);
+        a.prev = h->interior[h->cur];
+        a.next = h->interior[GPE_HPSI];
+        cudaError_t e = launch_dot(a, h->p.precision, h->g.C, h->obs_out, s);
+        if (e != cudaSuccess) return cuda_fail(e, "itp dot");
+        h->launches += 2;
+        double r[OBS_COUNT];
+        CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        *mu_out = r[OBS_NORM] * dv;
+    }
+    return GPE_OK;
+}
+
+extern "C" uint64_t gpe_launch_count(const gpe_handle* h) { return h ? h->launches : 0; }
+
+extern "C" uint64_t gpe_sites(const gpe_handle* h) {
+    return h ? (uint64_t)h->g.X * h->g.Y * h->g.Z * h->g.V : 0;
+}

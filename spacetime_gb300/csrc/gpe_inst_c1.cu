@@ -1,0 +1,25 @@
+// Explicit instantiation of the C=1 kernels (one translation unit per spinor
+// size so that the build compiles them in parallel).
+#include "gpe_kernels.cuh"
+
+namespace gpe {
+GPE_INSTANTIATE(float, 1)
+GPE_INSTANTIATE(double, 1)
+
+cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s) {
+    if (precision == GPE_FP64) {
+        if (C == 1) return launch_dot_t<double, 1>(a, out, s);
+        if (C == 3) return launch_dot_t<double, 3>(a, out, s);
+        return launch_dot_t<double, 5>(a, out, s);
+    }
+    if (C == 1) return launch_dot_t<float, 1>(a, out, s);
+    if (C == 3) return launch_dot_t<float, 3>(a, out, s);
+    return launch_dot_t<float, 5>(a, out, s);
+}
+
+cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
+                            uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s) {
+    if (precision == GPE_FP64) return launch_pack<double>(packed, dev_base, X, Y, Z, vals, pitch, slice, to_device, s);
+    return launch_pack<float>(packed, dev_base, X, Y, Z, vals, pitch, slice, to_device, s);
+}
+}  // namespace gpe

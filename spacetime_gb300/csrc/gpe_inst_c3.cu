@@ -1,0 +1,8 @@
+// Explicit instantiation of the C=3 kernels (one translation unit per spinor
+// size so that the build compiles them in parallel).
+#include "gpe_kernels.cuh"
+
+namespace gpe {
+GPE_INSTANTIATE(float, 3)
+GPE_INSTANTIATE(double, 3)
+}  // namespace gpe

@@ -1,0 +1,128 @@
+// gpe_internal.h -- shared host/device definitions of libgpe (not part of the ABI).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gpe.h"
+
+namespace gpe {
+
+// Largest tables the kernels stage in shared memory.  C15 (V=136, 544 stencil
+// entries, E=272) is the largest lattice of the reference.
+constexpr int kMaxNodes = 160;
+constexpr int kMaxEntries = 640;
+constexpr int kMaxEdges = 320;
+constexpr int kMaxFaces = 8;
+
+// Unsigned division by a run-time constant: q = umulhi(n, mul) >> shift
+// (Granlund & Montgomery, "Division by invariant integers using multiplication", 1994).
+struct FastDiv {
+    uint32_t d, mul, shift;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    if (d == 1) {
+        f.mul = 0;
+        f.shift = 0;
+        return f;
+    }
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    // mul = floor(2^32 * (2^l - d) / d) + 1, shift = l - 1 for the "add" variant; we use
+    // the 64-bit form q = (umulhi(n, m) + n) >> l which is exact for all 32-bit n.
+    uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    f.mul = (uint32_t)m;
+    f.shift = l;
+    return f;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+    if (f.d == 1) return n;
+    uint32_t t = __umulhi(n, f.mul);
+    return (uint32_t)(((uint64_t)t + n) >> f.shift);
+}
+#endif
+
+// Observables accumulated per block (FP64), in this order.
+enum ObsIndex {
+    OBS_NORM = 0,
+    OBS_HEXP,
+    OBS_EINT,
+    OBS_MAGX,
+    OBS_MAGY,
+    OBS_MAGZ,
+    OBS_SPIN,
+    OBS_COMX,
+    OBS_COMY,
+    OBS_COMZ,
+    OBS_MAXABS,
+    OBS_NONFINITE,
+    OBS_COUNT
+};
+
+// Geometry of one state buffer (bytes).
+struct Grid {
+    uint32_t X, Y, Z;
+    uint32_t V, C, E;
+    size_t pitch, slice;         // psi buffers
+    size_t qpitch, qslice;       // q buffers
+    uint32_t cell_bytes, qcell_bytes;
+};
+
+// Physics constants of a step (double; converted per kernel).
+struct Phys {
+    double p0[3];
+    double bs;
+    double bw[3];
+    double dt;
+    double lambda[3];
+    double trap_offset;
+    double trap_off_time;
+    double c0, c2, c4, alpha, sigma;
+    double quad_center[3];
+    int flags;
+};
+
+// Per-handle device tables.  Byte offsets are relative to the base of the
+// thread's own cell in the buffer being read.
+struct DevTables {
+    int32_t* row_ptr;     // V+1
+    int32_t* nb_off;      // entries: byte offset of the neighbour value in prev
+    double* w64;          // entries: (-0.5*h)/bs^2
+    float* w32;
+    double* pos64;        // V*3
+    float* pos32;
+    int32_t* inc_off;     // V*F: byte offset of the incident edge value in q (relative to own q cell)
+    double* inc_w64;      // V*F
+    float* inc_w32;
+    int32_t* e_from_off;  // E: byte offset of from-node in own psi cell
+    int32_t* e_to_off;    // E: byte offset of to-node relative to own psi cell base
+    int entries;
+    int faces;
+};
+
+struct StepArgs {
+    const char* prev;
+    char* next;
+    char* hpsi;
+    const char* q;        // hyperbolic: q_prev
+    char* qnext;          // hyperbolic: q_next
+    Grid g;
+    DevTables tab;
+    Phys ph;
+    gpe_fields B;
+    double t;
+    FastDiv divV, divRow, divY;   // nodes: within-row node index, X*V per row, rows
+    FastDiv divE, divRowE;        // edges: within-row edge index, X*E per row
+    uint32_t row_items;   // X*V
+    uint32_t row_items_e; // X*E
+    uint64_t total;       // total threads of work
+    double* partials;     // observables
+};
+
+}  // namespace gpe

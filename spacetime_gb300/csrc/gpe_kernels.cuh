@@ -1,0 +1,838 @@
+// gpe_kernels.cuh -- the per-step DEC stencil + nonlinear update kernels.
+//
+// One thread advances one dual node (all C spinor components) of one block cell;
+// consecutive threads take consecutive nodes of consecutive cells along x, so a
+// warp reads and writes one contiguous run of the reference's BlockPsis layout
+// (coalesced 8-byte (re,im) accesses).  The node stencil, positions and weights
+// live in shared memory; neighbour values are read through the read-only path
+// and are served mostly by L1/L2 (each value is read from HBM once per step).
+//
+// Real = float is the fused FP32 stepper; Real = double the FP64 plain stepper
+// that mirrors the reference kernels (Spin1GpeBCC.cu:793-917, Spin2GpeBCC.cu:845-990,
+// GPUGrossPitaevskii_BCC.cu:327-347, RelativisticSpin2Gpe.cu:971-1132).
+#pragma once
+
+#include "gpe_internal.h"
+
+namespace gpe {
+
+// Constants exactly as the reference spells them (Spin1GpeBCC.cu:91-92).
+#define GPE_REF_SQRT_2 1.41421356237309
+#define GPE_REF_INV_SQRT_2 0.70710678118655
+
+template <typename R>
+struct Cx {
+    R x, y;
+};
+
+template <typename R>
+__device__ __forceinline__ Cx<R> cx(R x, R y) {
+    Cx<R> c;
+    c.x = x;
+    c.y = y;
+    return c;
+}
+template <typename R>
+__device__ __forceinline__ Cx<R> operator+(Cx<R> a, Cx<R> b) { return cx<R>(a.x + b.x, a.y + b.y); }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator-(Cx<R> a, Cx<R> b) { return cx<R>(a.x - b.x, a.y - b.y); }
+template <typename R>
+__device__ __forceinline__ Cx<R> operator*(R s, Cx<R> a) { return cx<R>(s * a.x, s * a.y); }
+// complex product with the reference's operation order (utils.h:71-74)
+template <typename R>
+__device__ __forceinline__ Cx<R> operator*(Cx<R> a, Cx<R> b) { return cx<R>(a.x * b.x - a.y * b.y, a.y * b.x + a.x * b.y); }
+template <typename R>
+__device__ __forceinline__ Cx<R> conj(Cx<R> a) { return cx<R>(a.x, -a.y); }
+template <typename R>
+__device__ __forceinline__ void operator+=(Cx<R>& a, Cx<R> b) { a.x += b.x; a.y += b.y; }
+
+template <typename R>
+__device__ __forceinline__ Cx<R> ldc(const char* p) {
+    if constexpr (sizeof(R) == 4) {
+        float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        return cx<R>(v.x, v.y);
+    } else {
+        double2 v = __ldg(reinterpret_cast<const double2*>(p));
+        return cx<R>(v.x, v.y);
+    }
+}
+// plain (coherent) load for buffers the kernel also writes
+template <typename R>
+__device__ __forceinline__ Cx<R> ldc_rw(const char* p) {
+    if constexpr (sizeof(R) == 4) {
+        float2 v = *reinterpret_cast<const float2*>(p);
+        return cx<R>(v.x, v.y);
+    } else {
+        double2 v = *reinterpret_cast<const double2*>(p);
+        return cx<R>(v.x, v.y);
+    }
+}
+template <typename R>
+__device__ __forceinline__ void stc(char* p, Cx<R> c) {
+    if constexpr (sizeof(R) == 4) {
+        *reinterpret_cast<float2*>(p) = make_float2(c.x, c.y);
+    } else {
+        *reinterpret_cast<double2*>(p) = make_double2(c.x, c.y);
+    }
+}
+
+template <typename R>
+struct PhysR {
+    R p0[3], bs, bw[3], lambda[3], trap_offset, c0, c2, c4, alpha, sigma, qc[3];
+    R bq, bb[3], bqq, bbq[3];
+    R dt;
+    bool trap_on;
+    int flags;
+};
+
+template <typename R>
+__device__ __forceinline__ PhysR<R> make_phys(const StepArgs& a) {
+    PhysR<R> P;
+    for (int i = 0; i < 3; ++i) {
+        P.p0[i] = (R)a.ph.p0[i];
+        P.bw[i] = (R)a.ph.bw[i];
+        P.lambda[i] = (R)a.ph.lambda[i];
+        P.qc[i] = (R)a.ph.quad_center[i];
+        P.bb[i] = (R)a.B.bb[i];
+        P.bbq[i] = (R)a.B.bb_quad[i];
+    }
+    P.bs = (R)a.ph.bs;
+    P.trap_offset = (R)a.ph.trap_offset;
+    P.c0 = (R)a.ph.c0;
+    P.c2 = (R)a.ph.c2;
+    P.c4 = (R)a.ph.c4;
+    P.alpha = (R)a.ph.alpha;
+    P.sigma = (R)a.ph.sigma;
+    P.bq = (R)a.B.bq;
+    P.bqq = (R)a.B.bq_quad;
+    P.dt = (R)a.ph.dt;
+    P.flags = a.ph.flags;
+    P.trap_on = !((a.ph.flags & GPE_FLAG_TRAP_OFF_AFTER) && a.t >= a.ph.trap_off_time);
+    return P;
+}
+
+// trap (Spin1GpeBCC.cu:112-122)
+template <typename R>
+__device__ __forceinline__ R trap(const PhysR<R>& P, const R r[3]) {
+    if (!P.trap_on) return (R)0;
+    R x = r[0] * P.lambda[0];
+    R y = r[1] * P.lambda[1];
+    R z = r[2] * P.lambda[2];
+    return (R)0.5 * (x * x + y * y + z * z) + P.trap_offset;
+}
+
+// magneticField (Spin1GpeBCC.cu:128-142)
+template <typename R>
+__device__ __forceinline__ void mag_field(const PhysR<R>& P, const R r[3], R Bq, const R Bb[3], R B[3]) {
+    if (P.flags & GPE_FLAG_QUADRUPOLE_OFFSET) {
+        B[0] = Bq * (r[0] - P.qc[0]) + Bb[0];
+        B[1] = Bq * (r[1] - P.qc[1]) + Bb[1];
+        B[2] = (R)-2 * Bq * (r[2] - P.qc[2]) + Bb[2];
+    } else {
+        B[0] = Bq * r[0] + Bb[0];
+        B[1] = Bq * r[1] + Bb[1];
+        B[2] = (R)-2 * Bq * r[2] + Bb[2];
+    }
+}
+
+// Local (non-kinetic) part of H for spin-1 (Spin1GpeBCC.cu:867-912).  ext: use the
+// external field (leapfrog / Euler); the imaginary-time kernel uses only c2<F>
+// (Spin1GpeBCC.cu:645-646).  pot = trap value; lossqz: loss and quadratic Zeeman
+// allowed.  totalPot_out receives trap + c0 rho for the hyperbolic c_K.
+template <typename R>
+__device__ __forceinline__ void local_spin1(const PhysR<R>& P, const R r[3], R pot, bool ext, bool lossqz,
+                                            bool hyper, const Cx<R>* ps, Cx<R>* H) {
+    const R n1 = ps[0].x * ps[0].x + ps[0].y * ps[0].y;
+    const R n_1 = ps[2].x * ps[2].x + ps[2].y * ps[2].y;
+    const R normSq = n1 + (ps[1].x * ps[1].x + ps[1].y * ps[1].y) + n_1;
+    Cx<R> totalPot = cx<R>(pot + P.c0 * normSq, (R)0);
+    if (lossqz && (P.flags & GPE_FLAG_THREE_BODY_LOSS)) totalPot.y = -P.alpha * normSq * normSq;
+    if (hyper) {
+        // RelativisticSpin1Gpe/common_kernels.h:229-235
+        const R cK = (R)1 + P.sigma * totalPot.x;
+        for (int s = 0; s < 3; ++s) H[s] = (-cK) * H[s];
+    }
+    H[0] += totalPot * ps[0];
+    H[1] += totalPot * ps[1];
+    H[2] += totalPot * ps[2];
+    const Cx<R> magXY = (R)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
+    R B[3];
+    if (ext) {
+        mag_field(P, r, P.bq, P.bb, B);
+        B[0] += P.c2 * magXY.x;
+        B[1] += P.c2 * magXY.y;
+        B[2] += P.c2 * (n1 - n_1);
+    } else {
+        B[0] = P.c2 * magXY.x;
+        B[1] = P.c2 * magXY.y;
+        B[2] = P.c2 * (n1 - n_1);
+    }
+    Cx<R> Bxy = (R)GPE_REF_INV_SQRT_2 * cx<R>(B[0], B[1]);
+    Cx<R> BxyConj = conj(Bxy);
+    H[0] += (B[2] * ps[0] + BxyConj * ps[1]);
+    H[1] += (Bxy * ps[0] + BxyConj * ps[2]);
+    H[2] += (Bxy * ps[1] - B[2] * ps[2]);
+    if (lossqz && (P.flags & GPE_FLAG_QUADRATIC_ZEEMAN)) {
+        // Spin1GpeBCC.cu:897-912
+        R Q[3];
+        mag_field(P, r, P.bqq, P.bbq, Q);
+        Bxy = (R)GPE_REF_INV_SQRT_2 * cx<R>(Q[0], Q[1]);
+        BxyConj = conj(Bxy);
+        const R BxyNormSq = (BxyConj * Bxy).x;
+        const Cx<R> BxySq = Bxy * Bxy;
+        const Cx<R> BxyConjSq = BxyConj * BxyConj;
+        const R BzSq = Q[2] * Q[2];
+        const Cx<R> BzBxy = Q[2] * Bxy;
+        const Cx<R> BzBxyConj = Q[2] * BxyConj;
+        H[0] += (BzSq + BxyNormSq) * ps[0] + BzBxyConj * ps[1] + BxyConjSq * ps[2];
+        H[1] += BzBxy * ps[0] + ((R)2 * BxyNormSq) * ps[1] - BzBxyConj * ps[2];
+        H[2] += BxySq * ps[0] - BzBxy * ps[1] + (BzSq + BxyNormSq) * ps[2];
+    }
+}
+
+// Local part of H for spin-2 (Spin2GpeBCC.cu:923-970; RelativisticSpin2Gpe.cu:1068-1125).
+template <typename R>
+__device__ __forceinline__ void local_spin2(const PhysR<R>& P, const R r[3], R pot, bool ext, bool loss, bool hyper,
+                                            const Cx<R>* ps, Cx<R>* H) {
+    R n[5];
+    for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+    const R normSq = n[0] + n[1] + n[2] + n[3] + n[4];
+    Cx<R> ab = cx<R>(pot + P.c0 * normSq, (R)0);
+    if (loss && (P.flags & GPE_FLAG_THREE_BODY_LOSS)) ab.y = -P.alpha * normSq * normSq;
+    if (hyper) {
+        const R cK = (R)1 + P.sigma * ab.x;
+        for (int s = 0; s < 5; ++s) H[s] = (-cK) * H[s];
+    }
+    R B[3] = {(R)0, (R)0, (R)0};
+    if (ext) mag_field(P, r, P.bq, P.bb, B);
+    const R c2 = P.c2, c4 = P.c4;
+    const R Fz = c2 * ((R)2 * n[0] + n[1] - n[3] - (R)2 * n[4]);
+    Cx<R> d[5];
+    d[0] = cx<R>((R)2 * Fz + (R)0.4 * c4 * n[4] - (R)2 * B[2], (R)0) + ab;
+    d[1] = cx<R>(Fz + (R)0.4 * c4 * n[3] - B[2], (R)0) + ab;
+    d[2] = cx<R>((R)0.2 * c4 * n[2], (R)0) + ab;
+    d[3] = cx<R>(-Fz + (R)0.4 * c4 * n[1] + B[2], (R)0) + ab;
+    d[4] = cx<R>((R)-2 * Fz + (R)0.4 * c4 * n[0] + (R)2 * B[2], (R)0) + ab;
+    for (int s = 0; s < 5; ++s) H[s] += d[s] * ps[s];
+    const Cx<R> s2 = ps[0], s1 = ps[1], s0 = ps[2], s_1 = ps[3], s_2 = ps[4];
+    const R sq6 = (R)2.449489742783178098, sq15 = (R)1.224744871391589049;  // sqrt(6), sqrt(1.5)
+    const Cx<R> den = c2 * ((R)2 * (s2 * conj(s1) + s_1 * conj(s_2)) + sq6 * (s1 * conj(s0) + s0 * conj(s_1))) -
+                      cx<R>(B[0], -B[1]);
+    const Cx<R> c12 = den - ((R)0.4 * c4 * s_1) * conj(s_2);
+    const Cx<R> c45 = den - ((R)0.4 * c4 * s2) * conj(s1);
+    const Cx<R> c13 = ((R)0.2 * c4 * s0) * conj(s_2);
+    const Cx<R> c35 = ((R)0.2 * c4 * s2) * conj(s0);
+    const Cx<R> c23 = sq15 * den - ((R)0.2 * c4 * s0) * conj(s_1);
+    const Cx<R> c34 = sq15 * den - ((R)0.2 * c4 * s1) * conj(s0);
+    H[0] += (c12 * s1 + c13 * s0);
+    H[1] += (conj(c12) * s2 + c23 * s0);
+    H[2] += (conj(c13) * s2 + c35 * s_2 + c34 * s_1 + conj(c23) * s1);
+    H[3] += (conj(c34) * s0 + c45 * s_2);
+    H[4] += (conj(c35) * s0 + conj(c45) * s_1);
+}
+
+template <typename R>
+__device__ __forceinline__ void local_scalar(const PhysR<R>& P, R pot, bool loss, bool hyper, const Cx<R>* ps, Cx<R>* H) {
+    // GPUGrossPitaevskii_BCC.cu:198-199; RelativisticGpeBCC.cu:244-253
+    const R normsq = ps[0].x * ps[0].x + ps[0].y * ps[0].y;
+    Cx<R> tp = cx<R>(pot + P.c0 * normsq, (R)0);
+    if (loss && (P.flags & GPE_FLAG_THREE_BODY_LOSS)) tp.y = -P.alpha * normsq * normsq;
+    if (hyper) {
+        const R cK = (R)1 + P.sigma * tp.x;
+        H[0] = (-cK) * H[0];
+    }
+    H[0] += tp * ps[0];
+}
+
+template <typename R, int C>
+__device__ __forceinline__ void local_terms(const PhysR<R>& P, const R r[3], R pot, int mode, bool hyper, const Cx<R>* ps,
+                                            Cx<R>* H) {
+    const bool ext = (mode != GPE_MODE_ITP);
+    if constexpr (C == 1) {
+        local_scalar<R>(P, pot, ext, hyper, ps, H);
+    } else if constexpr (C == 3) {
+        local_spin1<R>(P, r, pot, ext, ext, hyper, ps, H);
+    } else {
+        local_spin2<R>(P, r, pot, ext, true, hyper, ps, H);
+    }
+}
+
+// Shared-memory copy of the per-handle tables.
+template <typename R>
+struct SmemTables {
+    int32_t row_ptr[kMaxNodes + 1];
+    int32_t nb_off[kMaxEntries];
+    R w[kMaxEntries];
+    R pos[kMaxNodes * 3];
+};
+
+template <typename R>
+__device__ __forceinline__ void load_tables(SmemTables<R>& s, const StepArgs& a) {
+    const int V = a.g.V;
+    const int n = a.tab.entries;
+    for (int i = threadIdx.x; i <= V; i += blockDim.x) s.row_ptr[i] = a.tab.row_ptr[i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        s.nb_off[i] = a.tab.nb_off[i];
+        if constexpr (sizeof(R) == 4) s.w[i] = a.tab.w32[i];
+        else s.w[i] = a.tab.w64[i];
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) s.pos[i] = a.tab.pos32[i];
+        else s.pos[i] = a.tab.pos64[i];
+    }
+}
+
+// Apply the time update to one node (Spin1GpeBCC.cu:914-916, :788-790, :655-661).
+template <typename R, int C>
+__device__ __forceinline__ void write_update(int mode, R dt, char* nxt, char* hp, const Cx<R>* prv, const Cx<R>* H) {
+#pragma unroll
+    for (int s = 0; s < C; ++s) {
+        char* p = nxt + s * 2 * sizeof(R);
+        if (mode == GPE_MODE_LEAPFROG) {
+            Cx<R> v = ldc_rw<R>(p);
+            v += ((R)2 * dt) * cx<R>(H[s].y, -H[s].x);
+            stc<R>(p, v);
+        } else if (mode == GPE_MODE_EULER) {
+            stc<R>(p, prv[s] + dt * cx<R>(H[s].y, -H[s].x));
+        } else {
+            if (hp) stc<R>(hp + s * 2 * sizeof(R), H[s]);
+            stc<R>(p, prv[s] - dt * H[s]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- parabolic
+
+// MODE: GPE_MODE_LEAPFROG / EULER / ITP.  One thread per (node, cell).
+template <typename R, int C, int MODE>
+__global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
+    __shared__ SmemTables<R> st;
+    load_tables<R>(st, a);
+    __syncthreads();
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= a.total) return;
+    const uint32_t i = (uint32_t)gid;
+    const uint32_t row = fdiv(i, a.divRow);
+    const uint32_t within = i - row * a.row_items;
+    const uint32_t x = fdiv(within, a.divV);
+    const uint32_t l = within - x * a.g.V;
+    const uint32_t z = fdiv(row, a.divY);
+    const uint32_t y = row - z * a.g.Y;
+
+    const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+    const char* base = a.prev + cell_off;
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    const char* own = base + l * node_bytes;
+
+    Cx<R> prv[C], H[C];
+#pragma unroll
+    for (int s = 0; s < C; ++s) {
+        prv[s] = ldc<R>(own + s * 2 * sizeof(R));
+        H[s] = cx<R>((R)0, (R)0);
+    }
+    // DEC Laplacian, sum_f w_f (psi_nb - psi) (Spin1GpeBCC.cu:835-865)
+    const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
+    for (int f = f0; f < f1; ++f) {
+        const char* nb = base + st.nb_off[f];
+        const R w = st.w[f];
+#pragma unroll
+        for (int s = 0; s < C; ++s) H[s] += w * (ldc<R>(nb + s * 2 * sizeof(R)) - prv[s]);
+    }
+    const PhysR<R> P = make_phys<R>(a);
+    R r[3];
+    r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
+    r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + st.pos[3 * l + 1]);
+    r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + st.pos[3 * l + 2]);
+    const R pot = trap<R>(P, r);
+    local_terms<R, C>(P, r, pot, MODE, false, prv, H);
+    char* nxt = a.next + cell_off + l * node_bytes;
+    char* hp = (MODE == GPE_MODE_ITP && a.hpsi) ? a.hpsi + cell_off + l * node_bytes : nullptr;
+    write_update<R, C>(MODE, P.dt, nxt, hp, prv, H);
+}
+
+// ---------------------------------------------------------------- hyperbolic
+
+template <typename R>
+struct SmemHyper {
+    int32_t inc_off[kMaxNodes * kMaxFaces];
+    R inc_w[kMaxNodes * kMaxFaces];
+    int32_t e_from[kMaxEdges];
+    int32_t e_to[kMaxEdges];
+    R pos[kMaxNodes * 3];
+};
+
+// Edge (q) update of one dual edge (RelativisticSpin2Gpe.cu:986-1019, :823-856).
+// QM: 0 hyperbolic leapfrog  next_q += i 2(dt/sigma)(prev_q + d0 psi)
+//     1 parabolic            next_q  = d0 psi
+//     2 forward Euler        next_q  = prev_q + i (dt/sigma)(prev_q + d0 psi)
+template <typename R, int C, int QM>
+__device__ __forceinline__ void q_update(const StepArgs& a, const SmemHyper<R>& sh, uint32_t x, uint32_t y,
+                                         uint32_t z, uint32_t e) {
+    const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+    const size_t qcell_off = (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x * a.g.qcell_bytes;
+    const char* pb = a.prev + cell_off;
+    const char* thisp = pb + sh.e_from[e];
+    const char* otherp = pb + sh.e_to[e];
+    const uint32_t edge_bytes = C * 2 * sizeof(R);
+    const char* qprev = a.q + qcell_off + e * edge_bytes;
+    char* qnext = a.qnext + qcell_off + e * edge_bytes;
+    const R dts = (R)(a.ph.dt / a.ph.sigma);
+#pragma unroll
+    for (int s = 0; s < C; ++s) {
+        const Cx<R> d0psi = ldc<R>(otherp + s * 2 * sizeof(R)) - ldc<R>(thisp + s * 2 * sizeof(R));
+        char* qn = qnext + s * 2 * sizeof(R);
+        if constexpr (QM == 1) {
+            stc<R>(qn, d0psi);
+        } else if constexpr (QM == 0) {
+            const Cx<R> qq = ((R)2 * dts) * (ldc_rw<R>(qprev + s * 2 * sizeof(R)) + d0psi);
+            Cx<R> v = ldc_rw<R>(qn);
+            v += cx<R>(-qq.y, qq.x);
+            stc<R>(qn, v);
+        } else {
+            const Cx<R> pq = ldc_rw<R>(qprev + s * 2 * sizeof(R));
+            const Cx<R> qq = dts * (pq + d0psi);
+            stc<R>(qn, pq + cx<R>(-qq.y, qq.x));
+        }
+    }
+}
+
+// Fused psi + q step.  The reference launches update_psi then update_q, both
+// reading the previous (psi, q) (RelativisticSpin2Gpe.cu:1873-1874); here one
+// launch does both.  Blocks are interleaved in groups of 1 + E/V: the first block
+// of a group updates 256 nodes, the next E/V blocks update the 256*E/V edges of
+// the same cells, so both halves of a group read the same psi/q lines from L2.
+// DO_PSI: psi update with MODE and HYPERB (-c_K scaling); QM < 0: no q update.
+template <typename R, int C, bool DO_PSI, int MODE, bool HYPERB, int QM>
+__global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t node_items, uint32_t edge_items,
+                                                         uint32_t ratio) {
+    __shared__ SmemHyper<R> sh;
+    const int V = a.g.V, E = a.g.E, F = a.tab.faces;
+    for (int i = threadIdx.x; i < V * F; i += blockDim.x) {
+        sh.inc_off[i] = a.tab.inc_off[i];
+        if constexpr (sizeof(R) == 4) sh.inc_w[i] = a.tab.inc_w32[i];
+        else sh.inc_w[i] = a.tab.inc_w64[i];
+    }
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        sh.e_from[i] = a.tab.e_from_off[i];
+        sh.e_to[i] = a.tab.e_to_off[i];
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) sh.pos[i] = a.tab.pos32[i];
+        else sh.pos[i] = a.tab.pos64[i];
+    }
+    __syncthreads();
+
+    uint32_t group, sub;
+    if (DO_PSI && QM >= 0) {
+        group = blockIdx.x / (1 + ratio);
+        sub = blockIdx.x - group * (1 + ratio);
+    } else if (DO_PSI) {
+        group = blockIdx.x;
+        sub = 0;
+    } else {
+        group = 0;
+        sub = 1 + blockIdx.x;  // edge block index = sub - 1
+    }
+    if (DO_PSI && sub == 0) {
+        const uint32_t i = group * blockDim.x + threadIdx.x;
+        if (i >= node_items) return;
+        const PhysR<R> P = make_phys<R>(a);
+        const uint32_t node_bytes = C * 2 * sizeof(R);
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+        const size_t qcell_off = (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x * a.g.qcell_bytes;
+        const char* own = a.prev + cell_off + l * node_bytes;
+        Cx<R> prv[C], H[C];
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            prv[s] = ldc<R>(own + s * 2 * sizeof(R));
+            H[s] = cx<R>((R)0, (R)0);
+        }
+        // d1 of q (RelativisticSpin2Gpe.cu:1051-1066)
+        const char* qb = a.q + qcell_off;
+        for (int k = 0; k < F; ++k) {
+            const char* qp = qb + sh.inc_off[l * F + k];
+            const R w = sh.inc_w[l * F + k];
+#pragma unroll
+            for (int s = 0; s < C; ++s) H[s] += w * ldc<R>(qp + s * 2 * sizeof(R));
+        }
+        R r[3];
+        r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + sh.pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + sh.pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + sh.pos[3 * l + 2]);
+        const R pot = trap<R>(P, r);
+        if constexpr (C == 1) {
+            local_scalar<R>(P, pot, false, HYPERB, prv, H);
+        } else if constexpr (C == 3) {
+            local_spin1<R>(P, r, pot, MODE != GPE_MODE_ITP, false, HYPERB, prv, H);
+        } else {
+            local_spin2<R>(P, r, pot, MODE != GPE_MODE_ITP, false, HYPERB, prv, H);
+        }
+        write_update<R, C>(MODE, P.dt, a.next + cell_off + l * node_bytes, nullptr, prv, H);
+    } else if constexpr (QM >= 0) {
+        const uint32_t eb = (DO_PSI ? group * ratio : 0) + (sub - 1);
+        const uint32_t i = eb * blockDim.x + threadIdx.x;
+        if (i >= edge_items) return;
+        const uint32_t row = fdiv(i, a.divRowE);
+        const uint32_t within = i - row * a.row_items_e;
+        const uint32_t x = fdiv(within, a.divE);
+        const uint32_t e = within - x * E;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        q_update<R, C, QM>(a, sh, x, y, z, e);
+    }
+}
+
+}  // namespace gpe
+
+namespace gpe {
+
+// ---------------------------------------------------------------- observables
+
+// FP64 observables of one psi buffer (density/integrate Spin1GpeBCC.cu:191-211,
+// 328-348; energy GPUGrossPitaevskii_BCC.cu:204-226; localAvgSpinAndDensity
+// Spin1GpeBCC.cu:235-271; com GPUGrossPitaevskii_BCC.cu:349-375).  Values are
+// loaded in the storage precision and everything after the load is FP64.  Each
+// block writes OBS_COUNT partial sums (warp shuffles, then shared memory); a
+// one-block kernel adds the partials in a fixed order, so results are
+// reproducible run to run.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
+    __shared__ SmemTables<double> st;
+    __shared__ double red[8][OBS_COUNT];
+    {
+        const int V = a.g.V, n = a.tab.entries;
+        for (int i = threadIdx.x; i <= V; i += blockDim.x) st.row_ptr[i] = a.tab.row_ptr[i];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            st.nb_off[i] = a.tab.nb_off[i];
+            st.w[i] = a.tab.w64[i];
+        }
+        for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) st.pos[i] = a.tab.pos64[i];
+    }
+    __syncthreads();
+    double acc[OBS_COUNT];
+#pragma unroll
+    for (int k = 0; k < OBS_COUNT; ++k) acc[k] = 0.0;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < a.total) {
+        const uint32_t i = (uint32_t)gid;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * a.g.V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+        const char* base = a.prev + cell_off;
+        const uint32_t node_bytes = C * 2 * sizeof(R);
+        Cx<double> ps[C], L[C], Hl[C], Hn[C];
+        double rho = 0, maxabs = 0, bad = 0;
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            const Cx<R> v = ldc<R>(base + l * node_bytes + s * 2 * sizeof(R));
+            ps[s] = cx<double>((double)v.x, (double)v.y);
+            L[s] = Hl[s] = Hn[s] = cx<double>(0.0, 0.0);
+            const double n2 = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+            rho += n2;
+            maxabs = fmax(maxabs, sqrt(n2));
+            if (!isfinite(ps[s].x) || !isfinite(ps[s].y)) bad += 1;
+        }
+        for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
+            const char* nb = base + st.nb_off[f];
+#pragma unroll
+            for (int s = 0; s < C; ++s) {
+                const Cx<R> v = ldc<R>(nb + s * 2 * sizeof(R));
+                L[s] += st.w[f] * (cx<double>((double)v.x, (double)v.y) - ps[s]);
+            }
+        }
+        PhysR<double> P = make_phys<double>(a);
+        double r[3];
+        r[0] = P.p0[0] + P.bs * ((double)x * P.bw[0] + st.pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((double)y * P.bw[1] + st.pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((double)z * P.bw[2] + st.pos[3 * l + 2]);
+        local_terms<double, C>(P, r, trap<double>(P, r), GPE_MODE_LEAPFROG, false, ps, Hl);
+        // interaction-only part: no trap, no external field, no loss / quadratic Zeeman
+        PhysR<double> Q = P;
+        Q.bq = Q.bqq = 0;
+        for (int k = 0; k < 3; ++k) Q.bb[k] = Q.bbq[k] = 0;
+        Q.flags &= ~(GPE_FLAG_THREE_BODY_LOSS | GPE_FLAG_QUADRATIC_ZEEMAN | GPE_FLAG_QUADRUPOLE_OFFSET);
+        local_terms<double, C>(Q, r, 0.0, GPE_MODE_LEAPFROG, false, ps, Hn);
+        double kin = 0, hl = 0, hn = 0;
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            kin += ps[s].x * L[s].x + ps[s].y * L[s].y;
+            hl += ps[s].x * Hl[s].x + ps[s].y * Hl[s].y;
+            hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
+        }
+        acc[OBS_NORM] = rho;
+        acc[OBS_HEXP] = kin + hl;
+        acc[OBS_EINT] = hn;
+        acc[OBS_COMX] = rho * r[0];
+        acc[OBS_COMY] = rho * r[1];
+        acc[OBS_COMZ] = rho * r[2];
+        acc[OBS_MAXABS] = maxabs;
+        acc[OBS_NONFINITE] = bad;
+        if constexpr (C == 3) {
+            const Cx<double> m = GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
+            const double fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
+            acc[OBS_MAGX] = m.x;
+            acc[OBS_MAGY] = m.y;
+            acc[OBS_MAGZ] = fz;
+            acc[OBS_SPIN] = sqrt(m.x * m.x + m.y * m.y + fz * fz);
+        } else if constexpr (C == 5) {
+            const Cx<double> fp = 2.0 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
+                                  2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
+            double n[5];
+            for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+            const double fz = 2 * n[0] + n[1] - n[3] - 2 * n[4];
+            acc[OBS_MAGX] = fp.x;
+            acc[OBS_MAGY] = fp.y;
+            acc[OBS_MAGZ] = fz;
+            acc[OBS_SPIN] = sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
+        }
+    }
+    // warp reduction
+#pragma unroll
+    for (int k = 0; k < OBS_COUNT; ++k) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_down_sync(0xffffffffu, v, o);
+            v = (k == OBS_MAXABS) ? fmax(v, u) : v + u;
+        }
+        acc[k] = v;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < OBS_COUNT; ++k) red[warp][k] = acc[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < OBS_COUNT) {
+        const int k = threadIdx.x;
+        double v = red[0][k];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = (k == OBS_MAXABS) ? fmax(v, red[w][k]) : v + red[w][k];
+        a.partials[(size_t)blockIdx.x * OBS_COUNT + k] = v;
+    }
+}
+
+// Adds nblocks x OBS_COUNT partials into out[OBS_COUNT] with one block of 256
+// threads; the order of additions depends only on nblocks.
+static __global__ void __launch_bounds__(256) observe_finalize_kernel(const double* partials, uint32_t nblocks, double* out) {
+    __shared__ double red[256];
+    for (int k = 0; k < OBS_COUNT; ++k) {
+        double v = (k == OBS_MAXABS) ? 0.0 : 0.0;
+        for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) {
+            const double u = partials[(size_t)b * OBS_COUNT + k];
+            v = (k == OBS_MAXABS) ? fmax(v, u) : v + u;
+        }
+        red[threadIdx.x] = v;
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s)
+                red[threadIdx.x] = (k == OBS_MAXABS) ? fmax(red[threadIdx.x], red[threadIdx.x + s])
+                                                     : red[threadIdx.x] + red[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[k] = red[0];
+        __syncthreads();
+    }
+}
+
+// Scale every interior value of a psi buffer by 1/sqrt(norm) where norm is read
+// from device memory (normalize, Spin1GpeBCC.cu:412-434).
+template <typename R, int C>
+__global__ void __launch_bounds__(256) scale_kernel(StepArgs a, const double* norm_sum, double dv) {
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= a.total) return;
+    const uint32_t i = (uint32_t)gid;
+    const uint32_t row = fdiv(i, a.divRow);
+    const uint32_t within = i - row * a.row_items;
+    const uint32_t x = fdiv(within, a.divV);
+    const uint32_t l = within - x * a.g.V;
+    const uint32_t z = fdiv(row, a.divY);
+    const uint32_t y = row - z * a.g.Y;
+    const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+    char* p = a.next + cell_off + l * (C * 2 * sizeof(R));
+    const double sq = sqrt(norm_sum[OBS_NORM] * dv);
+#pragma unroll
+    for (int s = 0; s < C; ++s) {
+        Cx<R> v = ldc_rw<R>(p + s * 2 * sizeof(R));
+        v.x = (R)((double)v.x / sq);
+        v.y = (R)((double)v.y / sq);
+        stc<R>(p + s * 2 * sizeof(R), v);
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+inline unsigned nblocks(uint64_t items, unsigned bs) { return (unsigned)((items + bs - 1) / bs); }
+
+template <typename R, int C>
+cudaError_t launch_parabolic(const StepArgs& a, int mode, cudaStream_t s) {
+    const unsigned nb = nblocks(a.total, 256);
+    if (nb == 0) return cudaSuccess;
+    switch (mode) {
+        case GPE_MODE_LEAPFROG: parabolic_step_kernel<R, C, GPE_MODE_LEAPFROG><<<nb, 256, 0, s>>>(a); break;
+        case GPE_MODE_EULER: parabolic_step_kernel<R, C, GPE_MODE_EULER><<<nb, 256, 0, s>>>(a); break;
+        default: parabolic_step_kernel<R, C, GPE_MODE_ITP><<<nb, 256, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
+// kinds of hyperbolic launches
+enum HyperKind {
+    HK_FUSED_LEAPFROG = 0,   // psi (hyperbolic, leapfrog) + q (hyperbolic leapfrog)
+    HK_PSI_PARA_LEAPFROG,    // psi only, parabolic kinetic from q, leapfrog
+    HK_PSI_PARA_EULER,       // psi only, parabolic, forward Euler (start step)
+    HK_PSI_HYPER_EULER,      // psi only, hyperbolic, forward Euler
+    HK_PSI_PARA_ITP,         // psi only, parabolic, imaginary time
+    HK_Q_PARA,               // q = d0 psi
+    HK_Q_EULER_HYPER,        // q = q + i dt/sigma (q + d0 psi)
+    HK_Q_HYPER               // q += i 2 dt/sigma (q + d0 psi)
+};
+
+template <typename R, int C>
+cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
+    const uint32_t nn = (uint32_t)((uint64_t)a.g.X * a.g.Y * a.g.Z * a.g.V);
+    const uint32_t ne = (uint32_t)((uint64_t)a.g.X * a.g.Y * a.g.Z * a.g.E);
+    const uint32_t ratio = a.g.V ? (a.g.E + a.g.V - 1) / a.g.V : 1;
+    const unsigned nbn = nblocks(nn, 256), nbe = nblocks(ne, 256);
+    switch (kind) {
+        case HK_FUSED_LEAPFROG: {
+            // every group of (1 + ratio) blocks holds one node block and `ratio` edge blocks
+            const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
+            hyper_step_kernel<R, C, true, GPE_MODE_LEAPFROG, true, 0><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        }
+        case HK_PSI_PARA_LEAPFROG:
+            hyper_step_kernel<R, C, true, GPE_MODE_LEAPFROG, false, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        case HK_PSI_PARA_EULER:
+            hyper_step_kernel<R, C, true, GPE_MODE_EULER, false, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        case HK_PSI_HYPER_EULER:
+            hyper_step_kernel<R, C, true, GPE_MODE_EULER, true, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        case HK_PSI_PARA_ITP:
+            hyper_step_kernel<R, C, true, GPE_MODE_ITP, false, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        case HK_Q_PARA: hyper_step_kernel<R, C, false, GPE_MODE_LEAPFROG, false, 1><<<nbe, 256, 0, s>>>(a, nn, ne, ratio); break;
+        case HK_Q_EULER_HYPER:
+            hyper_step_kernel<R, C, false, GPE_MODE_LEAPFROG, false, 2><<<nbe, 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        default: hyper_step_kernel<R, C, false, GPE_MODE_LEAPFROG, false, 0><<<nbe, 256, 0, s>>>(a, nn, ne, ratio); break;
+    }
+    return cudaGetLastError();
+}
+
+template <typename R, int C>
+cudaError_t launch_observe(const StepArgs& a, double* out, cudaStream_t s) {
+    const unsigned nb = nblocks(a.total, 256);
+    observe_kernel<R, C><<<nb, 256, 0, s>>>(a);
+    observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
+    return cudaGetLastError();
+}
+
+template <typename R, int C>
+cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s) {
+    scale_kernel<R, C><<<nblocks(a.total, 256), 256, 0, s>>>(a, norm_sum, dv);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE(R, C)                                                               \
+    template cudaError_t launch_parabolic<R, C>(const StepArgs&, int, cudaStream_t);       \
+    template cudaError_t launch_hyper<R, C>(const StepArgs&, int, cudaStream_t);           \
+    template cudaError_t launch_observe<R, C>(const StepArgs&, double*, cudaStream_t);     \
+    template cudaError_t launch_scale<R, C>(const StepArgs&, const double*, double, cudaStream_t);
+
+}  // namespace gpe
+
+namespace gpe {
+
+// sum_interior Re(conj(a) b) into partials[.][OBS_NORM] (innerProduct,
+// Spin1GpeBCC.cu:213-233); a = StepArgs::prev, b = StepArgs::next.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) dot_kernel(StepArgs a) {
+    __shared__ double red[8];
+    double acc = 0;
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < a.total) {
+        const uint32_t i = (uint32_t)gid;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * a.g.V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        const size_t off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes + l * (C * 2 * sizeof(R));
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            const Cx<R> u = ldc<R>(a.prev + off + s * 2 * sizeof(R));
+            const Cx<R> v = ldc<R>(a.next + off + s * 2 * sizeof(R));
+            acc += (double)u.x * (double)v.x + (double)u.y * (double)v.y;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < OBS_COUNT) {
+        double v = 0;
+        if (threadIdx.x == OBS_NORM)
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+        a.partials[(size_t)blockIdx.x * OBS_COUNT + threadIdx.x] = v;
+    }
+}
+
+template <typename R, int C>
+cudaError_t launch_dot_t(const StepArgs& a, double* out, cudaStream_t s) {
+    const unsigned nb = nblocks(a.total, 256);
+    dot_kernel<R, C><<<nb, 256, 0, s>>>(a);
+    observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
+    return cudaGetLastError();
+}
+
+}  // namespace gpe
+
+namespace gpe {
+
+// Copy between a packed FP64 array in the reference file layout
+// ((Z+2)(Y+2)(X+2) cells of `vals` doubles, halo included) and a pitched device
+// buffer of storage type R.  TO_DEVICE: interior cells are converted, the device
+// halo is left untouched (zero).  Otherwise the packed array receives the
+// interior values and zeros in the halo.
+template <typename R, bool TO_DEVICE>
+__global__ void __launch_bounds__(256) pack_kernel(double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
+                                                   uint32_t vals, size_t pitch, size_t slice, uint64_t total) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t cell = i / vals;
+        const uint32_t within = (uint32_t)(i - cell * vals);
+        const uint32_t x = (uint32_t)(cell % (X + 2));
+        const uint64_t yz = cell / (X + 2);
+        const uint32_t y = (uint32_t)(yz % (Y + 2));
+        const uint32_t z = (uint32_t)(yz / (Y + 2));
+        const bool halo = x == 0 || y == 0 || z == 0 || x == X + 1 || y == Y + 1 || z == Z + 1;
+        R* d = reinterpret_cast<R*>(dev_base + (size_t)z * slice + (size_t)y * pitch + (size_t)x * vals * sizeof(R)) + within;
+        if (TO_DEVICE) {
+            if (!halo) *d = (R)packed[i];
+        } else {
+            packed[i] = halo ? 0.0 : (double)*d;
+        }
+    }
+}
+
+template <typename R>
+cudaError_t launch_pack(double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z, uint32_t vals, size_t pitch,
+                        size_t slice, bool to_device, cudaStream_t s) {
+    const uint64_t total = (uint64_t)(X + 2) * (Y + 2) * (Z + 2) * vals;
+    const unsigned nb = (unsigned)((total + 255) / 256 < 152u * 64u ? (total + 255) / 256 : 152u * 64u);
+    if (to_device) pack_kernel<R, true><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total);
+    else pack_kernel<R, false><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total);
+    return cudaGetLastError();
+}
+
+}  // namespace gpe

@@ -1,0 +1,104 @@
+"""Python front end of libgpe: one Stepper per condensate.
+
+Mirrors the time loop of the reference programs (integrateInTime in
+Spin1GpeBCC.cu:1105-1743, RelativisticSpin2Gpe.cu:1295-...): upload an initial
+state into PSI_ODD, take the forward-Euler start step, then leapfrog steps with
+the field ramp evaluated per step, and FP64 observables when wanted.  All the
+work happens in libgpe's CUDA kernels; a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+
+
+class Stepper:
+    def __init__(self, lattice, params: "capi.Params"):
+        self.lib = capi.load_library()
+        self.lattice = lattice if isinstance(lattice, capi.Lattice) else capi.Lattice(lattice)
+        self.params = params
+        self._lat = C.c_void_p()
+        capi.check(self.lib.gpe_lattice_create(C.byref(self.lattice.desc), C.byref(self._lat)), "gpe_lattice_create")
+        self._h = C.c_void_p()
+        st = self.lib.gpe_create(self._lat, C.byref(params), C.byref(self._h))
+        if st != capi.GPE_OK:
+            self.lib.gpe_lattice_destroy(self._lat)
+            self._lat = None
+            capi.check(st, "gpe_create")
+        self.stream = None
+
+    # ------------------------------------------------------------- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.gpe_destroy(self._h)
+            self._h = None
+        if getattr(self, "_lat", None):
+            self.lib.gpe_lattice_destroy(self._lat)
+            self._lat = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ----------------------------------------------------------------- state
+    def shape(self, edges=False):
+        return capi.buffer_shape(self.lattice, self.params, edges)
+
+    def upload(self, slot: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        capi.check(self.lib.gpe_upload(self._h, slot, a.ctypes.data_as(C.POINTER(C.c_double)), a.size, self.stream), "gpe_upload")
+
+    def download(self, slot: int) -> np.ndarray:
+        edges = slot in (capi.Q_EVEN, capi.Q_ODD)
+        out = np.zeros(self.shape(edges))
+        capi.check(self.lib.gpe_download(self._h, slot, out.ctypes.data_as(C.POINTER(C.c_double)), out.size, self.stream), "gpe_download")
+        return out
+
+    def buffer(self, slot: int):
+        p = capi.Pitched()
+        cb = C.c_size_t()
+        capi.check(self.lib.gpe_buffer(self._h, slot, C.byref(p), C.byref(cb)), "gpe_buffer")
+        return p, cb.value
+
+    # ------------------------------------------------------------------ time
+    def set_ramp(self, ramp, t0: float = 0.0):
+        capi.check(self.lib.gpe_set_ramp(self._h, C.byref(ramp) if ramp is not None else None, t0), "gpe_set_ramp")
+
+    def start(self):
+        capi.check(self.lib.gpe_start(self._h, self.stream), "gpe_start")
+
+    def step(self, n: int = 1):
+        capi.check(self.lib.gpe_step(self._h, n, self.stream), "gpe_step")
+
+    def step_explicit(self, next_slot, prev_slot, fields=None, t=0.0, mode=capi.MODE_LEAPFROG):
+        f = C.byref(fields) if fields is not None else None
+        capi.check(self.lib.gpe_step_explicit(self._h, next_slot, prev_slot, f, t, mode, self.stream), "gpe_step_explicit")
+
+    def itp(self, n: int, want_mu: bool = True):
+        mu = C.c_double(0.0)
+        capi.check(self.lib.gpe_itp(self._h, n, C.byref(mu) if want_mu else None, self.stream), "gpe_itp")
+        return mu.value
+
+    def observe(self, slot: int, t: float = 0.0) -> dict:
+        o = capi.Observables()
+        capi.check(self.lib.gpe_observe(self._h, slot, t, C.byref(o), self.stream), "gpe_observe")
+        return o.as_dict()
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.gpe_launch_count(self._h))
+
+    @property
+    def sites(self) -> int:
+        return int(self.lib.gpe_sites(self._h))

@@ -1,0 +1,273 @@
+"""CUDA kernels (through the C ABI) against the FP64 CPU oracle.
+
+FP64 plain kernels: max |gpu - oracle| <= 1e-12 * max|oracle| (the kernels contract
+multiply-adds, the oracle does not; differences are rounding only).
+FP32 fused kernels: max |gpu - oracle| <= 2e-5 * max|oracle| after a few steps from
+moderate random states (FP32 has a 6e-8 unit roundoff; a handful of steps of a
+4-neighbour stencil stays well inside this bound).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from spacetime_gb300 import capi, states
+from spacetime_gb300.stepper import Stepper
+
+pytestmark = pytest.mark.gpu
+
+TOL = {capi.FP64: 1e-12, capi.FP32: 2e-5}
+
+FIELDS = dict(bq=0.3, bb=(0.1, -0.2, 0.5), bq_quad=0.2, bb_quad=(0.05, 0.1, -0.3))
+
+
+def _params(lat, C, prec, dims, **kw):
+    base = dict(components=C, precision=prec, dims=dims, block_scale=0.3, dt=2e-4, trap_offset=100.0,
+                trap_lambda=(1.0, 1.1, 1.3), c0=120.0, c2=-7.0, c4=3.0, lattice=lat)
+    base.update(kw)
+    return capi.make_params(**base)
+
+
+def _rand(lat, p, seed, amp=0.2, edges=False):
+    return amp * states.random_state(capi.buffer_shape(lat, p, edges), seed=seed)
+
+
+def _close(gpu, ref, prec, what=""):
+    scale = float(np.max(np.abs(ref)))
+    err = float(np.max(np.abs(gpu - ref)))
+    assert err <= TOL[prec] * max(scale, 1e-30), "%s: max|gpu-oracle| = %.3e, scale %.3e" % (what, err, scale)
+
+
+CASES = [
+    ("bcc", 1), ("bcc", 3), ("bcc", 5),
+    ("bcc227", 1), ("cube", 1), ("cube", 3),
+    ("fcc", 1), ("fcc", 3), ("a15", 1), ("a15", 3), ("c15", 1), ("c15", 5), ("z", 1), ("z", 3),
+]
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C", CASES)
+def test_parabolic_leapfrog(gpu, name, C, prec):
+    """leapfrog (Spin1GpeBCC.cu:793-917 / Spin2GpeBCC.cu:845-990 / BCC.cu:327-347),
+    3 steps with external fields, ragged grid."""
+    lat = capi.Lattice(name)
+    dims = (5, 3, 4) if lat.nodes > 40 else (7, 5, 4)
+    p = _params(lat, C, prec, dims)
+    even, odd = _rand(lat, p, 11), _rand(lat, p, 12)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        bufs = [capi.PSI_EVEN, capi.PSI_ODD]
+        for n in range(3):
+            s.step_explicit(bufs[(n + 1) % 2], bufs[n % 2], f, t=0.1 * n)
+        got_e, got_o = s.download(capi.PSI_EVEN), s.download(capi.PSI_ODD)
+    e, o = even.copy(), odd.copy()
+    b = [e, o]
+    for n in range(3):
+        oracle.parabolic_step(lat, p, f, 0.1 * n, oracle.LEAPFROG, b[(n + 1) % 2], b[n % 2])
+    _close(got_e, e, prec, "even")
+    _close(got_o, o, prec, "odd")
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("flags", [capi.FLAG_THREE_BODY_LOSS, capi.FLAG_QUADRATIC_ZEEMAN, capi.FLAG_QUADRUPOLE_OFFSET,
+                                   capi.FLAG_TRAP_OFF_AFTER | capi.FLAG_QUADRATIC_ZEEMAN | capi.FLAG_THREE_BODY_LOSS])
+def test_spin1_physics_toggles(gpu, flags, prec):
+    """Three-body loss (Spin1GpeBCC.cu:877-880), quadratic Zeeman (:897-912),
+    quadrupole offset (:128-137), trap switched off after a time (:114)."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, prec, (6, 4, 3), flags=flags, alpha=0.7, quad_center=(-0.2, -0.49, -0.27), trap_off_time=0.05)
+    even, odd = _rand(lat, p, 21), _rand(lat, p, 22)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.1)
+        got = s.download(capi.PSI_ODD)
+    oracle.parabolic_step(lat, p, f, 0.1, oracle.LEAPFROG, odd, even)
+    _close(got, odd, prec)
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("C", [1, 3, 5])
+@pytest.mark.parametrize("mode", [capi.MODE_EULER, capi.MODE_ITP])
+def test_euler_and_itp_modes(gpu, C, mode, prec):
+    """forwardEuler (Spin1GpeBCC.cu:667-791) and itp (:554-662), H psi stored for ITP."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, C, prec, (5, 4, 3))
+    prev = _rand(lat, p, 31)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_ODD, prev)
+        s.step_explicit(capi.PSI_EVEN, capi.PSI_ODD, f, t=0.0, mode=mode)
+        got = s.download(capi.PSI_EVEN)
+        hp = s.download(capi.HPSI) if mode == capi.MODE_ITP else None
+    nxt = np.zeros_like(prev)
+    href = np.zeros_like(prev)
+    oracle.parabolic_step(lat, p, f, 0.0, mode, nxt, prev, href)
+    _close(got, nxt, prec, "next")
+    if hp is not None:
+        _close(hp, href, prec, "hpsi")
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C", [("bcc", 1), ("bcc", 3), ("bcc", 5), ("bcc227", 1), ("cube", 3), ("c15", 5), ("c15", 1)])
+def test_hyperbolic_fused_step(gpu, name, C, prec):
+    """One fused launch = update_psi + update_q (RelativisticSpin2Gpe.cu:971-1132,
+    RelativisticSpin1Gpe common/hyper kernels, RelativisticGpeBCC.cu:179-255)."""
+    lat = capi.Lattice(name)
+    dims = (4, 3, 3) if lat.nodes > 40 else (6, 5, 4)
+    p = _params(lat, C, prec, dims, scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01)
+    pe, po = _rand(lat, p, 41), _rand(lat, p, 42)
+    qe, qo = _rand(lat, p, 43, edges=True), _rand(lat, p, 44, edges=True)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        for slot, a in ((capi.PSI_EVEN, pe), (capi.PSI_ODD, po), (capi.Q_EVEN, qe), (capi.Q_ODD, qo)):
+            s.upload(slot, a)
+        s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.2)
+        s.step_explicit(capi.PSI_EVEN, capi.PSI_ODD, f, t=0.3)
+        got = [s.download(k) for k in (capi.PSI_EVEN, capi.PSI_ODD, capi.Q_EVEN, capi.Q_ODD)]
+    oracle.q_psi_step(lat, p, f, 0.2, oracle.LEAPFROG, True, po, pe, qe)
+    oracle.q_step(lat, p, oracle.Q_HYPER, qo, qe, pe)
+    oracle.q_psi_step(lat, p, f, 0.3, oracle.LEAPFROG, True, pe, po, qo)
+    oracle.q_step(lat, p, oracle.Q_HYPER, qe, qo, po)
+    for g, r, w in zip(got, (pe, po, qe, qo), ("psi_even", "psi_odd", "q_even", "q_odd")):
+        _close(g, r, prec, w)
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("C", [1, 3, 5])
+def test_hyperbolic_start_and_run(gpu, C, prec):
+    """gpe_start (RelativisticSpin2Gpe.cu:1628-1630) then 6 fused steps with a ramp."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, C, prec, (6, 4, 5), scheme=capi.SCHEME_HYPERBOLIC, sigma=0.02)
+    psi = _rand(lat, p, 51)
+    ramp = capi.make_ramp(bq_segments=[(0.25, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0, 0, 0.5), 0.0, capi.RAMP_CONSTANT), ((0, 0, -0.5), 4 * p.dt, capi.RAMP_LINEAR),
+                                       ((0, 0, -0.5), 1e9, capi.RAMP_CONSTANT)])
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_ODD, psi)
+        s.set_ramp(ramp, 0.0)
+        s.start()
+        s.step(6)
+        got_p, got_q = s.download(capi.PSI_EVEN), s.download(capi.Q_EVEN)
+    po, pe = psi.copy(), np.zeros_like(psi)
+    qo = np.zeros(capi.buffer_shape(lat, p, True))
+    qe = np.zeros_like(qo)
+    f0 = oracle.ramp_eval(ramp, 0.0)
+    oracle.q_step(lat, p, oracle.Q_PARA, qo, qo, po)
+    oracle.q_psi_step(lat, p, f0, 0.0, oracle.EULER, False, pe, po, qo)
+    oracle.q_step(lat, p, oracle.Q_PARA, qe, qe, pe)
+    rp, rq = oracle.hyper_run(lat, p, pe, po, qe, qo, 6, ramp=ramp)
+    _close(got_p, rp, prec, "psi")
+    _close(got_q, rq, prec, "q")
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C", [("bcc", 1), ("bcc", 3), ("bcc", 5), ("fcc", 3), ("c15", 5)])
+def test_observables(gpu, name, C, prec):
+    """FP64 reductions (density/energy/magnetisation/centre of mass) against the oracle."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, prec, (5, 4, 3))
+    psi = _rand(lat, p, 61)
+    if prec == capi.FP32:
+        psi = psi.astype(np.float32).astype(np.float64)  # same stored values on both sides
+    f = capi.make_fields(**FIELDS)
+    ramp = capi.make_ramp(bq_segments=[(f.bq, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[(tuple(f.bb), 1e9, capi.RAMP_CONSTANT)])
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, psi)
+        s.set_ramp(ramp, 0.0)
+        got = s.observe(capi.PSI_EVEN, t=0.0)
+    want = oracle.observe(lat, p, oracle.ramp_eval(ramp, 0.0), 0.0, psi)
+    for k in ("norm", "energy", "h_expect", "spin_norm", "max_abs"):
+        assert got[k] == pytest.approx(want[k], rel=1e-11, abs=1e-12), k
+    for k in ("magnetization", "com"):
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-11, atol=1e-12)
+    assert got["nonfinite"] == 0
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+def test_imaginary_time(gpu, prec):
+    """gpe_itp = itp + normalize, twice per iteration pair (Spin1GpeBCC.cu:1470-1490)."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, prec, (6, 5, 4), dt=1e-3)
+    psi = np.abs(_rand(lat, p, 71)) + 0.0
+    psi = states.normalize(psi, lat, p)
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_ODD, psi)
+        mu = s.itp(4)
+        got = s.download(capi.PSI_EVEN)
+        obs = s.observe(capi.PSI_EVEN)
+    cur = psi.copy()
+    hp = np.zeros_like(psi)
+    for _ in range(4):
+        nxt = np.zeros_like(psi)
+        oracle.parabolic_step(lat, p, capi.make_fields(), 0.0, oracle.ITP, nxt, cur, hp)
+        oracle.normalize(lat, p, nxt)
+        cur = nxt
+    dv = p.block_scale ** 3 * lat.volume
+    mu_ref = float(np.sum(cur[1:-1, 1:-1, 1:-1] * hp[1:-1, 1:-1, 1:-1])) * dv
+    _close(got, cur, prec)
+    assert obs["norm"] == pytest.approx(1.0, rel=1e-10 if prec == capi.FP64 else 1e-6)
+    assert mu == pytest.approx(mu_ref, rel=1e-11 if prec == capi.FP64 else 1e-5)
+
+
+def test_leapfrog_run_with_ramp_matches_oracle(gpu):
+    """gpe_start + gpe_step(n) with the device-side schedule of a ramp (config-2 shape:
+    linear Bz ramp plus a quadrupole gradient) against the oracle time loop."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, capi.FP64, (8, 6, 5), dt=5e-5, c0=2000.0, c2=-50.0, trap_lambda=(1, 1, 1))
+    psi = states.spinor_state(lat, p, states.POLAR, seed=2, noise=1e-2)
+    ramp = capi.make_ramp(bq_segments=[(0.2, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0, 0, 0.5), 0.0, capi.RAMP_CONSTANT), ((0, 0, -0.5), 30 * p.dt, capi.RAMP_LINEAR),
+                                       ((0, 0, -0.5), 1e9, capi.RAMP_CONSTANT)])
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_ODD, psi)
+        s.set_ramp(ramp)
+        s.start()
+        s.step(41)
+        got = s.download(capi.PSI_ODD)
+    po, pe = psi.copy(), np.zeros_like(psi)
+    oracle.parabolic_step(lat, p, oracle.ramp_eval(ramp, 0.0), 0.0, oracle.EULER, pe, po)
+    ref = oracle.leapfrog_run(lat, p, pe, po, 41, ramp=ramp)
+    _close(got, ref, capi.FP64)
+
+
+def test_edge_sizes(gpu):
+    """1x1x1 grid and a long thin grid: halo handling at every face."""
+    lat = capi.Lattice("bcc")
+    for dims in ((1, 1, 1), (17, 1, 2), (1, 9, 1)):
+        p = _params(lat, 3, capi.FP64, dims)
+        even, odd = _rand(lat, p, 81), _rand(lat, p, 82)
+        f = capi.make_fields(**FIELDS)
+        with Stepper(lat, p) as s:
+            s.upload(capi.PSI_EVEN, even)
+            s.upload(capi.PSI_ODD, odd)
+            s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.0)
+            got = s.download(capi.PSI_ODD)
+        oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, odd, even)
+        _close(got, odd, capi.FP64, str(dims))
+        assert np.all(got[0] == 0) and np.all(got[-1] == 0) and np.all(got[:, 0] == 0) and np.all(got[:, :, -1] == 0)
+
+
+def test_nonfinite_is_reported(gpu):
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, capi.FP32, (4, 4, 4))
+    psi = _rand(lat, p, 91)
+    psi[2, 2, 2, 3, 1, 0] = np.nan
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, psi)
+        with pytest.raises(capi.GpeError) as ei:
+            s.observe(capi.PSI_EVEN)
+        assert ei.value.status == 5
+
+
+def test_launch_count(gpu):
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, capi.FP32, (4, 4, 4))
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_ODD, _rand(lat, p, 1))
+        s.start()
+        s.step(10)
+        assert s.launches == 11
