@@ -235,9 +235,8 @@ def run_gpu(args):
     s.stream = C.c_void_p(stream.cuda_stream)
     sites = s.sites
 
-    # the newest state slot after k steps
     def cur_slot():
-        return capi.PSI_EVEN if (s._nsteps % 2 == 0) else capi.PSI_ODD
+        return s.current
 
     s._nsteps = 0
 

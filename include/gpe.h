@@ -238,6 +238,10 @@ typedef struct {
 } gpe_observables;
 gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream);
 
+/* Slot (GPE_PSI_EVEN or GPE_PSI_ODD) holding the newest state after the last
+ * gpe_start / gpe_step / gpe_itp call. */
+int32_t gpe_current_slot(const gpe_handle* h);
+
 /* Number of CUDA kernel launches this handle has issued (for accounting). */
 uint64_t gpe_launch_count(const gpe_handle* h);
 

@@ -288,6 +288,7 @@ def load_library(path: str = LIB_PATH):
         "gpe_itp": (C.c_int, [vp, C.c_int32, P(C.c_double), vp]),
         "gpe_observe": (C.c_int, [vp, C.c_int32, C.c_double, P(Observables), vp]),
         "gpe_launch_count": (C.c_uint64, [vp]),
+        "gpe_current_slot": (C.c_int32, [vp]),
         "gpe_sites": (C.c_uint64, [vp]),
         "gpe_last_error": (C.c_char_p, []),
         "gpe_version": (C.c_char_p, []),

@@ -479,6 +479,31 @@ static gpe_fields fields_at(const gpe_handle* h, double t) {
     return f;
 }
 
+template <typename R>
+static void fill_phys(PhysR<R>& P, const Phys& ph, const gpe_fields& B, double t) {
+    for (int i = 0; i < 3; ++i) {
+        P.p0[i] = (R)ph.p0[i];
+        P.bw[i] = (R)ph.bw[i];
+        P.lambda[i] = (R)ph.lambda[i];
+        P.qc[i] = (R)ph.quad_center[i];
+        P.bb[i] = (R)B.bb[i];
+        P.bbq[i] = (R)B.bb_quad[i];
+    }
+    P.bs = (R)ph.bs;
+    P.trap_offset = (R)ph.trap_offset;
+    P.c0 = (R)ph.c0;
+    P.c2 = (R)ph.c2;
+    P.c4 = (R)ph.c4;
+    P.alpha = (R)ph.alpha;
+    P.sigma = (R)ph.sigma;
+    P.bq = (R)B.bq;
+    P.bqq = (R)B.bq_quad;
+    P.dt = (R)ph.dt;
+    P.dts = ph.sigma > 0 ? (R)(ph.dt / ph.sigma) : (R)0;
+    P.flags = ph.flags;
+    P.trap_on = !((ph.flags & GPE_FLAG_TRAP_OFF_AFTER) && t >= ph.trap_off_time);
+}
+
 static StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t) {
     StepArgs a;
     std::memset(&a, 0, sizeof a);
@@ -513,6 +538,8 @@ static StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t) {
     a.divRowE = make_fastdiv(a.row_items_e ? a.row_items_e : 1);
     a.total = (uint64_t)g.X * g.Y * g.Z * g.V;
     a.partials = h->partials;
+    fill_phys(a.pf, a.ph, B, t);
+    fill_phys(a.pd, a.ph, B, t);
     return a;
 }
 
@@ -722,6 +749,8 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
     }
     return GPE_OK;
 }
+
+extern "C" int32_t gpe_current_slot(const gpe_handle* h) { return h ? h->cur : -1; }
 
 extern "C" uint64_t gpe_launch_count(const gpe_handle* h) { return h ? h->launches : 0; }
 

@@ -88,6 +88,17 @@ struct Phys {
     int flags;
 };
 
+// Physics constants of a step in the arithmetic type of a kernel, prepared on the
+// host so that kernels do no precision conversion (FP64 is slow on GB300).
+template <typename R>
+struct PhysR {
+    R p0[3], bs, bw[3], lambda[3], trap_offset, c0, c2, c4, alpha, sigma, qc[3];
+    R bq, bb[3], bqq, bbq[3];
+    R dt, dts;       // dt and dt/sigma
+    int trap_on;     // trap() is zero after trap_off_time (Spin1GpeBCC.cu:114)
+    int flags;
+};
+
 // Per-handle device tables.  Byte offsets are relative to the base of the
 // thread's own cell in the buffer being read.
 struct DevTables {
@@ -117,6 +128,8 @@ struct StepArgs {
     Phys ph;
     gpe_fields B;
     double t;
+    PhysR<float> pf;
+    PhysR<double> pd;
     FastDiv divV, divRow, divY;   // nodes: within-row node index, X*V per row, rows
     FastDiv divE, divRowE;        // edges: within-row edge index, X*E per row
     uint32_t row_items;   // X*V

@@ -77,38 +77,9 @@ __device__ __forceinline__ void stc(char* p, Cx<R> c) {
 }
 
 template <typename R>
-struct PhysR {
-    R p0[3], bs, bw[3], lambda[3], trap_offset, c0, c2, c4, alpha, sigma, qc[3];
-    R bq, bb[3], bqq, bbq[3];
-    R dt;
-    bool trap_on;
-    int flags;
-};
-
-template <typename R>
-__device__ __forceinline__ PhysR<R> make_phys(const StepArgs& a) {
-    PhysR<R> P;
-    for (int i = 0; i < 3; ++i) {
-        P.p0[i] = (R)a.ph.p0[i];
-        P.bw[i] = (R)a.ph.bw[i];
-        P.lambda[i] = (R)a.ph.lambda[i];
-        P.qc[i] = (R)a.ph.quad_center[i];
-        P.bb[i] = (R)a.B.bb[i];
-        P.bbq[i] = (R)a.B.bb_quad[i];
-    }
-    P.bs = (R)a.ph.bs;
-    P.trap_offset = (R)a.ph.trap_offset;
-    P.c0 = (R)a.ph.c0;
-    P.c2 = (R)a.ph.c2;
-    P.c4 = (R)a.ph.c4;
-    P.alpha = (R)a.ph.alpha;
-    P.sigma = (R)a.ph.sigma;
-    P.bq = (R)a.B.bq;
-    P.bqq = (R)a.B.bq_quad;
-    P.dt = (R)a.ph.dt;
-    P.flags = a.ph.flags;
-    P.trap_on = !((a.ph.flags & GPE_FLAG_TRAP_OFF_AFTER) && a.t >= a.ph.trap_off_time);
-    return P;
+__device__ __forceinline__ const PhysR<R>& make_phys(const StepArgs& a) {
+    if constexpr (sizeof(R) == 4) return a.pf;
+    else return a.pd;
 }
 
 // trap (Spin1GpeBCC.cu:112-122)
@@ -338,7 +309,7 @@ __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
 #pragma unroll
         for (int s = 0; s < C; ++s) H[s] += w * (ldc<R>(nb + s * 2 * sizeof(R)) - prv[s]);
     }
-    const PhysR<R> P = make_phys<R>(a);
+    const PhysR<R>& P = make_phys<R>(a);
     R r[3];
     r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
     r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + st.pos[3 * l + 1]);
@@ -376,7 +347,7 @@ __device__ __forceinline__ void q_update(const StepArgs& a, const SmemHyper<R>& 
     const uint32_t edge_bytes = C * 2 * sizeof(R);
     const char* qprev = a.q + qcell_off + e * edge_bytes;
     char* qnext = a.qnext + qcell_off + e * edge_bytes;
-    const R dts = (R)(a.ph.dt / a.ph.sigma);
+    const R dts = make_phys<R>(a).dts;
 #pragma unroll
     for (int s = 0; s < C; ++s) {
         const Cx<R> d0psi = ldc<R>(otherp + s * 2 * sizeof(R)) - ldc<R>(thisp + s * 2 * sizeof(R));
@@ -436,7 +407,7 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
     if (DO_PSI && sub == 0) {
         const uint32_t i = group * blockDim.x + threadIdx.x;
         if (i >= node_items) return;
-        const PhysR<R> P = make_phys<R>(a);
+        const PhysR<R>& P = make_phys<R>(a);
         const uint32_t node_bytes = C * 2 * sizeof(R);
         const uint32_t row = fdiv(i, a.divRow);
         const uint32_t within = i - row * a.row_items;
@@ -550,7 +521,7 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
                 L[s] += st.w[f] * (cx<double>((double)v.x, (double)v.y) - ps[s]);
             }
         }
-        PhysR<double> P = make_phys<double>(a);
+        const PhysR<double>& P = make_phys<double>(a);
         double r[3];
         r[0] = P.p0[0] + P.bs * ((double)x * P.bw[0] + st.pos[3 * l + 0]);
         r[1] = P.p0[1] + P.bs * ((double)y * P.bw[1] + st.pos[3 * l + 1]);

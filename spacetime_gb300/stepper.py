@@ -96,6 +96,11 @@ class Stepper:
         return o.as_dict()
 
     @property
+    def current(self) -> int:
+        """Slot holding the newest state."""
+        return int(self.lib.gpe_current_slot(self._h))
+
+    @property
     def launches(self) -> int:
         return int(self.lib.gpe_launch_count(self._h))
 

@@ -197,8 +197,9 @@ def test_imaginary_time(gpu, prec):
     with Stepper(lat, p) as s:
         s.upload(capi.PSI_ODD, psi)
         mu = s.itp(4)
-        got = s.download(capi.PSI_EVEN)
-        obs = s.observe(capi.PSI_EVEN)
+        assert s.current == capi.PSI_ODD  # 4 iterations from PSI_ODD end in PSI_ODD
+        got = s.download(s.current)
+        obs = s.observe(s.current)
     cur = psi.copy()
     hp = np.zeros_like(psi)
     for _ in range(4):
@@ -268,6 +269,8 @@ def test_launch_count(gpu):
     p = _params(lat, 3, capi.FP32, (4, 4, 4))
     with Stepper(lat, p) as s:
         s.upload(capi.PSI_ODD, _rand(lat, p, 1))
+        n0 = s.launches
         s.start()
         s.step(10)
-        assert s.launches == 11
+        assert s.launches - n0 == 11
+        assert s.current == capi.PSI_EVEN
