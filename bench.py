@@ -244,6 +244,11 @@ def run_gpu(args):
         s.step(INNER)
         s._nsteps += INNER
 
+    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_step_kernel<float,3,LEAPFROG>"}
+    if args.kernel:
+        s.set_tuning(capi.TUNE_KERNEL, args.kernel)
+    chosen = s.get_tuning(capi.TUNE_KERNEL)
+    tile = s.get_tuning(capi.TUNE_TILE_CELLS)
     with torch.cuda.stream(stream):
         s.upload(capi.PSI_ODD, psi0)
         s.set_ramp(ramp, 0.0)
@@ -337,7 +342,7 @@ def run_gpu(args):
         "parallelism": "replicas" if world > 1 else "single",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "parabolic_step_kernel<float,3,LEAPFROG>", "algorithmic_bytes_per_launch": algo_bytes,
+                     "kernel": kernel_name[chosen], "tile_cells": tile, "algorithmic_bytes_per_launch": algo_bytes,
                      "avg_launch_ms": launch_ms},
         "e2e": {"value": e2e_value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
                 "d2h_bytes_per_step": 8 * 12, "steps": e2e_steps,
@@ -408,6 +413,7 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 gather kernel, 2 row-tile kernel")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -238,6 +238,15 @@ typedef struct {
 } gpe_observables;
 gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream);
 
+/* Kernel selection and tile shape (the autotuner's knobs).
+ * GPE_TUNE_KERNEL: 0 = automatic, 1 = one-node-per-thread gather kernel,
+ *                  2 = row-tile kernel (TMA bulk copies of a row of cells into shared
+ *                      memory; needs a cell size that is a multiple of 16 bytes).
+ * GPE_TUNE_TILE_CELLS: cells per row tile (0 = automatic). */
+enum { GPE_TUNE_KERNEL = 0, GPE_TUNE_TILE_CELLS = 1 };
+gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value);
+gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);
+
 /* Slot (GPE_PSI_EVEN or GPE_PSI_ODD) holding the newest state after the last
  * gpe_start / gpe_step / gpe_itp call. */
 int32_t gpe_current_slot(const gpe_handle* h);

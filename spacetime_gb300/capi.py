@@ -35,6 +35,8 @@ RAMP_CONSTANT, RAMP_LINEAR, RAMP_SQRT = 0, 1, 2
 RAMP_MAX_SEGMENTS = 32
 PSI_EVEN, PSI_ODD, Q_EVEN, Q_ODD, HPSI = 0, 1, 2, 3, 4
 MODE_LEAPFROG, MODE_EULER, MODE_ITP = 0, 1, 2
+TUNE_KERNEL, TUNE_TILE_CELLS = 0, 1
+KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE = 0, 1, 2
 
 
 class StencilEntry(C.Structure):
@@ -289,6 +291,8 @@ def load_library(path: str = LIB_PATH):
         "gpe_observe": (C.c_int, [vp, C.c_int32, C.c_double, P(Observables), vp]),
         "gpe_launch_count": (C.c_uint64, [vp]),
         "gpe_current_slot": (C.c_int32, [vp]),
+        "gpe_set_tuning": (C.c_int, [vp, C.c_int32, C.c_int32]),
+        "gpe_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
         "gpe_sites": (C.c_uint64, [vp]),
         "gpe_last_error": (C.c_char_p, []),
         "gpe_version": (C.c_char_p, []),

@@ -19,6 +19,8 @@ cudaError_t launch_observe(const StepArgs& a, double* out, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s);
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, cudaStream_t s);
 cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
                             uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
 enum HyperKind {
@@ -86,6 +88,9 @@ struct gpe_handle {
     int cur = 0;          // psi slot holding the newest state
     uint64_t nstep = 0;   // leapfrog steps since gpe_start / gpe_set_ramp
     uint64_t launches = 0;
+    int* err = nullptr;    // device error flag
+    int tune_kernel = 0;   // GPE_TUNE_KERNEL
+    int tune_tile = 0;     // GPE_TUNE_TILE_CELLS
 };
 
 extern "C" const char* gpe_last_error(void) { return g_last_error.c_str(); }
@@ -231,6 +236,7 @@ static void release(gpe_handle* h) {
     if (h->partials) cudaFree(h->partials);
     if (h->obs_out) cudaFree(h->obs_out);
     if (h->stage) cudaFree(h->stage);
+    if (h->err) cudaFree(h->err);
 }
 
 static gpe_status build_tables(gpe_handle* h) {
@@ -239,7 +245,7 @@ static gpe_status build_tables(gpe_handle* h) {
     const double bs2 = h->p.block_scale * h->p.block_scale;
     const size_t node_bytes = (size_t)g.C * 2 * h->real_bytes;
     const int n = (int)L.stencil.size();
-    std::vector<int32_t> nb_off(n);
+    std::vector<int32_t> nb_off(n), nb_soff(n);
     std::vector<double> w64(n);
     std::vector<float> w32(n);
     for (int f = 0; f < n; ++f) {
@@ -248,6 +254,9 @@ static gpe_status build_tables(gpe_handle* h) {
                               (long long)e.dx * g.cell_bytes + (long long)e.node * node_bytes;
         if (off > INT32_MAX || off < INT32_MIN) return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
         nb_off[f] = (int32_t)off;
+        // offset inside a contiguous row of cells (row-tile kernel), or off-row marker
+        nb_soff[f] = (e.dy == 0 && e.dz == 0) ? (int32_t)((long long)e.dx * g.cell_bytes + (long long)e.node * node_bytes)
+                                              : INT32_MIN;
         w64[f] = (-0.5 * e.hodge) / bs2;  // hodges[i] = -0.5*hodges[i]; hodge/(bs*bs) (Spin1GpeBCC.cu:1169, :859)
         w32[f] = (float)w64[f];
     }
@@ -256,6 +265,7 @@ static gpe_status build_tables(gpe_handle* h) {
     gpe_status st;
     if ((st = upload_table(h, L.row_ptr, &h->tab.row_ptr))) return st;
     if ((st = upload_table(h, nb_off, &h->tab.nb_off))) return st;
+    if ((st = upload_table(h, nb_soff, &h->tab.nb_soff))) return st;
     if ((st = upload_table(h, w64, &h->tab.w64))) return st;
     if ((st = upload_table(h, w32, &h->tab.w32))) return st;
     if ((st = upload_table(h, pos64, &h->tab.pos64))) return st;
@@ -357,7 +367,8 @@ extern "C" gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* p, gp
     }
     h->partial_blocks = (sites + 255) / 256;
     if (cudaMalloc(&h->partials, h->partial_blocks * OBS_COUNT * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&h->obs_out, OBS_COUNT * sizeof(double)) != cudaSuccess) {
+        cudaMalloc(&h->obs_out, OBS_COUNT * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&h->err, sizeof(int)) != cudaSuccess || cudaMemset(h->err, 0, sizeof(int)) != cudaSuccess) {
         release(h);
         delete h;
         return fail(GPE_ERR_OOM, "cudaMalloc of reduction scratch failed");
@@ -408,6 +419,18 @@ static size_t host_count(const gpe_handle* h, bool is_q) {
     return (size_t)(g.X + 2) * (g.Y + 2) * (g.Z + 2) * (is_q ? g.E : g.V) * g.C * 2;
 }
 
+// A bounded device wait that ran out sets the handle's error flag; surface it.
+static gpe_status check_device_error(gpe_handle* h, cudaStream_t s) {
+    int flag = 0;
+    CUDA_TRY(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    if (flag) {
+        cudaMemsetAsync(h->err, 0, sizeof(int), s);
+        return fail(GPE_ERR_TIMEOUT, "a bounded device wait ran out (bulk copy did not complete)");
+    }
+    return GPE_OK;
+}
+
 static gpe_status ensure_stage(gpe_handle* h, size_t count) {
     if (h->stage_count >= count) return GPE_OK;
     if (h->stage) cudaFree(h->stage);
@@ -445,7 +468,7 @@ static gpe_status transfer(gpe_handle* h, int32_t slot, double* host, size_t cou
     h->launches += 1;
     if (!up) CUDA_TRY(cudaMemcpyAsync(host, h->stage, count * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    return GPE_OK;
+    return up ? GPE_OK : check_device_error(h, s);
 }
 
 extern "C" gpe_status gpe_upload(gpe_handle* h, int32_t slot, const double* host, size_t count, void* stream) {
@@ -538,6 +561,7 @@ static StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t) {
     a.divRowE = make_fastdiv(a.row_items_e ? a.row_items_e : 1);
     a.total = (uint64_t)g.X * g.Y * g.Z * g.V;
     a.partials = h->partials;
+    a.err = h->err;
     fill_phys(a.pf, a.ph, B, t);
     fill_phys(a.pd, a.ph, B, t);
     return a;
@@ -588,6 +612,33 @@ static cudaError_t dispatch_scale(const gpe_handle* h, const StepArgs& a, const 
     }
 }
 
+// Row-tile kernel eligibility and tile length (0 = use the gather kernel).
+static uint32_t tile_cells(const gpe_handle* h) {
+    if (h->tune_kernel == 1) return 0;
+    if (h->g.cell_bytes % 16 != 0) return 0;
+    const uint32_t V = h->g.V, X = h->g.X;
+    uint32_t tmax = 256 / V;
+    if (tmax == 0) tmax = 1;
+    if (V * tmax > 1024) return 0;
+    if (h->tune_tile > 0) return (uint32_t)h->tune_tile <= X && (uint32_t)h->tune_tile * V <= 1024 ? (uint32_t)h->tune_tile : 0;
+    if (tmax >= X) return X;
+    for (uint32_t t = tmax; t * 2 > tmax; --t)
+        if (X % t == 0) return t;
+    return tmax;
+}
+
+template <int C>
+static cudaError_t dispatch_tile_c(const gpe_handle* h, const StepArgs& a, uint32_t T, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_leapfrog_tile<double, C>(a, T, s) : launch_leapfrog_tile<float, C>(a, T, s);
+}
+static cudaError_t dispatch_tile(const gpe_handle* h, const StepArgs& a, uint32_t T, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_tile_c<1>(h, a, T, s);
+        case 3: return dispatch_tile_c<3>(h, a, T, s);
+        default: return dispatch_tile_c<5>(h, a, T, s);
+    }
+}
+
 static double cell_dv(const gpe_handle* h) {
     const double bs = h->p.block_scale;
     return bs * bs * bs * h->lat.volume;  // volume = bs^3 * VOLUME (Spin1GpeBCC.cu:1385)
@@ -601,7 +652,9 @@ static gpe_status one_step(gpe_handle* h, int next, int prev, const gpe_fields& 
     cudaError_t e;
     if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
         a.hpsi = mode == GPE_MODE_ITP ? h->interior[GPE_HPSI] : nullptr;
-        e = dispatch_parabolic(h, a, mode, s);
+        const uint32_t T = tile_cells(h);
+        if (mode == GPE_MODE_LEAPFROG && T > 0) e = dispatch_tile(h, a, T, s);
+        else e = dispatch_parabolic(h, a, mode, s);
         h->launches += 1;
     } else {
         if (mode != GPE_MODE_LEAPFROG) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme: explicit steps are leapfrog only");
@@ -692,6 +745,8 @@ extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_obs
     double r[OBS_COUNT];
     CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
+    gpe_status dst = check_device_error(h, s);
+    if (dst) return dst;
     const double dv = cell_dv(h);
     std::memset(out, 0, sizeof *out);
     out->norm = r[OBS_NORM] * dv;
@@ -747,6 +802,31 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
         CUDA_TRY(cudaStreamSynchronize(s));
         *mu_out = r[OBS_NORM] * dv;
     }
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (key == GPE_TUNE_KERNEL) {
+        if (value < 0 || value > 2) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
+        if (value == 2 && h->g.cell_bytes % 16 != 0) return fail(GPE_ERR_UNSUPPORTED, "row tiles need 16-byte cells");
+        h->tune_kernel = value;
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_TILE_CELLS) {
+        if (value < 0 || (uint32_t)value > h->g.X || (uint64_t)value * h->g.V > 1024)
+            return fail(GPE_ERR_INVALID_ARG, "tile length");
+        h->tune_tile = value;
+        return GPE_OK;
+    }
+    return fail(GPE_ERR_INVALID_ARG, "unknown tuning key");
+}
+
+extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value) {
+    if (!h || !value) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (key == GPE_TUNE_KERNEL) *value = tile_cells(h) > 0 ? 2 : 1;
+    else if (key == GPE_TUNE_TILE_CELLS) *value = (int32_t)tile_cells(h);
+    else return fail(GPE_ERR_INVALID_ARG, "unknown tuning key");
     return GPE_OK;
 }
 

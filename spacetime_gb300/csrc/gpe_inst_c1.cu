@@ -5,6 +5,8 @@
 namespace gpe {
 GPE_INSTANTIATE(float, 1)
 GPE_INSTANTIATE(double, 1)
+GPE_INSTANTIATE_TILE(float, 1)
+GPE_INSTANTIATE_TILE(double, 1)
 
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s) {
     if (precision == GPE_FP64) {

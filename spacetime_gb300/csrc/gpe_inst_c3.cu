@@ -5,4 +5,6 @@
 namespace gpe {
 GPE_INSTANTIATE(float, 3)
 GPE_INSTANTIATE(double, 3)
+GPE_INSTANTIATE_TILE(float, 3)
+GPE_INSTANTIATE_TILE(double, 3)
 }  // namespace gpe

@@ -5,4 +5,6 @@
 namespace gpe {
 GPE_INSTANTIATE(float, 5)
 GPE_INSTANTIATE(double, 5)
+GPE_INSTANTIATE_TILE(float, 5)
+GPE_INSTANTIATE_TILE(double, 5)
 }  // namespace gpe

@@ -104,6 +104,7 @@ struct PhysR {
 struct DevTables {
     int32_t* row_ptr;     // V+1
     int32_t* nb_off;      // entries: byte offset of the neighbour value in prev
+    int32_t* nb_soff;     // entries: offset inside a contiguous row of cells, INT32_MIN if the neighbour is off-row
     double* w64;          // entries: (-0.5*h)/bs^2
     float* w32;
     double* pos64;        // V*3
@@ -136,6 +137,7 @@ struct StepArgs {
     uint32_t row_items_e; // X*E
     uint64_t total;       // total threads of work
     double* partials;     // observables
+    int* err;             // device error flag (bounded waits that ran out)
 };
 
 }  // namespace gpe

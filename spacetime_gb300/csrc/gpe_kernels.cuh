@@ -26,6 +26,17 @@ struct Cx {
 };
 
 template <typename R>
+struct Vec2;
+template <>
+struct Vec2<float> {
+    using type = float2;
+};
+template <>
+struct Vec2<double> {
+    using type = double2;
+};
+
+template <typename R>
 __device__ __forceinline__ Cx<R> cx(R x, R y) {
     Cx<R> c;
     c.x = x;
@@ -805,5 +816,194 @@ cudaError_t launch_pack(double* packed, char* dev_base, uint32_t X, uint32_t Y, 
     else pack_kernel<R, false><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total);
     return cudaGetLastError();
 }
+
+}  // namespace gpe
+
+namespace gpe {
+
+// ---------------------------------------------------------- TMA row tiles
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// 1-D bulk copy global -> shared completing on an mbarrier (addresses 16-byte
+// aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+
+// Bounded wait on an mbarrier phase; every thread of the block gets the same
+// answer (false only if the copies did not land within the limit).
+__device__ __forceinline__ bool block_wait(uint64_t* bar, uint32_t parity, int* err) {
+    bool ok = false;
+    for (uint32_t spin = 0; spin < (1u << 22) && !(ok = mbar_try_wait(bar, parity)); ++spin) {
+    }
+    ok = __syncthreads_and(ok) != 0;
+    if (!ok && threadIdx.x == 0 && err) atomicExch(err, 1);
+    return ok;
+}
+
+// Leapfrog step on a row tile of T cells (BCC spin-1 FP32: T = 16 cells,
+// 192 nodes, one thread per node).  The previous state of cells [x0-1, x0+T]
+// (the x halo included) and the old next state of [x0, x0+T) are brought into
+// shared memory by two bulk copies; in-row neighbours (dy = dz = 0) are read
+// from shared memory, off-row neighbours from global memory (L2); the updated
+// tile goes back with one bulk store.  Requires cell_bytes % 16 == 0.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) leapfrog_tile_kernel(StepArgs a, uint32_t T, uint32_t tiles_per_row) {
+    extern __shared__ __align__(128) unsigned char dyn[];
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t cb = a.g.cell_bytes;
+    const int V = a.g.V, n = a.tab.entries;
+    char* s_prev = reinterpret_cast<char*>(dyn);
+    char* s_next = s_prev + (size_t)(T + 2) * cb;
+    int32_t* s_goff = reinterpret_cast<int32_t*>(s_next + (size_t)T * cb);
+    int32_t* s_soff = s_goff + n;
+    R* s_w = reinterpret_cast<R*>(s_soff + n);
+    R* s_pos = s_w + n;
+    int32_t* s_row = reinterpret_cast<int32_t*>(s_pos + 3 * V);
+
+    const uint32_t tile = blockIdx.x % tiles_per_row;
+    const uint32_t row = blockIdx.x / tiles_per_row;
+    const uint32_t z = fdiv(row, a.divY);
+    const uint32_t y = row - z * a.g.Y;
+    const uint32_t x0 = tile * T;
+    const uint32_t Tc = min(T, a.g.X - x0);
+    const size_t row_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch;
+    const char* g_prev = a.prev + row_off + (size_t)x0 * cb - cb;  // cell x0 - 1 (halo at x0 = 0)
+    char* g_next = a.next + row_off + (size_t)x0 * cb;
+    const uint32_t bytes_prev = (Tc + 2) * cb, bytes_next = Tc * cb;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, bytes_prev + bytes_next);
+        bulk_load(s_prev, g_prev, bytes_prev, &bar);
+        bulk_load(s_next, g_next, bytes_next, &bar);
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        s_goff[i] = a.tab.nb_off[i];
+        s_soff[i] = a.tab.nb_soff[i];
+        if constexpr (sizeof(R) == 4) s_w[i] = a.tab.w32[i];
+        else s_w[i] = a.tab.w64[i];
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) s_pos[i] = a.tab.pos32[i];
+        else s_pos[i] = a.tab.pos64[i];
+    }
+    for (int i = threadIdx.x; i <= V; i += blockDim.x) s_row[i] = a.tab.row_ptr[i];
+    if (!block_wait(&bar, 0, a.err)) return;  // uniform across the block
+
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    const uint32_t i = threadIdx.x;
+    if (i < Tc * V) {
+        using V2 = typename Vec2<R>::type;
+        const uint32_t xl = fdiv(i, a.divV);
+        const uint32_t l = i - xl * V;
+        const char* s_own = s_prev + (size_t)(xl + 1) * cb + l * node_bytes;
+        const char* g_cell = g_prev + (size_t)(xl + 1) * cb;
+        Cx<R> prv[C], H[C];
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            const V2 v = reinterpret_cast<const V2*>(s_own)[s];
+            prv[s] = cx<R>(v.x, v.y);
+            H[s] = cx<R>((R)0, (R)0);
+        }
+        const char* s_cell = s_own - l * node_bytes;
+        const int f0 = s_row[l], f1 = s_row[l + 1];
+        for (int f = f0; f < f1; ++f) {
+            const int32_t so = s_soff[f];
+            const R w = s_w[f];
+            if (so != INT32_MIN) {
+                // in-row neighbour: shared memory (8- or 16-byte accesses)
+                const V2* p = reinterpret_cast<const V2*>(s_cell + so);
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const V2 v = p[c];
+                    H[c] += w * (cx<R>(v.x, v.y) - prv[c]);
+                }
+            } else {
+                // off-row neighbour: read-only global path (L2)
+                const char* g = g_cell + s_goff[f];
+#pragma unroll
+                for (int c = 0; c < C; ++c) H[c] += w * (ldc<R>(g + c * 2 * sizeof(R)) - prv[c]);
+            }
+        }
+        const PhysR<R>& P = make_phys<R>(a);
+        const uint32_t x = x0 + xl;
+        R r[3];
+        r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + s_pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + s_pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + s_pos[3 * l + 2]);
+        const R pot = trap<R>(P, r);
+        local_terms<R, C>(P, r, pot, GPE_MODE_LEAPFROG, false, prv, H);
+        V2* q = reinterpret_cast<V2*>(s_next + (size_t)xl * cb + l * node_bytes);
+        const R dt2 = (R)2 * P.dt;
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            V2 v = q[c];
+            v.x += dt2 * H[c].y;
+            v.y += dt2 * -H[c].x;
+            q[c] = v;
+        }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bulk_store(g_next, s_next, bytes_next);
+        bulk_commit();
+        bulk_wait_read_all();
+    }
+}
+
+template <typename R, int C>
+size_t tile_smem_bytes(const StepArgs& a, uint32_t T) {
+    return (size_t)(2 * T + 2) * a.g.cell_bytes + (size_t)a.tab.entries * (8 + sizeof(R)) + 3 * a.g.V * sizeof(R) +
+           (a.g.V + 1) * 4;
+}
+
+template <typename R, int C>
+cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
+    const uint32_t tiles = (a.g.X + T - 1) / T;
+    const uint32_t threads = ((T * a.g.V + 31) / 32) * 32;
+    const size_t smem = tile_smem_bytes<R, C>(a, T);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(leapfrog_tile_kernel<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        configured = true;
+    }
+    const uint64_t blocks = (uint64_t)tiles * a.g.Y * a.g.Z;
+    leapfrog_tile_kernel<R, C><<<(unsigned)blocks, threads, smem, s>>>(a, T, tiles);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE_TILE(R, C) template cudaError_t launch_leapfrog_tile<R, C>(const StepArgs&, uint32_t, cudaStream_t);
 
 }  // namespace gpe

@@ -95,6 +95,14 @@ class Stepper:
         capi.check(self.lib.gpe_observe(self._h, slot, t, C.byref(o), self.stream), "gpe_observe")
         return o.as_dict()
 
+    def set_tuning(self, key: int, value: int):
+        capi.check(self.lib.gpe_set_tuning(self._h, key, value), "gpe_set_tuning")
+
+    def get_tuning(self, key: int) -> int:
+        v = C.c_int32()
+        capi.check(self.lib.gpe_get_tuning(self._h, key, C.byref(v)), "gpe_get_tuning")
+        return v.value
+
     @property
     def current(self) -> int:
         """Slot holding the newest state."""

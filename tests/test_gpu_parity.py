@@ -44,17 +44,20 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("kernel", [capi.KERNEL_GATHER, capi.KERNEL_AUTO])
 @pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
 @pytest.mark.parametrize("name,C", CASES)
-def test_parabolic_leapfrog(gpu, name, C, prec):
+def test_parabolic_leapfrog(gpu, name, C, prec, kernel):
     """leapfrog (Spin1GpeBCC.cu:793-917 / Spin2GpeBCC.cu:845-990 / BCC.cu:327-347),
-    3 steps with external fields, ragged grid."""
+    3 steps with external fields, ragged grid; both the gather kernel and the
+    automatic choice (the TMA row-tile kernel wherever cells are 16-byte multiples)."""
     lat = capi.Lattice(name)
     dims = (5, 3, 4) if lat.nodes > 40 else (7, 5, 4)
     p = _params(lat, C, prec, dims)
     even, odd = _rand(lat, p, 11), _rand(lat, p, 12)
     f = capi.make_fields(**FIELDS)
     with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_KERNEL, kernel)
         s.upload(capi.PSI_EVEN, even)
         s.upload(capi.PSI_ODD, odd)
         bufs = [capi.PSI_EVEN, capi.PSI_ODD]
@@ -274,3 +277,37 @@ def test_launch_count(gpu):
         s.step(10)
         assert s.launches - n0 == 11
         assert s.current == capi.PSI_EVEN
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C,tile", [("bcc", 3, 5), ("bcc", 3, 16), ("bcc", 1, 3), ("bcc", 5, 7), ("fcc", 3, 4),
+                                         ("a15", 1, 2), ("z", 3, 1), ("c15", 5, 1)])
+def test_tile_kernel_tile_lengths(gpu, name, C, tile, prec):
+    """Row-tile kernel with tile lengths that do not divide X (partial last tile)."""
+    lat = capi.Lattice(name)
+    X = 17 if lat.nodes < 40 else 5
+    p = _params(lat, C, prec, (X, 3, 2))
+    even, odd = _rand(lat, p, 101), _rand(lat, p, 102)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_TILE)
+        s.set_tuning(capi.TUNE_TILE_CELLS, min(tile, X))
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_TILE
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.0)
+        s.step_explicit(capi.PSI_EVEN, capi.PSI_ODD, f, t=0.1)
+        ge, go = s.download(capi.PSI_EVEN), s.download(capi.PSI_ODD)
+    oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, odd, even)
+    oracle.parabolic_step(lat, p, f, 0.1, oracle.LEAPFROG, even, odd)
+    _close(ge, even, prec, "even")
+    _close(go, odd, prec, "odd")
+
+
+def test_tile_kernel_rejected_for_unaligned_cells(gpu):
+    lat = capi.Lattice("cube")  # 1 node: 24-byte FP32 spin-1 cells
+    p = _params(lat, 3, capi.FP32, (4, 4, 4))
+    with Stepper(lat, p) as s:
+        with pytest.raises(capi.GpeError):
+            s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_TILE)
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER
