@@ -251,6 +251,26 @@ gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);
  * gpe_start / gpe_step / gpe_itp call. */
 int32_t gpe_current_slot(const gpe_handle* h);
 
+/* Observables of a caller-owned psi buffer with no device allocation at all.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory at the point where they want the norm, energy and magnetisation of
+ * their state: memory owned by another framework's pool, or a time loop that
+ * laid out all its buffers up front and must keep a fixed footprint.  No
+ * handle is needed: psi is the interior cell (0,0,0) of a pitched buffer in the
+ * reference layout (halo zero), in p->precision, and the results are the same
+ * quantities gpe_observe computes.  The reduction scratch is one fixed-size
+ * device array inside the library (2049 x 12 doubles, about 197 KB per GPU that
+ * loads the library, held until the process exits); lattices larger than
+ * 160 nodes / 640 stencil entries per cell and grids of 2^32 sites or more are
+ * rejected with GPE_ERR_INVALID_ARG.  The first call on each device looks up
+ * the scratch array's device address with that device current; make that first
+ * call before any stream capture.  Calls share the scratch: calls that overlap on
+ * the GPU race, so order them on one stream.  Synchronises `stream`; errors are
+ * reported through gpe_last_error(). */
+gpe_status gpe_observe_noalloc(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_fields* fields,
+                               double t, const void* psi, size_t pitch, size_t slice_pitch,
+                               gpe_observables* out, void* stream);
+
 /* Number of CUDA kernel launches this handle has issued (for accounting). */
 uint64_t gpe_launch_count(const gpe_handle* h);
 

@@ -292,6 +292,7 @@ def load_library(path: str = LIB_PATH):
         "gpe_launch_count": (C.c_uint64, [vp]),
         "gpe_current_slot": (C.c_int32, [vp]),
         "gpe_set_tuning": (C.c_int, [vp, C.c_int32, C.c_int32]),
+        "gpe_observe_noalloc": (C.c_int, [P(LatticeDesc), P(Params), P(Fields), C.c_double, vp, C.c_size_t, C.c_size_t, P(Observables), vp]),
         "gpe_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
         "gpe_sites": (C.c_uint64, [vp]),
         "gpe_last_error": (C.c_char_p, []),

@@ -94,6 +94,8 @@ struct gpe_handle {
 };
 
 extern "C" const char* gpe_last_error(void) { return g_last_error.c_str(); }
+
+void gpe::set_last_error(const std::string& msg) { g_last_error = msg; }
 extern "C" const char* gpe_version(void) { return "libgpe 0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------------ lattices

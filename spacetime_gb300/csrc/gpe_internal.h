@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "../../include/gpe.h"
@@ -139,5 +140,8 @@ struct StepArgs {
     double* partials;     // observables
     int* err;             // device error flag (bounded waits that ran out)
 };
+
+// Sets the text returned by gpe_last_error() for this thread (gpe_capi.cu).
+void set_last_error(const std::string& msg);
 
 }  // namespace gpe
