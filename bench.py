@@ -38,6 +38,19 @@ RAMP_STEPS = 4000
 BYTES_PER_SITE_FP32 = 72    # read psi_prev (24 B) + read/write psi_next (48 B), spin-1 FP32
 BYTES_PER_SITE_FP64 = 144
 
+# Optional legs (--workload): the other configurations of the benchmark plan.
+#  scalar-bcc32: scalar GPE, BCC 32^3 cells, box [-8,8]^3, g = 2000, TF vortex + 1e-3 noise, dt = 1e-4
+#  spin2-c15-128: relativistic spin-2, C15 128^3 cells (285,212,672 sites), hyperbolic psi+q,
+#                 c0 = 2000, c2 = -20, c4 = 40, cyclic spinor + 1e-3 noise, sigma = 0.00225, dt = 2e-5
+LEGS = {
+    "scalar-bcc32": dict(lattice="bcc", C=1, dims=(32, 32, 32), c0=2000.0, c2=0.0, c4=0.0, dt=1e-4, scheme=0,
+                         sigma=0.0, zeta=(1.0,), kappa=1, noise_abs=1e-3, noise_rel=0.0, bytes_fp32=24, seed=1),
+    "spin2-c15-128": dict(lattice="c15", C=5, dims=(128, 128, 128), c0=2000.0, c2=-20.0, c4=40.0, dt=2e-5, scheme=1,
+                          sigma=0.00225, zeta=(math.sqrt(1 / 3), 0, 0, math.sqrt(2 / 3), 0), kappa=0, noise_abs=0.0,
+                          noise_rel=1e-3, bytes_fp32=360, seed=3),
+}
+LEGS["spin2-c15-48"] = dict(LEGS["spin2-c15-128"], dims=(48, 48, 48))   # small case for profiling
+
 
 def workload(precision):
     from spacetime_gb300 import capi, states
@@ -51,6 +64,70 @@ def workload(precision):
                                        ((0, 0, -0.5), 1e30, capi.RAMP_CONSTANT)])
     psi0 = states.spinor_state(lat, p, states.POLAR, seed=2, noise=1e-3)
     return lat, p, ramp, psi0
+
+
+def run_leg(args):
+    """An optional configuration: device-side initial state, start, `steps` x 100
+    steps timed with CUDA events, FP64 observables per bench step."""
+    import ctypes as C
+
+    import torch
+
+    from spacetime_gb300 import capi
+    from spacetime_gb300.stepper import Stepper
+
+    w = LEGS[args.workload]
+    lat = capi.Lattice(w["lattice"])
+    bs = BOX / (w["dims"][0] * lat.block_width[0])
+    p = capi.make_params(components=w["C"], scheme=w["scheme"], precision=capi.FP32, dims=w["dims"], block_scale=bs,
+                         dt=w["dt"], trap_offset=100.0, c0=w["c0"], c2=w["c2"], c4=w["c4"], sigma=w["sigma"], lattice=lat)
+    stream = torch.cuda.Stream()
+    s = Stepper(lat, p)
+    s.stream = C.c_void_p(stream.cuda_stream)
+    inner = args.inner or INNER
+    with torch.cuda.stream(stream):
+        s.init_state(capi.PSI_ODD, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
+                                                  noise_rel=w["noise_rel"], seed=w["seed"]))
+        s.start()
+        e0 = s.observe(s.current, 0.0)
+        for _ in range(args.warmup):
+            s.step(inner)
+        torch.cuda.synchronize()
+        n0 = s.launches
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        obs = []
+        with ClockSampler(0) as clk:
+            a.record(stream)
+            step_ms = 0.0
+            for _ in range(args.steps):
+                x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                x.record(stream)
+                s.step(inner)
+                y.record(stream)
+                obs.append(s.observe(s.current))
+                step_ms += x.elapsed_time(y)
+            b.record(stream)
+            torch.cuda.synchronize()
+        total_ms = a.elapsed_time(b)
+        launches = s.launches - n0
+    sites = s.sites
+    launch_ms = step_ms / (inner * args.steps)
+    algo = w["bytes_fp32"] * sites
+    peak, kind = measured_peak()
+    name = "hyper_step_kernel<float,%d,fused>" % w["C"] if w["scheme"] else "leapfrog kernel (auto) C=%d" % w["C"]
+    res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
+           "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic", "config": dict(w, workload=args.workload, sites=sites, inner_steps_per_step=inner),
+           "roofline": {"bound": "hbm", "achieved": algo / (launch_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": algo / (launch_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": name,
+                        "algorithmic_bytes_per_launch": algo, "avg_launch_ms": launch_ms, "traffic": None},
+           "gpu_launches": launches, "clocks": clk.summary(),
+           "energy_rel_drift": abs(obs[-1]["energy"] - e0["energy"]) / abs(e0["energy"]) if obs else None,
+           "norm_last": obs[-1]["norm"] if obs else None}
+    s.close()
+    print(json.dumps(res))
+    return 0
 
 
 def config_dict():
@@ -244,11 +321,20 @@ def run_gpu(args):
         s.step(INNER)
         s._nsteps += INNER
 
-    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_step_kernel<float,3,LEAPFROG>"}
+    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_step_kernel<float,3,LEAPFROG>",
+                   capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
+    for key, val in ((capi.TUNE_TILE_CELLS, args.tile), (capi.TUNE_TILE_ROWS, args.rows), (capi.TUNE_ZCHUNK, args.zchunk),
+                     (capi.TUNE_THREADS, args.threads)):
+        if val:
+            s.set_tuning(key, val)
+    tuning_report = None
+    if args.autotune:
+        with torch.cuda.stream(stream):
+            tuning_report = s.autotune(steps=10)
     chosen = s.get_tuning(capi.TUNE_KERNEL)
-    tile = s.get_tuning(capi.TUNE_TILE_CELLS)
+    tile = [s.get_tuning(capi.TUNE_TILE_CELLS), s.get_tuning(capi.TUNE_TILE_ROWS), s.get_tuning(capi.TUNE_ZCHUNK)]
     with torch.cuda.stream(stream):
         s.upload(capi.PSI_ODD, psi0)
         s.set_ramp(ramp, 0.0)
@@ -342,7 +428,7 @@ def run_gpu(args):
         "parallelism": "replicas" if world > 1 else "single",
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": kernel_name[chosen], "tile_cells": tile, "algorithmic_bytes_per_launch": algo_bytes,
+                     "kernel": kernel_name[chosen], "tile_cells_rows_zchunk": tile, "algorithmic_bytes_per_launch": algo_bytes,
                      "avg_launch_ms": launch_ms},
         "e2e": {"value": e2e_value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
                 "d2h_bytes_per_step": 8 * 12, "steps": e2e_steps,
@@ -350,6 +436,7 @@ def run_gpu(args):
         "fp64_plain": {"value": fp64_value, "unit": "lattice-site-updates/s", "ms_per_launch": fp64_ms,
                        "speedup_fp32_fused": (sites / (launch_ms * 1e-3)) / fp64_value},
         "gpu_launches": launches,
+        "autotune": tuning_report,
         "clocks": clocks,
         "observables_last": obs[-1] if obs else None,
     }
@@ -413,12 +500,21 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 gather kernel, 2 row-tile kernel")
+    ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 gather, 2 row tile, 3 z-march, 4 multi-row tile")
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--rows", type=int, default=0)
+    ap.add_argument("--zchunk", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--autotune", action="store_true", help="run gpe_autotune before timing")
+    ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96"] + sorted(LEGS))
+    ap.add_argument("--inner", type=int, default=0, help="leapfrog steps per bench step for --workload legs")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "spin1-bcc96":
+        return run_leg(args)
     return run_gpu(args)
 
 

@@ -194,6 +194,27 @@ gpe_status gpe_buffer(const gpe_handle* h, int32_t slot, gpe_pitched* out, size_
 gpe_status gpe_upload(gpe_handle* h, int32_t slot, const double* host, size_t count, void* stream);
 gpe_status gpe_download(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream);
 
+/* Seeded initial state written on the device (no host array): Thomas-Fermi
+ * amplitude sqrt(max(mu - V, 0)/c0) for V = 0.5 |lambda r|^2 and
+ * mu = 0.5 (15 c0 lx ly lz / 4 pi)^(2/5), times the spinor zeta and, if
+ * vortex_kappa != 0, exp(i kappa phi) (a straight z-vortex); plus Gaussian noise
+ * noise_abs * sqrt(mu/c0) * N(0,1) + noise_rel * sqrt(rho) * N(0,1) per re/im part
+ * (the relative form is Spin1GpeBCC.cu:1272-1285's), drawn by Box-Muller from
+ * SplitMix64 numbers 2k+1, 2k+2 of stream `seed` for pair k = node * C + m, with
+ * nodes numbered ((z Y + y) X + x) V + l; then normalised to unit norm if
+ * `normalize`.  Replaces the ground-state file + polarState/cyclicState set-up of
+ * the reference (Spin1GpeBCC.cu:1228-1398, Spin2GpeBCC.cu:523-558), whose noise
+ * comes from an implementation-defined std::default_random_engine. */
+typedef struct {
+    double zeta[5][2];
+    int32_t vortex_kappa;
+    double noise_abs;
+    double noise_rel;
+    uint64_t seed;
+    int32_t normalize;
+} gpe_init;
+gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init* init, void* stream);
+
 /* Install the field ramp used by gpe_step / gpe_start (device-side getSignal). */
 gpe_status gpe_set_ramp(gpe_handle* h, const gpe_ramp* ramp, double t0);
 
@@ -241,11 +262,32 @@ gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* o
 /* Kernel selection and tile shape (the autotuner's knobs).
  * GPE_TUNE_KERNEL: 0 = automatic, 1 = one-node-per-thread gather kernel,
  *                  2 = row-tile kernel (TMA bulk copies of a row of cells into shared
- *                      memory; needs a cell size that is a multiple of 16 bytes).
- * GPE_TUNE_TILE_CELLS: cells per row tile (0 = automatic). */
-enum { GPE_TUNE_KERNEL = 0, GPE_TUNE_TILE_CELLS = 1 };
+ *                      memory; needs a cell size that is a multiple of 16 bytes),
+ *                  3 = 2.5-D z-march kernel (tiles of T cells x TY rows streamed
+ *                      along z through a ring of shared-memory slabs; needs 16-byte
+ *                      cells, T | X and TY | Y),
+ *                  4 = row-block kernel (a block of RY x RZ output rows; bulk copies
+ *                      of every row the block's stencil touches; all gathers from
+ *                      shared memory; needs 16-byte cells, RY | Y, RZ | Z).  The
+ *                      automatic choice is 2 where cells are 16-byte multiples, else
+ *                      1; gpe_autotune may pick any of them.
+ * GPE_TUNE_TILE_CELLS: cells per tile row (0 = automatic).
+ * GPE_TUNE_TILE_ROWS: rows per tile along y (z-march TY, row-block RY; 0 = automatic).
+ * GPE_TUNE_ZCHUNK: z-march planes per block, or row-block RZ (0 = automatic).
+ * GPE_TUNE_THREADS: threads per row-block (a multiple of 32, at most 384; each
+ *                   thread loops over the block's nodes; 0 = automatic). */
+enum { GPE_TUNE_KERNEL = 0, GPE_TUNE_TILE_CELLS = 1, GPE_TUNE_TILE_ROWS = 2, GPE_TUNE_ZCHUNK = 3, GPE_TUNE_THREADS = 4 };
 gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value);
 gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);
+
+/* Autotuner: times every eligible step kernel and tile shape (cells per tile, rows
+ * per block, threads per block) on this handle's own buffers with CUDA events,
+ * `steps` leapfrog steps each, and keeps the fastest.  The psi buffers are saved
+ * before and restored after the trials (temporary device copies).  `report`, if
+ * given, receives a JSON list of the timings.  Synchronises `stream`.  No
+ * counterpart in the reference (its launch shapes are compile-time #defines,
+ * THREAD_BLOCK_X/Y/Z, Spin1GpeBCC.cu:39-41). */
+gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, size_t report_len, void* stream);
 
 /* Slot (GPE_PSI_EVEN or GPE_PSI_ODD) holding the newest state after the last
  * gpe_start / gpe_step / gpe_itp call. */

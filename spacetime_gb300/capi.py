@@ -35,8 +35,8 @@ RAMP_CONSTANT, RAMP_LINEAR, RAMP_SQRT = 0, 1, 2
 RAMP_MAX_SEGMENTS = 32
 PSI_EVEN, PSI_ODD, Q_EVEN, Q_ODD, HPSI = 0, 1, 2, 3, 4
 MODE_LEAPFROG, MODE_EULER, MODE_ITP = 0, 1, 2
-TUNE_KERNEL, TUNE_TILE_CELLS = 0, 1
-KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE = 0, 1, 2
+TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS = 0, 1, 2, 3, 4
+KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS = 0, 1, 2, 3, 4
 
 
 class StencilEntry(C.Structure):
@@ -108,6 +108,25 @@ class Ramp(C.Structure):
         ("bq_quad_scale", C.c_double),
         ("bb_quad_scale", C.c_double),
     ]
+
+
+class Init(C.Structure):
+    _fields_ = [("zeta", (C.c_double * 2) * 5), ("vortex_kappa", C.c_int32), ("noise_abs", C.c_double),
+                ("noise_rel", C.c_double), ("seed", C.c_uint64), ("normalize", C.c_int32)]
+
+
+def make_init(zeta=(1.0,), kappa=0, noise_abs=0.0, noise_rel=0.0, seed=1, normalize=True) -> Init:
+    it = Init()
+    for m, z in enumerate(zeta):
+        z = complex(z)
+        it.zeta[m][0] = z.real
+        it.zeta[m][1] = z.imag
+    it.vortex_kappa = kappa
+    it.noise_abs = noise_abs
+    it.noise_rel = noise_rel
+    it.seed = seed
+    it.normalize = 1 if normalize else 0
+    return it
 
 
 class Pitched(C.Structure):
@@ -292,6 +311,8 @@ def load_library(path: str = LIB_PATH):
         "gpe_launch_count": (C.c_uint64, [vp]),
         "gpe_current_slot": (C.c_int32, [vp]),
         "gpe_set_tuning": (C.c_int, [vp, C.c_int32, C.c_int32]),
+        "gpe_init_state": (C.c_int, [vp, C.c_int32, P(Init), vp]),
+        "gpe_autotune": (C.c_int, [vp, C.c_int32, C.c_char_p, C.c_size_t, vp]),
         "gpe_observe_noalloc": (C.c_int, [P(LatticeDesc), P(Params), P(Fields), C.c_double, vp, C.c_size_t, C.c_size_t, P(Observables), vp]),
         "gpe_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
         "gpe_sites": (C.c_uint64, [vp]),

@@ -19,8 +19,21 @@ cudaError_t launch_observe(const StepArgs& a, double* out, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s);
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s);
+struct InitArgs {
+    double zeta[5][2];
+    double mu, c0inv, noise_abs, noise_rel;
+    int kappa;
+    uint64_t seed;
+};
+template <typename R, int C>
+cudaError_t launch_init(const StepArgs& a, const InitArgs& in, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_leapfrog_rows(const StepArgs& a, uint32_t T, uint32_t RY, uint32_t RZ, uint32_t K, uint32_t nbuf,
+                                 const int32_t* blk, uint32_t threads, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads, cudaStream_t s);
 cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
                             uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
 enum HyperKind {
@@ -91,6 +104,13 @@ struct gpe_handle {
     int* err = nullptr;    // device error flag
     int tune_kernel = 0;   // GPE_TUNE_KERNEL
     int tune_tile = 0;     // GPE_TUNE_TILE_CELLS
+    int tune_rows = 0;     // GPE_TUNE_TILE_ROWS
+    int tune_zchunk = 0;   // GPE_TUNE_ZCHUNK
+    int tune_threads = 0;  // GPE_TUNE_THREADS
+    uint32_t nrows = 0;    // multi-row tile kernel: (dy, dz) rows the stencil uses, own row first
+    int32_t rdy[9] = {0}, rdz[9] = {0};
+    int32_t* blk = nullptr;   // device row-block table of the current shape
+    uint32_t blk_ry = 0, blk_rz = 0, blk_nbuf = 0;
 };
 
 extern "C" const char* gpe_last_error(void) { return g_last_error.c_str(); }
@@ -239,6 +259,7 @@ static void release(gpe_handle* h) {
     if (h->obs_out) cudaFree(h->obs_out);
     if (h->stage) cudaFree(h->stage);
     if (h->err) cudaFree(h->err);
+    if (h->blk) cudaFree(h->blk);
 }
 
 static gpe_status build_tables(gpe_handle* h) {
@@ -262,12 +283,37 @@ static gpe_status build_tables(gpe_handle* h) {
         w64[f] = (-0.5 * e.hodge) / bs2;  // hodges[i] = -0.5*hodges[i]; hodge/(bs*bs) (Spin1GpeBCC.cu:1169, :859)
         w32[f] = (float)w64[f];
     }
+    std::vector<int4> ent4(n);
+    for (int f = 0; f < n; ++f) ent4[f] = make_int4(L.stencil[f].dx, L.stencil[f].dy, L.stencil[f].dz, L.stencil[f].node);
+    int udeg = L.row_ptr[1] - L.row_ptr[0];
+    for (int l = 0; l < L.V; ++l)
+        if (L.row_ptr[l + 1] - L.row_ptr[l] != udeg) udeg = 0;
+    h->tab.uniform_deg = udeg;
+    // rows (dy, dz) touched by the stencil, the own row first
+    h->nrows = 1;
+    h->rdy[0] = h->rdz[0] = 0;
+    for (int f = 0; f < n; ++f) {
+        const int dy = L.stencil[f].dy, dz = L.stencil[f].dz;
+        bool seen = false;
+        for (uint32_t r = 0; r < h->nrows; ++r) seen = seen || (h->rdy[r] == dy && h->rdz[r] == dz);
+        if (!seen && h->nrows < 9) {
+            h->rdy[h->nrows] = dy;
+            h->rdz[h->nrows] = dz;
+            h->nrows++;
+        }
+    }
     std::vector<double> pos64(L.pos);
     std::vector<float> pos32(L.pos.begin(), L.pos.end());
     gpe_status st;
     if ((st = upload_table(h, L.row_ptr, &h->tab.row_ptr))) return st;
     if ((st = upload_table(h, nb_off, &h->tab.nb_off))) return st;
     if ((st = upload_table(h, nb_soff, &h->tab.nb_soff))) return st;
+    if ((st = upload_table(h, ent4, &h->tab.ent4))) return st;
+    std::vector<int32_t> ent_row(n, 0);
+    for (int f = 0; f < n; ++f)
+        for (uint32_t r = 0; r < h->nrows; ++r)
+            if (h->rdy[r] == L.stencil[f].dy && h->rdz[r] == L.stencil[f].dz) ent_row[f] = (int32_t)r;
+    if ((st = upload_table(h, ent_row, &h->tab.ent_row))) return st;
     if ((st = upload_table(h, w64, &h->tab.w64))) return st;
     if ((st = upload_table(h, w32, &h->tab.w32))) return st;
     if ((st = upload_table(h, pos64, &h->tab.pos64))) return st;
@@ -614,15 +660,196 @@ static cudaError_t dispatch_scale(const gpe_handle* h, const StepArgs& a, const 
     }
 }
 
+// Shape of the 2.5-D z-march kernel (T = 0: not used).
+struct MarchShape {
+    uint32_t T = 0, TY = 0, ZC = 0, threads = 0;
+};
+
+static size_t march_smem(const gpe_handle* h, uint32_t T, uint32_t TY) {
+    const size_t cb = h->g.cell_bytes;
+    const size_t ent = 16;
+    return 4 * (size_t)(TY + 2) * (T + 2) * cb + 2 * (size_t)TY * T * cb + h->lat.stencil.size() * ent +
+           3 * h->g.V * h->real_bytes + (h->g.V + 1) * 4;
+}
+
+static MarchShape march_shape(const gpe_handle* h) {
+    MarchShape m;
+    if (h->tune_kernel != 3) return m;  // only on request: the multi-row kernel is faster where both apply
+    if (h->g.cell_bytes % 16 != 0) return m;
+    const uint32_t X = h->g.X, Y = h->g.Y, Z = h->g.Z, V = h->g.V;
+    const size_t limit = 200 * 1024;
+    auto fits = [&](uint32_t T, uint32_t TY) {
+        return T > 0 && TY > 0 && X % T == 0 && Y % TY == 0 && march_smem(h, T, TY) <= limit && T * TY * V <= 8192;
+    };
+    uint32_t T = 0, TY = 0;
+    if (h->tune_tile > 0 && h->tune_rows > 0) {
+        if (fits((uint32_t)h->tune_tile, (uint32_t)h->tune_rows)) {
+            T = (uint32_t)h->tune_tile;
+            TY = (uint32_t)h->tune_rows;
+        }
+    } else if (h->tune_kernel == 3 || (X >= 8 && Y >= 2 && Z >= 8)) {
+        // prefer about 192-384 nodes per row, two rows, the smallest halo overhead that fits
+        const uint32_t tcand[] = {16, 32, 24, 12, 8, 20, 6, 4, 3, 2, 1};
+        const uint32_t ycand[] = {2, 4, 3, 1};
+        for (uint32_t ty : ycand) {
+            for (uint32_t t : tcand)
+                if (fits(t, ty) && t * V <= 512) {
+                    T = t;
+                    TY = ty;
+                    break;
+                }
+            if (T) break;
+        }
+    }
+    if (!T) return m;
+    m.T = T;
+    m.TY = TY;
+    m.ZC = h->tune_zchunk > 0 ? (uint32_t)h->tune_zchunk : (Z >= 64 ? 32u : Z);
+    if (m.ZC > Z) m.ZC = Z;
+    const uint32_t nodes = T * TY * V;
+    m.threads = nodes >= 1024 ? 1024 : ((nodes + 31) / 32) * 32;
+    return m;
+}
+
+template <int C>
+static cudaError_t dispatch_march_c(const gpe_handle* h, const StepArgs& a, const MarchShape& m, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_leapfrog_march<double, C>(a, m.T, m.TY, m.ZC, m.threads, s)
+                              : launch_leapfrog_march<float, C>(a, m.T, m.TY, m.ZC, m.threads, s);
+}
+static cudaError_t dispatch_march(const gpe_handle* h, const StepArgs& a, const MarchShape& m, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_march_c<1>(h, a, m, s);
+        case 3: return dispatch_march_c<3>(h, a, m, s);
+        default: return dispatch_march_c<5>(h, a, m, s);
+    }
+}
+
+static uint32_t auto_tile_length(const gpe_handle* h) {
+    const uint32_t V = h->g.V, X = h->g.X;
+    uint32_t tmax = 256 / V;
+    if (tmax == 0) tmax = 1;
+    if (tmax >= X) return X;
+    for (uint32_t t = tmax; t * 2 > tmax; --t)
+        if (X % t == 0) return t;
+    return tmax;
+}
+
+// Row buffers a block of RY x RZ output rows needs: the distinct (y, z) rows
+// (relative to the block origin) reached by the stencil's (dy, dz) offsets.
+static void row_block_table(const gpe_handle* h, uint32_t RY, uint32_t RZ, std::vector<int32_t>& dy,
+                            std::vector<int32_t>& dz, std::vector<int32_t>& map) {
+    dy.clear();
+    dz.clear();
+    map.assign((size_t)RY * RZ * h->nrows, 0);
+    for (uint32_t rz = 0; rz < RZ; ++rz)
+        for (uint32_t ry = 0; ry < RY; ++ry)
+            for (uint32_t k = 0; k < h->nrows; ++k) {
+                const int32_t y = (int32_t)ry + h->rdy[k], z = (int32_t)rz + h->rdz[k];
+                int32_t b = -1;
+                for (size_t i = 0; i < dy.size() && b < 0; ++i)
+                    if (dy[i] == y && dz[i] == z) b = (int32_t)i;
+                if (b < 0) {
+                    b = (int32_t)dy.size();
+                    dy.push_back(y);
+                    dz.push_back(z);
+                }
+                map[((size_t)rz * RY + ry) * h->nrows + k] = b;
+            }
+}
+
+struct RowsShape {
+    uint32_t T = 0, RY = 0, RZ = 0, nbuf = 0;
+};
+
+static size_t rows_smem(const gpe_handle* h, uint32_t T, uint32_t RY, uint32_t RZ, uint32_t nbuf) {
+    const size_t cb = h->g.cell_bytes;
+    return (size_t)nbuf * (T + 2) * cb + (size_t)RY * RZ * T * cb + h->lat.stencil.size() * (h->real_bytes == 8 ? 16 : 8) +
+           3 * h->g.V * h->real_bytes + (h->g.V + 1) * 4 + (size_t)RY * RZ * h->nrows * 4;
+}
+
+// Multi-row tile kernel shape (T = 0: not used).
+static RowsShape rows_shape(const gpe_handle* h) {
+    RowsShape r;
+    if (h->tune_kernel != 4) return r;  // on request or by the autotuner (the row tile is faster on BCC)
+    if (h->g.cell_bytes % 16 != 0 || h->nrows == 0) return r;
+    uint32_t cand[4][2] = {{2, 2}, {2, 1}, {1, 2}, {1, 1}};
+    if (h->tune_rows > 0) {
+        // explicit: RY = tune_rows, RZ = tune_zchunk (or 1)
+        cand[0][0] = (uint32_t)h->tune_rows;
+        cand[0][1] = h->tune_zchunk > 0 ? (uint32_t)h->tune_zchunk : 1u;
+        for (int i = 1; i < 4; ++i) cand[i][0] = cand[i][1] = 0;
+    }
+    for (auto& c : cand) {
+        const uint32_t RY = c[0], RZ = c[1];
+        if (!RY || !RZ || h->g.Y % RY || h->g.Z % RZ) continue;
+        uint32_t T = (uint32_t)h->tune_tile;
+        if (T == 0) {
+            // about 384 nodes per block, preferring a divisor of X
+            const uint32_t want = 384 / (RY * RZ * h->g.V) > 0 ? 384 / (RY * RZ * h->g.V) : 1;
+            T = want >= h->g.X ? h->g.X : want;
+            for (uint32_t t = T; t * 2 > T && t > 0; --t)
+                if (h->g.X % t == 0) {
+                    T = t;
+                    break;
+                }
+        }
+        if (T == 0 || T > h->g.X) continue;
+        if ((uint64_t)RY * RZ * T * h->g.V > 4096) continue;
+        std::vector<int32_t> dy, dz, map;
+        row_block_table(h, RY, RZ, dy, dz, map);
+        if (rows_smem(h, T, RY, RZ, (uint32_t)dy.size()) > 200 * 1024) continue;
+        r.T = T;
+        r.RY = RY;
+        r.RZ = RZ;
+        r.nbuf = (uint32_t)dy.size();
+        return r;
+    }
+    return r;
+}
+
+static uint32_t rows_cells(const gpe_handle* h) { return rows_shape(h).T; }
+
+// Device copy of the row-block table for the shape (rebuilt when the shape changes).
+static gpe_status ensure_row_block(gpe_handle* h, const RowsShape& r) {
+    if (h->blk && h->blk_ry == r.RY && h->blk_rz == r.RZ) return GPE_OK;
+    std::vector<int32_t> dy, dz, map;
+    row_block_table(h, r.RY, r.RZ, dy, dz, map);
+    std::vector<int32_t> t;
+    t.insert(t.end(), dy.begin(), dy.end());
+    t.insert(t.end(), dz.begin(), dz.end());
+    t.insert(t.end(), map.begin(), map.end());
+    if (h->blk) cudaFree(h->blk);
+    h->blk = nullptr;
+    if (cudaMalloc(&h->blk, t.size() * sizeof(int32_t)) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (row table)");
+    CUDA_TRY(cudaMemcpy(h->blk, t.data(), t.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    h->blk_ry = r.RY;
+    h->blk_rz = r.RZ;
+    h->blk_nbuf = (uint32_t)dy.size();
+    return GPE_OK;
+}
+
+template <int C>
+static cudaError_t dispatch_rows_c(const gpe_handle* h, const StepArgs& a, const RowsShape& r, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_leapfrog_rows<double, C>(a, r.T, r.RY, r.RZ, h->nrows, r.nbuf, h->blk, (uint32_t)h->tune_threads, s)
+                              : launch_leapfrog_rows<float, C>(a, r.T, r.RY, r.RZ, h->nrows, r.nbuf, h->blk, (uint32_t)h->tune_threads, s);
+}
+static cudaError_t dispatch_rows(const gpe_handle* h, const StepArgs& a, const RowsShape& r, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_rows_c<1>(h, a, r, s);
+        case 3: return dispatch_rows_c<3>(h, a, r, s);
+        default: return dispatch_rows_c<5>(h, a, r, s);
+    }
+}
+
 // Row-tile kernel eligibility and tile length (0 = use the gather kernel).
 static uint32_t tile_cells(const gpe_handle* h) {
-    if (h->tune_kernel == 1) return 0;
+    if (h->tune_kernel == 1 || h->tune_kernel == 3) return 0;
     if (h->g.cell_bytes % 16 != 0) return 0;
     const uint32_t V = h->g.V, X = h->g.X;
     uint32_t tmax = 256 / V;
     if (tmax == 0) tmax = 1;
-    if (V * tmax > 1024) return 0;
-    if (h->tune_tile > 0) return (uint32_t)h->tune_tile <= X && (uint32_t)h->tune_tile * V <= 1024 ? (uint32_t)h->tune_tile : 0;
+    if (V * tmax > 256) return 0;
+    if (h->tune_tile > 0) return (uint32_t)h->tune_tile <= X && (uint32_t)h->tune_tile * V <= 256 ? (uint32_t)h->tune_tile : 0;
     if (tmax >= X) return X;
     for (uint32_t t = tmax; t * 2 > tmax; --t)
         if (X % t == 0) return t;
@@ -654,8 +881,16 @@ static gpe_status one_step(gpe_handle* h, int next, int prev, const gpe_fields& 
     cudaError_t e;
     if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
         a.hpsi = mode == GPE_MODE_ITP ? h->interior[GPE_HPSI] : nullptr;
+        const MarchShape ms = march_shape(h);
         const uint32_t T = tile_cells(h);
-        if (mode == GPE_MODE_LEAPFROG && T > 0) e = dispatch_tile(h, a, T, s);
+        const RowsShape rs = rows_shape(h);
+        if (mode == GPE_MODE_LEAPFROG && rs.T > 0) {
+            gpe_status bst = ensure_row_block(h, rs);
+            if (bst) return bst;
+            e = dispatch_rows(h, a, rs, s);
+        }
+        else if (mode == GPE_MODE_LEAPFROG && ms.T > 0) e = dispatch_march(h, a, ms, s);
+        else if (mode == GPE_MODE_LEAPFROG && T > 0) e = dispatch_tile(h, a, T, s);
         else e = dispatch_parabolic(h, a, mode, s);
         h->launches += 1;
     } else {
@@ -810,9 +1045,33 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
 extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
     if (key == GPE_TUNE_KERNEL) {
-        if (value < 0 || value > 2) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
-        if (value == 2 && h->g.cell_bytes % 16 != 0) return fail(GPE_ERR_UNSUPPORTED, "row tiles need 16-byte cells");
+        if (value < 0 || value > 4) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
+        if (value >= 2 && h->g.cell_bytes % 16 != 0) return fail(GPE_ERR_UNSUPPORTED, "tiled kernels need 16-byte cells");
+        const int old = h->tune_kernel;
         h->tune_kernel = value;
+        if (value == 3 && march_shape(h).T == 0) {
+            h->tune_kernel = old;
+            return fail(GPE_ERR_UNSUPPORTED, "no z-march tile shape divides the grid within the shared-memory limit");
+        }
+        if (value == 4 && rows_cells(h) == 0) {
+            h->tune_kernel = old;
+            return fail(GPE_ERR_UNSUPPORTED, "the multi-row tile does not fit in shared memory");
+        }
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_TILE_ROWS) {
+        if (value < 0 || (uint32_t)value > h->g.Y) return fail(GPE_ERR_INVALID_ARG, "tile rows");
+        h->tune_rows = value;
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_THREADS) {
+        if (value < 0 || value > 1024 || value % 32) return fail(GPE_ERR_INVALID_ARG, "threads must be a multiple of 32");
+        h->tune_threads = value;
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_ZCHUNK) {
+        if (value < 0 || (uint32_t)value > h->g.Z) return fail(GPE_ERR_INVALID_ARG, "z chunk");
+        h->tune_zchunk = value;
         return GPE_OK;
     }
     if (key == GPE_TUNE_TILE_CELLS) {
@@ -826,8 +1085,13 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
 
 extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value) {
     if (!h || !value) return fail(GPE_ERR_INVALID_ARG, "null argument");
-    if (key == GPE_TUNE_KERNEL) *value = tile_cells(h) > 0 ? 2 : 1;
-    else if (key == GPE_TUNE_TILE_CELLS) *value = (int32_t)tile_cells(h);
+    const MarchShape ms = march_shape(h);
+    const uint32_t tr = rows_cells(h);
+    if (key == GPE_TUNE_KERNEL) *value = tr > 0 ? 4 : ms.T > 0 ? 3 : (tile_cells(h) > 0 ? 2 : 1);
+    else if (key == GPE_TUNE_TILE_CELLS) *value = (int32_t)(tr > 0 ? tr : ms.T > 0 ? ms.T : tile_cells(h));
+    else if (key == GPE_TUNE_TILE_ROWS) *value = (int32_t)(tr > 0 ? rows_shape(h).RY : ms.TY);
+    else if (key == GPE_TUNE_ZCHUNK) *value = (int32_t)(tr > 0 ? rows_shape(h).RZ : ms.ZC);
+    else if (key == GPE_TUNE_THREADS) *value = h->tune_threads;
     else return fail(GPE_ERR_INVALID_ARG, "unknown tuning key");
     return GPE_OK;
 }
@@ -838,4 +1102,149 @@ extern "C" uint64_t gpe_launch_count(const gpe_handle* h) { return h ? h->launch
 
 extern "C" uint64_t gpe_sites(const gpe_handle* h) {
     return h ? (uint64_t)h->g.X * h->g.Y * h->g.Z * h->g.V : 0;
+}
+
+// ------------------------------------------------------------------ autotuner
+
+// Times candidate step kernels and tile shapes on this handle's buffers and keeps
+// the fastest (the tile shape and threads per block per lattice type).  The state
+// is saved before and restored after the trials.
+extern "C" gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, size_t report_len, void* stream) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (steps <= 0) steps = 10;
+    cudaStream_t s = (cudaStream_t)stream;
+    struct Cand {
+        int kernel, tile, rows, zchunk, threads;
+    };
+    std::vector<Cand> cands;
+    cands.push_back({1, 0, 0, 0, 0});
+    if (h->g.cell_bytes % 16 == 0) {
+        cands.push_back({2, 0, 0, 0, 0});
+        const uint32_t ryz[4][2] = {{1, 1}, {2, 1}, {1, 2}, {2, 2}};
+        for (auto& b : ryz) {
+            if (h->g.Y % b[0] || h->g.Z % b[1]) continue;
+            const uint32_t base = 384 / (b[0] * b[1] * h->g.V) > 0 ? 384 / (b[0] * b[1] * h->g.V) : 1;
+            const uint32_t ts[3] = {base / 2, base, base * 2};
+            for (uint32_t t : ts) {
+                if (t == 0 || t > h->g.X) continue;
+                for (int th : {0, 192, 256})
+                    cands.push_back({4, (int)t, (int)b[0], (int)b[1], th});
+            }
+        }
+    }
+    const int saved_k = h->tune_kernel, saved_t = h->tune_tile, saved_r = h->tune_rows, saved_z = h->tune_zchunk,
+              saved_th = h->tune_threads;
+    // save the two psi buffers
+    const size_t bytes = h->alloc_bytes[GPE_PSI_EVEN];
+    void* save[2] = {nullptr, nullptr};
+    if (cudaMalloc(&save[0], bytes) != cudaSuccess || cudaMalloc(&save[1], bytes) != cudaSuccess) {
+        if (save[0]) cudaFree(save[0]);
+        return fail(GPE_ERR_OOM, "cudaMalloc (autotune save)");
+    }
+    CUDA_TRY(cudaMemcpyAsync(save[0], h->alloc[GPE_PSI_EVEN], bytes, cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(save[1], h->alloc[GPE_PSI_ODD], bytes, cudaMemcpyDeviceToDevice, s));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    gpe_fields B;
+    std::memset(&B, 0, sizeof B);
+    float best_ms = 1e30f;
+    Cand best = {saved_k, saved_t, saved_r, saved_z, saved_th};
+    std::string rep = "[";
+    for (const Cand& c : cands) {
+        h->tune_kernel = c.kernel;
+        h->tune_tile = c.tile;
+        h->tune_rows = c.rows;
+        h->tune_zchunk = c.zchunk;
+        h->tune_threads = c.threads;
+        if (c.kernel == 4 && rows_shape(h).T == 0) continue;
+        if (c.kernel == 2 && tile_cells(h) == 0) continue;
+        bool ok = true;
+        for (int k = 0; k < 2 && ok; ++k) ok = one_step(h, GPE_PSI_ODD, GPE_PSI_EVEN, B, 0.0, GPE_MODE_LEAPFROG, s) == GPE_OK;
+        cudaEventRecord(e0, s);
+        for (int k = 0; k < steps && ok; ++k)
+            ok = one_step(h, (k & 1) ? GPE_PSI_EVEN : GPE_PSI_ODD, (k & 1) ? GPE_PSI_ODD : GPE_PSI_EVEN, B, 0.0,
+                          GPE_MODE_LEAPFROG, s) == GPE_OK;
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess || !ok) {
+            cudaGetLastError();
+            continue;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)steps;
+        char line[160];
+        std::snprintf(line, sizeof line, "%s{\"kernel\":%d,\"tile\":%d,\"rows\":%d,\"zchunk\":%d,\"threads\":%d,\"ms\":%.5f}",
+                      rep.size() > 1 ? "," : "", c.kernel, c.tile, c.rows, c.zchunk, c.threads, ms);
+        rep += line;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    rep += "]";
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->tune_kernel = best.kernel;
+    h->tune_tile = best.tile;
+    h->tune_rows = best.rows;
+    h->tune_zchunk = best.zchunk;
+    h->tune_threads = best.threads;
+    CUDA_TRY(cudaMemcpyAsync(h->alloc[GPE_PSI_EVEN], save[0], bytes, cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(h->alloc[GPE_PSI_ODD], save[1], bytes, cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(save[0]);
+    cudaFree(save[1]);
+    if (report && report_len) {
+        std::snprintf(report, report_len, "%s", rep.c_str());
+    }
+    return GPE_OK;
+}
+
+// ---------------------------------------------------------------- init state
+
+template <int C>
+static cudaError_t dispatch_init_c(const gpe_handle* h, const StepArgs& a, const InitArgs& in, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_init<double, C>(a, in, s) : launch_init<float, C>(a, in, s);
+}
+
+extern "C" gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init* init, void* stream) {
+    if (!h || !init) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (slot != GPE_PSI_EVEN && slot != GPE_PSI_ODD) return fail(GPE_ERR_INVALID_ARG, "psi slot");
+    if (!(h->p.c0 > 0)) return fail(GPE_ERR_INVALID_ARG, "the Thomas-Fermi profile needs c0 > 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    gpe_fields zero;
+    std::memset(&zero, 0, sizeof zero);
+    StepArgs a = make_args(h, zero, 0.0);
+    a.next = h->interior[slot];
+    InitArgs in;
+    std::memset(&in, 0, sizeof in);
+    for (int c = 0; c < 5; ++c) {
+        in.zeta[c][0] = init->zeta[c][0];
+        in.zeta[c][1] = init->zeta[c][1];
+    }
+    const double lx = h->p.trap_lambda[0], ly = h->p.trap_lambda[1], lz = h->p.trap_lambda[2];
+    in.mu = 0.5 * std::pow(15.0 * h->p.c0 * lx * ly * lz / (4.0 * 3.141592653589793), 0.4);
+    in.c0inv = 1.0 / h->p.c0;
+    in.noise_abs = init->noise_abs * std::sqrt(in.mu * in.c0inv);
+    in.noise_rel = init->noise_rel;
+    in.kappa = init->vortex_kappa;
+    in.seed = init->seed;
+    cudaError_t e;
+    switch (h->g.C) {
+        case 1: e = dispatch_init_c<1>(h, a, in, s); break;
+        case 3: e = dispatch_init_c<3>(h, a, in, s); break;
+        default: e = dispatch_init_c<5>(h, a, in, s); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "init kernel");
+    h->launches += 1;
+    if (init->normalize) {
+        a.prev = h->interior[slot];
+        e = dispatch_observe(h, a, h->obs_out, s);
+        if (e == cudaSuccess) e = dispatch_scale(h, a, h->obs_out, cell_dv(h), s);
+        if (e != cudaSuccess) return cuda_fail(e, "init normalisation");
+        h->launches += 3;
+    }
+    h->cur = slot;
+    return GPE_OK;
 }

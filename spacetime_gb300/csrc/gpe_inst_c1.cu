@@ -7,6 +7,12 @@ GPE_INSTANTIATE(float, 1)
 GPE_INSTANTIATE(double, 1)
 GPE_INSTANTIATE_TILE(float, 1)
 GPE_INSTANTIATE_TILE(double, 1)
+GPE_INSTANTIATE_MARCH(float, 1)
+GPE_INSTANTIATE_MARCH(double, 1)
+GPE_INSTANTIATE_ROWS(float, 1)
+GPE_INSTANTIATE_ROWS(double, 1)
+GPE_INSTANTIATE_INIT(float, 1)
+GPE_INSTANTIATE_INIT(double, 1)
 
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s) {
     if (precision == GPE_FP64) {

@@ -7,4 +7,10 @@ GPE_INSTANTIATE(float, 3)
 GPE_INSTANTIATE(double, 3)
 GPE_INSTANTIATE_TILE(float, 3)
 GPE_INSTANTIATE_TILE(double, 3)
+GPE_INSTANTIATE_MARCH(float, 3)
+GPE_INSTANTIATE_MARCH(double, 3)
+GPE_INSTANTIATE_ROWS(float, 3)
+GPE_INSTANTIATE_ROWS(double, 3)
+GPE_INSTANTIATE_INIT(float, 3)
+GPE_INSTANTIATE_INIT(double, 3)
 }  // namespace gpe

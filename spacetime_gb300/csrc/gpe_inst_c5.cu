@@ -7,4 +7,10 @@ GPE_INSTANTIATE(float, 5)
 GPE_INSTANTIATE(double, 5)
 GPE_INSTANTIATE_TILE(float, 5)
 GPE_INSTANTIATE_TILE(double, 5)
+GPE_INSTANTIATE_MARCH(float, 5)
+GPE_INSTANTIATE_MARCH(double, 5)
+GPE_INSTANTIATE_ROWS(float, 5)
+GPE_INSTANTIATE_ROWS(double, 5)
+GPE_INSTANTIATE_INIT(float, 5)
+GPE_INSTANTIATE_INIT(double, 5)
 }  // namespace gpe

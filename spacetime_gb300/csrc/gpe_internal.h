@@ -115,8 +115,11 @@ struct DevTables {
     float* inc_w32;
     int32_t* e_from_off;  // E: byte offset of from-node in own psi cell
     int32_t* e_to_off;    // E: byte offset of to-node relative to own psi cell base
+    int4* ent4;           // entries: (dx, dy, dz, node)
+    int32_t* ent_row;     // entries: index of the (dy, dz) row in the multi-row tile
     int entries;
     int faces;
+    int uniform_deg;      // > 0 when every node has the same number of entries
 };
 
 struct StepArgs {

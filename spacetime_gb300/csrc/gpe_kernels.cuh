@@ -12,6 +12,8 @@
 // GPUGrossPitaevskii_BCC.cu:327-347, RelativisticSpin2Gpe.cu:971-1132).
 #pragma once
 
+#include <type_traits>
+
 #include "gpe_internal.h"
 
 namespace gpe {
@@ -1005,5 +1007,539 @@ cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, cudaStream_t s) 
 }
 
 #define GPE_INSTANTIATE_TILE(R, C) template cudaError_t launch_leapfrog_tile<R, C>(const StepArgs&, uint32_t, cudaStream_t);
+
+}  // namespace gpe
+
+namespace gpe {
+
+// ----------------------------------------------------------- 2.5-D z-march
+
+// Packed stencil entry of the z-march kernel: the neighbour's plane (dz) and its
+// byte offset inside a (TY+2) x (T+2)-cell slab relative to the own node's cell.
+template <typename R>
+struct __align__(16) MarchEntry {
+    int32_t soff;
+    int32_t dz;
+    R w;
+};
+static_assert(sizeof(MarchEntry<float>) == 16 && sizeof(MarchEntry<double>) == 16, "16-byte stencil entries");
+
+struct MarchArgs {
+    uint32_t T, TY, ZC;          // cells per row tile, rows per tile, planes per block
+    uint32_t tiles_x, tiles_y;   // tiles along x and y
+    uint32_t nodes;              // T * TY * V
+    FastDiv div_row_nodes;       // T * V
+    uint32_t slab_bytes, tile_bytes;
+    int uniform_deg;             // > 0: every node has this many entries (no row_ptr lookups)
+};
+
+// Leapfrog step, 2.5-D: block = T cells x TY rows of one z-chunk of ZC planes.
+// A ring of four slabs holds psi_prev of planes z-1, z, z+1 and the prefetch of
+// z+2, each slab the (TY+2) x (T+2) cells around the tile, brought in by TY+2
+// bulk copies of contiguous row segments; the old psi_next of the tile is
+// double-buffered.  Every neighbour is read from shared memory.  Requires
+// cell_bytes % 16 == 0, T | X and TY | Y.
+template <typename R, int C>
+__global__ void __launch_bounds__(1024) leapfrog_march_kernel(StepArgs a, MarchArgs m) {
+    extern __shared__ __align__(128) unsigned char dyn[];
+    __shared__ __align__(8) uint64_t bar_slab[4];
+    __shared__ __align__(8) uint64_t bar_tile[2];
+    using V2 = typename Vec2<R>::type;
+    const uint32_t cb = a.g.cell_bytes;
+    const int V = a.g.V, n = a.tab.entries;
+    char* slab = reinterpret_cast<char*>(dyn);
+    char* tilebuf = slab + 4 * (size_t)m.slab_bytes;
+    MarchEntry<R>* s_ent = reinterpret_cast<MarchEntry<R>*>(tilebuf + 2 * (size_t)m.tile_bytes);
+    R* s_pos = reinterpret_cast<R*>(s_ent + n);
+    int32_t* s_row = reinterpret_cast<int32_t*>(s_pos + 3 * V);
+
+    const uint32_t tx = blockIdx.x % m.tiles_x;
+    const uint32_t rest = blockIdx.x / m.tiles_x;
+    const uint32_t ty = rest % m.tiles_y;
+    const uint32_t tz = rest / m.tiles_y;
+    const uint32_t x0 = tx * m.T, y0 = ty * m.TY, zb = tz * m.ZC;
+    const uint32_t ze = min(zb + m.ZC, a.g.Z);
+    const uint32_t seg_bytes = (m.T + 2) * cb;        // one row segment of a slab
+    const uint32_t row_bytes = m.T * cb;              // one row of the tile
+
+    // issue the copies of slab for plane zz (zz in [-1, Z]) into ring slot s
+    auto load_slab = [&](int zz, int s) {
+        mbar_expect_tx(&bar_slab[s], (m.TY + 2) * seg_bytes);
+        for (uint32_t r = 0; r < m.TY + 2; ++r) {
+            const char* src = a.prev + (ptrdiff_t)zz * (ptrdiff_t)a.g.slice + ((ptrdiff_t)y0 + r - 1) * (ptrdiff_t)a.g.pitch +
+                              ((ptrdiff_t)x0 - 1) * cb;
+            bulk_load(slab + (size_t)s * m.slab_bytes + (size_t)r * seg_bytes, src, seg_bytes, &bar_slab[s]);
+        }
+    };
+    auto load_tile = [&](uint32_t zz, int s) {
+        mbar_expect_tx(&bar_tile[s], m.TY * row_bytes);
+        for (uint32_t r = 0; r < m.TY; ++r) {
+            const char* src = a.next + (size_t)zz * a.g.slice + (size_t)(y0 + r) * a.g.pitch + (size_t)x0 * cb;
+            bulk_load(tilebuf + (size_t)s * m.tile_bytes + (size_t)r * row_bytes, src, row_bytes, &bar_tile[s]);
+        }
+    };
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < 4; ++s) mbar_init(&bar_slab[s], 1);
+        for (int s = 0; s < 2; ++s) mbar_init(&bar_tile[s], 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    // prologue: slabs of planes zb-1, zb, zb+1 (ring slots 0, 1, 2) and the tile of zb
+    if (threadIdx.x == 0) {
+        load_slab((int)zb - 1, 0);
+        load_slab((int)zb, 1);
+        load_slab((int)zb + 1, 2);
+        load_tile(zb, 0);
+    }
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        // slab offset of the neighbour relative to the own cell: (dy (T+2) + dx) cells + node
+        const int4 q = a.tab.ent4[i];
+        MarchEntry<R> e;
+        e.soff = (q.y * (int)(m.T + 2) + q.x) * (int)cb + q.w * (int)node_bytes;
+        e.dz = q.z;
+        if constexpr (sizeof(R) == 4) e.w = a.tab.w32[i];
+        else e.w = a.tab.w64[i];
+        s_ent[i] = e;
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) s_pos[i] = a.tab.pos32[i];
+        else s_pos[i] = a.tab.pos64[i];
+    }
+    for (int i = threadIdx.x; i <= V; i += blockDim.x) s_row[i] = a.tab.row_ptr[i];
+    __syncthreads();
+
+    const PhysR<R>& P = make_phys<R>(a);
+    const R dt2 = (R)2 * P.dt;
+    uint32_t slab_phase = 0;   // bit s: parity to wait for on slab slot s
+    uint32_t tile_phase = 0;
+    bool ok = true;
+    for (uint32_t z = zb; z < ze; ++z) {
+        const uint32_t k = z - zb;
+        const int s_mid = (int)((k + 1) & 3), s_lo = (int)(k & 3), s_hi = (int)((k + 2) & 3), s_pre = (int)((k + 3) & 3);
+        const int t_cur = (int)(k & 1), t_nxt = (int)((k + 1) & 1);
+        if (threadIdx.x == 0) {
+            // the store of plane z-1 used tile slot t_nxt: let it finish reading shared memory
+            bulk_wait_read_all();
+            // prefetch what the next iteration needs (plane z+2 <= Z: plane Z is the zero halo)
+            if (z + 1 < ze) {
+                load_slab((int)z + 2, s_pre);
+                load_tile(z + 1, t_nxt);
+            }
+        }
+        // wait for slab z+1 (slabs z-1 and z were waited for already) and tile z
+        if (k == 0) {
+            ok = ok && block_wait(&bar_slab[0], 0, a.err);
+            ok = ok && block_wait(&bar_slab[1], 0, a.err);
+            slab_phase ^= 0x3;
+        }
+        ok = ok && block_wait(&bar_slab[s_hi], (slab_phase >> s_hi) & 1, a.err);
+        slab_phase ^= 1u << s_hi;
+        ok = ok && block_wait(&bar_tile[t_cur], (tile_phase >> t_cur) & 1, a.err);
+        tile_phase ^= 1u << t_cur;
+        if (!ok) break;
+
+        (void)s_lo;
+        const char* sl_mid = slab + (size_t)s_mid * m.slab_bytes;
+        char* tl = tilebuf + (size_t)t_cur * m.tile_bytes;
+        for (uint32_t i = threadIdx.x; i < m.nodes; i += blockDim.x) {
+            const uint32_t r = fdiv(i, m.div_row_nodes);
+            const uint32_t j = i - r * (m.T * V);
+            const uint32_t xl = fdiv(j, a.divV);
+            const uint32_t l = j - xl * V;
+            const size_t own_cell = ((size_t)(r + 1) * (m.T + 2) + (xl + 1)) * cb;
+            const char* own = sl_mid + own_cell + l * node_bytes;
+            Cx<R> prv[C], H[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const V2 v = reinterpret_cast<const V2*>(own)[c];
+                prv[c] = cx<R>(v.x, v.y);
+                H[c] = cx<R>((R)0, (R)0);
+            }
+            int f0, f1;
+            if (m.uniform_deg > 0) {
+                f0 = (int)l * m.uniform_deg;
+                f1 = f0 + m.uniform_deg;
+            } else {
+                f0 = s_row[l];
+                f1 = s_row[l + 1];
+            }
+            for (int f = f0; f < f1; ++f) {
+                const MarchEntry<R> e = s_ent[f];
+                // plane z+dz sits in ring slot (s_mid + dz) mod 4
+                const V2* p = reinterpret_cast<const V2*>(slab + (size_t)((s_mid + e.dz) & 3) * m.slab_bytes + own_cell + e.soff);
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const V2 v = p[c];
+                    H[c] += e.w * (cx<R>(v.x, v.y) - prv[c]);
+                }
+            }
+            R rr[3];
+            rr[0] = P.p0[0] + P.bs * ((R)(x0 + xl) * P.bw[0] + s_pos[3 * l + 0]);
+            rr[1] = P.p0[1] + P.bs * ((R)(y0 + r) * P.bw[1] + s_pos[3 * l + 1]);
+            rr[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + s_pos[3 * l + 2]);
+            const R pot = trap<R>(P, rr);
+            local_terms<R, C>(P, rr, pot, GPE_MODE_LEAPFROG, false, prv, H);
+            V2* q = reinterpret_cast<V2*>(tl + ((size_t)r * m.T + xl) * cb + l * node_bytes);
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                V2 v = q[c];
+                v.x += dt2 * H[c].y;
+                v.y += dt2 * -H[c].x;
+                q[c] = v;
+            }
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t r = 0; r < m.TY; ++r) {
+                char* dst = a.next + (size_t)z * a.g.slice + (size_t)(y0 + r) * a.g.pitch + (size_t)x0 * cb;
+                bulk_store(dst, tl + (size_t)r * row_bytes, row_bytes);
+            }
+            bulk_commit();
+        }
+    }
+    if (threadIdx.x == 0) bulk_wait_read_all();
+    if (!ok) {
+        // a wait ran out: give the copies in flight a bounded time to land before exiting
+        for (int s = 0; s < 4; ++s)
+            for (uint32_t spin = 0; spin < (1u << 16) && !mbar_try_wait(&bar_slab[s], (slab_phase >> s) & 1); ++spin) {
+            }
+    }
+}
+
+template <typename R, int C>
+size_t march_smem_bytes(const StepArgs& a, const MarchArgs& m) {
+    return 4 * (size_t)m.slab_bytes + 2 * (size_t)m.tile_bytes + (size_t)a.tab.entries * sizeof(MarchEntry<R>) +
+           3 * a.g.V * sizeof(R) + (a.g.V + 1) * 4;
+}
+
+template <typename R, int C>
+cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads,
+                                  cudaStream_t s) {
+    MarchArgs m;
+    m.T = T;
+    m.TY = TY;
+    m.ZC = ZC;
+    m.tiles_x = a.g.X / T;
+    m.tiles_y = a.g.Y / TY;
+    m.nodes = T * TY * a.g.V;
+    m.div_row_nodes = make_fastdiv(T * a.g.V);
+    m.slab_bytes = (TY + 2) * (T + 2) * a.g.cell_bytes;
+    m.tile_bytes = TY * T * a.g.cell_bytes;
+    m.uniform_deg = a.tab.uniform_deg;
+    const size_t smem = march_smem_bytes<R, C>(a, m);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(leapfrog_march_kernel<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const uint64_t blocks = (uint64_t)m.tiles_x * m.tiles_y * ((a.g.Z + ZC - 1) / ZC);
+    leapfrog_march_kernel<R, C><<<(unsigned)blocks, threads, smem, s>>>(a, m);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE_MARCH(R, C) \
+    template cudaError_t launch_leapfrog_march<R, C>(const StepArgs&, uint32_t, uint32_t, uint32_t, uint32_t, cudaStream_t);
+
+}  // namespace gpe
+
+namespace gpe {
+
+// ------------------------------------------------------ multi-row tiles
+
+// Packed stencil entry: byte offset of the neighbour relative to the own cell in
+// row buffer 0, and the weight.
+template <typename R>
+struct __align__(8) RowsEntry {
+    int32_t off;
+    float w;
+};
+template <>
+struct __align__(16) RowsEntry<double> {
+    int32_t off;
+    int32_t pad;
+    double w;
+};
+
+struct RowsArgs {
+    uint32_t T;             // cells per tile row
+    uint32_t RY, RZ;        // output rows per block along y and z
+    uint32_t tiles_x, tiles_y;
+    uint32_t K;             // distinct (dy, dz) row offsets of the stencil, (0, 0) first
+    uint32_t nbuf;          // row buffers staged per block
+    uint32_t row_buf_bytes; // (T + 2) * cell_bytes
+    FastDiv div_row_nodes;  // T * V
+    const int32_t* blk;     // [nbuf dy][nbuf dz][RY*RZ*K buffer index of (own row, offset k)]
+};
+
+// Leapfrog step on a block of RY x RZ output rows (y, z) of T cells each.  Bulk
+// copies bring psi_prev of cells [x0-1, x0+T] of every row the block's stencil
+// touches (BCC, 2 x 2 rows: 14 rows, 3.5 per output row) into shared memory,
+// plus the old psi_next of the block; every neighbour is then read from shared
+// memory.  L2 supplies each psi_prev line a few times per step (the measured L2
+// bandwidth is ~5x HBM); HBM still sees each value once.  Requires
+// cell_bytes % 16 == 0, RY | Y and RZ | Z.
+// Launch bounds of the row-block kernel: 384 threads; four resident blocks
+// (<= 42 registers) for FP32 with up to three components, two otherwise.
+template <typename R, int C>
+struct RowsLB {
+    static constexpr int threads = 384;
+    static constexpr int blocks = (sizeof(R) == 4 && C <= 3) ? 4 : 2;
+};
+
+template <typename R, int C>
+__global__ void __launch_bounds__(RowsLB<R, C>::threads, RowsLB<R, C>::blocks) leapfrog_rows_kernel(StepArgs a, RowsArgs m) {
+    extern __shared__ __align__(128) unsigned char dyn[];
+    __shared__ __align__(8) uint64_t bar;
+    using V2 = typename Vec2<R>::type;
+    const uint32_t cb = a.g.cell_bytes;
+    const int V = a.g.V, n = a.tab.entries;
+    const uint32_t own_rows = m.RY * m.RZ;
+    char* s_rows = reinterpret_cast<char*>(dyn);
+    char* s_next = s_rows + (size_t)m.nbuf * m.row_buf_bytes;
+    RowsEntry<R>* s_ent = reinterpret_cast<RowsEntry<R>*>(s_next + (size_t)own_rows * m.T * cb);
+    R* s_pos = reinterpret_cast<R*>(s_ent + n);
+    int32_t* s_row = reinterpret_cast<int32_t*>(s_pos + 3 * V);
+    int32_t* s_map = s_row + (V + 1);   // own_rows * K buffer indices
+
+    const uint32_t tx = blockIdx.x % m.tiles_x;
+    const uint32_t rest = blockIdx.x / m.tiles_x;
+    const uint32_t ty = rest % m.tiles_y;
+    const uint32_t tz = rest / m.tiles_y;
+    const uint32_t x0 = tx * m.T, y0 = ty * m.RY, z0 = tz * m.RZ;
+    const uint32_t Tc = min(m.T, a.g.X - x0);
+    const uint32_t bytes_row = (Tc + 2) * cb, bytes_next = Tc * cb;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, m.nbuf * bytes_row + own_rows * bytes_next);
+        for (uint32_t b = 0; b < m.nbuf; ++b) {
+            const int dy = m.blk[b], dz = m.blk[m.nbuf + b];
+            const char* src = a.prev + ((ptrdiff_t)z0 + dz) * (ptrdiff_t)a.g.slice + ((ptrdiff_t)y0 + dy) * (ptrdiff_t)a.g.pitch +
+                              ((ptrdiff_t)x0 - 1) * cb;
+            bulk_load(s_rows + (size_t)b * m.row_buf_bytes, src, bytes_row, &bar);
+        }
+        for (uint32_t q = 0; q < own_rows; ++q) {
+            const uint32_t ry = q % m.RY, rz = q / m.RY;
+            const char* src = a.next + (size_t)(z0 + rz) * a.g.slice + (size_t)(y0 + ry) * a.g.pitch + (size_t)x0 * cb;
+            bulk_load(s_next + (size_t)q * m.T * cb, src, bytes_next, &bar);
+        }
+    }
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int4 q = a.tab.ent4[i];
+        RowsEntry<R> e;
+        // offset k of (dy, dz) in the high byte, in-row byte offset below
+        e.off = (a.tab.ent_row[i] << 24) + (q.x * (int)cb + q.w * (int)node_bytes + (1 << 23));
+        if constexpr (sizeof(R) == 4) e.w = a.tab.w32[i];
+        else e.w = a.tab.w64[i];
+        s_ent[i] = e;
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) s_pos[i] = a.tab.pos32[i];
+        else s_pos[i] = a.tab.pos64[i];
+    }
+    for (int i = threadIdx.x; i <= V; i += blockDim.x) s_row[i] = a.tab.row_ptr[i];
+    for (uint32_t i = threadIdx.x; i < own_rows * m.K; i += blockDim.x) s_map[i] = m.blk[2 * m.nbuf + i];
+    if (!block_wait(&bar, 0, a.err)) return;  // uniform across the block
+
+    const PhysR<R>& P = make_phys<R>(a);
+    const R dt2 = (R)2 * P.dt;
+    const uint32_t tile_nodes = Tc * V;
+    for (uint32_t i = threadIdx.x; i < own_rows * m.T * V; i += blockDim.x) {
+        const uint32_t q = fdiv(i, m.div_row_nodes);
+        const uint32_t j = i - q * (m.T * V);
+        if (j >= tile_nodes) continue;
+        const uint32_t xl = fdiv(j, a.divV);
+        const uint32_t l = j - xl * V;
+        const int32_t* map = s_map + q * m.K;
+        const size_t cell_in_row = (size_t)(xl + 1) * cb;
+        const char* own = s_rows + (size_t)map[0] * m.row_buf_bytes + cell_in_row + l * node_bytes;
+        Cx<R> prv[C], H[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const V2 v = reinterpret_cast<const V2*>(own)[c];
+            prv[c] = cx<R>(v.x, v.y);
+            H[c] = cx<R>((R)0, (R)0);
+        }
+        int f0, f1;
+        if (a.tab.uniform_deg > 0) {
+            f0 = (int)l * a.tab.uniform_deg;
+            f1 = f0 + a.tab.uniform_deg;
+        } else {
+            f0 = s_row[l];
+            f1 = s_row[l + 1];
+        }
+        for (int f = f0; f < f1; ++f) {
+            const RowsEntry<R> e = s_ent[f];
+            const int k = e.off >> 24;
+            const int in_row = (e.off & 0xffffff) - (1 << 23);
+            const V2* p = reinterpret_cast<const V2*>(s_rows + (size_t)map[k] * m.row_buf_bytes + cell_in_row + in_row);
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const V2 v = p[c];
+                H[c] += (R)e.w * (cx<R>(v.x, v.y) - prv[c]);
+            }
+        }
+        const uint32_t ry = q % m.RY, rz = q / m.RY;
+        R r[3];
+        r[0] = P.p0[0] + P.bs * ((R)(x0 + xl) * P.bw[0] + s_pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((R)(y0 + ry) * P.bw[1] + s_pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((R)(z0 + rz) * P.bw[2] + s_pos[3 * l + 2]);
+        const R pot = trap<R>(P, r);
+        local_terms<R, C>(P, r, pot, GPE_MODE_LEAPFROG, false, prv, H);
+        V2* o = reinterpret_cast<V2*>(s_next + ((size_t)q * m.T + xl) * cb + l * node_bytes);
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            V2 v = o[c];
+            v.x += dt2 * H[c].y;
+            v.y += dt2 * -H[c].x;
+            o[c] = v;
+        }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (uint32_t q = 0; q < own_rows; ++q) {
+            const uint32_t ry = q % m.RY, rz = q / m.RY;
+            char* dst = a.next + (size_t)(z0 + rz) * a.g.slice + (size_t)(y0 + ry) * a.g.pitch + (size_t)x0 * cb;
+            bulk_store(dst, s_next + (size_t)q * m.T * cb, bytes_next);
+        }
+        bulk_commit();
+        bulk_wait_read_all();
+    }
+}
+
+template <typename R, int C>
+size_t rows_smem_bytes(const StepArgs& a, const RowsArgs& m) {
+    return (size_t)m.nbuf * m.row_buf_bytes + (size_t)m.RY * m.RZ * m.T * a.g.cell_bytes +
+           (size_t)a.tab.entries * sizeof(RowsEntry<R>) + 3 * a.g.V * sizeof(R) + (a.g.V + 1) * 4 + m.RY * m.RZ * m.K * 4;
+}
+
+// blk: device table [nbuf dy][nbuf dz][RY*RZ*K map], built by the host for this shape
+template <typename R, int C>
+cudaError_t launch_leapfrog_rows(const StepArgs& a, uint32_t T, uint32_t RY, uint32_t RZ, uint32_t K, uint32_t nbuf,
+                                 const int32_t* blk, uint32_t threads, cudaStream_t s) {
+    RowsArgs m;
+    m.T = T;
+    m.RY = RY;
+    m.RZ = RZ;
+    m.tiles_x = (a.g.X + T - 1) / T;
+    m.tiles_y = a.g.Y / RY;
+    m.K = K;
+    m.nbuf = nbuf;
+    m.row_buf_bytes = (T + 2) * a.g.cell_bytes;
+    m.div_row_nodes = make_fastdiv(T * a.g.V);
+    m.blk = blk;
+    const size_t smem = rows_smem_bytes<R, C>(a, m);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(leapfrog_rows_kernel<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const uint32_t nodes = RY * RZ * T * a.g.V;
+    const uint32_t cap = RowsLB<R, C>::threads;
+    if (threads == 0) threads = nodes >= cap ? cap : ((nodes + 31) / 32) * 32;
+    if (threads > cap || threads % 32) return cudaErrorInvalidValue;
+    const uint64_t blocks = (uint64_t)m.tiles_x * m.tiles_y * (a.g.Z / RZ);
+    leapfrog_rows_kernel<R, C><<<(unsigned)blocks, threads, smem, s>>>(a, m);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE_ROWS(R, C)                                                                        \
+    template cudaError_t launch_leapfrog_rows<R, C>(const StepArgs&, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, \
+                                                    const int32_t*, uint32_t, cudaStream_t);
+
+}  // namespace gpe
+
+namespace gpe {
+
+// ------------------------------------------------------------ initial states
+
+struct InitArgs {
+    double zeta[5][2];
+    double mu, c0inv, noise_abs, noise_rel;
+    int kappa;
+    uint64_t seed;
+};
+
+// SplitMix64 (Steele, Lea & Flood 2014) output number `counter` (1-based) of stream `seed`.
+__device__ __forceinline__ uint64_t splitmix64_at(uint64_t seed, uint64_t counter) {
+    uint64_t z = seed + counter * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double uniform01_at(uint64_t seed, uint64_t counter) {
+    return ((double)(splitmix64_at(seed, counter) >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+// Thomas-Fermi state psi_m = sqrt(rho_TF) zeta_m (times exp(i kappa phi)), plus
+// noise (abs: noise_abs * N(0,1) per re/im; rel: sqrt(rho) noise_rel N(0,1)), the
+// Gaussians drawn by Box-Muller from SplitMix64 pair number (node * C + m).
+template <typename R, int C>
+__global__ void __launch_bounds__(256) init_kernel(StepArgs a, InitArgs in) {
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= a.total) return;
+    const uint32_t i = (uint32_t)gid;
+    const uint32_t row = fdiv(i, a.divRow);
+    const uint32_t within = i - row * a.row_items;
+    const uint32_t x = fdiv(within, a.divV);
+    const uint32_t l = within - x * a.g.V;
+    const uint32_t z = fdiv(row, a.divY);
+    const uint32_t y = row - z * a.g.Y;
+    const PhysR<double>& P = a.pd;
+    double r[3];
+    r[0] = P.p0[0] + P.bs * ((double)x * P.bw[0] + a.tab.pos64[3 * l + 0]);
+    r[1] = P.p0[1] + P.bs * ((double)y * P.bw[1] + a.tab.pos64[3 * l + 1]);
+    r[2] = P.p0[2] + P.bs * ((double)z * P.bw[2] + a.tab.pos64[3 * l + 2]);
+    const double lx = P.lambda[0] * r[0], ly = P.lambda[1] * r[1], lz = P.lambda[2] * r[2];
+    const double V = 0.5 * (lx * lx + ly * ly + lz * lz);
+    const double rho = fmax(in.mu - V, 0.0) * in.c0inv;
+    const double amp = sqrt(rho);
+    double cph = 1.0, sph = 0.0;
+    if (in.kappa) {
+        const double phi = atan2(r[1], r[0]);
+        cph = cos(in.kappa * phi);
+        sph = sin(in.kappa * phi);
+    }
+    const size_t off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes + l * (C * 2 * sizeof(R));
+    const uint64_t node = gid;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const double zr = in.zeta[c][0] * cph - in.zeta[c][1] * sph;
+        const double zi = in.zeta[c][0] * sph + in.zeta[c][1] * cph;
+        double re = amp * zr, im = amp * zi;
+        if (in.noise_abs != 0.0 || in.noise_rel != 0.0) {
+            const uint64_t pair = node * C + c;
+            const double u1 = uniform01_at(in.seed, 2 * pair + 1), u2 = uniform01_at(in.seed, 2 * pair + 2);
+            const double rr = sqrt(-2.0 * log(u1));
+            const double th = 6.283185307179586 * u2;
+            const double g1 = rr * cos(th), g2 = rr * sin(th);
+            const double s = in.noise_abs + in.noise_rel * amp;
+            re += s * g1;
+            im += s * g2;
+        }
+        stc<R>(a.next + off + c * 2 * sizeof(R), cx<R>((R)re, (R)im));
+    }
+}
+
+template <typename R, int C>
+cudaError_t launch_init(const StepArgs& a, const InitArgs& in, cudaStream_t s) {
+    init_kernel<R, C><<<nblocks(a.total, 256), 256, 0, s>>>(a, in);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE_INIT(R, C) template cudaError_t launch_init<R, C>(const StepArgs&, const InitArgs&, cudaStream_t);
 
 }  // namespace gpe

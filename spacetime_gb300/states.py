@@ -87,9 +87,15 @@ def normalize(buf: np.ndarray, lat: "capi.Lattice", params: "capi.Params") -> np
     return buf / math.sqrt(n)
 
 
+def tf_mu(c0: float, lam=(1.0, 1.0, 1.0)) -> float:
+    lx, ly, lz = lam
+    return 0.5 * (15.0 * c0 * lx * ly * lz / (4.0 * math.pi)) ** 0.4
+
+
 def vortex_state(lat, params, seed=1, noise=1e-3, kappa=1) -> np.ndarray:
     """Scalar: Thomas-Fermi amplitude times exp(i kappa phi) (a straight z-vortex),
-    plus complex Gaussian noise of amplitude noise*max|psi0|, normalised to 1."""
+    plus complex Gaussian noise of amplitude noise * sqrt(mu/c0) (the TF peak
+    amplitude), normalised to 1.  Same numbers as gpe_init_state."""
     r = node_positions(lat, params)
     lam = tuple(params.trap_lambda[i] for i in range(3))
     amp = np.sqrt(thomas_fermi_density(r, params.c0, lam))
@@ -99,7 +105,7 @@ def vortex_state(lat, params, seed=1, noise=1e-3, kappa=1) -> np.ndarray:
     psi[..., 0, 1] = amp * np.sin(kappa * phi)
     if noise:
         g = gaussian_pairs(seed, psi[..., 0, 0].size).reshape(psi.shape[:4] + (2,))
-        psi[..., 0, :] += noise * float(amp.max()) * g
+        psi[..., 0, :] += noise * math.sqrt(tf_mu(params.c0, lam) / params.c0) * g
     return normalize(_embed(psi), lat, params)
 
 

@@ -65,6 +65,10 @@ class Stepper:
         capi.check(self.lib.gpe_download(self._h, slot, out.ctypes.data_as(C.POINTER(C.c_double)), out.size, self.stream), "gpe_download")
         return out
 
+    def init_state(self, slot: int, init: "capi.Init"):
+        """Seeded Thomas-Fermi state written on the device (gpe_init_state)."""
+        capi.check(self.lib.gpe_init_state(self._h, slot, C.byref(init), self.stream), "gpe_init_state")
+
     def buffer(self, slot: int):
         p = capi.Pitched()
         cb = C.c_size_t()
@@ -102,6 +106,14 @@ class Stepper:
         v = C.c_int32()
         capi.check(self.lib.gpe_get_tuning(self._h, key, C.byref(v)), "gpe_get_tuning")
         return v.value
+
+    def autotune(self, steps: int = 10) -> list:
+        """Pick the fastest step kernel / tile shape for this handle (gpe_autotune)."""
+        import json
+
+        buf = C.create_string_buffer(1 << 16)
+        capi.check(self.lib.gpe_autotune(self._h, steps, buf, len(buf), self.stream), "gpe_autotune")
+        return json.loads(buf.value.decode() or "[]")
 
     @property
     def current(self) -> int:

@@ -311,3 +311,142 @@ def test_tile_kernel_rejected_for_unaligned_cells(gpu):
         with pytest.raises(capi.GpeError):
             s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_TILE)
         assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C,dims,shape", [
+    ("bcc", 3, (8, 4, 5), (4, 2, 2)),      # partial last z-chunk
+    ("bcc", 3, (16, 6, 7), (8, 3, 3)),
+    ("bcc", 1, (12, 4, 4), (6, 4, 4)),
+    ("bcc", 5, (8, 4, 6), (8, 2, 5)),
+    ("bcc227", 1, (6, 6, 3), (3, 1, 1)),
+    ("fcc", 3, (8, 4, 5), (4, 2, 3)),       # per-node degree 4 or 8
+    ("a15", 3, (4, 2, 3), (2, 1, 2)),
+    ("z", 1, (4, 4, 3), (2, 2, 2)),
+    ("c15", 1, (2, 2, 3), (1, 1, 2)),
+])
+def test_march_kernel(gpu, name, C, dims, shape, prec):
+    """2.5-D z-march kernel (ring of shared-memory slabs filled by bulk copies)
+    against the oracle over three steps, with explicit tile shapes."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, prec, dims)
+    even, odd = _rand(lat, p, 111), _rand(lat, p, 112)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_TILE_CELLS, shape[0])
+        s.set_tuning(capi.TUNE_TILE_ROWS, shape[1])
+        s.set_tuning(capi.TUNE_ZCHUNK, shape[2])
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_MARCH)
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_MARCH
+        assert s.get_tuning(capi.TUNE_TILE_ROWS) == shape[1]
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        bufs = [capi.PSI_EVEN, capi.PSI_ODD]
+        for n in range(3):
+            s.step_explicit(bufs[(n + 1) % 2], bufs[n % 2], f, t=0.1 * n)
+        ge, go = s.download(capi.PSI_EVEN), s.download(capi.PSI_ODD)
+    b = [even, odd]
+    for n in range(3):
+        oracle.parabolic_step(lat, p, f, 0.1 * n, oracle.LEAPFROG, b[(n + 1) % 2], b[n % 2])
+    _close(ge, even, prec, "even")
+    _close(go, odd, prec, "odd")
+
+
+def test_kernel_choice_on_config2_shape(gpu):
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, capi.FP32, (96, 96, 96))
+    with Stepper(lat, p) as s:
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_TILE
+        assert s.get_tuning(capi.TUNE_TILE_CELLS) == 16
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_ROWS)
+        assert s.get_tuning(capi.TUNE_TILE_CELLS) == 8
+        assert (s.get_tuning(capi.TUNE_TILE_ROWS), s.get_tuning(capi.TUNE_ZCHUNK)) == (2, 2)
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C,dims,tile", [("bcc", 3, (17, 3, 4), 5), ("bcc", 1, (7, 5, 4), 0), ("bcc", 5, (9, 3, 3), 4),
+                                              ("fcc", 3, (7, 4, 3), 3), ("a15", 3, (5, 3, 2), 2), ("z", 1, (5, 3, 3), 0),
+                                              ("c15", 5, (3, 2, 2), 1), ("c15", 1, (4, 3, 2), 2), ("bcc227", 1, (6, 4, 3), 6)])
+@pytest.mark.parametrize("block", [(0, 0, 0), (1, 1, 0), (2, 1, 64), (1, 2, 32)])
+def test_rows_kernel(gpu, name, C, dims, tile, prec, block):
+    """Row-block kernel (every row the stencil touches staged in shared memory) over
+    three steps; partial last tiles, per-node degrees 4/8 (FCC), explicit RY x RZ
+    blocks and thread counts smaller than the node count included."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, prec, dims)
+    even, odd = _rand(lat, p, 121), _rand(lat, p, 122)
+    f = capi.make_fields(**FIELDS)
+    ry, rz, threads = block
+    if ry and (dims[1] % ry or dims[2] % rz):
+        pytest.skip("block does not divide the grid")
+    with Stepper(lat, p) as s:
+        if tile:
+            s.set_tuning(capi.TUNE_TILE_CELLS, tile)
+        if ry:
+            s.set_tuning(capi.TUNE_TILE_ROWS, ry)
+            s.set_tuning(capi.TUNE_ZCHUNK, rz)
+        if threads:
+            s.set_tuning(capi.TUNE_THREADS, threads)
+        try:
+            s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_ROWS)
+        except capi.GpeError as e:
+            if e.status == 6 and (ry > 1 or rz > 1):
+                pytest.skip("row block does not fit in shared memory")
+            raise
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_ROWS)
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_ROWS
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        bufs = [capi.PSI_EVEN, capi.PSI_ODD]
+        for n in range(3):
+            s.step_explicit(bufs[(n + 1) % 2], bufs[n % 2], f, t=0.1 * n)
+        ge, go = s.download(capi.PSI_EVEN), s.download(capi.PSI_ODD)
+    b = [even, odd]
+    for n in range(3):
+        oracle.parabolic_step(lat, p, f, 0.1 * n, oracle.LEAPFROG, b[(n + 1) % 2], b[n % 2])
+    _close(ge, even, prec, "even")
+    _close(go, odd, prec, "odd")
+
+
+def test_autotune_keeps_state_and_picks_a_kernel(gpu):
+    """gpe_autotune restores the state, and stepping after it still matches the oracle."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, capi.FP32, (16, 4, 4))
+    even, odd = _rand(lat, p, 131), _rand(lat, p, 132)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        rep = s.autotune(steps=3)
+        assert len(rep) >= 3 and all(r["ms"] > 0 for r in rep)
+        best = min(rep, key=lambda r: r["ms"])
+        assert s.get_tuning(capi.TUNE_KERNEL) in (best["kernel"], capi.KERNEL_ROWS, capi.KERNEL_TILE, capi.KERNEL_GATHER)
+        np.testing.assert_array_equal(s.download(capi.PSI_EVEN), even.astype(np.float32).astype(np.float64))
+        s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.0)
+        got = s.download(capi.PSI_ODD)
+    oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, odd, even)
+    _close(got, odd, capi.FP32)
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C,kind", [("bcc", 1, "vortex"), ("bcc", 3, "polar"), ("c15", 5, "cyclic")])
+def test_device_initial_state_matches_numpy(gpu, name, C, kind, prec):
+    """gpe_init_state reproduces states.vortex_state / spinor_state (SplitMix64 +
+    Box-Muller, same counters) to rounding."""
+    lat = capi.Lattice(name)
+    dims = (6, 5, 4) if lat.nodes < 40 else (3, 2, 2)
+    p = _params(lat, C, prec, dims, c0=2000.0, trap_lambda=(1.0, 1.0, 1.0), block_scale=16.0 / (dims[0] * lat.block_width[0]))
+    if kind == "vortex":
+        want = states.vortex_state(lat, p, seed=5, noise=1e-2, kappa=1)
+        init = capi.make_init(zeta=(1.0,), kappa=1, noise_abs=1e-2, seed=5)
+    else:
+        zeta = states.POLAR if kind == "polar" else states.CYCLIC
+        want = states.spinor_state(lat, p, zeta, seed=6, noise=1e-2)
+        init = capi.make_init(zeta=zeta, noise_rel=1e-2, seed=6)
+    with Stepper(lat, p) as s:
+        s.init_state(capi.PSI_ODD, init)
+        assert s.current == capi.PSI_ODD
+        got = s.download(capi.PSI_ODD)
+        assert s.observe(capi.PSI_ODD)["norm"] == pytest.approx(1.0, rel=1e-12 if prec == capi.FP64 else 1e-6)
+    tol = 1e-12 if prec == capi.FP64 else 1e-6
+    assert np.max(np.abs(got - want)) <= tol * np.max(np.abs(want))
