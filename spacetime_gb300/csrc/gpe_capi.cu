@@ -33,6 +33,8 @@ template <typename R, int C>
 cudaError_t launch_leapfrog_rows(const StepArgs& a, uint32_t T, uint32_t RY, uint32_t RZ, uint32_t K, uint32_t nbuf,
                                  const int32_t* blk, uint32_t threads, cudaStream_t s);
 template <typename R, int C>
+cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s);
+template <typename R, int C>
 cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads, cudaStream_t s);
 cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
                             uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
@@ -321,7 +323,7 @@ static gpe_status build_tables(gpe_handle* h) {
     h->tab.entries = n;
     if (L.E > 0) {
         const int F = L.F;
-        std::vector<int32_t> inc_off(L.V * F), efrom(L.E), eto(L.E);
+        std::vector<int32_t> inc_off(L.V * F), efrom(L.E), eto(L.E), inc_soff(L.V * F), eto_s(L.E);
         std::vector<double> iw64(L.V * F);
         std::vector<float> iw32(L.V * F);
         for (int i = 0; i < L.V * F; ++i) {
@@ -330,6 +332,8 @@ static gpe_status build_tables(gpe_handle* h) {
                                   (long long)r.dx * g.qcell_bytes + (long long)r.edge * node_bytes;
             if (off > INT32_MAX || off < INT32_MIN) return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
             inc_off[i] = (int32_t)off;
+            inc_soff[i] = (r.dy == 0 && r.dz == 0) ? (int32_t)((long long)r.dx * g.qcell_bytes + (long long)r.edge * node_bytes)
+                                                  : INT32_MIN;
             iw64[i] = (-0.5 * r.hodge) / bs2;
             iw32[i] = (float)iw64[i];
         }
@@ -340,12 +344,16 @@ static gpe_status build_tables(gpe_handle* h) {
                                   (long long)r.dx * g.cell_bytes + (long long)r.to * node_bytes;
             if (off > INT32_MAX || off < INT32_MIN) return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit offsets");
             eto[e] = (int32_t)off;
+            eto_s[e] = (r.dy == 0 && r.dz == 0) ? (int32_t)((long long)r.dx * g.cell_bytes + (long long)r.to * node_bytes)
+                                                : INT32_MIN;
         }
         if ((st = upload_table(h, inc_off, &h->tab.inc_off))) return st;
         if ((st = upload_table(h, iw64, &h->tab.inc_w64))) return st;
         if ((st = upload_table(h, iw32, &h->tab.inc_w32))) return st;
         if ((st = upload_table(h, efrom, &h->tab.e_from_off))) return st;
         if ((st = upload_table(h, eto, &h->tab.e_to_off))) return st;
+        if ((st = upload_table(h, eto_s, &h->tab.e_to_soff))) return st;
+        if ((st = upload_table(h, inc_soff, &h->tab.inc_soff))) return st;
         h->tab.faces = F;
     }
     return GPE_OK;
@@ -868,6 +876,41 @@ static cudaError_t dispatch_tile(const gpe_handle* h, const StepArgs& a, uint32_
     }
 }
 
+// Hyperbolic row-tile kernel eligibility and tile length (0 = gather kernel).
+static uint32_t hyper_tile_cells(const gpe_handle* h) {
+    if (h->tune_kernel == 1 || h->g.E == 0) return 0;
+    if (h->g.cell_bytes % 16 != 0 || h->g.qcell_bytes % 16 != 0) return 0;
+    const uint32_t per = h->g.V + h->g.E;
+    uint32_t T = h->tune_tile > 0 ? (uint32_t)h->tune_tile : 0;
+    if (T == 0) {
+        T = 576 / per > 0 ? 576 / per : 1;
+        if (T > h->g.X) T = h->g.X;
+        for (uint32_t t = T; t * 2 > T && t > 0; --t)
+            if (h->g.X % t == 0) {
+                T = t;
+                break;
+            }
+    }
+    if (T == 0 || T > h->g.X || (uint64_t)T * per > 4096) return 0;
+    const size_t smem = (size_t)(2 * T + 2) * (h->g.cell_bytes + h->g.qcell_bytes) +
+                        (size_t)h->g.V * h->lat.F * (8 + h->real_bytes) + (size_t)(3 * h->g.E + 1) * 4 +
+                        3 * h->g.V * h->real_bytes;
+    if (smem > 200 * 1024) return 0;
+    return T;
+}
+
+template <int C>
+static cudaError_t dispatch_hyper_tile_c(const gpe_handle* h, const StepArgs& a, uint32_t T, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_hyper_tile<double, C>(a, T, s) : launch_hyper_tile<float, C>(a, T, s);
+}
+static cudaError_t dispatch_hyper_tile(const gpe_handle* h, const StepArgs& a, uint32_t T, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_hyper_tile_c<1>(h, a, T, s);
+        case 3: return dispatch_hyper_tile_c<3>(h, a, T, s);
+        default: return dispatch_hyper_tile_c<5>(h, a, T, s);
+    }
+}
+
 static double cell_dv(const gpe_handle* h) {
     const double bs = h->p.block_scale;
     return bs * bs * bs * h->lat.volume;  // volume = bs^3 * VOLUME (Spin1GpeBCC.cu:1385)
@@ -899,7 +942,9 @@ static gpe_status one_step(gpe_handle* h, int next, int prev, const gpe_fields& 
         const int qnext = next == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
         a.q = h->interior[qprev];
         a.qnext = h->interior[qnext];
-        e = dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
+        const uint32_t T = hyper_tile_cells(h);
+        if (T > 0) e = dispatch_hyper_tile(h, a, T, s);
+        else e = dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
         h->launches += 1;
     }
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");

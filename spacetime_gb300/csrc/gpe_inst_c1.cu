@@ -13,6 +13,8 @@ GPE_INSTANTIATE_ROWS(float, 1)
 GPE_INSTANTIATE_ROWS(double, 1)
 GPE_INSTANTIATE_INIT(float, 1)
 GPE_INSTANTIATE_INIT(double, 1)
+GPE_INSTANTIATE_HYPER_TILE(float, 1)
+GPE_INSTANTIATE_HYPER_TILE(double, 1)
 
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s) {
     if (precision == GPE_FP64) {

@@ -13,4 +13,6 @@ GPE_INSTANTIATE_ROWS(float, 3)
 GPE_INSTANTIATE_ROWS(double, 3)
 GPE_INSTANTIATE_INIT(float, 3)
 GPE_INSTANTIATE_INIT(double, 3)
+GPE_INSTANTIATE_HYPER_TILE(float, 3)
+GPE_INSTANTIATE_HYPER_TILE(double, 3)
 }  // namespace gpe

@@ -13,4 +13,6 @@ GPE_INSTANTIATE_ROWS(float, 5)
 GPE_INSTANTIATE_ROWS(double, 5)
 GPE_INSTANTIATE_INIT(float, 5)
 GPE_INSTANTIATE_INIT(double, 5)
+GPE_INSTANTIATE_HYPER_TILE(float, 5)
+GPE_INSTANTIATE_HYPER_TILE(double, 5)
 }  // namespace gpe

@@ -115,6 +115,8 @@ struct DevTables {
     float* inc_w32;
     int32_t* e_from_off;  // E: byte offset of from-node in own psi cell
     int32_t* e_to_off;    // E: byte offset of to-node relative to own psi cell base
+    int32_t* e_to_soff;   // E: the same inside a contiguous row of cells, INT32_MIN if off-row
+    int32_t* inc_soff;    // V*F: incident edge inside a contiguous row of q cells, INT32_MIN if off-row
     int4* ent4;           // entries: (dx, dy, dz, node)
     int32_t* ent_row;     // entries: index of the (dy, dz) row in the multi-row tile
     int entries;

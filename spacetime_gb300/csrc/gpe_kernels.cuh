@@ -1543,3 +1543,201 @@ cudaError_t launch_init(const StepArgs& a, const InitArgs& in, cudaStream_t s) {
 #define GPE_INSTANTIATE_INIT(R, C) template cudaError_t launch_init<R, C>(const StepArgs&, const InitArgs&, cudaStream_t);
 
 }  // namespace gpe
+
+namespace gpe {
+
+// ------------------------------------------------- hyperbolic row tiles (TMA)
+
+// Fused hyperbolic psi+q leapfrog step on a row tile of T cells.  One bulk copy
+// each brings psi_prev and q_prev of cells [x0-1, x0+T] and the old psi_next and
+// q_next of [x0, x0+T) into shared memory; threads [0, T*V) update nodes and
+// threads [T*V, T*(V+E)) update edges.  In-row neighbours (the d1 incidences of a
+// node, the d0 end points of an edge) are read from shared memory, off-row ones
+// from global memory (L2).  Both updated tiles go back by bulk stores.  Requires
+// cell_bytes and qcell_bytes to be multiples of 16.
+template <typename R, int C>
+__global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T, uint32_t tiles_per_row) {
+    extern __shared__ __align__(128) unsigned char dyn[];
+    __shared__ __align__(8) uint64_t bar;
+    using V2 = typename Vec2<R>::type;
+    const uint32_t cb = a.g.cell_bytes, qb = a.g.qcell_bytes;
+    const int V = a.g.V, E = a.g.E, F = a.tab.faces;
+    char* s_psi = reinterpret_cast<char*>(dyn);                  // (T+2) psi cells
+    char* s_q = s_psi + (size_t)(T + 2) * cb;                    // (T+2) q cells
+    char* s_psin = s_q + (size_t)(T + 2) * qb;                   // T psi cells
+    char* s_qn = s_psin + (size_t)T * cb;                        // T q cells
+    int32_t* s_inc_soff = reinterpret_cast<int32_t*>(s_qn + (size_t)T * qb);  // V*F
+    int32_t* s_inc_goff = s_inc_soff + V * F;
+    R* s_inc_w = reinterpret_cast<R*>(s_inc_goff + V * F);
+    int32_t* s_e_from = reinterpret_cast<int32_t*>(s_inc_w + V * F);          // E
+    int32_t* s_e_tos = s_e_from + E;
+    int32_t* s_e_tog = s_e_tos + E;
+    R* s_pos = reinterpret_cast<R*>(s_e_tog + E + (E & 1));                    // 3V (8-aligned)
+
+    const uint32_t tile = blockIdx.x % tiles_per_row;
+    const uint32_t row = blockIdx.x / tiles_per_row;
+    const uint32_t z = fdiv(row, a.divY);
+    const uint32_t y = row - z * a.g.Y;
+    const uint32_t x0 = tile * T;
+    const uint32_t Tc = min(T, a.g.X - x0);
+    const char* g_psi = a.prev + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x0 * cb - cb;
+    const char* g_q = a.q + (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x0 * qb - qb;
+    char* g_psin = a.next + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x0 * cb;
+    char* g_qn = a.qnext + (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x0 * qb;
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, (Tc + 2) * (cb + qb) + Tc * (cb + qb));
+        bulk_load(s_psi, g_psi, (Tc + 2) * cb, &bar);
+        bulk_load(s_q, g_q, (Tc + 2) * qb, &bar);
+        bulk_load(s_psin, g_psin, Tc * cb, &bar);
+        bulk_load(s_qn, g_qn, Tc * qb, &bar);
+    }
+    for (int i = threadIdx.x; i < V * F; i += blockDim.x) {
+        s_inc_soff[i] = a.tab.inc_soff[i];
+        s_inc_goff[i] = a.tab.inc_off[i];
+        if constexpr (sizeof(R) == 4) s_inc_w[i] = a.tab.inc_w32[i];
+        else s_inc_w[i] = a.tab.inc_w64[i];
+    }
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        s_e_from[i] = a.tab.e_from_off[i];
+        s_e_tos[i] = a.tab.e_to_soff[i];
+        s_e_tog[i] = a.tab.e_to_off[i];
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) s_pos[i] = a.tab.pos32[i];
+        else s_pos[i] = a.tab.pos64[i];
+    }
+    if (!block_wait(&bar, 0, a.err)) return;  // uniform across the block
+
+    const PhysR<R>& P = make_phys<R>(a);
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    for (uint32_t i = threadIdx.x; i < T * (V + E); i += blockDim.x) {
+        if (i < T * V) {
+            if (i >= Tc * V) continue;
+            const uint32_t xl = fdiv(i, a.divV);
+            const uint32_t l = i - xl * V;
+            const char* own = s_psi + (size_t)(xl + 1) * cb + l * node_bytes;
+            Cx<R> prv[C], H[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const V2 v = reinterpret_cast<const V2*>(own)[c];
+                prv[c] = cx<R>(v.x, v.y);
+                H[c] = cx<R>((R)0, (R)0);
+            }
+            // d1 of q (RelativisticSpin2Gpe.cu:1051-1066)
+            const char* s_qcell = s_q + (size_t)(xl + 1) * qb;
+            const char* g_qcell = g_q + (size_t)(xl + 1) * qb;
+            for (int k = 0; k < F; ++k) {
+                const int so = s_inc_soff[l * F + k];
+                const R w = s_inc_w[l * F + k];
+                if (so != INT32_MIN) {
+                    const V2* p = reinterpret_cast<const V2*>(s_qcell + so);
+#pragma unroll
+                    for (int c = 0; c < C; ++c) {
+                        const V2 v = p[c];
+                        H[c] += w * cx<R>(v.x, v.y);
+                    }
+                } else {
+                    const char* g = g_qcell + s_inc_goff[l * F + k];
+#pragma unroll
+                    for (int c = 0; c < C; ++c) H[c] += w * ldc<R>(g + c * 2 * sizeof(R));
+                }
+            }
+            R r[3];
+            r[0] = P.p0[0] + P.bs * ((R)(x0 + xl) * P.bw[0] + s_pos[3 * l + 0]);
+            r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + s_pos[3 * l + 1]);
+            r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + s_pos[3 * l + 2]);
+            const R pot = trap<R>(P, r);
+            if constexpr (C == 1) {
+                local_scalar<R>(P, pot, false, true, prv, H);
+            } else if constexpr (C == 3) {
+                local_spin1<R>(P, r, pot, true, false, true, prv, H);
+            } else {
+                local_spin2<R>(P, r, pot, true, false, true, prv, H);
+            }
+            V2* o = reinterpret_cast<V2*>(s_psin + (size_t)xl * cb + l * node_bytes);
+            const R dt2 = (R)2 * P.dt;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                V2 v = o[c];
+                v.x += dt2 * H[c].y;
+                v.y += dt2 * -H[c].x;
+                o[c] = v;
+            }
+        } else {
+            // q update (RelativisticSpin2Gpe.cu:986-1015)
+            const uint32_t j = i - T * V;
+            const uint32_t xl = fdiv(j, a.divE);
+            if (xl >= Tc) continue;
+            const uint32_t e = j - xl * E;
+            const char* s_cell = s_psi + (size_t)(xl + 1) * cb;
+            const char* thisp = s_cell + s_e_from[e];
+            const int ts = s_e_tos[e];
+            const bool to_in_row = ts != INT32_MIN;
+            const char* otherp = to_in_row ? s_cell + ts : g_psi + (size_t)(xl + 1) * cb + s_e_tog[e];
+            const char* qprev = s_q + (size_t)(xl + 1) * qb + e * node_bytes;
+            V2* qn = reinterpret_cast<V2*>(s_qn + (size_t)xl * qb + e * node_bytes);
+            const R dts2 = (R)2 * P.dts;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                const V2 tv = reinterpret_cast<const V2*>(thisp)[c];
+                Cx<R> ov;
+                if (to_in_row) {
+                    const V2 w2 = reinterpret_cast<const V2*>(otherp)[c];
+                    ov = cx<R>(w2.x, w2.y);
+                } else {
+                    ov = ldc<R>(otherp + c * 2 * sizeof(R));
+                }
+                const Cx<R> d0psi = ov - cx<R>(tv.x, tv.y);
+                const V2 pq = reinterpret_cast<const V2*>(qprev)[c];
+                const Cx<R> qq = dts2 * (cx<R>(pq.x, pq.y) + d0psi);
+                V2 v = qn[c];
+                v.x += -qq.y;
+                v.y += qq.x;
+                qn[c] = v;
+            }
+        }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bulk_store(g_psin, s_psin, Tc * cb);
+        bulk_store(g_qn, s_qn, Tc * qb);
+        bulk_commit();
+        bulk_wait_read_all();
+    }
+}
+
+template <typename R, int C>
+size_t hyper_tile_smem_bytes(const StepArgs& a, uint32_t T) {
+    const int V = a.g.V, E = a.g.E, F = a.tab.faces;
+    return (size_t)(2 * T + 2) * (a.g.cell_bytes + a.g.qcell_bytes) + (size_t)V * F * (8 + sizeof(R)) +
+           (size_t)(3 * E + (E & 1)) * 4 + 3 * V * sizeof(R);
+}
+
+template <typename R, int C>
+cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
+    const uint32_t tiles = (a.g.X + T - 1) / T;
+    const uint32_t tasks = T * (a.g.V + a.g.E);
+    const uint32_t threads = tasks >= 1024 ? 1024 : ((tasks + 31) / 32) * 32;
+    const size_t smem = hyper_tile_smem_bytes<R, C>(a, T);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(hyper_tile_kernel<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    const uint64_t blocks = (uint64_t)tiles * a.g.Y * a.g.Z;
+    hyper_tile_kernel<R, C><<<(unsigned)blocks, threads, smem, s>>>(a, T, tiles);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE_HYPER_TILE(R, C) template cudaError_t launch_hyper_tile<R, C>(const StepArgs&, uint32_t, cudaStream_t);
+
+}  // namespace gpe

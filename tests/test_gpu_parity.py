@@ -113,18 +113,26 @@ def test_euler_and_itp_modes(gpu, C, mode, prec):
         _close(hp, href, prec, "hpsi")
 
 
+@pytest.mark.parametrize("kernel,tile", [(capi.KERNEL_GATHER, 0), (capi.KERNEL_AUTO, 0), (capi.KERNEL_AUTO, 4)])
 @pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
 @pytest.mark.parametrize("name,C", [("bcc", 1), ("bcc", 3), ("bcc", 5), ("bcc227", 1), ("cube", 3), ("c15", 5), ("c15", 1)])
-def test_hyperbolic_fused_step(gpu, name, C, prec):
+def test_hyperbolic_fused_step(gpu, name, C, prec, kernel, tile):
     """One fused launch = update_psi + update_q (RelativisticSpin2Gpe.cu:971-1132,
-    RelativisticSpin1Gpe common/hyper kernels, RelativisticGpeBCC.cu:179-255)."""
+    RelativisticSpin1Gpe common/hyper kernels, RelativisticGpeBCC.cu:179-255): the
+    gather kernel, the TMA row-tile kernel (automatic where cells are 16-byte
+    multiples), and partial row tiles."""
     lat = capi.Lattice(name)
     dims = (4, 3, 3) if lat.nodes > 40 else (6, 5, 4)
+    if tile and lat.nodes > 40:
+        tile = 3
     p = _params(lat, C, prec, dims, scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01)
     pe, po = _rand(lat, p, 41), _rand(lat, p, 42)
     qe, qo = _rand(lat, p, 43, edges=True), _rand(lat, p, 44, edges=True)
     f = capi.make_fields(**FIELDS)
     with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_KERNEL, kernel)
+        if tile:
+            s.set_tuning(capi.TUNE_TILE_CELLS, tile)
         for slot, a in ((capi.PSI_EVEN, pe), (capi.PSI_ODD, po), (capi.Q_EVEN, qe), (capi.Q_ODD, qo)):
             s.upload(slot, a)
         s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.2)
