@@ -313,6 +313,31 @@ gpe_status gpe_observe_noalloc(const gpe_lattice_desc* lat, const gpe_params* p,
                                double t, const void* psi, size_t pitch, size_t slice_pitch,
                                gpe_observables* out, void* stream);
 
+/* Reverse-mode derivatives of a field-ramp run (parabolic scheme).  No
+ * counterpart in the reference, which only runs forward; the forward run these
+ * differentiate is its time loop (forwardEuler + leapfrog, Spin1GpeBCC.cu:1428-1603).
+ *
+ * gpe_adjoint_forward runs n_steps steps from the state in GPE_PSI_ODD: the
+ * forward-Euler start (step 0) and n_steps-1 leapfrog steps, step j using
+ * fields[j] at time t_j = t0 + j*dt (t0 from gpe_set_ramp, else 0) -- the same
+ * steps gpe_start + gpe_step(n_steps-1) take with a ramp whose value at t_j is
+ * fields[j].  It keeps checkpoints (u_{kS}, u_{kS+1}) every `stride` steps
+ * (stride <= 0: ceil(sqrt(n_steps))) in device memory owned by the handle, and
+ * writes out[5] = (Re <T|u_N>, Im <T|u_N>, M_x, M_y, M_z): the overlap with
+ * `target` (host FP64, file layout, `count` doubles) and the magnetization of
+ * the final state, integrated with dv as gpe_observe does.  Synchronises.
+ *
+ * gpe_adjoint_backward takes seed[5] = dL/d(out[k]) for a loss L of those five
+ * numbers and writes grad[4*j + m] = dL/d(field m of step j) for
+ * m = 0: bq, 1..3: bb[0..2] (n_steps x 4 doubles).  It recomputes the states of
+ * one checkpoint segment at a time with the forward kernel and runs the adjoint
+ * (reverse-time) kernel of the step back through it.  Valid while no other call
+ * has written the handle's psi buffers since gpe_adjoint_forward; may be called
+ * again with another seed.  Synchronises. */
+gpe_status gpe_adjoint_forward(gpe_handle* h, int32_t n_steps, const gpe_fields* fields, int32_t stride,
+                               const double* target, size_t count, double* out, void* stream);
+gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, double* grad, void* stream);
+
 /* Number of CUDA kernel launches this handle has issued (for accounting). */
 uint64_t gpe_launch_count(const gpe_handle* h);
 

@@ -315,6 +315,8 @@ def load_library(path: str = LIB_PATH):
         "gpe_autotune": (C.c_int, [vp, C.c_int32, C.c_char_p, C.c_size_t, vp]),
         "gpe_observe_noalloc": (C.c_int, [P(LatticeDesc), P(Params), P(Fields), C.c_double, vp, C.c_size_t, C.c_size_t, P(Observables), vp]),
         "gpe_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
+        "gpe_adjoint_forward": (C.c_int, [vp, C.c_int32, P(Fields), C.c_int32, P(C.c_double), C.c_size_t, P(C.c_double), vp]),
+        "gpe_adjoint_backward": (C.c_int, [vp, P(C.c_double), P(C.c_double), vp]),
         "gpe_sites": (C.c_uint64, [vp]),
         "gpe_last_error": (C.c_char_p, []),
         "gpe_version": (C.c_char_p, []),

@@ -1,0 +1,609 @@
+// gpe_adjoint.cu -- reverse-mode (adjoint) derivative of the parabolic leapfrog
+// run with respect to the per-step magnetic fields, with sqrt(N) checkpointing.
+//
+// Forward run of N steps from u_0 (the reference's time loop, Spin1GpeBCC.cu:1428-1603):
+//     u_1     = u_0 + (1/2) F_0(u_0)                    forwardEuler, :667-791
+//     u_{j+1} = u_{j-1} + F_j(u_j),   j = 1..N-1         leapfrog,     :793-917
+// with F_j(u) = 2 dt (-i) H(u; B_j, t_j) u and t_j = t0 + j dt.  For a loss L(u_N)
+// the discrete adjoint lambda_j = dL/du_j obeys the same leapfrog backwards,
+//     lambda_j = lambda_{j+2} + (dF_j/du)^T lambda_{j+1},   lambda_{N+1} = 0,
+// and dL/dB_j = (dF_j/dB)^T lambda_{j+1} (dt instead of 2 dt for j = 0).  With
+// b = i lambda_{j+1} (i times a vector is the transpose of -i times one):
+//     (dF_j/du)^T lambda = 2 dt [ L^T b + (dh/du)^T b ],
+// L the DEC Laplacian (L^T takes each entry's weight from its reverse entry) and
+// h(u) the local part of H(u) u (trap, interaction, Zeeman, loss).  The local
+// Jacobian-transpose products are exact: the step kernels' own local_terms
+// templates evaluated on forward-mode dual numbers, once per real coordinate of
+// the node (2C evaluations) and once per field parameter (Bq, Bb.x, Bb.y, Bb.z).
+//
+// Checkpointing: the forward run keeps (u_{kS}, u_{kS+1}) for every segment k of
+// S steps; the reverse run recomputes one segment at a time from its pair with the
+// forward step kernel itself (bit-identical states) and walks it backwards.
+// Memory: 2 ceil(N/S) + S - 2 state buffers; S = ceil(sqrt(N)) by default.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "gpe_handle.h"
+#include "gpe_kernels.cuh"
+
+namespace gpe {
+
+// ------------------------------------------------------------- dual numbers
+
+template <typename R>
+struct Dual {
+    R v, d;
+    __device__ __forceinline__ Dual() {}
+    __device__ __forceinline__ Dual(double x) : v((R)x), d((R)0) {}
+    __device__ __forceinline__ Dual(R x, R dx) : v(x), d(dx) {}
+};
+template <typename R>
+__device__ __forceinline__ Dual<R> operator+(Dual<R> a, Dual<R> b) { return Dual<R>(a.v + b.v, a.d + b.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R> operator-(Dual<R> a, Dual<R> b) { return Dual<R>(a.v - b.v, a.d - b.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R> operator-(Dual<R> a) { return Dual<R>(-a.v, -a.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R> operator*(Dual<R> a, Dual<R> b) { return Dual<R>(a.v * b.v, a.d * b.v + a.v * b.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R>& operator+=(Dual<R>& a, Dual<R> b) {
+    a.v += b.v;
+    a.d += b.d;
+    return a;
+}
+
+template <typename R>
+__device__ __forceinline__ Dual<R> cd(R v) { return Dual<R>(v, (R)0); }
+
+template <typename R>
+__device__ __forceinline__ PhysR<Dual<R>> dual_phys(const PhysR<R>& P) {
+    PhysR<Dual<R>> Q;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        Q.p0[i] = cd<R>(P.p0[i]);
+        Q.bw[i] = cd<R>(P.bw[i]);
+        Q.lambda[i] = cd<R>(P.lambda[i]);
+        Q.qc[i] = cd<R>(P.qc[i]);
+        Q.bb[i] = cd<R>(P.bb[i]);
+        Q.bbq[i] = cd<R>(P.bbq[i]);
+    }
+    Q.bs = cd<R>(P.bs);
+    Q.trap_offset = cd<R>(P.trap_offset);
+    Q.c0 = cd<R>(P.c0);
+    Q.c2 = cd<R>(P.c2);
+    Q.c4 = cd<R>(P.c4);
+    Q.alpha = cd<R>(P.alpha);
+    Q.sigma = cd<R>(P.sigma);
+    Q.bq = cd<R>(P.bq);
+    Q.bqq = cd<R>(P.bqq);
+    Q.dt = cd<R>(P.dt);
+    Q.dts = cd<R>(P.dts);
+    Q.trap_on = P.trap_on;
+    Q.flags = P.flags;
+    return Q;
+}
+
+// sum_c (b_c . dH_c) over the derivative parts of a dual evaluation
+template <typename R, int C>
+__device__ __forceinline__ R dot_d(const Cx<R>* b, const Cx<Dual<R>>* H) {
+    R s = 0;
+#pragma unroll
+    for (int c = 0; c < C; ++c) s += b[c].x * H[c].x.d + b[c].y * H[c].y.d;
+    return s;
+}
+
+// Local spin density <F> (unnormalised), the quantity gpe_observe integrates.
+template <typename R, int C>
+__device__ __forceinline__ void local_mag(const Cx<R>* ps, R M[3]) {
+    if constexpr (C == 3) {
+        const Cx<R> m = (R)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
+        M[0] = m.x;
+        M[1] = m.y;
+        M[2] = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
+    } else if constexpr (C == 5) {
+        const Cx<R> fp = (R)2 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
+                         (R)2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
+        R n[5];
+#pragma unroll
+        for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+        M[0] = fp.x;
+        M[1] = fp.y;
+        M[2] = (R)2 * n[0] + n[1] - n[3] - (R)2 * n[4];
+    } else {
+        M[0] = M[1] = M[2] = (R)0;
+    }
+}
+
+struct AdjArgs {
+    const char* a_prev;     // lambda_{j+1}: neighbours read
+    char* a_next;           // lambda_{j+2} -> lambda_j: read-modify-write
+    const char* psi;        // forward state u_j (own node only)
+    const double* wT64;     // per entry: weight of the reverse entry (0 for repeated entries)
+    const float* wT32;
+    double factor;          // 2 dt (leapfrog) or dt (Euler start)
+    int update;             // 0: field gradients only (the start step)
+};
+
+constexpr int kGradCount = 4;  // dL/dBq, dL/dBb.x, dL/dBb.y, dL/dBb.z
+
+__device__ __forceinline__ void node_coords(const StepArgs& a, uint32_t i, uint32_t& x, uint32_t& y, uint32_t& z,
+                                            uint32_t& l) {
+    const uint32_t row = fdiv(i, a.divRow);
+    const uint32_t within = i - row * a.row_items;
+    x = fdiv(within, a.divV);
+    l = within - x * a.g.V;
+    z = fdiv(row, a.divY);
+    y = row - z * a.g.Y;
+}
+
+// Block sum of K doubles per thread into partials[blockIdx.x * K + k] (blockDim 256).
+template <int K>
+__device__ __forceinline__ void block_partials(double (&v)[K], double* partials) {
+    __shared__ double red[8][K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) red[threadIdx.x >> 5][k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * K + threadIdx.x] = s;
+    }
+}
+
+// One reverse step: lambda_j = lambda_{j+2} + factor [L^T b + (dh/du)^T b] and the
+// field gradients factor (dh/dB)^T b, b = i lambda_{j+1}.  One thread per node.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) adjoint_step_kernel(StepArgs a, AdjArgs j) {
+    __shared__ SmemTables<R> st;
+    __shared__ R wT[kMaxEntries];
+    load_tables<R>(st, a);
+    for (int i = threadIdx.x; i < a.tab.entries; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) wT[i] = j.wT32[i];
+        else wT[i] = j.wT64[i];
+    }
+    __syncthreads();
+    double gsum[kGradCount] = {0, 0, 0, 0};
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < a.total) {
+        uint32_t x, y, z, l;
+        node_coords(a, (uint32_t)gid, x, y, z, l);
+        const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+        const uint32_t node_bytes = C * 2 * sizeof(R);
+        const char* abase = j.a_prev + cell_off;
+        Cx<R> b[C], u[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const Cx<R> av = ldc<R>(abase + l * node_bytes + c * 2 * sizeof(R));
+            b[c] = cx<R>(-av.y, av.x);
+            u[c] = ldc<R>(j.psi + cell_off + l * node_bytes + c * 2 * sizeof(R));
+        }
+        const PhysR<R>& P = make_phys<R>(a);
+        R r[3];
+        r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + st.pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + st.pos[3 * l + 2]);
+        const PhysR<Dual<R>> PD = dual_phys<R>(P);
+        const Dual<R> rD[3] = {cd<R>(r[0]), cd<R>(r[1]), cd<R>(r[2])};
+        const Dual<R> potD = cd<R>(trap<R>(P, r));
+        Cx<Dual<R>> psD[C], H[C];
+        if (j.update) {
+            // L^T b = sum_f wT_f b_nb(f) - (sum_f w_f) b
+            Cx<R> K[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) K[c] = cx<R>((R)0, (R)0);
+            R diag = 0;
+            for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
+                const char* nb = abase + st.nb_off[f];
+                diag += st.w[f];
+                const R wt = wT[f];
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const Cx<R> av = ldc<R>(nb + c * 2 * sizeof(R));
+                    K[c] += wt * cx<R>(-av.y, av.x);
+                }
+            }
+            // (dh/du)^T b: one dual evaluation per real input coordinate
+            R g[2 * C];
+#pragma unroll
+            for (int k = 0; k < 2 * C; ++k) {
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    psD[c] = cx<Dual<R>>(Dual<R>(u[c].x, (R)(k == 2 * c)), Dual<R>(u[c].y, (R)(k == 2 * c + 1)));
+                    H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
+                }
+                local_terms<Dual<R>, C>(PD, rD, potD, GPE_MODE_LEAPFROG, false, psD, H);
+                g[k] = dot_d<R, C>(b, H);
+            }
+            char* o = j.a_next + cell_off + l * node_bytes;
+            const R fac = (R)j.factor;
+#pragma unroll
+            for (int c = 0; c < C; ++c) {
+                Cx<R> v = ldc_rw<R>(o + c * 2 * sizeof(R));
+                v.x += fac * (K[c].x - diag * b[c].x + g[2 * c]);
+                v.y += fac * (K[c].y - diag * b[c].y + g[2 * c + 1]);
+                stc<R>(o + c * 2 * sizeof(R), v);
+            }
+        }
+        // field parameters: (dh/dBq)^T b and (dh/dBb_k)^T b
+#pragma unroll
+        for (int c = 0; c < C; ++c) psD[c] = cx<Dual<R>>(cd<R>(u[c].x), cd<R>(u[c].y));
+#pragma unroll
+        for (int q = 0; q < kGradCount; ++q) {
+            PhysR<Dual<R>> Q = PD;
+            if (q == 0) Q.bq = Dual<R>(P.bq, (R)1);
+            else Q.bb[q - 1] = Dual<R>(P.bb[q - 1], (R)1);
+#pragma unroll
+            for (int c = 0; c < C; ++c) H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
+            local_terms<Dual<R>, C>(Q, rD, potD, GPE_MODE_LEAPFROG, false, psD, H);
+            gsum[q] = j.factor * (double)dot_d<R, C>(b, H);
+        }
+    }
+    block_partials<kGradCount>(gsum, a.partials);
+}
+
+// Adds nblocks x K partials into out[0..K) * scale in a fixed order (one block of 256).
+__global__ void __launch_bounds__(256) adjoint_sum_kernel(const double* partials, uint32_t nblocks, int K, double scale,
+                                                          double* out) {
+    __shared__ double red[256];
+    for (int k = 0; k < K; ++k) {
+        double s = 0;
+        for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(size_t)b * K + k];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[k] = red[0] * scale;
+        __syncthreads();
+    }
+}
+
+constexpr int kFinalCount = 5;  // Re <T|u>, Im <T|u>, Mx, My, Mz
+
+// Final-state quantities: the overlap sum conj(T) u and the spin density sums.
+// a.prev = target T, a.next = u_N.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) adjoint_final_kernel(StepArgs a) {
+    double v[kFinalCount] = {0, 0, 0, 0, 0};
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid < a.total) {
+        uint32_t x, y, z, l;
+        node_coords(a, (uint32_t)gid, x, y, z, l);
+        const size_t off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes +
+                           l * (C * 2 * sizeof(R));
+        Cx<double> u[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const Cx<R> t = ldc<R>(a.prev + off + c * 2 * sizeof(R));
+            const Cx<R> p = ldc<R>(a.next + off + c * 2 * sizeof(R));
+            u[c] = cx<double>((double)p.x, (double)p.y);
+            v[0] += (double)t.x * p.x + (double)t.y * p.y;
+            v[1] += (double)t.x * p.y - (double)t.y * p.x;
+        }
+        double M[3];
+        local_mag<double, C>(u, M);
+        v[2] = M[0];
+        v[3] = M[1];
+        v[4] = M[2];
+    }
+    block_partials<kFinalCount>(v, a.partials);
+}
+
+// lambda_N = dv [ (s0 + i s1) T + sum_m s_{2+m} grad M_m(u_N) ].
+// a.prev = target T, a.next = lambda buffer, psi = u_N.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) adjoint_seed_kernel(StepArgs a, const char* psi, double s0, double s1, double sx,
+                                                           double sy, double sz, double dv) {
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= a.total) return;
+    uint32_t x, y, z, l;
+    node_coords(a, (uint32_t)gid, x, y, z, l);
+    const size_t off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes +
+                       l * (C * 2 * sizeof(R));
+    Cx<double> u[C], g[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        const Cx<R> t = ldc<R>(a.prev + off + c * 2 * sizeof(R));
+        const Cx<R> p = ldc<R>(psi + off + c * 2 * sizeof(R));
+        u[c] = cx<double>((double)p.x, (double)p.y);
+        g[c] = cx<double>(s0 * t.x - s1 * t.y, s0 * t.y + s1 * t.x);
+    }
+    if (C > 1 && (sx != 0.0 || sy != 0.0 || sz != 0.0)) {
+#pragma unroll
+        for (int k = 0; k < 2 * C; ++k) {
+            Cx<Dual<double>> uD[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c)
+                uD[c] = cx<Dual<double>>(Dual<double>(u[c].x, (double)(k == 2 * c)),
+                                         Dual<double>(u[c].y, (double)(k == 2 * c + 1)));
+            Dual<double> M[3];
+            local_mag<Dual<double>, C>(uD, M);
+            const double d = sx * M[0].d + sy * M[1].d + sz * M[2].d;
+            if (k & 1) g[k >> 1].y += d;
+            else g[k >> 1].x += d;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) stc<R>(a.next + off + c * 2 * sizeof(R), cx<R>((R)(dv * g[c].x), (R)(dv * g[c].y)));
+}
+
+template <typename R, int C>
+static cudaError_t launch_adjoint_step(const StepArgs& a, const AdjArgs& j, double* out, cudaStream_t s) {
+    const unsigned nb = nblocks(a.total, 256);
+    adjoint_step_kernel<R, C><<<nb, 256, 0, s>>>(a, j);
+    adjoint_sum_kernel<<<1, 256, 0, s>>>(a.partials, nb, kGradCount, 1.0, out);
+    return cudaGetLastError();
+}
+
+template <typename R, int C>
+static cudaError_t launch_adjoint_final(const StepArgs& a, double dv, double* out, cudaStream_t s) {
+    const unsigned nb = nblocks(a.total, 256);
+    adjoint_final_kernel<R, C><<<nb, 256, 0, s>>>(a);
+    adjoint_sum_kernel<<<1, 256, 0, s>>>(a.partials, nb, kFinalCount, dv, out);
+    return cudaGetLastError();
+}
+
+template <typename R, int C>
+static cudaError_t launch_adjoint_seed(const StepArgs& a, const char* psi, const double* sd, double dv, cudaStream_t s) {
+    adjoint_seed_kernel<R, C><<<nblocks(a.total, 256), 256, 0, s>>>(a, psi, sd[0], sd[1], sd[2], sd[3], sd[4], dv);
+    return cudaGetLastError();
+}
+
+// Instantiates FN for the handle's precision and component count.
+#define GPE_ADJ_DISPATCH(FN, H, ...)                                                               \
+    ((H)->real_bytes == 8 ? ((H)->g.C == 1   ? FN<double, 1>(__VA_ARGS__)                         \
+                             : (H)->g.C == 3 ? FN<double, 3>(__VA_ARGS__)                         \
+                                             : FN<double, 5>(__VA_ARGS__))                        \
+                          : ((H)->g.C == 1   ? FN<float, 1>(__VA_ARGS__)                          \
+                             : (H)->g.C == 3 ? FN<float, 3>(__VA_ARGS__)                          \
+                                             : FN<float, 5>(__VA_ARGS__)))
+
+// ------------------------------------------------------------------ host side
+
+void adjoint_release(gpe_handle* h) {
+    AdjointStore& A = h->adj;
+    for (void* p : A.ckpt) cudaFree(p);
+    for (void* p : A.seg) cudaFree(p);
+    A.ckpt.clear();
+    A.seg.clear();
+    for (void*& p : A.adj) {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+    if (A.target) cudaFree(A.target);
+    if (A.grad) cudaFree(A.grad);
+    if (A.out) cudaFree(A.out);
+    if (A.wT64) cudaFree(A.wT64);
+    if (A.wT32) cudaFree(A.wT32);
+    A.target = nullptr;
+    A.grad = A.out = A.wT64 = nullptr;
+    A.wT32 = nullptr;
+    A.valid = false;
+    A.n = A.stride = A.segments = 0;
+}
+
+static char* interior_of(const gpe_handle* h, void* base) {
+    return static_cast<char*>(base) + h->g.slice + h->g.pitch + h->g.cell_bytes;
+}
+
+// Transposed Laplacian weights: entry f of row j (j -> node i at offset d) gets the
+// sum of the weights of row i's entries (i -> j at offset -d); a repeated (d, i)
+// in row j gets 0 so that the sum is counted once.  Every entry must have a
+// reverse entry, or L^T would need entries that row j does not hold.
+static gpe_status build_transpose(gpe_handle* h) {
+    const gpe_lattice& L = h->lat;
+    const double bs2 = h->p.block_scale * h->p.block_scale;
+    const int n = (int)L.stencil.size();
+    auto same = [](const gpe_stencil_entry& a, int dx, int dy, int dz, int node) {
+        return a.dx == dx && a.dy == dy && a.dz == dz && a.node == node;
+    };
+    std::vector<double> wT(n, 0.0);
+    for (int jn = 0; jn < L.V; ++jn) {
+        for (int f = L.row_ptr[jn]; f < L.row_ptr[jn + 1]; ++f) {
+            const gpe_stencil_entry& e = L.stencil[f];
+            bool repeated = false;
+            for (int f2 = L.row_ptr[jn]; f2 < f && !repeated; ++f2) repeated = same(L.stencil[f2], e.dx, e.dy, e.dz, e.node);
+            if (repeated) continue;
+            double s = 0;
+            bool found = false;
+            for (int g = L.row_ptr[e.node]; g < L.row_ptr[e.node + 1]; ++g)
+                if (same(L.stencil[g], -e.dx, -e.dy, -e.dz, jn)) {
+                    s += (-0.5 * L.stencil[g].hodge) / bs2;
+                    found = true;
+                }
+            if (!found) return fail(GPE_ERR_UNSUPPORTED, "adjoint: a stencil entry has no reverse entry");
+            wT[f] = s;
+        }
+    }
+    std::vector<float> wT32(wT.begin(), wT.end());
+    AdjointStore& A = h->adj;
+    if (cudaMalloc(&A.wT64, n * sizeof(double)) != cudaSuccess || cudaMalloc(&A.wT32, n * sizeof(float)) != cudaSuccess)
+        return fail(GPE_ERR_OOM, "cudaMalloc (adjoint tables)");
+    cudaError_t e = cudaMemcpy(A.wT64, wT.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(A.wT32, wT32.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (adjoint tables)");
+    return GPE_OK;
+}
+
+static gpe_status ensure_adjoint_buffers(gpe_handle* h, int n, int stride) {
+    AdjointStore& A = h->adj;
+    const int segments = (n + stride - 1) / stride;
+    const size_t bytes = h->alloc_bytes[GPE_PSI_EVEN];
+    const size_t want_ckpt = (size_t)2 * segments, want_seg = stride > 2 ? (size_t)(stride - 2) : 0;
+    auto resize = [&](std::vector<void*>& v, size_t want) -> bool {
+        while (v.size() > want) {
+            cudaFree(v.back());
+            v.pop_back();
+        }
+        while (v.size() < want) {
+            void* p = nullptr;
+            if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
+            v.push_back(p);
+        }
+        return true;
+    };
+    if (!resize(A.ckpt, want_ckpt) || !resize(A.seg, want_seg)) {
+        adjoint_release(h);
+        return fail(GPE_ERR_OOM, "cudaMalloc (adjoint checkpoints)");
+    }
+    // recompute and adjoint buffers keep zero halos: checkpoint copies carry the
+    // (zero) halo of a handle buffer and every kernel writes the interior only
+    for (void*& p : A.adj)
+        if (!p && cudaMalloc(&p, bytes) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (adjoint state)");
+    if (!A.target) {
+        if (cudaMalloc(&A.target, bytes) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (target)");
+        if (cudaMemset(A.target, 0, bytes) != cudaSuccess) return fail(GPE_ERR_CUDA, "cudaMemset (target)");
+    }
+    if (A.grad && A.n < n) {
+        cudaFree(A.grad);
+        A.grad = nullptr;
+    }
+    if (!A.grad && cudaMalloc(&A.grad, (size_t)n * kGradCount * sizeof(double)) != cudaSuccess)
+        return fail(GPE_ERR_OOM, "cudaMalloc (gradients)");
+    if (!A.out && cudaMalloc(&A.out, 8 * sizeof(double)) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (adjoint out)");
+    if (!A.wT64) {
+        gpe_status st = build_transpose(h);
+        if (st) return st;
+    }
+    A.buf_bytes = bytes;
+    A.segments = segments;
+    return GPE_OK;
+}
+
+static gpe_status copy_state(gpe_handle* h, void* dst, const void* src, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, h->alloc_bytes[GPE_PSI_EVEN], cudaMemcpyDeviceToDevice, s);
+    return e == cudaSuccess ? GPE_OK : cuda_fail(e, "checkpoint copy");
+}
+
+}  // namespace gpe
+
+using namespace gpe;
+
+extern "C" gpe_status gpe_adjoint_forward(gpe_handle* h, int32_t n_steps, const gpe_fields* fields, int32_t stride,
+                                          const double* target, size_t count, double* out, void* stream) {
+    if (!h || !fields || !target || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (h->p.scheme != GPE_SCHEME_PARABOLIC) return fail(GPE_ERR_UNSUPPORTED, "the adjoint is built for the parabolic scheme");
+    if (n_steps < 1) return fail(GPE_ERR_INVALID_ARG, "n_steps must be at least 1");
+    if (count != host_count(h, false)) return fail(GPE_ERR_INVALID_ARG, "target size does not match the grid");
+    if (stride <= 0) stride = (int32_t)std::ceil(std::sqrt((double)n_steps));
+    if (stride > n_steps) stride = n_steps;
+    AdjointStore& A = h->adj;
+    A.valid = false;
+    gpe_status st = ensure_adjoint_buffers(h, n_steps, stride);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    // target: host FP64 file layout -> device buffer in the handle's precision
+    if ((st = ensure_stage(h, count))) return st;
+    const Grid& g = h->g;
+    cudaError_t e = cudaMemcpyAsync(h->stage, target, count * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = launch_pack_any(h->p.precision, h->stage, static_cast<char*>(A.target), g.X, g.Y, g.Z,
+                            (uint32_t)(g.cell_bytes / h->real_bytes), g.pitch, g.slice, true, s);
+    if (e != cudaSuccess) return cuda_fail(e, "target upload");
+    h->launches += 1;
+    A.n = n_steps;
+    A.stride = stride;
+    A.t0 = h->t0;
+    A.fields.assign(fields, fields + n_steps);
+    const double dt = h->p.dt;
+    // u_j lives in PSI_ODD for even j and in PSI_EVEN for odd j
+    auto slot_of = [](int j) { return (j & 1) ? GPE_PSI_EVEN : GPE_PSI_ODD; };
+    if ((st = step_buffers(h, h->interior[GPE_PSI_EVEN], h->interior[GPE_PSI_ODD], fields[0], A.t0, GPE_MODE_EULER, s)))
+        return st;
+    if ((st = copy_state(h, A.ckpt[0], h->alloc[GPE_PSI_ODD], s))) return st;
+    if ((st = copy_state(h, A.ckpt[1], h->alloc[GPE_PSI_EVEN], s))) return st;
+    for (int j = 1; j < n_steps; ++j) {
+        const int prev = slot_of(j), next = slot_of(j + 1);
+        if ((st = step_buffers(h, h->interior[next], h->interior[prev], fields[j], A.t0 + j * dt, GPE_MODE_LEAPFROG, s)))
+            return st;
+        if (j % stride == 0) {
+            const int k = j / stride;
+            if ((st = copy_state(h, A.ckpt[2 * k], h->alloc[prev], s))) return st;
+            if ((st = copy_state(h, A.ckpt[2 * k + 1], h->alloc[next], s))) return st;
+        }
+    }
+    h->cur = slot_of(n_steps);
+    h->nstep = (uint64_t)(n_steps - 1);
+    StepArgs a = make_args(h, fields[n_steps - 1], A.t0 + n_steps * dt);
+    a.prev = interior_of(h, A.target);
+    a.next = h->interior[h->cur];
+    e = GPE_ADJ_DISPATCH(launch_adjoint_final, h, a, cell_dv(h), A.out, s);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint final kernel");
+    h->launches += 2;
+    double r[kFinalCount];
+    e = cudaMemcpyAsync(r, A.out, sizeof r, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint forward");
+    if ((st = check_device_error(h, s))) return st;
+    for (int k = 0; k < kFinalCount; ++k) out[k] = r[k];
+    A.valid = true;
+    A.epoch = h->epoch;
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, double* grad, void* stream) {
+    if (!h || !seed || !grad) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    AdjointStore& A = h->adj;
+    if (!A.valid || A.epoch != h->epoch)
+        return fail(GPE_ERR_INVALID_ARG, "no recorded forward run (or the state changed since gpe_adjoint_forward)");
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint64_t epoch = h->epoch;
+    const int n = A.n, S = A.stride;
+    const double dt = h->p.dt;
+    gpe_status st;
+    cudaError_t e = cudaMemsetAsync(A.adj[0], 0, A.buf_bytes, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.adj[1], 0, A.buf_bytes, s);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint clear");
+    {
+        StepArgs a = make_args(h, A.fields[n - 1], A.t0 + n * dt);
+        a.prev = interior_of(h, A.target);
+        a.next = interior_of(h, A.adj[0]);
+        e = GPE_ADJ_DISPATCH(launch_adjoint_seed, h, a, h->interior[h->cur], seed, cell_dv(h), s);
+        if (e != cudaSuccess) return cuda_fail(e, "adjoint seed kernel");
+        h->launches += 1;
+    }
+    char* P = interior_of(h, A.adj[0]);  // lambda_{j+1}
+    char* Q = interior_of(h, A.adj[1]);  // lambda_{j+2} -> lambda_j
+    std::vector<void*> state((size_t)S, nullptr);
+    for (int k = A.segments - 1; k >= 0; --k) {
+        const int lo = k * S, hi = std::min(lo + S, n), len = hi - lo;
+        state[0] = A.ckpt[2 * k];
+        if (len > 1) state[1] = A.ckpt[2 * k + 1];
+        for (int m = 2; m < len; ++m) {
+            state[m] = A.seg[m - 2];
+            if ((st = copy_state(h, state[m], state[m - 2], s))) return st;
+            const int jj = lo + m - 1;
+            if ((st = step_buffers(h, interior_of(h, state[m]), interior_of(h, state[m - 1]), A.fields[jj],
+                                   A.t0 + jj * dt, GPE_MODE_LEAPFROG, s)))
+                return st;
+        }
+        for (int j = hi - 1; j >= lo; --j) {
+            StepArgs a = make_args(h, A.fields[j], A.t0 + j * dt);
+            AdjArgs aj;
+            aj.a_prev = P;
+            aj.a_next = Q;
+            aj.psi = interior_of(h, state[j - lo]);
+            aj.wT64 = A.wT64;
+            aj.wT32 = A.wT32;
+            aj.factor = j >= 1 ? 2.0 * dt : dt;
+            aj.update = j >= 1 ? 1 : 0;
+            e = GPE_ADJ_DISPATCH(launch_adjoint_step, h, a, aj, A.grad + (size_t)j * kGradCount, s);
+            if (e != cudaSuccess) return cuda_fail(e, "adjoint step kernel");
+            h->launches += 2;
+            if (j >= 1) std::swap(P, Q);
+        }
+    }
+    e = cudaMemcpyAsync(grad, A.grad, (size_t)n * kGradCount * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // the recomputation ran the step kernel on the adjoint's own buffers only
+    h->epoch = epoch;
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint backward");
+    return check_device_error(h, s);
+}

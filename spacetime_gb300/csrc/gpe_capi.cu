@@ -7,7 +7,7 @@
 #include <string>
 #include <vector>
 
-#include "gpe_internal.h"
+#include "gpe_handle.h"
 
 namespace gpe {
 template <typename R, int C>
@@ -36,8 +36,6 @@ template <typename R, int C>
 cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads, cudaStream_t s);
-cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
-                            uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
 enum HyperKind {
     HK_FUSED_LEAPFROG = 0,
     HK_PSI_PARA_LEAPFROG,
@@ -54,12 +52,12 @@ using namespace gpe;
 
 static thread_local std::string g_last_error = "";
 
-static gpe_status fail(gpe_status st, const std::string& msg) {
+gpe_status gpe::fail(gpe_status st, const std::string& msg) {
     g_last_error = msg;
     return st;
 }
 
-static gpe_status cuda_fail(cudaError_t e, const char* where) {
+gpe_status gpe::cuda_fail(cudaError_t e, const char* where) {
     return fail(GPE_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
@@ -68,52 +66,6 @@ static gpe_status cuda_fail(cudaError_t e, const char* where) {
         cudaError_t _e = (expr);                          \
         if (_e != cudaSuccess) return cuda_fail(_e, #expr); \
     } while (0)
-
-struct gpe_lattice {
-    int V = 0;
-    double bw[3] = {0, 0, 0};
-    double volume = 0;
-    std::vector<double> pos;
-    std::vector<int32_t> row_ptr;
-    std::vector<gpe_stencil_entry> stencil;
-    int E = 0, F = 0;
-    std::vector<gpe_edge> edges;
-    std::vector<gpe_incidence> incidence;
-};
-
-struct gpe_handle {
-    gpe_lattice lat;
-    gpe_params p;
-    int device = 0;
-    size_t real_bytes = 4;
-    Grid g{};
-    void* alloc[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    char* interior[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    size_t alloc_bytes[5] = {0, 0, 0, 0, 0};
-    DevTables tab{};
-    std::vector<void*> dev_tables;
-    double* partials = nullptr;
-    size_t partial_blocks = 0;
-    double* obs_out = nullptr;
-    double* stage = nullptr;   // FP64 staging for uploads/downloads (allocated on first use)
-    size_t stage_count = 0;
-    gpe_ramp ramp{};
-    bool has_ramp = false;
-    double t0 = 0;
-    int cur = 0;          // psi slot holding the newest state
-    uint64_t nstep = 0;   // leapfrog steps since gpe_start / gpe_set_ramp
-    uint64_t launches = 0;
-    int* err = nullptr;    // device error flag
-    int tune_kernel = 0;   // GPE_TUNE_KERNEL
-    int tune_tile = 0;     // GPE_TUNE_TILE_CELLS
-    int tune_rows = 0;     // GPE_TUNE_TILE_ROWS
-    int tune_zchunk = 0;   // GPE_TUNE_ZCHUNK
-    int tune_threads = 0;  // GPE_TUNE_THREADS
-    uint32_t nrows = 0;    // multi-row tile kernel: (dy, dz) rows the stencil uses, own row first
-    int32_t rdy[9] = {0}, rdz[9] = {0};
-    int32_t* blk = nullptr;   // device row-block table of the current shape
-    uint32_t blk_ry = 0, blk_rz = 0, blk_nbuf = 0;
-};
 
 extern "C" const char* gpe_last_error(void) { return g_last_error.c_str(); }
 
@@ -262,6 +214,7 @@ static void release(gpe_handle* h) {
     if (h->stage) cudaFree(h->stage);
     if (h->err) cudaFree(h->err);
     if (h->blk) cudaFree(h->blk);
+    adjoint_release(h);
 }
 
 static gpe_status build_tables(gpe_handle* h) {
@@ -470,13 +423,13 @@ extern "C" gpe_status gpe_buffer(const gpe_handle* h, int32_t slot, gpe_pitched*
     return GPE_OK;
 }
 
-static size_t host_count(const gpe_handle* h, bool is_q) {
+size_t gpe::host_count(const gpe_handle* h, bool is_q) {
     const Grid& g = h->g;
     return (size_t)(g.X + 2) * (g.Y + 2) * (g.Z + 2) * (is_q ? g.E : g.V) * g.C * 2;
 }
 
 // A bounded device wait that ran out sets the handle's error flag; surface it.
-static gpe_status check_device_error(gpe_handle* h, cudaStream_t s) {
+gpe_status gpe::check_device_error(gpe_handle* h, cudaStream_t s) {
     int flag = 0;
     CUDA_TRY(cudaMemcpyAsync(&flag, h->err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
@@ -487,7 +440,7 @@ static gpe_status check_device_error(gpe_handle* h, cudaStream_t s) {
     return GPE_OK;
 }
 
-static gpe_status ensure_stage(gpe_handle* h, size_t count) {
+gpe_status gpe::ensure_stage(gpe_handle* h, size_t count) {
     if (h->stage_count >= count) return GPE_OK;
     if (h->stage) cudaFree(h->stage);
     h->stage = nullptr;
@@ -503,6 +456,7 @@ static gpe_status ensure_stage(gpe_handle* h, size_t count) {
 // is needed.
 static gpe_status transfer(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream, bool up) {
     if (!h || !host) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (up) h->epoch += 1;
     if (up && slot == GPE_HPSI) {
         gpe_status st = ensure_hpsi(h);
         if (st) return st;
@@ -583,7 +537,7 @@ static void fill_phys(PhysR<R>& P, const Phys& ph, const gpe_fields& B, double t
     P.trap_on = !((ph.flags & GPE_FLAG_TRAP_OFF_AFTER) && t >= ph.trap_off_time);
 }
 
-static StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t) {
+StepArgs gpe::make_args(const gpe_handle* h, const gpe_fields& B, double t) {
     StepArgs a;
     std::memset(&a, 0, sizeof a);
     a.g = h->g;
@@ -911,42 +865,51 @@ static cudaError_t dispatch_hyper_tile(const gpe_handle* h, const StepArgs& a, u
     }
 }
 
-static double cell_dv(const gpe_handle* h) {
+double gpe::cell_dv(const gpe_handle* h) {
     const double bs = h->p.block_scale;
     return bs * bs * bs * h->lat.volume;  // volume = bs^3 * VOLUME (Spin1GpeBCC.cu:1385)
 }
 
+// One parabolic step next <- prev on interior pointers of the handle's geometry.
+gpe_status gpe::step_buffers(gpe_handle* h, char* next, const char* prev, const gpe_fields& B, double t, int mode,
+                             cudaStream_t s) {
+    StepArgs a = make_args(h, B, t);
+    a.prev = prev;
+    a.next = next;
+    a.hpsi = mode == GPE_MODE_ITP ? h->interior[GPE_HPSI] : nullptr;
+    const MarchShape ms = march_shape(h);
+    const uint32_t T = tile_cells(h);
+    const RowsShape rs = rows_shape(h);
+    cudaError_t e;
+    if (mode == GPE_MODE_LEAPFROG && rs.T > 0) {
+        gpe_status bst = ensure_row_block(h, rs);
+        if (bst) return bst;
+        e = dispatch_rows(h, a, rs, s);
+    }
+    else if (mode == GPE_MODE_LEAPFROG && ms.T > 0) e = dispatch_march(h, a, ms, s);
+    else if (mode == GPE_MODE_LEAPFROG && T > 0) e = dispatch_tile(h, a, T, s);
+    else e = dispatch_parabolic(h, a, mode, s);
+    h->launches += 1;
+    h->epoch += 1;
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return GPE_OK;
+}
+
 // psi[next] <- psi[prev] (and q when hyperbolic), one step at time t.
 static gpe_status one_step(gpe_handle* h, int next, int prev, const gpe_fields& B, double t, int mode, cudaStream_t s) {
+    if (h->p.scheme == GPE_SCHEME_PARABOLIC) return step_buffers(h, h->interior[next], h->interior[prev], B, t, mode, s);
     StepArgs a = make_args(h, B, t);
     a.prev = h->interior[prev];
     a.next = h->interior[next];
-    cudaError_t e;
-    if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
-        a.hpsi = mode == GPE_MODE_ITP ? h->interior[GPE_HPSI] : nullptr;
-        const MarchShape ms = march_shape(h);
-        const uint32_t T = tile_cells(h);
-        const RowsShape rs = rows_shape(h);
-        if (mode == GPE_MODE_LEAPFROG && rs.T > 0) {
-            gpe_status bst = ensure_row_block(h, rs);
-            if (bst) return bst;
-            e = dispatch_rows(h, a, rs, s);
-        }
-        else if (mode == GPE_MODE_LEAPFROG && ms.T > 0) e = dispatch_march(h, a, ms, s);
-        else if (mode == GPE_MODE_LEAPFROG && T > 0) e = dispatch_tile(h, a, T, s);
-        else e = dispatch_parabolic(h, a, mode, s);
-        h->launches += 1;
-    } else {
-        if (mode != GPE_MODE_LEAPFROG) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme: explicit steps are leapfrog only");
-        const int qprev = prev == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
-        const int qnext = next == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
-        a.q = h->interior[qprev];
-        a.qnext = h->interior[qnext];
-        const uint32_t T = hyper_tile_cells(h);
-        if (T > 0) e = dispatch_hyper_tile(h, a, T, s);
-        else e = dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
-        h->launches += 1;
-    }
+    if (mode != GPE_MODE_LEAPFROG) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme: explicit steps are leapfrog only");
+    const int qprev = prev == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
+    const int qnext = next == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
+    a.q = h->interior[qprev];
+    a.qnext = h->interior[qnext];
+    const uint32_t T = hyper_tile_cells(h);
+    cudaError_t e = T > 0 ? dispatch_hyper_tile(h, a, T, s) : dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
+    h->launches += 1;
+    h->epoch += 1;
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
     return GPE_OK;
 }
@@ -993,6 +956,7 @@ extern "C" gpe_status gpe_start(gpe_handle* h, void* stream) {
         a.qnext = h->interior[GPE_Q_EVEN];
         if ((e = dispatch_hyper(h, a, HK_Q_PARA, s)) != cudaSuccess) return cuda_fail(e, "q init");
         h->launches += 3;
+        h->epoch += 1;
     }
     h->cur = GPE_PSI_EVEN;
     h->nstep = 0;
@@ -1283,6 +1247,7 @@ extern "C" gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init
     }
     if (e != cudaSuccess) return cuda_fail(e, "init kernel");
     h->launches += 1;
+    h->epoch += 1;
     if (init->normalize) {
         a.prev = h->interior[slot];
         e = dispatch_observe(h, a, h->obs_out, s);

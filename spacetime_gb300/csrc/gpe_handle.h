@@ -1,0 +1,96 @@
+// gpe_handle.h -- host-side definition of the libgpe handle (not part of the ABI).
+// Shared by the translation units that implement entry points on a handle.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "gpe_internal.h"
+
+struct gpe_lattice {
+    int V = 0;
+    double bw[3] = {0, 0, 0};
+    double volume = 0;
+    std::vector<double> pos;
+    std::vector<int32_t> row_ptr;
+    std::vector<gpe_stencil_entry> stencil;
+    int E = 0, F = 0;
+    std::vector<gpe_edge> edges;
+    std::vector<gpe_incidence> incidence;
+};
+
+namespace gpe {
+// Device memory of the reverse-mode (adjoint) driver: checkpoints of the forward
+// run, the recomputed states of one segment, two adjoint buffers and the target.
+struct AdjointStore {
+    int n = 0;                      // steps of the recorded forward run
+    int stride = 0;                 // steps per checkpoint segment
+    int segments = 0;
+    double t0 = 0;
+    std::vector<gpe_fields> fields; // per step
+    std::vector<void*> ckpt;        // 2 per segment: (u_{kS}, u_{kS+1})
+    std::vector<void*> seg;         // stride buffers for the recomputed segment
+    void* adj[2] = {nullptr, nullptr};
+    void* target = nullptr;
+    size_t buf_bytes = 0;
+    double* grad = nullptr;         // device, n x 4
+    double* out = nullptr;          // device, 8
+    double* wT64 = nullptr;         // transposed Laplacian weights
+    float* wT32 = nullptr;
+    bool valid = false;
+    uint64_t epoch = 0;             // handle epoch at the end of the recorded forward run
+};
+}  // namespace gpe
+
+struct gpe_handle {
+    gpe_lattice lat;
+    gpe_params p;
+    int device = 0;
+    size_t real_bytes = 4;
+    gpe::Grid g{};
+    void* alloc[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    char* interior[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    size_t alloc_bytes[5] = {0, 0, 0, 0, 0};
+    gpe::DevTables tab{};
+    std::vector<void*> dev_tables;
+    double* partials = nullptr;
+    size_t partial_blocks = 0;
+    double* obs_out = nullptr;
+    double* stage = nullptr;   // FP64 staging for uploads/downloads (allocated on first use)
+    size_t stage_count = 0;
+    gpe_ramp ramp{};
+    bool has_ramp = false;
+    double t0 = 0;
+    int cur = 0;          // psi slot holding the newest state
+    uint64_t nstep = 0;   // leapfrog steps since gpe_start / gpe_set_ramp
+    uint64_t launches = 0;
+    uint64_t epoch = 0;   // bumped by every call that writes a psi buffer
+    int* err = nullptr;    // device error flag
+    int tune_kernel = 0;   // GPE_TUNE_KERNEL
+    int tune_tile = 0;     // GPE_TUNE_TILE_CELLS
+    int tune_rows = 0;     // GPE_TUNE_TILE_ROWS
+    int tune_zchunk = 0;   // GPE_TUNE_ZCHUNK
+    int tune_threads = 0;  // GPE_TUNE_THREADS
+    uint32_t nrows = 0;    // multi-row tile kernel: (dy, dz) rows the stencil uses, own row first
+    int32_t rdy[9] = {0}, rdz[9] = {0};
+    int32_t* blk = nullptr;   // device row-block table of the current shape
+    uint32_t blk_ry = 0, blk_rz = 0, blk_nbuf = 0;
+    gpe::AdjointStore adj;
+};
+
+namespace gpe {
+gpe_status fail(gpe_status st, const std::string& msg);
+gpe_status cuda_fail(cudaError_t e, const char* where);
+StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t);
+// One parabolic step on arbitrary buffers of the handle's geometry (interior
+// pointers), with the same kernel choice as the slot-based steps.
+gpe_status step_buffers(gpe_handle* h, char* next, const char* prev, const gpe_fields& B, double t, int mode,
+                        cudaStream_t s);
+double cell_dv(const gpe_handle* h);
+size_t host_count(const gpe_handle* h, bool is_q);
+gpe_status ensure_stage(gpe_handle* h, size_t count);
+gpe_status check_device_error(gpe_handle* h, cudaStream_t s);
+cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
+                            uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
+void adjoint_release(gpe_handle* h);
+}  // namespace gpe

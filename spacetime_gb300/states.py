@@ -129,6 +129,34 @@ def spinor_state(lat, params, zeta, seed=2, noise=1e-3) -> np.ndarray:
     return normalize(_embed(psi), lat, params)
 
 
+def monopole_state(lat, params, seed=4, noise=1e-3, center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Spin-1 hedgehog: at each node the polar spinor (0, 1, 0) rotated so that its
+    director points along r_hat = (r - center)/|r - center|, i.e. components
+    (m = +1, 0, -1) = (-(n_x - i n_y)/sqrt 2, n_z, (n_x + i n_y)/sqrt 2) for
+    n = r_hat (the rotation D^1_{m0}(phi, theta, 0) of |1, 0>), times the
+    Thomas-Fermi amplitude, plus seeded complex Gaussian noise of amplitude
+    noise * sqrt(rho) per component; normalised to 1.  A target state for the
+    ramp-control loss 1 - |<target|psi(T)>|^2."""
+    r = node_positions(lat, params) - np.asarray(center, dtype=np.float64)
+    lam = tuple(params.trap_lambda[i] for i in range(3))
+    rho = thomas_fermi_density(r + np.asarray(center), params.c0, lam)
+    amp = np.sqrt(rho)
+    d = np.linalg.norm(r, axis=-1)
+    safe = np.where(d > 0, d, 1.0)
+    nx = np.where(d > 0, r[..., 0] / safe, 0.0)
+    ny = np.where(d > 0, r[..., 1] / safe, 0.0)
+    nz = np.where(d > 0, r[..., 2] / safe, 1.0)
+    s = 1.0 / math.sqrt(2.0)
+    psi = np.empty(r.shape[:4] + (3, 2))
+    psi[..., 0, 0], psi[..., 0, 1] = -s * nx * amp, s * ny * amp
+    psi[..., 1, 0], psi[..., 1, 1] = nz * amp, 0.0
+    psi[..., 2, 0], psi[..., 2, 1] = s * nx * amp, s * ny * amp
+    if noise:
+        g = gaussian_pairs(seed, psi[..., 0].size).reshape(psi.shape)
+        psi += noise * amp[..., None, None] * g
+    return normalize(_embed(psi), lat, params)
+
+
 POLAR = (0.0, 1.0, 0.0)                      # spin-1 polar (polarState, Spin1GpeBCC.cu:463-491)
 FERRO = (1.0, 0.0, 0.0)                      # spin-1 ferromagnetic (Spin1GpeBCC.cu:493-521)
 CYCLIC = (math.sqrt(1 / 3), 0, 0, math.sqrt(2 / 3), 0)  # spin-2 cyclic, phase 0 (Spin2GpeBCC.cu:523-558)

@@ -89,6 +89,40 @@ class Stepper:
         f = C.byref(fields) if fields is not None else None
         capi.check(self.lib.gpe_step_explicit(self._h, next_slot, prev_slot, f, t, mode, self.stream), "gpe_step_explicit")
 
+    # --------------------------------------------------------------- adjoint
+    def adjoint_forward(self, fields, target: np.ndarray, stride: int = 0) -> np.ndarray:
+        """Recorded forward run from PSI_ODD (gpe_adjoint_forward).
+
+        fields: (n, 4) = (bq, bb_x, bb_y, bb_z) or (n, 8) gpe_fields rows, one per
+        step (row 0 drives the Euler start).  Returns (Re <T|psi_N>, Im <T|psi_N>,
+        M_x, M_y, M_z)."""
+        f = np.asarray(fields, dtype=np.float64)
+        if f.ndim != 2 or f.shape[1] not in (4, 8) or f.shape[0] < 1:
+            raise ValueError("fields must have shape (n, 4) or (n, 8)")
+        rows = np.zeros((f.shape[0], 8))
+        rows[:, : f.shape[1]] = f
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        out = np.zeros(5)
+        dp = C.POINTER(C.c_double)
+        capi.check(self.lib.gpe_adjoint_forward(self._h, rows.shape[0], rows.ctypes.data_as(C.POINTER(capi.Fields)), stride,
+                                                t.ctypes.data_as(dp), t.size, out.ctypes.data_as(dp), self.stream),
+                   "gpe_adjoint_forward")
+        self._adj_steps = rows.shape[0]
+        return out
+
+    def adjoint_backward(self, seed) -> np.ndarray:
+        """dL/d(fields) of the recorded run, shape (n, 4) = (bq, bb_x, bb_y, bb_z),
+        for seed = dL/d(the five numbers adjoint_forward returned)."""
+        sd = np.zeros(5)
+        s = np.asarray(seed, dtype=np.float64).ravel()
+        sd[: s.size] = s
+        n = getattr(self, "_adj_steps", 0)
+        grad = np.zeros((max(n, 1), 4))
+        dp = C.POINTER(C.c_double)
+        capi.check(self.lib.gpe_adjoint_backward(self._h, sd.ctypes.data_as(dp), grad.ctypes.data_as(dp), self.stream),
+                   "gpe_adjoint_backward")
+        return grad[:n]
+
     def itp(self, n: int, want_mu: bool = True):
         mu = C.c_double(0.0)
         capi.check(self.lib.gpe_itp(self._h, n, C.byref(mu) if want_mu else None, self.stream), "gpe_itp")
