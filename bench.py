@@ -130,6 +130,106 @@ def run_leg(args):
     return 0
 
 
+# Adjoint ramp control: spin-1, BCC 64^3 cells, 2000 steps, Bz(t) and Bq(t) with 16
+# piecewise-linear knots each (seeded uniform in [-1, 1]), loss 1 - |<T|psi(T)>|^2
+# against a seeded hedgehog (monopole-like) target, 45-step checkpoints, central
+# differences (h = 1e-4) of the FP64 run on 8 random knots.
+ADJ = dict(dims=(64, 64, 64), steps=2000, stride=45, knots=16, fd_knots=8, h=1e-4, seed=4)
+
+
+def run_adjoint(args):
+    """--workload adjoint-bcc64: gradient of the ramp-control loss through the adjoint
+    kernel (FP32 and FP64), timed, and checked against central differences."""
+    import torch
+
+    from spacetime_gb300 import capi, states
+    from spacetime_gb300.adjoint import RampControl
+    from spacetime_gb300.stepper import Stepper
+
+    lat = capi.Lattice("bcc")
+    dims = ADJ["dims"]
+    bs = BOX / (dims[0] * lat.block_width[0])
+
+    def params(prec):
+        return capi.make_params(components=3, precision=prec, dims=dims, block_scale=bs, dt=DT, trap_offset=100.0,
+                                c0=C0, c2=C2, lattice=lat)
+
+    init = capi.make_init(zeta=states.POLAR, noise_rel=1e-3, seed=2)
+    k = 2.0 * states.uniform01(ADJ["seed"], 2 * ADJ["knots"]).reshape(2, ADJ["knots"]) - 1.0
+    target = states.monopole_state(lat, params(capi.FP64), seed=ADJ["seed"], noise=1e-3)
+    out = {}
+    for prec in (capi.FP32, capi.FP64):
+        s = Stepper(lat, params(prec))
+        rc = RampControl(s, ADJ["steps"], ADJ["knots"], lambda: s.init_state(capi.PSI_ODD, init), target,
+                         stride=ADJ["stride"])
+        reps = max(1, args.steps) if prec == capi.FP32 else 1
+        fwd, bwd, grads, loss = [], [], None, None
+        n0 = s.launches
+        for it in range(reps + (1 if prec == capi.FP32 else 0)):
+            bq = torch.tensor(k[0], requires_grad=True)
+            bz = torch.tensor(k[1], requires_grad=True)
+            t0 = time.perf_counter()
+            loss = rc.loss(bq, bz)
+            t1 = time.perf_counter()
+            loss.backward()
+            t2 = time.perf_counter()
+            if prec == capi.FP32 and it == 0:
+                n0 = s.launches
+                continue  # warm-up
+            fwd.append(t1 - t0)
+            bwd.append(t2 - t1)
+            grads = np.concatenate([bq.grad.numpy(), bz.grad.numpy()])
+        launches = (s.launches - n0) / len(fwd)
+        r = {"loss": float(loss.detach()), "grad": grads, "forward_s": statistics.median(fwd), "backward_s": statistics.median(bwd),
+             "launches_per_gradient": launches}
+        if prec == capi.FP64:
+            rng = np.random.default_rng(ADJ["seed"])
+            picks = rng.choice(2 * ADJ["knots"], ADJ["fd_knots"], replace=False)
+            fd = []
+            for i in picks:
+                kp, km = k.copy().ravel(), k.copy().ravel()
+                kp[i] += ADJ["h"]
+                km[i] -= ADJ["h"]
+                # central difference of L = 1 - |o|^2 taken as -(|o+|^2 - |o-|^2) / 2h: the
+                # overlap of the polar state with the hedgehog is O(1e-4), and adding the
+                # constant 1 first would round |o|^2 to a few digits
+                with torch.no_grad():
+                    op = rc.observables(torch.tensor(kp[:16]), torch.tensor(kp[16:]))
+                    om = rc.observables(torch.tensor(km[:16]), torch.tensor(km[16:]))
+                lp = -float(op[0] ** 2 + op[1] ** 2)
+                lm = -float(om[0] ** 2 + om[1] ** 2)
+                fd.append((lp - lm) / (2 * ADJ["h"]))
+            r["fd_knots"] = [int(i) for i in picks]
+            r["fd"] = fd
+        out[prec] = r
+        s.close()
+    g32, g64 = out[capi.FP32]["grad"], out[capi.FP64]["grad"]
+    picks, fd = out[capi.FP64]["fd_knots"], np.array(out[capi.FP64]["fd"])
+    rel_fd64 = np.abs(g64[picks] - fd) / np.maximum(np.abs(fd), 1e-300)
+    rel_fd32 = np.abs(g32[picks] - fd) / np.maximum(np.abs(fd), 1e-300)
+    sites = lat.nodes * dims[0] * dims[1] * dims[2]
+    f32 = out[capi.FP32]
+    grad_s = f32["forward_s"] + f32["backward_s"]
+    res = {"metric": "adjoint gradient evaluations/s (forward + reverse run, 2000 steps)", "value": 1.0 / grad_s,
+           "unit": "gradients/s", "n_gpus": 1, "steps": max(1, args.steps), "warmup": 1,
+           "ms_per_step": 1e3 * grad_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "adjoint ramp control, spin-1 BCC 64^3 cells (%d sites), %d steps, %d+%d knots, "
+                                  "%d-step checkpoints" % (sites, ADJ["steps"], ADJ["knots"], ADJ["knots"], ADJ["stride"]),
+                      "dt": DT, "c0": C0, "c2": C2, "loss": "1 - |<monopole|psi(T)>|^2"},
+           "forward_ms": 1e3 * f32["forward_s"], "backward_ms": 1e3 * f32["backward_s"],
+           "reverse_site_updates_per_s": sites * ADJ["steps"] / f32["backward_s"],
+           "gpu_launches": f32["launches_per_gradient"],
+           "loss_fp32": f32["loss"], "loss_fp64": out[capi.FP64]["loss"],
+           "fp64_adjoint_vs_fd_max_rel": float(rel_fd64.max()), "fp32_adjoint_vs_fd_max_rel": float(rel_fd32.max()),
+           "fp32_vs_fp64_adjoint_rel": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
+           "fd_h": ADJ["h"], "fd_knots": picks, "fd": [float(x) for x in fd],
+           "adjoint_fp64_at_fd_knots": [float(x) for x in g64[picks]],
+           "fp64_forward_ms": 1e3 * out[capi.FP64]["forward_s"], "fp64_backward_ms": 1e3 * out[capi.FP64]["backward_s"]}
+    print(json.dumps(res))
+    return 0
+
+
 def config_dict():
     return {"workload": "spin-1 GPE, BCC 96^3 block cells (10,616,832 sites), leapfrog FP32 fused + FP64 observables every 100 steps",
             "lattice": "bcc", "cells": list(DIMS), "components": 3, "dt": DT, "c0": C0, "c2": C2,
@@ -506,13 +606,15 @@ def main():
     ap.add_argument("--zchunk", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--autotune", action="store_true", help="run gpe_autotune before timing")
-    ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96"] + sorted(LEGS))
+    ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96", "adjoint-bcc64"] + sorted(LEGS))
     ap.add_argument("--inner", type=int, default=0, help="leapfrog steps per bench step for --workload legs")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "adjoint-bcc64":
+        return run_adjoint(args)
     if args.workload != "spin1-bcc96":
         return run_leg(args)
     return run_gpu(args)

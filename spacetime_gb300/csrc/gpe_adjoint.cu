@@ -11,10 +11,13 @@
 // b = i lambda_{j+1} (i times a vector is the transpose of -i times one):
 //     (dF_j/du)^T lambda = 2 dt [ L^T b + (dh/du)^T b ],
 // L the DEC Laplacian (L^T takes each entry's weight from its reverse entry) and
-// h(u) the local part of H(u) u (trap, interaction, Zeeman, loss).  The local
-// Jacobian-transpose products are exact: the step kernels' own local_terms
-// templates evaluated on forward-mode dual numbers, once per real coordinate of
-// the node (2C evaluations) and once per field parameter (Bq, Bb.x, Bb.y, Bb.z).
+// h(u) the local part of H(u) u (trap, interaction, Zeeman, loss).  Without the
+// loss term h is the Wirtinger gradient dE/d(conj u) of a real local energy, so
+// its real Jacobian is symmetric and (dh/du)^T b = (dh/du) b: one evaluation of
+// the step kernels' own local_terms template on forward-mode dual numbers along
+// b.  The three-body loss term -i alpha n^2 u is not Hermitian; its transpose is
+// added in closed form.  The field gradients use dh/dBb_k = F_k u (Zeeman) and
+// dB/dBq from mag_field.
 //
 // Checkpointing: the forward run keeps (u_{kS}, u_{kS+1}) for every segment k of
 // S steps; the reverse run recomputes one segment at a time from its pair with the
@@ -84,15 +87,6 @@ __device__ __forceinline__ PhysR<Dual<R>> dual_phys(const PhysR<R>& P) {
     return Q;
 }
 
-// sum_c (b_c . dH_c) over the derivative parts of a dual evaluation
-template <typename R, int C>
-__device__ __forceinline__ R dot_d(const Cx<R>* b, const Cx<Dual<R>>* H) {
-    R s = 0;
-#pragma unroll
-    for (int c = 0; c < C; ++c) s += b[c].x * H[c].x.d + b[c].y * H[c].y.d;
-    return s;
-}
-
 // Local spin density <F> (unnormalised), the quantity gpe_observe integrates.
 template <typename R, int C>
 __device__ __forceinline__ void local_mag(const Cx<R>* ps, R M[3]) {
@@ -122,6 +116,7 @@ struct AdjArgs {
     const double* wT64;     // per entry: weight of the reverse entry (0 for repeated entries)
     const float* wT32;
     double factor;          // 2 dt (leapfrog) or dt (Euler start)
+    float factor32;         // the same, for the FP32 kernel
     int update;             // 0: field gradients only (the start step)
 };
 
@@ -137,10 +132,12 @@ __device__ __forceinline__ void node_coords(const StepArgs& a, uint32_t i, uint3
     y = row - z * a.g.Y;
 }
 
-// Block sum of K doubles per thread into partials[blockIdx.x * K + k] (blockDim 256).
-template <int K>
-__device__ __forceinline__ void block_partials(double (&v)[K], double* partials) {
-    __shared__ double red[8][K];
+// Block sum of K values per thread into partials[blockIdx.x * K + k] * scale
+// (blockDim 256): warp and block sums in the thread's type T, one conversion to
+// FP64 per block and value (FP64 and conversions share GB300's narrow FP64 pipe).
+template <int K, typename T>
+__device__ __forceinline__ void block_partials(T (&v)[K], double scale, double* partials) {
+    __shared__ T red[8][K];
 #pragma unroll
     for (int k = 0; k < K; ++k)
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
@@ -150,9 +147,9 @@ __device__ __forceinline__ void block_partials(double (&v)[K], double* partials)
     }
     __syncthreads();
     if (threadIdx.x < K) {
-        double s = 0;
+        T s = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
-        partials[(size_t)blockIdx.x * K + threadIdx.x] = s;
+        partials[(size_t)blockIdx.x * K + threadIdx.x] = (double)s * scale;
     }
 }
 
@@ -168,7 +165,7 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(StepArgs a, AdjArgs j
         else wT[i] = j.wT64[i];
     }
     __syncthreads();
-    double gsum[kGradCount] = {0, 0, 0, 0};
+    R gsum[kGradCount] = {(R)0, (R)0, (R)0, (R)0};
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid < a.total) {
         uint32_t x, y, z, l;
@@ -188,10 +185,7 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(StepArgs a, AdjArgs j
         r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
         r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + st.pos[3 * l + 1]);
         r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + st.pos[3 * l + 2]);
-        const PhysR<Dual<R>> PD = dual_phys<R>(P);
-        const Dual<R> rD[3] = {cd<R>(r[0]), cd<R>(r[1]), cd<R>(r[2])};
-        const Dual<R> potD = cd<R>(trap<R>(P, r));
-        Cx<Dual<R>> psD[C], H[C];
+        const R pot = trap<R>(P, r);
         if (j.update) {
             // L^T b = sum_f wT_f b_nb(f) - (sum_f w_f) b
             Cx<R> K[C];
@@ -208,61 +202,110 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(StepArgs a, AdjArgs j
                     K[c] += wt * cx<R>(-av.y, av.x);
                 }
             }
-            // (dh/du)^T b: one dual evaluation per real input coordinate
-            R g[2 * C];
+            // (dh/du)^T b.  Apart from three-body loss, h = dE/d(conj u) for a real
+            // energy E (trap, c0 n^2/2, Zeeman B.<F>, c2 <F>^2/2, quadratic Zeeman,
+            // spin-2 singlet |A00|^2), so its real Jacobian is half the Hessian of E,
+            // symmetric: J^T b = J b, one dual evaluation along b.
+            PhysR<Dual<R>> PD = dual_phys<R>(P);
+            PD.flags &= ~GPE_FLAG_THREE_BODY_LOSS;
+            const Dual<R> rD[3] = {cd<R>(r[0]), cd<R>(r[1]), cd<R>(r[2])};
+            Cx<Dual<R>> psD[C], H[C];
 #pragma unroll
-            for (int k = 0; k < 2 * C; ++k) {
+            for (int c = 0; c < C; ++c) {
+                psD[c] = cx<Dual<R>>(Dual<R>(u[c].x, b[c].x), Dual<R>(u[c].y, b[c].y));
+                H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
+            }
+            local_terms<Dual<R>, C>(PD, rD, cd<R>(pot), GPE_MODE_LEAPFROG, false, psD, H);
+            Cx<R> g[C];
+#pragma unroll
+            for (int c = 0; c < C; ++c) g[c] = cx<R>(H[c].x.d, H[c].y.d);
+            if (P.flags & GPE_FLAG_THREE_BODY_LOSS) {
+                // h_loss = -i alpha n^2 u: J^T b = i alpha n^2 b + 4 alpha n Im(b^H u) u
+                R n = 0, im = 0;
 #pragma unroll
                 for (int c = 0; c < C; ++c) {
-                    psD[c] = cx<Dual<R>>(Dual<R>(u[c].x, (R)(k == 2 * c)), Dual<R>(u[c].y, (R)(k == 2 * c + 1)));
-                    H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
+                    n += u[c].x * u[c].x + u[c].y * u[c].y;
+                    im += b[c].x * u[c].y - b[c].y * u[c].x;
                 }
-                local_terms<Dual<R>, C>(PD, rD, potD, GPE_MODE_LEAPFROG, false, psD, H);
-                g[k] = dot_d<R, C>(b, H);
+                const R an2 = P.alpha * n * n, k4 = (R)4 * P.alpha * n * im;
+#pragma unroll
+                for (int c = 0; c < C; ++c) g[c] += cx<R>(-an2 * b[c].y + k4 * u[c].x, an2 * b[c].x + k4 * u[c].y);
             }
             char* o = j.a_next + cell_off + l * node_bytes;
-            const R fac = (R)j.factor;
+            R fac;
+            if constexpr (sizeof(R) == 4) fac = j.factor32;
+            else fac = j.factor;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
                 Cx<R> v = ldc_rw<R>(o + c * 2 * sizeof(R));
-                v.x += fac * (K[c].x - diag * b[c].x + g[2 * c]);
-                v.y += fac * (K[c].y - diag * b[c].y + g[2 * c + 1]);
+                v.x += fac * (K[c].x - diag * b[c].x + g[c].x);
+                v.y += fac * (K[c].y - diag * b[c].y + g[c].y);
                 stc<R>(o + c * 2 * sizeof(R), v);
             }
         }
-        // field parameters: (dh/dBq)^T b and (dh/dBb_k)^T b
+        // field parameters.  h depends on Bb only through the Zeeman term (B.F) u,
+        // so dh/dBb_k = F_k u: the local terms with every coefficient zero except
+        // Bb = e_k.  dB/dBq is mag_field's B at Bq = 1, Bb = 0.
+        if constexpr (C > 1) {
+            PhysR<R> Z = P;
+            Z.c0 = Z.c2 = Z.c4 = Z.alpha = Z.bq = Z.bqq = (R)0;
+            Z.flags = 0;
+            Z.trap_on = 0;
+            R s3[3];
 #pragma unroll
-        for (int c = 0; c < C; ++c) psD[c] = cx<Dual<R>>(cd<R>(u[c].x), cd<R>(u[c].y));
+            for (int k = 0; k < 3; ++k) {
 #pragma unroll
-        for (int q = 0; q < kGradCount; ++q) {
-            PhysR<Dual<R>> Q = PD;
-            if (q == 0) Q.bq = Dual<R>(P.bq, (R)1);
-            else Q.bb[q - 1] = Dual<R>(P.bb[q - 1], (R)1);
+                for (int i = 0; i < 3; ++i) Z.bb[i] = (R)(i == k);
+                Cx<R> H[C];
 #pragma unroll
-            for (int c = 0; c < C; ++c) H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
-            local_terms<Dual<R>, C>(Q, rD, potD, GPE_MODE_LEAPFROG, false, psD, H);
-            gsum[q] = j.factor * (double)dot_d<R, C>(b, H);
+                for (int c = 0; c < C; ++c) H[c] = cx<R>((R)0, (R)0);
+                local_terms<R, C>(Z, r, (R)0, GPE_MODE_LEAPFROG, false, u, H);
+                R d = 0;
+#pragma unroll
+                for (int c = 0; c < C; ++c) d += b[c].x * H[c].x + b[c].y * H[c].y;
+                s3[k] = d;
+            }
+            const R zero3[3] = {(R)0, (R)0, (R)0};
+            R w[3];
+            mag_field<R>(P, r, (R)1, zero3, w);
+            gsum[0] = w[0] * s3[0] + w[1] * s3[1] + w[2] * s3[2];
+            gsum[1] = s3[0];
+            gsum[2] = s3[1];
+            gsum[3] = s3[2];
         }
     }
-    block_partials<kGradCount>(gsum, a.partials);
+    block_partials<kGradCount, R>(gsum, j.factor, a.partials);
 }
 
-// Adds nblocks x K partials into out[0..K) * scale in a fixed order (one block of 256).
-__global__ void __launch_bounds__(256) adjoint_sum_kernel(const double* partials, uint32_t nblocks, int K, double scale,
-                                                          double* out) {
-    __shared__ double red[256];
-    for (int k = 0; k < K; ++k) {
-        double s = 0;
-        for (uint32_t b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(size_t)b * K + k];
-        red[threadIdx.x] = s;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
+// Block g adds the nblocks x K partials at partials + g * nblocks * K into
+// out[g * K + k] * scale in a fixed order: thread t sums partial blocks t,
+// t + kSumThreads, ... for all K values at once, then a tree over the threads.
+// One launch reduces the partials of every step of a checkpoint segment.
+constexpr int kSumThreads = 1024;
+template <int K>
+__global__ void __launch_bounds__(kSumThreads) adjoint_sum_kernel(const double* partials, uint32_t nblocks, double scale,
+                                                                  double* out) {
+    __shared__ double red[K][kSumThreads];
+    const double* src = partials + (size_t)blockIdx.x * nblocks * K;
+    double s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = 0.0;
+#pragma unroll 4
+    for (uint32_t b = threadIdx.x; b < nblocks; b += kSumThreads) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] += src[(size_t)b * K + k];
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k][threadIdx.x] = s[k];
+    __syncthreads();
+    for (int w = kSumThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
         }
-        if (threadIdx.x == 0) out[k] = red[0] * scale;
         __syncthreads();
     }
+    if (threadIdx.x < K) out[(size_t)blockIdx.x * K + threadIdx.x] = red[threadIdx.x][0] * scale;
 }
 
 constexpr int kFinalCount = 5;  // Re <T|u>, Im <T|u>, Mx, My, Mz
@@ -293,7 +336,7 @@ __global__ void __launch_bounds__(256) adjoint_final_kernel(StepArgs a) {
         v[3] = M[1];
         v[4] = M[2];
     }
-    block_partials<kFinalCount>(v, a.partials);
+    block_partials<kFinalCount, double>(v, 1.0, a.partials);
 }
 
 // lambda_N = dv [ (s0 + i s1) T + sum_m s_{2+m} grad M_m(u_N) ].
@@ -334,11 +377,10 @@ __global__ void __launch_bounds__(256) adjoint_seed_kernel(StepArgs a, const cha
     for (int c = 0; c < C; ++c) stc<R>(a.next + off + c * 2 * sizeof(R), cx<R>((R)(dv * g[c].x), (R)(dv * g[c].y)));
 }
 
+// One reverse step; its block partials go to a.partials (nblocks x kGradCount).
 template <typename R, int C>
-static cudaError_t launch_adjoint_step(const StepArgs& a, const AdjArgs& j, double* out, cudaStream_t s) {
-    const unsigned nb = nblocks(a.total, 256);
-    adjoint_step_kernel<R, C><<<nb, 256, 0, s>>>(a, j);
-    adjoint_sum_kernel<<<1, 256, 0, s>>>(a.partials, nb, kGradCount, 1.0, out);
+static cudaError_t launch_adjoint_step(const StepArgs& a, const AdjArgs& j, cudaStream_t s) {
+    adjoint_step_kernel<R, C><<<nblocks(a.total, 256), 256, 0, s>>>(a, j);
     return cudaGetLastError();
 }
 
@@ -346,7 +388,7 @@ template <typename R, int C>
 static cudaError_t launch_adjoint_final(const StepArgs& a, double dv, double* out, cudaStream_t s) {
     const unsigned nb = nblocks(a.total, 256);
     adjoint_final_kernel<R, C><<<nb, 256, 0, s>>>(a);
-    adjoint_sum_kernel<<<1, 256, 0, s>>>(a.partials, nb, kFinalCount, dv, out);
+    adjoint_sum_kernel<kFinalCount><<<1, kSumThreads, 0, s>>>(a.partials, nb, dv, out);
     return cudaGetLastError();
 }
 
@@ -380,6 +422,9 @@ void adjoint_release(gpe_handle* h) {
     if (A.target) cudaFree(A.target);
     if (A.grad) cudaFree(A.grad);
     if (A.out) cudaFree(A.out);
+    if (A.part) cudaFree(A.part);
+    A.part = nullptr;
+    A.part_count = 0;
     if (A.wT64) cudaFree(A.wT64);
     if (A.wT32) cudaFree(A.wT32);
     A.target = nullptr;
@@ -468,6 +513,15 @@ static gpe_status ensure_adjoint_buffers(gpe_handle* h, int n, int stride) {
     if (!A.grad && cudaMalloc(&A.grad, (size_t)n * kGradCount * sizeof(double)) != cudaSuccess)
         return fail(GPE_ERR_OOM, "cudaMalloc (gradients)");
     if (!A.out && cudaMalloc(&A.out, 8 * sizeof(double)) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (adjoint out)");
+    const size_t part = (size_t)stride * h->partial_blocks * kGradCount;
+    if (A.part && A.part_count < part) {
+        cudaFree(A.part);
+        A.part = nullptr;
+    }
+    if (!A.part) {
+        if (cudaMalloc(&A.part, part * sizeof(double)) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (adjoint partials)");
+        A.part_count = part;
+    }
     if (!A.wT64) {
         gpe_status st = build_transpose(h);
         if (st) return st;
@@ -584,8 +638,10 @@ extern "C" gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, do
                                    A.t0 + jj * dt, GPE_MODE_LEAPFROG, s)))
                 return st;
         }
+        const unsigned nb = nblocks(h->g.X * (uint64_t)h->g.Y * h->g.Z * h->g.V, 256);
         for (int j = hi - 1; j >= lo; --j) {
             StepArgs a = make_args(h, A.fields[j], A.t0 + j * dt);
+            a.partials = A.part + (size_t)(j - lo) * nb * kGradCount;
             AdjArgs aj;
             aj.a_prev = P;
             aj.a_next = Q;
@@ -593,12 +649,17 @@ extern "C" gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, do
             aj.wT64 = A.wT64;
             aj.wT32 = A.wT32;
             aj.factor = j >= 1 ? 2.0 * dt : dt;
+            aj.factor32 = (float)aj.factor;
             aj.update = j >= 1 ? 1 : 0;
-            e = GPE_ADJ_DISPATCH(launch_adjoint_step, h, a, aj, A.grad + (size_t)j * kGradCount, s);
+            e = GPE_ADJ_DISPATCH(launch_adjoint_step, h, a, aj, s);
             if (e != cudaSuccess) return cuda_fail(e, "adjoint step kernel");
-            h->launches += 2;
+            h->launches += 1;
             if (j >= 1) std::swap(P, Q);
         }
+        // the field gradients of the segment's steps, one block per step
+        adjoint_sum_kernel<kGradCount><<<len, kSumThreads, 0, s>>>(A.part, nb, 1.0, A.grad + (size_t)lo * kGradCount);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "adjoint gradient sums");
+        h->launches += 1;
     }
     e = cudaMemcpyAsync(grad, A.grad, (size_t)n * kGradCount * sizeof(double), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

@@ -35,6 +35,8 @@ struct AdjointStore {
     size_t buf_bytes = 0;
     double* grad = nullptr;         // device, n x 4
     double* out = nullptr;          // device, 8
+    double* part = nullptr;         // device, stride x blocks x 4: block partials of one segment
+    size_t part_count = 0;
     double* wT64 = nullptr;         // transposed Laplacian weights
     float* wT32 = nullptr;
     bool valid = false;
