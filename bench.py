@@ -230,6 +230,117 @@ def run_adjoint(args):
     return 0
 
 
+# Batched ensemble: 256 condensates, block-cell edge n ~ U{24..80}, lattice ~ U{BCC,
+# FCC, A15, C15}, scalar or spin-1, trap omega ~ U[0.8, 1.2]^3, seeded ramps (Bz
+# linear between two values in [-1, 1] over 2000 steps, Bq constant in [0, 0.5]),
+# box [-8, 8]^3, dt = 5e-5, FP32 with FP64 observables; all advanced by the
+# persistent batch kernel, n steps recorded in one CUDA graph.
+ENS = dict(members=256, edge=(24, 80), lattices=("bcc", "fcc", "a15", "c15"), seed=5, dt=5e-5, ramp_steps=2000)
+
+
+def ensemble_members(count=None):
+    """The seeded ensemble: a list of (lattice, components, edge, omega, ramp) tuples."""
+    from spacetime_gb300 import capi, states
+
+    out = []
+    for i in range(count or ENS["members"]):
+        u = states.uniform01(ENS["seed"], 8, offset=8 * i)
+        lo, hi = ENS["edge"]
+        n = lo + min(int(u[0] * (hi - lo + 1)), hi - lo)
+        lat = ENS["lattices"][min(int(u[1] * 4), 3)]
+        comps = 1 if u[2] < 0.5 else 3
+        omega = tuple(0.8 + 0.4 * u[3:6])
+        bz0, bz1, bq = 2 * u[6] - 1, 2 * u[7] - 1, 0.5 * u[5]
+        ramp = capi.make_ramp(bq_segments=[(bq, 1e30, capi.RAMP_CONSTANT)],
+                              bb_segments=[((0, 0, bz0), 0.0, capi.RAMP_CONSTANT),
+                                           ((0, 0, bz1), ENS["ramp_steps"] * ENS["dt"], capi.RAMP_LINEAR),
+                                           ((0, 0, bz1), 1e30, capi.RAMP_CONSTANT)])
+        out.append((lat, comps, n, omega, ramp))
+    return out
+
+
+def run_ensemble(args):
+    """--workload ensemble-256: every member advanced by the persistent batch kernel,
+    `inner` steps per graph replay, timed with CUDA events."""
+    import ctypes as C
+
+    import torch
+
+    from spacetime_gb300 import capi, states
+    from spacetime_gb300.batch import Batch
+    from spacetime_gb300.stepper import Stepper
+
+    inner = args.inner or 100
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    members, algo, state_bytes, specs = [], 0, 0, ensemble_members()
+    t_setup = time.perf_counter()
+    for i, (name, comps, n, omega, ramp) in enumerate(specs):
+        lat = capi.Lattice(name)
+        bs = BOX / (n * lat.block_width[0])
+        p = capi.make_params(components=comps, precision=capi.FP32, dims=(n, n, n), block_scale=bs, dt=ENS["dt"],
+                             trap_offset=100.0, trap_lambda=omega, c0=C0, c2=C2 if comps == 3 else 0.0, lattice=lat)
+        s = Stepper(lat, p)
+        s.stream = sp
+        init = capi.make_init(zeta=states.POLAR, noise_rel=1e-3, seed=1000 + i) if comps == 3 else \
+            capi.make_init(zeta=(1.0,), kappa=1, noise_abs=1e-3, seed=1000 + i)
+        s.init_state(capi.PSI_ODD, init)
+        s.set_ramp(ramp)
+        s.start()
+        members.append(s)
+        algo += (72 if comps == 3 else 24) * s.sites
+        state_bytes += (24 if comps == 3 else 8) * s.sites
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    b = Batch(members)
+    b.stream = sp
+    sites = b.sites
+    tune = b.autotune(steps=2)
+    e_first = [members[k].observe(members[k].current) for k in (0, len(members) // 2, len(members) - 1)]
+    b.capture(inner, sp)
+    for _ in range(max(1, args.warmup)):
+        b.replay()
+    n0 = b.launches
+    ev = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            x.record(stream)
+            b.replay()
+            y.record(stream)
+            ev.append((x, y))
+        torch.cuda.synchronize()
+    ms = [x.elapsed_time(y) for x, y in ev]
+    total_ms = sum(ms)
+    launches = b.launches - n0
+    e_last = [members[k].observe(members[k].current) for k in (0, len(members) // 2, len(members) - 1)]
+    peak, kind = measured_peak()
+    step_ms = total_ms / (args.steps * inner)
+    counts = {}
+    for name, comps, n, _, _ in specs:
+        key = "%s/%s" % (name, "spin1" if comps == 3 else "scalar")
+        counts[key] = counts.get(key, 0) + 1
+    res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
+           "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup),
+           "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "ensemble of %d condensates (edge 24..80, BCC/FCC/A15/C15, scalar + spin-1), "
+                                  "%d leapfrog steps per CUDA-graph replay" % (len(members), inner),
+                      "sites": sites, "members": counts, "dt": ENS["dt"],
+                      "l2": "inputs larger than L2 (%.1f GB per state buffer set), no flush" % (state_bytes / 1e9)},
+           "roofline": {"bound": "hbm", "achieved": algo / (step_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": algo / (step_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": "batch_kernel<float,3>",
+                        "algorithmic_bytes_per_step": algo, "avg_step_ms": step_ms, "traffic": None},
+           "gpu_launches": launches, "graph_replays": args.steps, "clocks": clk.summary(), "setup_s": setup_s,
+           "autotune": tune,
+           "norm_rel_change": [abs(b2["norm"] - a2["norm"]) / a2["norm"] for a2, b2 in zip(e_first, e_last)]}
+    b.close()
+    for s in members:
+        s.close()
+    print(json.dumps(res))
+    return 0
+
+
 def config_dict():
     return {"workload": "spin-1 GPE, BCC 96^3 block cells (10,616,832 sites), leapfrog FP32 fused + FP64 observables every 100 steps",
             "lattice": "bcc", "cells": list(DIMS), "components": 3, "dt": DT, "c0": C0, "c2": C2,
@@ -606,7 +717,7 @@ def main():
     ap.add_argument("--zchunk", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--autotune", action="store_true", help="run gpe_autotune before timing")
-    ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96", "adjoint-bcc64"] + sorted(LEGS))
+    ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96", "adjoint-bcc64", "ensemble-256"] + sorted(LEGS))
     ap.add_argument("--inner", type=int, default=0, help="leapfrog steps per bench step for --workload legs")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
@@ -615,6 +726,8 @@ def main():
         return run_reference(args)
     if args.workload == "adjoint-bcc64":
         return run_adjoint(args)
+    if args.workload == "ensemble-256":
+        return run_ensemble(args)
     if args.workload != "spin1-bcc96":
         return run_leg(args)
     return run_gpu(args)

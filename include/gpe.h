@@ -338,6 +338,48 @@ gpe_status gpe_adjoint_forward(gpe_handle* h, int32_t n_steps, const gpe_fields*
                                const double* target, size_t count, double* out, void* stream);
 gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, double* grad, void* stream);
 
+/* Batched stepping of many condensates (parabolic scheme).  No counterpart in the
+ * reference, which runs one condensate per process and one kernel launch per step
+ * (Spin1GpeBCC.cu:1574-1603).  A batch is built over existing handles of one
+ * precision -- any lattices, grid sizes, component counts (1, 3, 5), traps and
+ * ramps -- and advances all of them with one cooperative persistent kernel: the
+ * members' rows are cut into work items of about GPE_BATCH_ITEM_NODES nodes, each
+ * block of the persistent grid processes its share of items, evaluates the next
+ * step's fields of the members from their own ramps on the device, and meets the
+ * other blocks at a grid barrier whose wait is bounded in time (GPE_ERR_TIMEOUT).
+ * Every member takes exactly the steps gpe_step would take (same time, fields,
+ * trap switch and update), and the members' handles are updated as if gpe_step(n)
+ * had been called on each, so gpe_observe / gpe_download / gpe_step keep working on
+ * them.  The handles must outlive the batch and must not be used concurrently
+ * with it; gpe_batch_step, _replay and _autotune synchronise the device before
+ * they read the members' state, so earlier calls on any stream are complete.
+ *
+ * gpe_batch_step: n steps now (ceil(n / GPE_BATCH_STEPS_PER_LAUNCH) launches;
+ *   0 = one launch).  Synchronises.
+ * gpe_batch_capture: records an n-step call into a CUDA graph on `stream` (which
+ *   must not be the legacy default stream); gpe_batch_replay launches it (one
+ *   graph launch per n steps of every member) and synchronises.  The graph reads
+ *   the members' current slot, step count and ramp at each replay.
+ * gpe_batch_autotune: per lattice (nodes and stencil entries per cell), times
+ *   `steps` steps of up to four of its members on scratch copies of their
+ *   buffers, on a grid scaled so that each block has the work it has in the
+ *   whole batch, for item sizes of 4K..256K nodes, and keeps the fastest; the
+ *   members' states are untouched.  Blocks own contiguous item ranges of equal
+ *   nodes x components.
+ *   `report` receives a JSON list of the timings. */
+typedef struct gpe_batch gpe_batch;
+enum { GPE_BATCH_ITEM_NODES = 0, GPE_BATCH_STEPS_PER_LAUNCH = 1, GPE_BATCH_BLOCKS_PER_SM = 2 };
+gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count, gpe_batch** out);
+gpe_status gpe_batch_destroy(gpe_batch* b);
+gpe_status gpe_batch_step(gpe_batch* b, int32_t n, void* stream);
+gpe_status gpe_batch_capture(gpe_batch* b, int32_t n, void* stream);
+gpe_status gpe_batch_replay(gpe_batch* b, void* stream);
+gpe_status gpe_batch_set_tuning(gpe_batch* b, int32_t key, int32_t value);
+gpe_status gpe_batch_get_tuning(const gpe_batch* b, int32_t key, int32_t* value);
+gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* report, size_t report_len, void* stream);
+uint64_t gpe_batch_sites(const gpe_batch* b);
+uint64_t gpe_batch_launch_count(const gpe_batch* b);
+
 /* Number of CUDA kernel launches this handle has issued (for accounting). */
 uint64_t gpe_launch_count(const gpe_handle* h);
 

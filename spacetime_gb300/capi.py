@@ -37,6 +37,7 @@ PSI_EVEN, PSI_ODD, Q_EVEN, Q_ODD, HPSI = 0, 1, 2, 3, 4
 MODE_LEAPFROG, MODE_EULER, MODE_ITP = 0, 1, 2
 TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS = 0, 1, 2, 3, 4
 KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS = 0, 1, 2, 3, 4
+BATCH_ITEM_NODES, BATCH_STEPS_PER_LAUNCH, BATCH_BLOCKS_PER_SM = 0, 1, 2
 
 
 class StencilEntry(C.Structure):
@@ -317,6 +318,16 @@ def load_library(path: str = LIB_PATH):
         "gpe_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
         "gpe_adjoint_forward": (C.c_int, [vp, C.c_int32, P(Fields), C.c_int32, P(C.c_double), C.c_size_t, P(C.c_double), vp]),
         "gpe_adjoint_backward": (C.c_int, [vp, P(C.c_double), P(C.c_double), vp]),
+        "gpe_batch_create": (C.c_int, [P(vp), C.c_int32, P(vp)]),
+        "gpe_batch_destroy": (C.c_int, [vp]),
+        "gpe_batch_step": (C.c_int, [vp, C.c_int32, vp]),
+        "gpe_batch_capture": (C.c_int, [vp, C.c_int32, vp]),
+        "gpe_batch_replay": (C.c_int, [vp, vp]),
+        "gpe_batch_set_tuning": (C.c_int, [vp, C.c_int32, C.c_int32]),
+        "gpe_batch_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
+        "gpe_batch_autotune": (C.c_int, [vp, C.c_int32, C.c_char_p, C.c_size_t, vp]),
+        "gpe_batch_sites": (C.c_uint64, [vp]),
+        "gpe_batch_launch_count": (C.c_uint64, [vp]),
         "gpe_sites": (C.c_uint64, [vp]),
         "gpe_last_error": (C.c_char_p, []),
         "gpe_version": (C.c_char_p, []),

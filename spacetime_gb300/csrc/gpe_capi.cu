@@ -151,39 +151,7 @@ extern "C" gpe_status gpe_ramp_eval(const gpe_ramp* r, double tau, gpe_fields* o
     if (r->bq_segments < 0 || r->bq_segments > GPE_RAMP_MAX_SEGMENTS || r->bb_segments < 0 ||
         r->bb_segments > GPE_RAMP_MAX_SEGMENTS)
         return fail(GPE_ERR_INVALID_ARG, "segment count out of range");
-    // walk consecutive segment durations; inside segment k interpolate from the
-    // previous target (0 before the first) by the segment's type.
-    auto channel = [](int nseg, const double* tgt, int stride, const double* dur, const int32_t* type, double tau,
-                      double* val, int dims) {
-        for (int a = 0; a < dims; ++a) val[a] = 0;
-        if (nseg == 0) return;
-        int k = 0;
-        double t = tau;
-        while (k < nseg && t - dur[k] >= 0) {
-            t -= dur[k];
-            ++k;
-        }
-        if (k == nseg) {  // past the end: hold the last target
-            k = nseg - 1;
-            t = dur[k];
-        }
-        for (int a = 0; a < dims; ++a) {
-            const double target = tgt[k * stride + a];
-            const double prev = k > 0 ? tgt[(k - 1) * stride + a] : 0.0;
-            if (type[k] == GPE_RAMP_CONSTANT) val[a] = target;
-            else if (type[k] == GPE_RAMP_LINEAR) val[a] = prev + t * (target - prev) / dur[k];
-            else val[a] = prev + (target - prev) * std::sqrt(t / dur[k]);
-        }
-    };
-    double bq = 0, bb[3];
-    channel(r->bq_segments, r->bq_target, 1, r->bq_duration, r->bq_type, tau, &bq, 1);
-    channel(r->bb_segments, &r->bb_target[0][0], 3, r->bb_duration, r->bb_type, tau, bb, 3);
-    out->bq = r->bq_scale * bq;
-    out->bq_quad = r->bq_quad_scale * bq;
-    for (int a = 0; a < 3; ++a) {
-        out->bb[a] = r->bb_scale * bb[a];
-        out->bb_quad[a] = r->bb_quad_scale * bb[a];
-    }
+    ramp_eval(*r, tau, *out);
     return GPE_OK;
 }
 

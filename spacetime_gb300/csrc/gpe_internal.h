@@ -1,6 +1,7 @@
 // gpe_internal.h -- shared host/device definitions of libgpe (not part of the ABI).
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -145,6 +146,52 @@ struct StepArgs {
     double* partials;     // observables
     int* err;             // device error flag (bounded waits that ran out)
 };
+
+#ifdef __CUDACC__
+#define GPE_HD __host__ __device__
+#else
+#define GPE_HD
+#endif
+
+// getSignal + scaling (Spin1GpeBCC/AliceRingRamps.h:74-141): each channel walks its
+// consecutive segment durations; inside segment k the value goes from the previous
+// target (0 before the first) to target k by the segment's type; past the end the
+// last target holds.  The same code runs on the host (gpe_ramp_eval) and on the
+// device (batched stepping).  Segment counts must be in [0, GPE_RAMP_MAX_SEGMENTS].
+GPE_HD inline void ramp_channel(int nseg, const double* tgt, int stride, const double* dur, const int32_t* type,
+                                double tau, double* val, int dims) {
+    for (int a = 0; a < dims; ++a) val[a] = 0;
+    if (nseg <= 0) return;
+    int k = 0;
+    double t = tau;
+    while (k < nseg && t - dur[k] >= 0) {
+        t -= dur[k];
+        ++k;
+    }
+    if (k == nseg) {
+        k = nseg - 1;
+        t = dur[k];
+    }
+    for (int a = 0; a < dims; ++a) {
+        const double target = tgt[k * stride + a];
+        const double prev = k > 0 ? tgt[(k - 1) * stride + a] : 0.0;
+        if (type[k] == GPE_RAMP_CONSTANT) val[a] = target;
+        else if (type[k] == GPE_RAMP_LINEAR) val[a] = prev + t * (target - prev) / dur[k];
+        else val[a] = prev + (target - prev) * sqrt(t / dur[k]);
+    }
+}
+
+GPE_HD inline void ramp_eval(const gpe_ramp& r, double tau, gpe_fields& out) {
+    double bq = 0, bb[3];
+    ramp_channel(r.bq_segments, r.bq_target, 1, r.bq_duration, r.bq_type, tau, &bq, 1);
+    ramp_channel(r.bb_segments, &r.bb_target[0][0], 3, r.bb_duration, r.bb_type, tau, bb, 3);
+    out.bq = r.bq_scale * bq;
+    out.bq_quad = r.bq_quad_scale * bq;
+    for (int a = 0; a < 3; ++a) {
+        out.bb[a] = r.bb_scale * bb[a];
+        out.bb_quad[a] = r.bb_quad_scale * bb[a];
+    }
+}
 
 // Sets the text returned by gpe_last_error() for this thread (gpe_capi.cu).
 void set_last_error(const std::string& msg);

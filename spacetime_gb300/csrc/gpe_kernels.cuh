@@ -287,24 +287,14 @@ __device__ __forceinline__ void write_update(int mode, R dt, char* nxt, char* hp
 
 // ---------------------------------------------------------------- parabolic
 
-// MODE: GPE_MODE_LEAPFROG / EULER / ITP.  One thread per (node, cell).
+// One node of a parabolic step: the DEC Laplacian gather, the local terms and the
+// time update (Spin1GpeBCC.cu:835-916).  prev/next/hpsi are the buffers' interior
+// pointers; (x, y, z) the cell, l the node.
 template <typename R, int C, int MODE>
-__global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
-    __shared__ SmemTables<R> st;
-    load_tables<R>(st, a);
-    __syncthreads();
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= a.total) return;
-    const uint32_t i = (uint32_t)gid;
-    const uint32_t row = fdiv(i, a.divRow);
-    const uint32_t within = i - row * a.row_items;
-    const uint32_t x = fdiv(within, a.divV);
-    const uint32_t l = within - x * a.g.V;
-    const uint32_t z = fdiv(row, a.divY);
-    const uint32_t y = row - z * a.g.Y;
-
-    const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
-    const char* base = a.prev + cell_off;
+__device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R>& st, const PhysR<R>& P, const char* prev,
+                                               char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l) {
+    const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
+    const char* base = prev + cell_off;
     const uint32_t node_bytes = C * 2 * sizeof(R);
     const char* own = base + l * node_bytes;
 
@@ -322,16 +312,33 @@ __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
 #pragma unroll
         for (int s = 0; s < C; ++s) H[s] += w * (ldc<R>(nb + s * 2 * sizeof(R)) - prv[s]);
     }
-    const PhysR<R>& P = make_phys<R>(a);
     R r[3];
     r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
     r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + st.pos[3 * l + 1]);
     r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + st.pos[3 * l + 2]);
     const R pot = trap<R>(P, r);
     local_terms<R, C>(P, r, pot, MODE, false, prv, H);
-    char* nxt = a.next + cell_off + l * node_bytes;
-    char* hp = (MODE == GPE_MODE_ITP && a.hpsi) ? a.hpsi + cell_off + l * node_bytes : nullptr;
+    char* nxt = next + cell_off + l * node_bytes;
+    char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
     write_update<R, C>(MODE, P.dt, nxt, hp, prv, H);
+}
+
+// MODE: GPE_MODE_LEAPFROG / EULER / ITP.  One thread per (node, cell).
+template <typename R, int C, int MODE>
+__global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
+    __shared__ SmemTables<R> st;
+    load_tables<R>(st, a);
+    __syncthreads();
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= a.total) return;
+    const uint32_t i = (uint32_t)gid;
+    const uint32_t row = fdiv(i, a.divRow);
+    const uint32_t within = i - row * a.row_items;
+    const uint32_t x = fdiv(within, a.divV);
+    const uint32_t l = within - x * a.g.V;
+    const uint32_t z = fdiv(row, a.divY);
+    const uint32_t y = row - z * a.g.Y;
+    parabolic_node<R, C, MODE>(a.g, st, make_phys<R>(a), a.prev, a.next, a.hpsi, x, y, z, l);
 }
 
 // ---------------------------------------------------------------- hyperbolic

@@ -1,0 +1,146 @@
+"""Batched stepping (gpe_batch_*) against the members stepped one by one.
+
+Members of different lattices, sizes, component counts, traps and ramps (one with
+the trap switched off mid-run) are advanced by the persistent batch kernel --
+directly, over several launches, and by CUDA-graph replay -- and compared with
+the same members stepped by gpe_step with the one-node-per-thread kernel, which
+computes the same per-node update: FP64 max |diff| <= 1e-12 * max|ref|, FP32
+<= 2e-6 * max|ref| (the fields are evaluated on the device instead of the host).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from spacetime_gb300 import capi, states
+from spacetime_gb300.batch import Batch
+from spacetime_gb300.stepper import Stepper
+
+pytestmark = pytest.mark.gpu
+
+TOL = {capi.FP64: 1e-12, capi.FP32: 2e-6}
+
+SPECS = [("bcc", 3, (7, 5, 4)), ("fcc", 1, (6, 5, 4)), ("a15", 3, (3, 4, 3)), ("c15", 1, (3, 2, 3)),
+         ("bcc", 1, (5, 6, 7)), ("c15", 3, (2, 3, 2)), ("bcc227", 5, (4, 3, 3))]
+
+
+def _member(spec, prec, idx, kernel=capi.KERNEL_GATHER):
+    name, comps, dims = spec
+    lat = capi.Lattice(name)
+    flags = capi.FLAG_TRAP_OFF_AFTER if idx == 1 else 0
+    p = capi.make_params(components=comps, precision=prec, dims=dims, block_scale=0.3, dt=2e-4, trap_offset=100.0,
+                         trap_lambda=(0.8 + 0.05 * idx, 1.0, 1.2 - 0.04 * idx), c0=120.0 + 10 * idx, c2=-7.0, c4=3.0,
+                         flags=flags, trap_off_time=1.5e-3, lattice=lat)
+    s = Stepper(lat, p)
+    s.set_tuning(capi.TUNE_KERNEL, kernel)
+    s.upload(capi.PSI_ODD, 0.2 * states.random_state(capi.buffer_shape(lat, p), seed=100 + idx))
+    ramp = capi.make_ramp(bq_segments=[(0.1 * idx, 0.0, capi.RAMP_CONSTANT), (0.3, 12 * 2e-4, capi.RAMP_LINEAR)],
+                          bb_segments=[((0.0, 0.0, 0.5), 0.0, capi.RAMP_CONSTANT),
+                                       ((0.1 * idx, -0.1, -0.5), 10 * 2e-4, capi.RAMP_LINEAR),
+                                       ((0.2, 0.0, 0.3), 6 * 2e-4, capi.RAMP_SQRT)],
+                          bq_quad_scale=0.5, bb_quad_scale=0.25)
+    s.set_ramp(ramp, t0=1e-4 * idx)
+    s.start()
+    return s
+
+
+def _pair(prec):
+    return [_member(sp, prec, i) for i, sp in enumerate(SPECS)], [_member(sp, prec, i) for i, sp in enumerate(SPECS)]
+
+
+def _compare(batched, ref, prec):
+    for a, b in zip(batched, ref):
+        assert a.current == b.current
+        for slot in (capi.PSI_EVEN, capi.PSI_ODD):
+            x, y = a.download(slot), b.download(slot)
+            scale = float(np.max(np.abs(y)))
+            err = float(np.max(np.abs(x - y)))
+            assert err <= TOL[prec] * scale, (slot, err, scale)
+
+
+def _close(ms):
+    for m in ms:
+        m.close()
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("per_launch", [0, 3])
+def test_batch_step_matches_members(gpu, prec, per_launch):
+    mem, ref = _pair(prec)
+    try:
+        with Batch(mem) as b:
+            b.set_tuning(capi.BATCH_ITEM_NODES, 200)  # several items per member
+            b.set_tuning(capi.BATCH_STEPS_PER_LAUNCH, per_launch)
+            b.step(11)
+            n0 = b.launches
+            assert n0 == (1 if per_launch == 0 else 4)
+        for r in ref:
+            r.step(11)
+        _compare(mem, ref, prec)
+    finally:
+        _close(mem + ref)
+
+
+def test_batch_graph_replay(gpu):
+    prec = capi.FP32
+    mem, ref = _pair(prec)
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    try:
+        with Batch(mem) as b:
+            b.stream = sp
+            b.set_tuning(capi.BATCH_STEPS_PER_LAUNCH, 2)
+            b.capture(5, sp)
+            b.replay()
+            b.replay()
+            for m in mem:  # the members stay usable on their own between batched calls
+                m.step(1)
+            b.replay()
+        for r in ref:
+            r.step(16)
+        _compare(mem, ref, prec)
+    finally:
+        _close(mem + ref)
+
+
+def test_batch_autotune_keeps_state(gpu):
+    prec = capi.FP32
+    mem, ref = _pair(prec)
+    try:
+        with Batch(mem) as b:
+            rep = b.autotune(steps=2)
+            assert len(rep) == 4 * 4 and all(r["ms_per_step"] > 0 for r in rep)  # 4 lattice keys x 4 sizes
+            b.step(4)
+        for r in ref:
+            r.step(4)
+        _compare(mem, ref, prec)
+    finally:
+        _close(mem + ref)
+
+
+def test_batch_rejects(gpu):
+    lat = capi.Lattice("bcc")
+    p32 = capi.make_params(components=3, precision=capi.FP32, dims=(4, 4, 4), block_scale=0.3, dt=1e-4, lattice=lat)
+    p64 = capi.make_params(components=3, precision=capi.FP64, dims=(4, 4, 4), block_scale=0.3, dt=1e-4, lattice=lat)
+    a, b2 = Stepper(lat, p32), Stepper(lat, p64)
+    try:
+        with pytest.raises(capi.GpeError):
+            Batch([a, b2])
+        with pytest.raises(capi.GpeError):
+            Batch([a, a])
+        hl = capi.Lattice("bcc")
+        ph = capi.make_params(components=3, scheme=capi.SCHEME_HYPERBOLIC, precision=capi.FP32, dims=(4, 4, 4),
+                              block_scale=0.3, dt=1e-4, sigma=0.01, lattice=hl)
+        try:
+            h = Stepper(hl, ph)
+        except capi.GpeError:
+            h = None
+        if h is not None:
+            with pytest.raises(capi.GpeError) as e:
+                Batch([a, h])
+            assert e.value.status == 6  # GPE_ERR_UNSUPPORTED
+            h.close()
+    finally:
+        a.close()
+        b2.close()
