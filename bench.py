@@ -160,7 +160,7 @@ def run_adjoint(args):
     out = {}
     for prec in (capi.FP32, capi.FP64):
         s = Stepper(lat, params(prec))
-        rc = RampControl(s, ADJ["steps"], ADJ["knots"], lambda: s.init_state(capi.PSI_ODD, init), target,
+        rc = RampControl(s, args.adjoint_steps, ADJ["knots"], lambda: s.init_state(capi.PSI_ODD, init), target,
                          stride=ADJ["stride"])
         reps = max(1, args.steps) if prec == capi.FP32 else 1
         fwd, bwd, grads, loss = [], [], None, None
@@ -184,7 +184,7 @@ def run_adjoint(args):
              "launches_per_gradient": launches}
         if prec == capi.FP64:
             rng = np.random.default_rng(ADJ["seed"])
-            picks = rng.choice(2 * ADJ["knots"], ADJ["fd_knots"], replace=False)
+            picks = rng.choice(2 * ADJ["knots"], args.fd_knots, replace=False)
             fd = []
             for i in picks:
                 kp, km = k.copy().ravel(), k.copy().ravel()
@@ -204,26 +204,27 @@ def run_adjoint(args):
         out[prec] = r
         s.close()
     g32, g64 = out[capi.FP32]["grad"], out[capi.FP64]["grad"]
-    picks, fd = out[capi.FP64]["fd_knots"], np.array(out[capi.FP64]["fd"])
-    rel_fd64 = np.abs(g64[picks] - fd) / np.maximum(np.abs(fd), 1e-300)
-    rel_fd32 = np.abs(g32[picks] - fd) / np.maximum(np.abs(fd), 1e-300)
+    picks, fd = out[capi.FP64]["fd_knots"], np.array(out[capi.FP64]["fd"], dtype=np.float64)
+    rel_fd64 = np.abs(g64[picks] - fd) / np.maximum(np.abs(fd), 1e-300) if len(picks) else np.zeros(1)
+    rel_fd32 = np.abs(g32[picks] - fd) / np.maximum(np.abs(fd), 1e-300) if len(picks) else np.zeros(1)
     sites = lat.nodes * dims[0] * dims[1] * dims[2]
     f32 = out[capi.FP32]
     grad_s = f32["forward_s"] + f32["backward_s"]
-    res = {"metric": "adjoint gradient evaluations/s (forward + reverse run, 2000 steps)", "value": 1.0 / grad_s,
+    res = {"metric": "adjoint gradient evaluations/s (forward + reverse run, %d steps)" % args.adjoint_steps,
+           "value": 1.0 / grad_s,
            "unit": "gradients/s", "n_gpus": 1, "steps": max(1, args.steps), "warmup": 1,
            "ms_per_step": 1e3 * grad_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic",
            "config": {"workload": "adjoint ramp control, spin-1 BCC 64^3 cells (%d sites), %d steps, %d+%d knots, "
-                                  "%d-step checkpoints" % (sites, ADJ["steps"], ADJ["knots"], ADJ["knots"], ADJ["stride"]),
+                                  "%d-step checkpoints" % (sites, args.adjoint_steps, ADJ["knots"], ADJ["knots"], ADJ["stride"]),
                       "dt": DT, "c0": C0, "c2": C2, "loss": "1 - |<monopole|psi(T)>|^2"},
            "forward_ms": 1e3 * f32["forward_s"], "backward_ms": 1e3 * f32["backward_s"],
-           "reverse_site_updates_per_s": sites * ADJ["steps"] / f32["backward_s"],
+           "reverse_site_updates_per_s": sites * args.adjoint_steps / f32["backward_s"],
            "gpu_launches": f32["launches_per_gradient"],
            "loss_fp32": f32["loss"], "loss_fp64": out[capi.FP64]["loss"],
            "fp64_adjoint_vs_fd_max_rel": float(rel_fd64.max()), "fp32_adjoint_vs_fd_max_rel": float(rel_fd32.max()),
            "fp32_vs_fp64_adjoint_rel": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
-           "fd_h": ADJ["h"], "fd_knots": picks, "fd": [float(x) for x in fd],
+           "fd_h": ADJ["h"], "fd_knots": [int(i) for i in picks], "fd": [float(x) for x in fd],
            "adjoint_fp64_at_fd_knots": [float(x) for x in g64[picks]],
            "fp64_forward_ms": 1e3 * out[capi.FP64]["forward_s"], "fp64_backward_ms": 1e3 * out[capi.FP64]["backward_s"]}
     print(json.dumps(res))
@@ -273,7 +274,7 @@ def run_ensemble(args):
     inner = args.inner or 100
     stream = torch.cuda.Stream()
     sp = C.c_void_p(stream.cuda_stream)
-    members, algo, state_bytes, specs = [], 0, 0, ensemble_members()
+    members, algo, state_bytes, specs = [], 0, 0, ensemble_members(args.members)
     t_setup = time.perf_counter()
     for i, (name, comps, n, omega, ramp) in enumerate(specs):
         lat = capi.Lattice(name)
@@ -342,7 +343,8 @@ def run_ensemble(args):
 
 
 def config_dict():
-    return {"workload": "spin-1 GPE, BCC 96^3 block cells (10,616,832 sites), leapfrog FP32 fused + FP64 observables every 100 steps",
+    return {"workload": "spin-1 GPE, BCC 96^3 block cells (10,616,832 sites), leapfrog FP32 fused + observables "
+                        "(FP32 node terms, FP64 sums) every 100 steps",
             "lattice": "bcc", "cells": list(DIMS), "components": 3, "dt": DT, "c0": C0, "c2": C2,
             "ramp": "Bz 0.5->-0.5 over 4000 steps, Bq 0.2", "inner_steps_per_step": INNER,
             "l2": "inputs larger than L2 (255 MB per psi buffer), no flush"}
@@ -522,6 +524,9 @@ def run_gpu(args):
     s = Stepper(lat, p)
     s.stream = C.c_void_p(stream.cuda_stream)
     sites = s.sites
+    # per-step observables: FP32 node terms, FP64 sums (the FP64-arithmetic form is
+    # kept for the drift check below and on request)
+    s.set_tuning(capi.TUNE_OBSERVE_ARITH, 0 if args.observe_fp64 else 1)
 
     def cur_slot():
         return s.current
@@ -644,6 +649,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
                 "d2h_bytes_per_step": 8 * 12, "steps": e2e_steps,
                 "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step(100) + gpe_observe"},
+        "observables": "FP64 node terms and sums" if args.observe_fp64 else "FP32 node terms, FP64 sums",
         "fp64_plain": {"value": fp64_value, "unit": "lattice-site-updates/s", "ms_per_launch": fp64_ms,
                        "speedup_fp32_fused": (sites / (launch_ms * 1e-3)) / fp64_value},
         "gpu_launches": launches,
@@ -719,6 +725,10 @@ def main():
     ap.add_argument("--autotune", action="store_true", help="run gpe_autotune before timing")
     ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96", "adjoint-bcc64", "ensemble-256"] + sorted(LEGS))
     ap.add_argument("--inner", type=int, default=0, help="leapfrog steps per bench step for --workload legs")
+    ap.add_argument("--observe-fp64", action="store_true", help="FP64 arithmetic for the per-step observables")
+    ap.add_argument("--adjoint-steps", type=int, default=ADJ["steps"], help="adjoint-bcc64: steps of the recorded run")
+    ap.add_argument("--fd-knots", type=int, default=ADJ["fd_knots"], help="adjoint-bcc64: knots checked by central differences")
+    ap.add_argument("--members", type=int, default=ENS["members"], help="ensemble-256: members of the ensemble (a prefix)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -275,8 +275,19 @@ gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* o
  * GPE_TUNE_TILE_ROWS: rows per tile along y (z-march TY, row-block RY; 0 = automatic).
  * GPE_TUNE_ZCHUNK: z-march planes per block, or row-block RZ (0 = automatic).
  * GPE_TUNE_THREADS: threads per row-block (a multiple of 32, at most 384; each
- *                   thread loops over the block's nodes; 0 = automatic). */
-enum { GPE_TUNE_KERNEL = 0, GPE_TUNE_TILE_CELLS = 1, GPE_TUNE_TILE_ROWS = 2, GPE_TUNE_ZCHUNK = 3, GPE_TUNE_THREADS = 4 };
+ *                   thread loops over the block's nodes; 0 = automatic).
+ * GPE_TUNE_OBSERVE_ARITH: arithmetic of gpe_observe's per-node terms on an FP32
+ *                   handle: 0 = FP64 (default; the same numbers as an FP64 run
+ *                   on the stored values), 1 = FP32.  The sums over nodes are FP64
+ *                   either way; mode 0 is bound by GB300's narrow FP64 pipe. */
+enum {
+    GPE_TUNE_KERNEL = 0,
+    GPE_TUNE_TILE_CELLS = 1,
+    GPE_TUNE_TILE_ROWS = 2,
+    GPE_TUNE_ZCHUNK = 3,
+    GPE_TUNE_THREADS = 4,
+    GPE_TUNE_OBSERVE_ARITH = 5
+};
 gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value);
 gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);
 

@@ -15,7 +15,7 @@ cudaError_t launch_parabolic(const StepArgs& a, int mode, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s);
 template <typename R, int C>
-cudaError_t launch_observe(const StepArgs& a, double* out, cudaStream_t s);
+cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s);
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s);
@@ -569,7 +569,8 @@ static cudaError_t dispatch_hyper(const gpe_handle* h, const StepArgs& a, int ki
 }
 template <int C>
 static cudaError_t dispatch_observe_c(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
-    return h->real_bytes == 8 ? launch_observe<double, C>(a, out, s) : launch_observe<float, C>(a, out, s);
+    return h->real_bytes == 8 ? launch_observe<double, C>(a, out, false, s)
+                              : launch_observe<float, C>(a, out, h->tune_observe != 0, s);
 }
 static cudaError_t dispatch_observe(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
     switch (h->g.C) {
@@ -1036,6 +1037,11 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
         }
         return GPE_OK;
     }
+    if (key == GPE_TUNE_OBSERVE_ARITH) {
+        if (value != 0 && value != 1) return fail(GPE_ERR_INVALID_ARG, "observe arithmetic: 0 (FP64) or 1 (storage precision)");
+        h->tune_observe = value;
+        return GPE_OK;
+    }
     if (key == GPE_TUNE_TILE_ROWS) {
         if (value < 0 || (uint32_t)value > h->g.Y) return fail(GPE_ERR_INVALID_ARG, "tile rows");
         h->tune_rows = value;
@@ -1069,6 +1075,7 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
     else if (key == GPE_TUNE_TILE_ROWS) *value = (int32_t)(tr > 0 ? rows_shape(h).RY : ms.TY);
     else if (key == GPE_TUNE_ZCHUNK) *value = (int32_t)(tr > 0 ? rows_shape(h).RZ : ms.ZC);
     else if (key == GPE_TUNE_THREADS) *value = h->tune_threads;
+    else if (key == GPE_TUNE_OBSERVE_ARITH) *value = h->tune_observe;
     else return fail(GPE_ERR_INVALID_ARG, "unknown tuning key");
     return GPE_OK;
 }

@@ -485,25 +485,30 @@ namespace gpe {
 
 // ---------------------------------------------------------------- observables
 
-// FP64 observables of one psi buffer (density/integrate Spin1GpeBCC.cu:191-211,
+// Observables of one psi buffer with FP64 sums (density/integrate Spin1GpeBCC.cu:191-211,
 // 328-348; energy GPUGrossPitaevskii_BCC.cu:204-226; localAvgSpinAndDensity
 // Spin1GpeBCC.cu:235-271; com GPUGrossPitaevskii_BCC.cu:349-375).  Values are
-// loaded in the storage precision and everything after the load is FP64.  Each
-// block writes OBS_COUNT partial sums (warp shuffles, then shared memory); a
-// one-block kernel adds the partials in a fixed order, so results are
+// loaded in the storage precision R; the per-node terms are computed in A (FP64,
+// or the FP32 storage precision when the handle asks for it) and accumulated in
+// FP64.  Each block writes OBS_COUNT partial sums (warp shuffles, then shared
+// memory); a one-block kernel adds the partials in a fixed order, so results are
 // reproducible run to run.
-template <typename R, int C>
+template <typename R, int C, typename A>
 __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
-    __shared__ SmemTables<double> st;
+    __shared__ SmemTables<A> st;
     __shared__ double red[8][OBS_COUNT];
     {
         const int V = a.g.V, n = a.tab.entries;
         for (int i = threadIdx.x; i <= V; i += blockDim.x) st.row_ptr[i] = a.tab.row_ptr[i];
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             st.nb_off[i] = a.tab.nb_off[i];
-            st.w[i] = a.tab.w64[i];
+            if constexpr (sizeof(A) == 4) st.w[i] = a.tab.w32[i];
+            else st.w[i] = a.tab.w64[i];
         }
-        for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) st.pos[i] = a.tab.pos64[i];
+        for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+            if constexpr (sizeof(A) == 4) st.pos[i] = a.tab.pos32[i];
+            else st.pos[i] = a.tab.pos64[i];
+        }
     }
     __syncthreads();
     double acc[OBS_COUNT];
@@ -521,14 +526,15 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
         const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
         const char* base = a.prev + cell_off;
         const uint32_t node_bytes = C * 2 * sizeof(R);
-        Cx<double> ps[C], L[C], Hl[C], Hn[C];
-        double rho = 0, maxabs = 0, bad = 0;
+        Cx<A> ps[C], L[C], Hl[C], Hn[C];
+        A rho = 0, maxabs = 0;
+        double bad = 0;
 #pragma unroll
         for (int s = 0; s < C; ++s) {
             const Cx<R> v = ldc<R>(base + l * node_bytes + s * 2 * sizeof(R));
-            ps[s] = cx<double>((double)v.x, (double)v.y);
-            L[s] = Hl[s] = Hn[s] = cx<double>(0.0, 0.0);
-            const double n2 = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+            ps[s] = cx<A>((A)v.x, (A)v.y);
+            L[s] = Hl[s] = Hn[s] = cx<A>((A)0, (A)0);
+            const A n2 = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
             rho += n2;
             maxabs = fmax(maxabs, sqrt(n2));
             if (!isfinite(ps[s].x) || !isfinite(ps[s].y)) bad += 1;
@@ -538,22 +544,22 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
 #pragma unroll
             for (int s = 0; s < C; ++s) {
                 const Cx<R> v = ldc<R>(nb + s * 2 * sizeof(R));
-                L[s] += st.w[f] * (cx<double>((double)v.x, (double)v.y) - ps[s]);
+                L[s] += st.w[f] * (cx<A>((A)v.x, (A)v.y) - ps[s]);
             }
         }
-        const PhysR<double>& P = make_phys<double>(a);
-        double r[3];
-        r[0] = P.p0[0] + P.bs * ((double)x * P.bw[0] + st.pos[3 * l + 0]);
-        r[1] = P.p0[1] + P.bs * ((double)y * P.bw[1] + st.pos[3 * l + 1]);
-        r[2] = P.p0[2] + P.bs * ((double)z * P.bw[2] + st.pos[3 * l + 2]);
-        local_terms<double, C>(P, r, trap<double>(P, r), GPE_MODE_LEAPFROG, false, ps, Hl);
+        const PhysR<A>& P = make_phys<A>(a);
+        A r[3];
+        r[0] = P.p0[0] + P.bs * ((A)x * P.bw[0] + st.pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((A)y * P.bw[1] + st.pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((A)z * P.bw[2] + st.pos[3 * l + 2]);
+        local_terms<A, C>(P, r, trap<A>(P, r), GPE_MODE_LEAPFROG, false, ps, Hl);
         // interaction-only part: no trap, no external field, no loss / quadratic Zeeman
-        PhysR<double> Q = P;
+        PhysR<A> Q = P;
         Q.bq = Q.bqq = 0;
         for (int k = 0; k < 3; ++k) Q.bb[k] = Q.bbq[k] = 0;
         Q.flags &= ~(GPE_FLAG_THREE_BODY_LOSS | GPE_FLAG_QUADRATIC_ZEEMAN | GPE_FLAG_QUADRUPOLE_OFFSET);
-        local_terms<double, C>(Q, r, 0.0, GPE_MODE_LEAPFROG, false, ps, Hn);
-        double kin = 0, hl = 0, hn = 0;
+        local_terms<A, C>(Q, r, (A)0, GPE_MODE_LEAPFROG, false, ps, Hn);
+        A kin = 0, hl = 0, hn = 0;
 #pragma unroll
         for (int s = 0; s < C; ++s) {
             kin += ps[s].x * L[s].x + ps[s].y * L[s].y;
@@ -561,26 +567,26 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
             hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
         }
         acc[OBS_NORM] = rho;
-        acc[OBS_HEXP] = kin + hl;
+        acc[OBS_HEXP] = (double)kin + (double)hl;
         acc[OBS_EINT] = hn;
-        acc[OBS_COMX] = rho * r[0];
-        acc[OBS_COMY] = rho * r[1];
-        acc[OBS_COMZ] = rho * r[2];
+        acc[OBS_COMX] = (double)rho * r[0];
+        acc[OBS_COMY] = (double)rho * r[1];
+        acc[OBS_COMZ] = (double)rho * r[2];
         acc[OBS_MAXABS] = maxabs;
         acc[OBS_NONFINITE] = bad;
         if constexpr (C == 3) {
-            const Cx<double> m = GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
-            const double fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
+            const Cx<A> m = (A)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
+            const A fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
             acc[OBS_MAGX] = m.x;
             acc[OBS_MAGY] = m.y;
             acc[OBS_MAGZ] = fz;
             acc[OBS_SPIN] = sqrt(m.x * m.x + m.y * m.y + fz * fz);
         } else if constexpr (C == 5) {
-            const Cx<double> fp = 2.0 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
-                                  2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
-            double n[5];
+            const Cx<A> fp = (A)2 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
+                             (A)2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
+            A n[5];
             for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
-            const double fz = 2 * n[0] + n[1] - n[3] - 2 * n[4];
+            const A fz = (A)2 * n[0] + n[1] - n[3] - (A)2 * n[4];
             acc[OBS_MAGX] = fp.x;
             acc[OBS_MAGY] = fp.y;
             acc[OBS_MAGZ] = fz;
@@ -721,10 +727,12 @@ cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// node_fp32: per-node terms in FP32 (FP32 storage only); sums are FP64 either way.
 template <typename R, int C>
-cudaError_t launch_observe(const StepArgs& a, double* out, cudaStream_t s) {
+cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaStream_t s) {
     const unsigned nb = nblocks(a.total, 256);
-    observe_kernel<R, C><<<nb, 256, 0, s>>>(a);
+    if (sizeof(R) == 4 && node_fp32) observe_kernel<R, C, float><<<nb, 256, 0, s>>>(a);
+    else observe_kernel<R, C, double><<<nb, 256, 0, s>>>(a);
     observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
     return cudaGetLastError();
 }
@@ -738,7 +746,7 @@ cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, c
 #define GPE_INSTANTIATE(R, C)                                                               \
     template cudaError_t launch_parabolic<R, C>(const StepArgs&, int, cudaStream_t);       \
     template cudaError_t launch_hyper<R, C>(const StepArgs&, int, cudaStream_t);           \
-    template cudaError_t launch_observe<R, C>(const StepArgs&, double*, cudaStream_t);     \
+    template cudaError_t launch_observe<R, C>(const StepArgs&, double*, bool, cudaStream_t);     \
     template cudaError_t launch_scale<R, C>(const StepArgs&, const double*, double, cudaStream_t);
 
 }  // namespace gpe

@@ -198,6 +198,29 @@ def test_observables(gpu, name, C, prec):
     assert got["nonfinite"] == 0
 
 
+@pytest.mark.parametrize("name,C", [("bcc", 1), ("bcc", 3), ("c15", 5)])
+def test_observables_fp32_node_terms(gpu, name, C):
+    """GPE_TUNE_OBSERVE_ARITH = 1: per-node terms in FP32, sums in FP64; within 1e-5
+    (relative to the norm / energy scale) of the FP64 oracle on the same stored values."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, capi.FP32, (6, 5, 4))
+    psi = _rand(lat, p, 62).astype(np.float32).astype(np.float64)
+    f = capi.make_fields(**FIELDS)
+    ramp = capi.make_ramp(bq_segments=[(f.bq, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[(tuple(f.bb), 1e9, capi.RAMP_CONSTANT)])
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, psi)
+        s.set_ramp(ramp, 0.0)
+        s.set_tuning(capi.TUNE_OBSERVE_ARITH, 1)
+        assert s.get_tuning(capi.TUNE_OBSERVE_ARITH) == 1
+        got = s.observe(capi.PSI_EVEN, t=0.0)
+    want = oracle.observe(lat, p, oracle.ramp_eval(ramp, 0.0), 0.0, psi)
+    for k in ("norm", "energy", "h_expect", "spin_norm"):
+        assert got[k] == pytest.approx(want[k], rel=1e-5, abs=1e-5 * abs(want["h_expect"])), k
+    np.testing.assert_allclose(got["magnetization"], want["magnetization"], rtol=1e-5, atol=1e-5 * want["norm"])
+    np.testing.assert_allclose(got["com"], want["com"], rtol=1e-5, atol=1e-5 * want["norm"])
+
+
 @pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
 def test_imaginary_time(gpu, prec):
     """gpe_itp = itp + normalize, twice per iteration pair (Spin1GpeBCC.cu:1470-1490)."""
