@@ -375,8 +375,8 @@ gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, double* grad,
  *   `steps` steps of up to four of its members on scratch copies of their
  *   buffers, on a grid scaled so that each block has the work it has in the
  *   whole batch, for item sizes of 4K..256K nodes, and keeps the fastest; the
- *   members' states are untouched.  Blocks own contiguous item ranges of equal
- *   nodes x components.
+ *   members' states are untouched.  Within a step the blocks take items from
+ *   one counter, so a block that finishes early takes more.
  *   `report` receives a JSON list of the timings. */
 typedef struct gpe_batch gpe_batch;
 enum { GPE_BATCH_ITEM_NODES = 0, GPE_BATCH_STEPS_PER_LAUNCH = 1, GPE_BATCH_BLOCKS_PER_SM = 2 };

@@ -5,8 +5,8 @@
 // The reference runs one condensate per process, one kernel launch per step
 // (Spin1GpeBCC.cu:1574-1603).  Here the members' interior rows are cut into work
 // items of about `item_nodes` nodes (whole rows of cells, sorted by lattice and
-// spin so that a block's consecutive items mostly share a member); each block of
-// the persistent grid owns a contiguous range of items, processes them with the
+// spin so that consecutive items mostly share a member); the blocks of the
+// persistent grid take items in list order from one counter per step, process them with the
 // same per-node update as the single-condensate gather kernel (parabolic_node),
 // evaluates the next step's fields of its share of the members on the device
 // (the members' own ramps, getSignal of AliceRingRamps.h:74-141), and meets the
@@ -61,7 +61,7 @@ struct BatchArgs {
     const BatchState* state;
     StepFieldsD* fields;       // 2 x nmembers, by step parity
     const BatchItem* items;
-    const uint32_t* block_start;  // gridDim.x + 1 item indices: block b owns [start[b], start[b+1])
+    unsigned* next_item;       // one counter per step of the launch (zeroed before it)
     uint32_t nmembers, nitems;
     uint32_t nsteps;           // steps of this launch
     uint32_t step_base;        // steps of this call taken by earlier launches
@@ -70,6 +70,7 @@ struct BatchArgs {
 };
 
 constexpr unsigned kBatchThreads = 256;
+constexpr int32_t kMaxStepsPerLaunch = 4096;  // item counters held for one launch
 constexpr unsigned long long kBarrierTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -169,18 +170,23 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs A) {
     __shared__ SmemTables<R> st;
     __shared__ PhysR<R> P;
     __shared__ BatchMember M;
+    __shared__ uint32_t grabbed;
     const uint32_t gtid = blockIdx.x * kBatchThreads + threadIdx.x;
     const uint32_t gthreads = gridDim.x * kBatchThreads;
-    // this block's contiguous range of items (equal shares of nodes x components)
-    const uint32_t it0 = A.block_start[blockIdx.x];
-    const uint32_t it1 = A.block_start[blockIdx.x + 1];
     for (uint32_t m = gtid; m < A.nmembers; m += gthreads) batch_fields(A, m, A.step_base, A.fields);
     if (!grid_barrier(A.bar, A.err)) return;
     for (uint32_t s = 0; s < A.nsteps; ++s) {
         const uint32_t k = A.step_base + s;
         const StepFieldsD* F = A.fields + (size_t)(s & 1) * A.nmembers;
         uint32_t loaded = 0xffffffffu;
-        for (uint32_t it = it0; it < it1; ++it) {
+        for (;;) {
+            // items are handed out in list order by one counter per step, so blocks
+            // that finish early take more and the step ends within about one item
+            if (threadIdx.x == 0) grabbed = atomicAdd(A.next_item + s, 1u);
+            __syncthreads();
+            const uint32_t it = grabbed;
+            __syncthreads();  // every thread has read `grabbed` before thread 0 rewrites it
+            if (it >= A.nitems) break;
             const BatchItem w = A.items[it];
             // items of one member share the staged tables: the block synchronises
             // only where the member changes (w.member is the same in every thread)
@@ -263,8 +269,7 @@ struct gpe_batch {
     size_t items_cap = 0;
     uint32_t nitems = 0;
     std::vector<uint64_t> item_cost;  // prefix sums of the items' nodes x components
-    uint32_t* d_block_start = nullptr;
-    size_t block_start_cap = 0;
+    unsigned* d_next = nullptr;       // per-step item counters of one launch
     unsigned* d_bar = nullptr;
     int* d_err = nullptr;
     cudaGraph_t graph = nullptr;
@@ -356,31 +361,6 @@ gpe_status rebuild_items(gpe_batch* b) {
     return upload_items(b, build_items(b, all), member_grids(b));
 }
 
-// Splits the uploaded items over `grid` blocks in contiguous ranges of equal cost
-// (block b starts at the first item whose cost prefix reaches b/grid of the total).
-gpe_status upload_block_ranges(gpe_batch* b, int grid, cudaStream_t s) {
-    std::vector<uint32_t> start((size_t)grid + 1);
-    const uint64_t total = b->item_cost.back();
-    size_t it = 0;
-    for (int k = 0; k <= grid; ++k) {
-        const uint64_t goal = (uint64_t)((unsigned __int128)total * (uint64_t)k / (uint64_t)grid);
-        while (it < b->nitems && b->item_cost[it] < goal) ++it;
-        start[k] = (uint32_t)it;
-    }
-    start[grid] = b->nitems;
-    if (start.size() > b->block_start_cap) {
-        if (b->d_block_start) cudaFree(b->d_block_start);
-        b->d_block_start = nullptr;
-        if (cudaMalloc(&b->d_block_start, start.size() * sizeof(uint32_t)) != cudaSuccess)
-            return fail(GPE_ERR_OOM, "cudaMalloc (batch block ranges)");
-        b->block_start_cap = start.size();
-    }
-    cudaError_t e = cudaMemcpyAsync(b->d_block_start, start.data(), start.size() * sizeof(uint32_t),
-                                    cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return e == cudaSuccess ? GPE_OK : cuda_fail(e, "batch block ranges");
-}
-
 void fill_state(gpe_batch* b) {
     for (size_t m = 0; m < b->members.size(); ++m) {
         const gpe_handle* h = b->members[m];
@@ -417,19 +397,21 @@ gpe_status enqueue_steps(gpe_batch* b, int32_t n, cudaStream_t s, const BatchMem
     cudaError_t e = cudaMemcpyAsync(b->d_state, h_state, nmembers * sizeof(BatchState), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return batch_fail_cuda(e, "batch state upload");
     void* fn = batch_kernel_for(b->precision, b->cmask);
-    const int32_t K = b->steps_per_launch > 0 ? b->steps_per_launch : n;
+    const int32_t K = std::min(b->steps_per_launch > 0 ? b->steps_per_launch : n, kMaxStepsPerLaunch);
     for (int32_t done = 0; done < n; done += K) {
-        if ((e = cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned), s)) != cudaSuccess)
+        const int32_t steps = std::min(K, n - done);
+        if ((e = cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned), s)) != cudaSuccess ||
+            (e = cudaMemsetAsync(b->d_next, 0, (size_t)steps * sizeof(unsigned), s)) != cudaSuccess)
             return batch_fail_cuda(e, "batch barrier reset");
         BatchArgs A;
         A.members = members;
         A.state = b->d_state;
         A.fields = b->d_fields;
         A.items = b->d_items;
-        A.block_start = b->d_block_start;
+        A.next_item = b->d_next;
         A.nmembers = nmembers;
         A.nitems = b->nitems;
-        A.nsteps = (uint32_t)std::min(K, n - done);
+        A.nsteps = (uint32_t)steps;
         A.step_base = (uint32_t)done;
         A.bar = b->d_bar;
         A.err = b->d_err;
@@ -479,7 +461,7 @@ void release_batch(gpe_batch* b) {
     if (b->h_state) cudaFreeHost(b->h_state);
     if (b->d_fields) cudaFree(b->d_fields);
     if (b->d_items) cudaFree(b->d_items);
-    if (b->d_block_start) cudaFree(b->d_block_start);
+    if (b->d_next) cudaFree(b->d_next);
     if (b->d_bar) cudaFree(b->d_bar);
     if (b->d_err) cudaFree(b->d_err);
 }
@@ -530,7 +512,8 @@ extern "C" gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count
         cudaMalloc(&b->d_state, count * sizeof(BatchState)) != cudaSuccess ||
         cudaMallocHost(&b->h_state, count * sizeof(BatchState)) != cudaSuccess ||
         cudaMalloc(&b->d_fields, 2 * (size_t)count * sizeof(StepFieldsD)) != cudaSuccess ||
-        cudaMalloc(&b->d_bar, 2 * sizeof(unsigned)) != cudaSuccess || cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&b->d_bar, 2 * sizeof(unsigned)) != cudaSuccess || cudaMalloc(&b->d_err, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&b->d_next, kMaxStepsPerLaunch * sizeof(unsigned)) != cudaSuccess) {
         release_batch(b);
         delete b;
         return fail(GPE_ERR_OOM, "batch allocation");
@@ -540,7 +523,6 @@ extern "C" gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count
     if (e != cudaSuccess) st = cuda_fail(e, "batch members upload");
     if (!st) st = grid_size(b);
     if (!st) st = rebuild_items(b);
-    if (!st) st = upload_block_ranges(b, b->grid, 0);
     if (st) {
         release_batch(b);
         delete b;
@@ -626,8 +608,7 @@ extern "C" gpe_status gpe_batch_set_tuning(gpe_batch* b, int32_t key, int32_t va
         if (value < 1) return fail(GPE_ERR_INVALID_ARG, "item nodes");
         b->item_nodes = value;
         b->item_nodes_by_lattice.clear();
-        gpe_status st = rebuild_items(b);
-        return st ? st : upload_block_ranges(b, b->grid, 0);
+        return rebuild_items(b);
     }
     if (key == GPE_BATCH_STEPS_PER_LAUNCH) {
         if (value < 0) return fail(GPE_ERR_INVALID_ARG, "steps per launch");
@@ -637,8 +618,7 @@ extern "C" gpe_status gpe_batch_set_tuning(gpe_batch* b, int32_t key, int32_t va
     if (key == GPE_BATCH_BLOCKS_PER_SM) {
         if (value < 0) return fail(GPE_ERR_INVALID_ARG, "blocks per SM");
         b->tune_blocks_per_sm = value;
-        gpe_status st = grid_size(b);
-        return st ? st : upload_block_ranges(b, b->grid, 0);
+        return grid_size(b);
     }
     return fail(GPE_ERR_INVALID_ARG, "unknown batch tuning key");
 }
@@ -730,8 +710,7 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
             // as many blocks as give each the work a block has in the whole batch
             const double share = (double)b->item_cost.back() / (double)full_cost;
             const int tgrid = std::max(1, std::min(b->grid, (int)std::lround(share * b->grid)));
-            if (upload_block_ranges(b, tgrid, s) != GPE_OK ||
-                enqueue_steps(b, 1, s, dm, (uint32_t)which.size(), ps, tgrid) != GPE_OK) {
+            if (enqueue_steps(b, 1, s, dm, (uint32_t)which.size(), ps, tgrid) != GPE_OK) {
                 ok = false;
                 break;
             }
@@ -762,7 +741,6 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
         if (ps) cudaFreeHost(ps);
         if (!ok) {
             rebuild_items(b);
-            upload_block_ranges(b, b->grid, s);
             return fail(GPE_ERR_CUDA, "batch autotune trial failed");
         }
         best_by_lattice.push_back({key, best});
@@ -770,7 +748,6 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
     rep += "]";
     b->item_nodes_by_lattice = best_by_lattice;
     gpe_status st = rebuild_items(b);
-    if (!st) st = upload_block_ranges(b, b->grid, s);
     if (st) return st;
     if (report && report_len) std::snprintf(report, report_len, "%s", rep.c_str());
     return check_batch_error(b, s);
