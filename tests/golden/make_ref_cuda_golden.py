@@ -1,0 +1,205 @@
+"""Golden vectors from the reference's own CUDA kernels (tests/golden/ref_cuda_*.npz).
+
+Needs a GPU and the cubins of oracle/build_ref_cuda.sh (built from the reference
+tree).  For every case it uploads seeded random states into an FP64 libgpe
+handle (whose buffers have the reference's BlockPsis / BlockEdges layout), runs
+a short sequence of the reference's kernels on those buffers through
+oracle/ref_cuda.py with per-step fields and times, and stores the parameters,
+the inputs and the outputs (interior cells only).  tests/test_ref_cuda_golden.py
+replays every sequence with the oracle (CPU) and with libgpe's kernels (GPU).
+
+    python tests/golden/make_ref_cuda_golden.py [outdir]
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import ref_cuda as R  # noqa: E402
+from spacetime_gb300 import capi, states  # noqa: E402
+from spacetime_gb300.stepper import Stepper  # noqa: E402
+
+NSTEPS = 4
+
+
+def fields_table(n, seed):
+    u = states.uniform01(seed, 8 * n).reshape(n, 8)
+    return 2.0 * u - 1.0  # bq, bb[3], bq_quad, bb_quad[3]
+
+
+def as_fields(row):
+    return capi.make_fields(bq=row[0], bb=tuple(row[1:4]), bq_quad=row[4], bb_quad=tuple(row[5:8]))
+
+
+def interior(a):
+    return np.ascontiguousarray(a[1:-1, 1:-1, 1:-1])
+
+
+def params_dict(p):
+    return {"components": p.components, "scheme": p.scheme, "flags": p.flags, "dims": list(p.dims),
+            "block_scale": p.block_scale, "p0": list(p.p0), "dt": p.dt, "trap_lambda": list(p.trap_lambda),
+            "trap_offset": p.trap_offset, "trap_off_time": p.trap_off_time, "c0": p.c0, "c2": p.c2, "c4": p.c4,
+            "alpha": p.alpha, "sigma": p.sigma, "quad_center": list(p.quad_center)}
+
+
+def spinor_case(drv, name, program, lattice, C, dims, flags, dt, c0, c2, c4, alpha, seed):
+    """forwardEuler (odd -> even) then NSTEPS-1 leapfrog steps (Spin1GpeBCC.cu:1428-1603)."""
+    lat = capi.Lattice(lattice)
+    p = capi.make_params(components=C, precision=capi.FP64, dims=dims, block_scale=0.3, dt=dt,
+                         trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, c4=c4,
+                         alpha=alpha, flags=flags, quad_center=R.QUAD_CENTER, lattice=lat)
+    s = Stepper(lat, p)
+    shape = capi.buffer_shape(lat, p)
+    even0 = 0.2 * states.random_state(shape, seed=seed)
+    odd0 = 0.2 * states.random_state(shape, seed=seed + 1)
+    s.upload(capi.PSI_EVEN, even0)
+    s.upload(capi.PSI_ODD, odd0)
+    ent, w = R.stencil_int4(lat)
+    d_ent, d_w = drv.upload(ent), drv.upload(w)
+    grid, block = R.spinor_grid(p, lat.nodes)
+    F = fields_table(NSTEPS, seed + 7)
+    times = 0.25 + np.arange(NSTEPS) * dt
+    bufs = [R.pitched(s, capi.PSI_ODD), R.pitched(s, capi.PSI_EVEN)]  # u_j lives in bufs[j % 2]
+    for j in range(NSTEPS):
+        kern = "euler" if j == 0 else "leapfrog"
+        nxt, prv = bufs[(j + 1) % 2], bufs[j % 2]
+        common = [nxt, prv, R.C.c_void_p(d_ent), R.C.c_void_p(d_w), R.mag_fields(as_fields(F[j])), R.uint3(p),
+                  R.C.c_double(p.block_scale), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2)]
+        if program == "spin1_bcc":
+            args = common + [R.C.c_double(alpha), R.C.c_bool(bool(flags & capi.FLAG_THREE_BODY_LOSS)),
+                             R.C.c_bool(bool(flags & capi.FLAG_QUADRATIC_ZEEMAN)),
+                             R.C.c_bool(bool(flags & capi.FLAG_QUADRUPOLE_OFFSET)), R.C.c_double(dt),
+                             R.C.c_double(times[j])]
+        else:  # spin-2: dt is a compile-time constant of the program
+            args = common + [R.C.c_double(c4), R.C.c_double(alpha), R.C.c_double(times[j])]
+        drv.launch(drv.function(program, kern), grid, block, args)
+    out = {"even": interior(s.download(capi.PSI_EVEN)), "odd": interior(s.download(capi.PSI_ODD))}
+    s.close()
+    return dict(kind="spinor", lattice=lattice, params=params_dict(p), fields=F, times=times,
+                in_even=interior(even0), in_odd=interior(odd0), **{"out_" + k: v for k, v in out.items()})
+
+
+def rel_case(drv, name, lattice, dims, dt, sigma, c0, c2, c4, seed):
+    """NSTEPS hyperbolic steps: update_psi then update_q per step
+    (RelativisticSpin2Gpe.cu:1859-1899)."""
+    lat = capi.Lattice(lattice)
+    p = capi.make_params(components=5, scheme=capi.SCHEME_HYPERBOLIC, precision=capi.FP64, dims=dims, block_scale=0.3,
+                         dt=dt, trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, c4=c4,
+                         sigma=sigma, lattice=lat)
+    s = Stepper(lat, p)
+    shape, qshape = capi.buffer_shape(lat, p), capi.buffer_shape(lat, p, edges=True)
+    ins = {"in_even": 0.2 * states.random_state(shape, seed=seed), "in_odd": 0.2 * states.random_state(shape, seed=seed + 1),
+           "in_qeven": 0.2 * states.random_state(qshape, seed=seed + 2),
+           "in_qodd": 0.2 * states.random_state(qshape, seed=seed + 3)}
+    s.upload(capi.PSI_EVEN, ins["in_even"])
+    s.upload(capi.PSI_ODD, ins["in_odd"])
+    s.upload(capi.Q_EVEN, ins["in_qeven"])
+    s.upload(capi.Q_ODD, ins["in_qodd"])
+    d0, d1, w = R.edge_tables(lat, s, p.block_scale)
+    d_d0, d_d1, d_w = drv.upload(d0), drv.upload(d1), drv.upload(w)
+    grid, pblock = R.spinor_grid(p, lat.nodes)
+    _, eblock = R.edge_grid(p, lat.edges)
+    F = fields_table(NSTEPS, seed + 7)
+    psi = [R.pitched(s, capi.PSI_EVEN), R.pitched(s, capi.PSI_ODD)]
+    q = [R.pitched(s, capi.Q_EVEN), R.pitched(s, capi.Q_ODD)]
+    for j in range(NSTEPS):
+        a, b = j % 2, (j + 1) % 2  # prev parity, next parity
+        drv.launch(drv.function("rel_spin2_bcc", "update_psi"), grid, pblock,
+                   [psi[b], psi[a], q[a], R.C.c_void_p(d_d1), R.C.c_void_p(d_w), R.mag_fields(as_fields(F[j])),
+                    R.uint3(p), R.C.c_double(p.block_scale), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2),
+                    R.C.c_double(c4), R.C.c_double(dt), R.C.c_bool(True), R.C.c_double(sigma)])
+        drv.launch(drv.function("rel_spin2_bcc", "update_q"), grid, eblock,
+                   [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(dt / sigma), R.C.c_bool(True)])
+    out = {"out_even": interior(s.download(capi.PSI_EVEN)), "out_odd": interior(s.download(capi.PSI_ODD)),
+           "out_qeven": interior(s.download(capi.Q_EVEN)), "out_qodd": interior(s.download(capi.Q_ODD))}
+    s.close()
+    return dict(kind="hyper", lattice=lattice, params=params_dict(p), fields=F, times=np.zeros(NSTEPS),
+                **{k: interior(v) for k, v in ins.items()}, **out)
+
+
+def scalar_case(drv, name, program, lattice, dims, dt, g, seed):
+    """NSTEPS leapfrog updates of the scalar programs.  Their update is
+    next += dt_ref (-i H) (GPUGrossPitaevskii_BCC.cu:345-346); the C15/A15/FCC
+    programs fold dt_ref into the weights, the potential and g
+    (GPUGrossPitaevskii_C15.cu:241-246).  libgpe's step is next += 2 dt (-i H),
+    so dt_ref = 2 dt.  The potential array holds the trap values libgpe computes."""
+    lat = capi.Lattice(lattice)
+    p = capi.make_params(components=1, precision=capi.FP64, dims=dims, block_scale=0.3, dt=dt,
+                         trap_lambda=(1.0, 1.1, 1.3), trap_offset=R.TRAP_OFFSET, c0=g, lattice=lat)
+    s = Stepper(lat, p)
+    shape = capi.buffer_shape(lat, p)
+    even0 = 0.2 * states.random_state(shape, seed=seed)
+    odd0 = 0.2 * states.random_state(shape, seed=seed + 1)
+    s.upload(capi.PSI_EVEN, even0)
+    s.upload(capi.PSI_ODD, odd0)
+    dt_ref = 2.0 * dt
+    folded = program != "scalar_bcc"
+    scale = 1.0 / (p.block_scale ** 2) * (dt_ref if folded else 1.0)
+    ent, w = R.stencil_int2(lat, s, scale)
+    pot = R.node_potential(lat, p) * (dt_ref if folded else 1.0)
+    d_ent, d_w = drv.upload(ent), drv.upload(w)
+    d_pot = R.pitched_upload(drv, pot)
+    grid, block = R.scalar_grid(p, lat.nodes)
+    bufs = [R.pitched(s, capi.PSI_EVEN), R.pitched(s, capi.PSI_ODD)]
+    for j in range(NSTEPS):
+        nxt, prv = bufs[(j + 1) % 2], bufs[j % 2]
+        args = [nxt, prv, d_pot, R.C.c_void_p(d_ent), R.C.c_void_p(d_w)]
+        if program == "scalar_fcc":
+            rp = lat.row_ptr
+            csr = np.stack([rp[:-1], np.diff(rp)], axis=1).astype(np.int32)
+            args.append(R.C.c_void_p(drv.upload(csr)))
+        args.append(R.C.c_double(g * dt_ref if folded else g))
+        args.append(R.uint3(p))
+        if not folded:
+            args.append(R.C.c_double(dt_ref))
+        drv.launch(drv.function(program, "update"), grid, block, args)
+    out = {"out_even": interior(s.download(capi.PSI_EVEN)), "out_odd": interior(s.download(capi.PSI_ODD))}
+    s.close()
+    return dict(kind="scalar", lattice=lattice, params=params_dict(p), fields=np.zeros((NSTEPS, 8)),
+                times=np.zeros(NSTEPS), in_even=interior(even0), in_odd=interior(odd0), **out)
+
+
+CASES = [
+    ("spin1_bcc", lambda d: spinor_case(d, "spin1_bcc", "spin1_bcc", "bcc", 3, (5, 3, 2), 0, 2e-4, 120.0, -7.0, 0.0, 0.0, 11)),
+    ("spin1_bcc_toggles", lambda d: spinor_case(d, "spin1_bcc_toggles", "spin1_bcc", "bcc", 3, (4, 3, 3),
+                                                capi.FLAG_THREE_BODY_LOSS | capi.FLAG_QUADRATIC_ZEEMAN | capi.FLAG_QUADRUPOLE_OFFSET,
+                                                2e-4, 120.0, -7.0, 0.0, 2.0, 21)),
+    ("spin2_bcc", lambda d: spinor_case(d, "spin2_bcc", "spin2_bcc", "bcc", 5, (5, 3, 2), capi.FLAG_THREE_BODY_LOSS,
+                                        R.SPIN2_DT, 120.0, -7.0, 3.0, 2.0, 31)),
+    ("rel_spin2_bcc", lambda d: rel_case(d, "rel_spin2_bcc", "bcc", (4, 3, 2), 2e-4, 0.01, 120.0, -7.0, 3.0, 41)),
+    ("scalar_bcc", lambda d: scalar_case(d, "scalar_bcc", "scalar_bcc", "bcc", (5, 3, 2), 2e-4, 150.0, 51)),
+    ("scalar_c15", lambda d: scalar_case(d, "scalar_c15", "scalar_c15", "c15", (2, 2, 2), 2e-4, 150.0, 61)),
+    ("scalar_a15", lambda d: scalar_case(d, "scalar_a15", "scalar_a15", "a15", (3, 2, 2), 2e-4, 150.0, 71)),
+    ("scalar_fcc", lambda d: scalar_case(d, "scalar_fcc", "scalar_fcc", "fcc", (3, 3, 2), 2e-4, 150.0, 81)),
+]
+
+
+def main(outdir):
+    os.makedirs(outdir, exist_ok=True)
+    # a handle first: it makes the primary context current for the driver API
+    warm = Stepper(capi.Lattice("bcc"), capi.make_params(components=1, precision=capi.FP64, dims=(2, 2, 2)))
+    drv = R.Driver()
+    try:
+        for name, fn in CASES:
+            program = name.replace("_toggles", "")
+            if not R.available(program):
+                print("skip %s: %s.cubin not built" % (name, program))
+                continue
+            case = fn(drv)
+            case["params"] = json.dumps(case["params"])
+            path = os.path.join(outdir, "ref_cuda_%s.npz" % name)
+            np.savez_compressed(path, **case)
+            print("wrote", path)
+    finally:
+        drv.close()
+        warm.close()
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden"))

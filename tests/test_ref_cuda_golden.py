@@ -1,0 +1,128 @@
+"""Parity with the reference's own CUDA kernels (golden vectors).
+
+tests/golden/ref_cuda_*.npz hold short runs of the reference's unmodified
+kernels -- spin-1 leapfrog/forwardEuler with and without loss, quadratic Zeeman
+and quadrupole offset (Spin1GpeBCC.cu:667-917), spin-2 (Spin2GpeBCC.cu:698-990),
+relativistic spin-2 update_psi + update_q (RelativisticSpin2Gpe.cu:971-1132),
+and the scalar BCC / C15 / A15 / FCC updates -- made by
+tests/golden/make_ref_cuda_golden.py on a GB300 from seeded inputs.
+
+CPU: the FP64 oracle replays each run: max |oracle - reference| <= 1e-12 * max|reference|
+(the reference contracts multiply-adds, the oracle does not; the scalar programs
+fold dt into their tables).  GPU: libgpe's FP64 kernels replay it to the same
+bound, its FP32 kernels to 2e-5 * max|reference|.
+"""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from spacetime_gb300 import capi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FILES = sorted(glob.glob(os.path.join(HERE, "golden", "ref_cuda_*.npz")))
+IDS = [os.path.basename(f)[9:-4] for f in FILES]
+
+
+def _load(path):
+    d = dict(np.load(path, allow_pickle=False))
+    d["params"] = json.loads(str(d["params"]))
+    d["kind"] = str(d["kind"])
+    d["lattice"] = str(d["lattice"])
+    return d
+
+
+def _params(d, precision):
+    pd = dict(d["params"])
+    lat = capi.Lattice(d["lattice"])
+    pd["precision"] = precision
+    pd["dims"] = tuple(pd["dims"])
+    pd["trap_lambda"] = tuple(pd["trap_lambda"])
+    pd["quad_center"] = tuple(pd["quad_center"])
+    return lat, capi.make_params(lattice=lat, **pd)
+
+
+def _embed(a):
+    out = np.zeros((a.shape[0] + 2, a.shape[1] + 2, a.shape[2] + 2) + a.shape[3:])
+    out[1:-1, 1:-1, 1:-1] = a
+    return out
+
+
+def _fields(row):
+    return capi.make_fields(bq=row[0], bb=tuple(row[1:4]), bq_quad=row[4], bb_quad=tuple(row[5:8]))
+
+
+def _check(got, want, tol, what):
+    g = got[1:-1, 1:-1, 1:-1] if got.shape != want.shape else got
+    scale = float(np.max(np.abs(want)))
+    err = float(np.max(np.abs(g - want)))
+    assert err <= tol * scale, "%s: max|diff| = %.3e, scale %.3e" % (what, err, scale)
+
+
+def test_golden_files_present():
+    assert len(FILES) >= 8, "reference-kernel golden vectors missing"
+
+
+@pytest.mark.parametrize("path", FILES, ids=IDS)
+def test_oracle_vs_reference_cuda(path):
+    d = _load(path)
+    lat, p = _params(d, capi.FP64)
+    n = d["fields"].shape[0]
+    if d["kind"] == "spinor":
+        even, odd = _embed(d["in_even"]), _embed(d["in_odd"])
+        bufs = [odd, even]
+        for j in range(n):
+            mode = oracle.EULER if j == 0 else oracle.LEAPFROG
+            oracle.parabolic_step(lat, p, _fields(d["fields"][j]), float(d["times"][j]), mode, bufs[(j + 1) % 2], bufs[j % 2])
+    elif d["kind"] == "scalar":
+        even, odd = _embed(d["in_even"]), _embed(d["in_odd"])
+        bufs = [even, odd]
+        for j in range(n):
+            oracle.parabolic_step(lat, p, capi.make_fields(), 0.0, oracle.LEAPFROG, bufs[(j + 1) % 2], bufs[j % 2])
+    else:
+        ps = [_embed(d["in_even"]), _embed(d["in_odd"])]
+        qs = [_embed(d["in_qeven"]), _embed(d["in_qodd"])]
+        for j in range(n):
+            a, b = j % 2, (j + 1) % 2
+            oracle.q_psi_step(lat, p, _fields(d["fields"][j]), 0.0, oracle.LEAPFROG, True, ps[b], ps[a], qs[a])
+            oracle.q_step(lat, p, oracle.Q_HYPER, qs[b], qs[a], ps[a])
+        even, odd = ps
+        _check(qs[0], d["out_qeven"], 1e-12, "q even")
+        _check(qs[1], d["out_qodd"], 1e-12, "q odd")
+    _check(even, d["out_even"], 1e-12, "even")
+    _check(odd, d["out_odd"], 1e-12, "odd")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("path", FILES, ids=IDS)
+def test_kernels_vs_reference_cuda(gpu, path, prec):
+    from spacetime_gb300.stepper import Stepper
+
+    d = _load(path)
+    lat, p = _params(d, prec)
+    tol = 1e-12 if prec == capi.FP64 else 2e-5
+    n = d["fields"].shape[0]
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
+        s.upload(capi.PSI_ODD, _embed(d["in_odd"]))
+        if d["kind"] == "hyper":
+            s.upload(capi.Q_EVEN, _embed(d["in_qeven"]))
+            s.upload(capi.Q_ODD, _embed(d["in_qodd"]))
+        for j in range(n):
+            if d["kind"] == "spinor":
+                slots = [capi.PSI_ODD, capi.PSI_EVEN]
+                mode = capi.MODE_EULER if j == 0 else capi.MODE_LEAPFROG
+                s.step_explicit(slots[(j + 1) % 2], slots[j % 2], _fields(d["fields"][j]), float(d["times"][j]), mode)
+            else:
+                slots = [capi.PSI_EVEN, capi.PSI_ODD]
+                f = _fields(d["fields"][j]) if d["kind"] == "hyper" else capi.make_fields()
+                s.step_explicit(slots[(j + 1) % 2], slots[j % 2], f, 0.0, capi.MODE_LEAPFROG)
+        _check(s.download(capi.PSI_EVEN), d["out_even"], tol, "even")
+        _check(s.download(capi.PSI_ODD), d["out_odd"], tol, "odd")
+        if d["kind"] == "hyper":
+            _check(s.download(capi.Q_EVEN), d["out_qeven"], tol, "q even")
+            _check(s.download(capi.Q_ODD), d["out_qodd"], tol, "q odd")
