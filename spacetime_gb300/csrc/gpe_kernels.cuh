@@ -12,6 +12,7 @@
 // GPUGrossPitaevskii_BCC.cu:327-347, RelativisticSpin2Gpe.cu:971-1132).
 #pragma once
 
+#include <algorithm>
 #include <type_traits>
 
 #include "gpe_internal.h"
@@ -514,8 +515,10 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
     double acc[OBS_COUNT];
 #pragma unroll
     for (int k = 0; k < OBS_COUNT; ++k) acc[k] = 0.0;
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid < a.total) {
+    // grid-stride: each thread sums many nodes, so the FP64 warp reduction (which
+    // runs on GB300's narrow FP64 pipe) is paid once per thread, not per node
+    for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
+         gid += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)gid;
         const uint32_t row = fdiv(i, a.divRow);
         const uint32_t within = i - row * a.row_items;
@@ -566,31 +569,31 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
             hl += ps[s].x * Hl[s].x + ps[s].y * Hl[s].y;
             hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
         }
-        acc[OBS_NORM] = rho;
-        acc[OBS_HEXP] = (double)kin + (double)hl;
-        acc[OBS_EINT] = hn;
-        acc[OBS_COMX] = (double)rho * r[0];
-        acc[OBS_COMY] = (double)rho * r[1];
-        acc[OBS_COMZ] = (double)rho * r[2];
-        acc[OBS_MAXABS] = maxabs;
-        acc[OBS_NONFINITE] = bad;
+        acc[OBS_NORM] += rho;
+        acc[OBS_HEXP] += (double)kin + (double)hl;
+        acc[OBS_EINT] += hn;
+        acc[OBS_COMX] += (double)rho * r[0];
+        acc[OBS_COMY] += (double)rho * r[1];
+        acc[OBS_COMZ] += (double)rho * r[2];
+        acc[OBS_MAXABS] = fmax(acc[OBS_MAXABS], (double)maxabs);
+        acc[OBS_NONFINITE] += bad;
         if constexpr (C == 3) {
             const Cx<A> m = (A)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
             const A fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
-            acc[OBS_MAGX] = m.x;
-            acc[OBS_MAGY] = m.y;
-            acc[OBS_MAGZ] = fz;
-            acc[OBS_SPIN] = sqrt(m.x * m.x + m.y * m.y + fz * fz);
+            acc[OBS_MAGX] += m.x;
+            acc[OBS_MAGY] += m.y;
+            acc[OBS_MAGZ] += fz;
+            acc[OBS_SPIN] += sqrt(m.x * m.x + m.y * m.y + fz * fz);
         } else if constexpr (C == 5) {
             const Cx<A> fp = (A)2 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
                              (A)2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
             A n[5];
             for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
             const A fz = (A)2 * n[0] + n[1] - n[3] - (A)2 * n[4];
-            acc[OBS_MAGX] = fp.x;
-            acc[OBS_MAGY] = fp.y;
-            acc[OBS_MAGZ] = fz;
-            acc[OBS_SPIN] = sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
+            acc[OBS_MAGX] += fp.x;
+            acc[OBS_MAGY] += fp.y;
+            acc[OBS_MAGZ] += fz;
+            acc[OBS_SPIN] += sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
         }
     }
     // warp reduction
@@ -730,7 +733,12 @@ cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
 // node_fp32: per-node terms in FP32 (FP32 storage only); sums are FP64 either way.
 template <typename R, int C>
 cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaStream_t s) {
-    const unsigned nb = nblocks(a.total, 256);
+    // a fixed grid of 8 blocks per SM (fewer for small grids); the partial sums are
+    // added in an order that depends only on the grid size
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), 8u * (unsigned)(sms > 0 ? sms : 1));
     if (sizeof(R) == 4 && node_fp32) observe_kernel<R, C, float><<<nb, 256, 0, s>>>(a);
     else observe_kernel<R, C, double><<<nb, 256, 0, s>>>(a);
     observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
