@@ -542,7 +542,7 @@ def run_gpu(args):
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
     for key, val in ((capi.TUNE_TILE_CELLS, args.tile), (capi.TUNE_TILE_ROWS, args.rows), (capi.TUNE_ZCHUNK, args.zchunk),
-                     (capi.TUNE_THREADS, args.threads)):
+                     (capi.TUNE_THREADS, args.threads), (capi.TUNE_CARVEOUT, args.carveout)):
         if val:
             s.set_tuning(key, val)
     tuning_report = None
@@ -722,6 +722,7 @@ def main():
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--zchunk", type=int, default=0)
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--carveout", type=int, default=0, help="shared-memory carveout percent for the row-tile kernel")
     ap.add_argument("--autotune", action="store_true", help="run gpe_autotune before timing")
     ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96", "adjoint-bcc64", "ensemble-256"] + sorted(LEGS))
     ap.add_argument("--inner", type=int, default=0, help="leapfrog steps per bench step for --workload legs")

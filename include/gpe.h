@@ -279,14 +279,18 @@ gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* o
  * GPE_TUNE_OBSERVE_ARITH: arithmetic of gpe_observe's per-node terms on an FP32
  *                   handle: 0 = FP64 (default; the same numbers as an FP64 run
  *                   on the stored values), 1 = FP32.  The sums over nodes are FP64
- *                   either way; mode 0 is bound by GB300's narrow FP64 pipe. */
+ *                   either way; mode 0 is bound by GB300's narrow FP64 pipe.
+ * GPE_TUNE_CARVEOUT: shared-memory share (percent) of the unified L1 / shared
+ *                   memory for the row-tile kernel; the rest caches its off-row
+ *                   gathers (0 = driver default). */
 enum {
     GPE_TUNE_KERNEL = 0,
     GPE_TUNE_TILE_CELLS = 1,
     GPE_TUNE_TILE_ROWS = 2,
     GPE_TUNE_ZCHUNK = 3,
     GPE_TUNE_THREADS = 4,
-    GPE_TUNE_OBSERVE_ARITH = 5
+    GPE_TUNE_OBSERVE_ARITH = 5,
+    GPE_TUNE_CARVEOUT = 6
 };
 gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value);
 gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);

@@ -28,7 +28,7 @@ struct InitArgs {
 template <typename R, int C>
 cudaError_t launch_init(const StepArgs& a, const InitArgs& in, cudaStream_t s);
 template <typename R, int C>
-cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, cudaStream_t s);
+cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, int carveout, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_leapfrog_rows(const StepArgs& a, uint32_t T, uint32_t RY, uint32_t RZ, uint32_t K, uint32_t nbuf,
                                  const int32_t* blk, uint32_t threads, cudaStream_t s);
@@ -789,7 +789,8 @@ static uint32_t tile_cells(const gpe_handle* h) {
 
 template <int C>
 static cudaError_t dispatch_tile_c(const gpe_handle* h, const StepArgs& a, uint32_t T, cudaStream_t s) {
-    return h->real_bytes == 8 ? launch_leapfrog_tile<double, C>(a, T, s) : launch_leapfrog_tile<float, C>(a, T, s);
+    return h->real_bytes == 8 ? launch_leapfrog_tile<double, C>(a, T, h->tune_carveout, s)
+                              : launch_leapfrog_tile<float, C>(a, T, h->tune_carveout, s);
 }
 static cudaError_t dispatch_tile(const gpe_handle* h, const StepArgs& a, uint32_t T, cudaStream_t s) {
     switch (h->g.C) {
@@ -1037,6 +1038,11 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
         }
         return GPE_OK;
     }
+    if (key == GPE_TUNE_CARVEOUT) {
+        if (value < 0 || value > 100) return fail(GPE_ERR_INVALID_ARG, "carveout: 0 (driver default) or 1..100 percent");
+        h->tune_carveout = value;
+        return GPE_OK;
+    }
     if (key == GPE_TUNE_OBSERVE_ARITH) {
         if (value != 0 && value != 1) return fail(GPE_ERR_INVALID_ARG, "observe arithmetic: 0 (FP64) or 1 (storage precision)");
         h->tune_observe = value;
@@ -1076,6 +1082,7 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
     else if (key == GPE_TUNE_ZCHUNK) *value = (int32_t)(tr > 0 ? rows_shape(h).RZ : ms.ZC);
     else if (key == GPE_TUNE_THREADS) *value = h->tune_threads;
     else if (key == GPE_TUNE_OBSERVE_ARITH) *value = h->tune_observe;
+    else if (key == GPE_TUNE_CARVEOUT) *value = h->tune_carveout;
     else return fail(GPE_ERR_INVALID_ARG, "unknown tuning key");
     return GPE_OK;
 }

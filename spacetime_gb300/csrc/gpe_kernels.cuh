@@ -1015,21 +1015,27 @@ size_t tile_smem_bytes(const StepArgs& a, uint32_t T) {
 }
 
 template <typename R, int C>
-cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
+cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, int carveout, cudaStream_t s) {
     const uint32_t tiles = (a.g.X + T - 1) / T;
     const uint32_t threads = ((T * a.g.V + 31) / 32) * 32;
     const size_t smem = tile_smem_bytes<R, C>(a, T);
     static bool configured = false;
+    static int carve = -2;
     if (!configured) {
         cudaFuncSetAttribute(leapfrog_tile_kernel<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         configured = true;
+    }
+    if (carveout != carve) {  // shared-memory share of the unified L1 (the rest caches off-row gathers)
+        cudaFuncSetAttribute(leapfrog_tile_kernel<R, C>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             carveout > 0 ? carveout : -1);
+        carve = carveout;
     }
     const uint64_t blocks = (uint64_t)tiles * a.g.Y * a.g.Z;
     leapfrog_tile_kernel<R, C><<<(unsigned)blocks, threads, smem, s>>>(a, T, tiles);
     return cudaGetLastError();
 }
 
-#define GPE_INSTANTIATE_TILE(R, C) template cudaError_t launch_leapfrog_tile<R, C>(const StepArgs&, uint32_t, cudaStream_t);
+#define GPE_INSTANTIATE_TILE(R, C) template cudaError_t launch_leapfrog_tile<R, C>(const StepArgs&, uint32_t, int, cudaStream_t);
 
 }  // namespace gpe
 
