@@ -805,10 +805,15 @@ static uint32_t hyper_tile_cells(const gpe_handle* h) {
     if (h->tune_kernel == 1 || h->g.E == 0) return 0;
     if (h->g.cell_bytes % 16 != 0 || h->g.qcell_bytes % 16 != 0) return 0;
     const uint32_t per = h->g.V + h->g.E;
+    const size_t tables = (size_t)h->g.V * h->lat.F * (8 + h->real_bytes) + (size_t)(3 * h->g.E + 1) * 4 +
+                          3 * h->g.V * h->real_bytes;
+    const size_t per_cell = 2 * (size_t)(h->g.cell_bytes + h->g.qcell_bytes);  // psi, q, psi_next, q_next
     uint32_t T = h->tune_tile > 0 ? (uint32_t)h->tune_tile : 0;
     if (T == 0) {
-        T = 576 / per > 0 ? 576 / per : 1;
-        if (T > h->g.X) T = h->g.X;
+        // the most cells that keep the block within ~48 KB of shared memory (four or
+        // more blocks per SM) and 1024 tasks, preferring a divisor of X
+        T = 1;
+        while (T < h->g.X && tables + (T + 1) * per_cell <= 48 * 1024 && (T + 1) * per <= 1024) ++T;
         for (uint32_t t = T; t * 2 > T && t > 0; --t)
             if (h->g.X % t == 0) {
                 T = t;
@@ -816,10 +821,7 @@ static uint32_t hyper_tile_cells(const gpe_handle* h) {
             }
     }
     if (T == 0 || T > h->g.X || (uint64_t)T * per > 4096) return 0;
-    const size_t smem = (size_t)(2 * T + 2) * (h->g.cell_bytes + h->g.qcell_bytes) +
-                        (size_t)h->g.V * h->lat.F * (8 + h->real_bytes) + (size_t)(3 * h->g.E + 1) * 4 +
-                        3 * h->g.V * h->real_bytes;
-    if (smem > 200 * 1024) return 0;
+    if (tables + T * per_cell > 200 * 1024) return 0;
     return T;
 }
 

@@ -1578,22 +1578,25 @@ namespace gpe {
 // ------------------------------------------------- hyperbolic row tiles (TMA)
 
 // Fused hyperbolic psi+q leapfrog step on a row tile of T cells.  One bulk copy
-// each brings psi_prev and q_prev of cells [x0-1, x0+T] and the old psi_next and
-// q_next of [x0, x0+T) into shared memory; threads [0, T*V) update nodes and
-// threads [T*V, T*(V+E)) update edges.  In-row neighbours (the d1 incidences of a
-// node, the d0 end points of an edge) are read from shared memory, off-row ones
-// from global memory (L2).  Both updated tiles go back by bulk stores.  Requires
-// cell_bytes and qcell_bytes to be multiples of 16.
+// each brings psi_prev, q_prev, the old psi_next and the old q_next of cells
+// [x0, x0+T) into shared memory; tasks [0, T*V) update nodes and tasks
+// [T*V, T*(V+E)) update edges, looped over the block's threads.  Neighbours
+// inside the tile (the d1 incidences of a node, the d0 end points of an edge) are
+// read from shared memory, all others -- other rows, and the cells just outside
+// the tile -- from global memory (L2): no halo cells are staged, which keeps the
+// C15 tile (16 KB of psi+q per cell) small enough for several blocks per SM.
+// Both updated tiles go back by bulk stores.  Requires cell_bytes and
+// qcell_bytes to be multiples of 16.
 template <typename R, int C>
-__global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T, uint32_t tiles_per_row) {
+__global__ void __launch_bounds__(256) hyper_tile_kernel(StepArgs a, uint32_t T, uint32_t tiles_per_row) {
     extern __shared__ __align__(128) unsigned char dyn[];
     __shared__ __align__(8) uint64_t bar;
     using V2 = typename Vec2<R>::type;
     const uint32_t cb = a.g.cell_bytes, qb = a.g.qcell_bytes;
     const int V = a.g.V, E = a.g.E, F = a.tab.faces;
-    char* s_psi = reinterpret_cast<char*>(dyn);                  // (T+2) psi cells
-    char* s_q = s_psi + (size_t)(T + 2) * cb;                    // (T+2) q cells
-    char* s_psin = s_q + (size_t)(T + 2) * qb;                   // T psi cells
+    char* s_psi = reinterpret_cast<char*>(dyn);                  // T psi cells
+    char* s_q = s_psi + (size_t)T * cb;                          // T q cells
+    char* s_psin = s_q + (size_t)T * qb;                         // T psi cells
     char* s_qn = s_psin + (size_t)T * cb;                        // T q cells
     int32_t* s_inc_soff = reinterpret_cast<int32_t*>(s_qn + (size_t)T * qb);  // V*F
     int32_t* s_inc_goff = s_inc_soff + V * F;
@@ -1609,8 +1612,8 @@ __global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T
     const uint32_t y = row - z * a.g.Y;
     const uint32_t x0 = tile * T;
     const uint32_t Tc = min(T, a.g.X - x0);
-    const char* g_psi = a.prev + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x0 * cb - cb;
-    const char* g_q = a.q + (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x0 * qb - qb;
+    const char* g_psi = a.prev + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x0 * cb;
+    const char* g_q = a.q + (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x0 * qb;
     char* g_psin = a.next + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x0 * cb;
     char* g_qn = a.qnext + (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x0 * qb;
 
@@ -1620,9 +1623,9 @@ __global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, (Tc + 2) * (cb + qb) + Tc * (cb + qb));
-        bulk_load(s_psi, g_psi, (Tc + 2) * cb, &bar);
-        bulk_load(s_q, g_q, (Tc + 2) * qb, &bar);
+        mbar_expect_tx(&bar, 2 * Tc * (cb + qb));
+        bulk_load(s_psi, g_psi, Tc * cb, &bar);
+        bulk_load(s_q, g_q, Tc * qb, &bar);
         bulk_load(s_psin, g_psin, Tc * cb, &bar);
         bulk_load(s_qn, g_qn, Tc * qb, &bar);
     }
@@ -1650,7 +1653,7 @@ __global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T
             if (i >= Tc * V) continue;
             const uint32_t xl = fdiv(i, a.divV);
             const uint32_t l = i - xl * V;
-            const char* own = s_psi + (size_t)(xl + 1) * cb + l * node_bytes;
+            const char* own = s_psi + (size_t)xl * cb + l * node_bytes;
             Cx<R> prv[C], H[C];
 #pragma unroll
             for (int c = 0; c < C; ++c) {
@@ -1659,20 +1662,20 @@ __global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T
                 H[c] = cx<R>((R)0, (R)0);
             }
             // d1 of q (RelativisticSpin2Gpe.cu:1051-1066)
-            const char* s_qcell = s_q + (size_t)(xl + 1) * qb;
-            const char* g_qcell = g_q + (size_t)(xl + 1) * qb;
+            const int32_t qrow = (int32_t)(xl * qb), qend = (int32_t)(Tc * qb);
             for (int k = 0; k < F; ++k) {
                 const int so = s_inc_soff[l * F + k];
                 const R w = s_inc_w[l * F + k];
-                if (so != INT32_MIN) {
-                    const V2* p = reinterpret_cast<const V2*>(s_qcell + so);
+                const int32_t tgt = qrow + so;  // byte offset from the tile's first q cell
+                if (so != INT32_MIN && tgt >= 0 && tgt < qend) {
+                    const V2* p = reinterpret_cast<const V2*>(s_q + tgt);
 #pragma unroll
                     for (int c = 0; c < C; ++c) {
                         const V2 v = p[c];
                         H[c] += w * cx<R>(v.x, v.y);
                     }
                 } else {
-                    const char* g = g_qcell + s_inc_goff[l * F + k];
+                    const char* g = so != INT32_MIN ? g_q + tgt : g_q + qrow + s_inc_goff[l * F + k];
 #pragma unroll
                     for (int c = 0; c < C; ++c) H[c] += w * ldc<R>(g + c * 2 * sizeof(R));
                 }
@@ -1704,12 +1707,13 @@ __global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T
             const uint32_t xl = fdiv(j, a.divE);
             if (xl >= Tc) continue;
             const uint32_t e = j - xl * E;
-            const char* s_cell = s_psi + (size_t)(xl + 1) * cb;
-            const char* thisp = s_cell + s_e_from[e];
+            const int32_t prow = (int32_t)(xl * cb);
+            const char* thisp = s_psi + prow + s_e_from[e];
             const int ts = s_e_tos[e];
-            const bool to_in_row = ts != INT32_MIN;
-            const char* otherp = to_in_row ? s_cell + ts : g_psi + (size_t)(xl + 1) * cb + s_e_tog[e];
-            const char* qprev = s_q + (size_t)(xl + 1) * qb + e * node_bytes;
+            const int32_t tgt = prow + ts;  // byte offset from the tile's first psi cell
+            const bool to_in_row = ts != INT32_MIN && tgt >= 0 && tgt < (int32_t)(Tc * cb);
+            const char* otherp = to_in_row ? s_psi + tgt : (ts != INT32_MIN ? g_psi + tgt : g_psi + prow + s_e_tog[e]);
+            const char* qprev = s_q + (size_t)xl * qb + e * node_bytes;
             V2* qn = reinterpret_cast<V2*>(s_qn + (size_t)xl * qb + e * node_bytes);
             const R dts2 = (R)2 * P.dts;
 #pragma unroll
@@ -1745,7 +1749,7 @@ __global__ void __launch_bounds__(1024) hyper_tile_kernel(StepArgs a, uint32_t T
 template <typename R, int C>
 size_t hyper_tile_smem_bytes(const StepArgs& a, uint32_t T) {
     const int V = a.g.V, E = a.g.E, F = a.tab.faces;
-    return (size_t)(2 * T + 2) * (a.g.cell_bytes + a.g.qcell_bytes) + (size_t)V * F * (8 + sizeof(R)) +
+    return (size_t)(2 * T) * (a.g.cell_bytes + a.g.qcell_bytes) + (size_t)V * F * (8 + sizeof(R)) +
            (size_t)(3 * E + (E & 1)) * 4 + 3 * V * sizeof(R);
 }
 
@@ -1753,7 +1757,9 @@ template <typename R, int C>
 cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
     const uint32_t tiles = (a.g.X + T - 1) / T;
     const uint32_t tasks = T * (a.g.V + a.g.E);
-    const uint32_t threads = tasks >= 1024 ? 1024 : ((tasks + 31) / 32) * 32;
+    // at most 256 threads; the tasks split evenly into passes of the block
+    const uint32_t passes = (tasks + 255) / 256;
+    const uint32_t threads = (((tasks + passes - 1) / passes) + 31) / 32 * 32;
     const size_t smem = hyper_tile_smem_bytes<R, C>(a, T);
     if (smem > 220 * 1024) return cudaErrorInvalidValue;
     static size_t configured = 0;
