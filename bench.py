@@ -111,10 +111,12 @@ def run_leg(args):
         total_ms = a.elapsed_time(b)
         launches = s.launches - n0
     sites = s.sites
+    s.close()
+    drift = leg_drift(w, lat, args.drift_steps) if args.leg_drift else None
     launch_ms = step_ms / (inner * args.steps)
     algo = w["bytes_fp32"] * sites
     peak, kind = measured_peak()
-    name = "hyper_step_kernel<float,%d,fused>" % w["C"] if w["scheme"] else "leapfrog kernel (auto) C=%d" % w["C"]
+    name = "hyper_tile_kernel<float,%d>" % w["C"] if w["scheme"] else "leapfrog kernel (auto) C=%d" % w["C"]
     res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
            "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -125,9 +127,46 @@ def run_leg(args):
            "gpu_launches": launches, "clocks": clk.summary(),
            "energy_rel_drift": abs(obs[-1]["energy"] - e0["energy"]) / abs(e0["energy"]) if obs else None,
            "norm_last": obs[-1]["norm"] if obs else None}
-    s.close()
+    if drift is not None:
+        res["drift"] = drift
     print(json.dumps(res))
     return 0
+
+
+def leg_drift(w, lat, nsteps, every=100):
+    """FP32 against FP64 on the leg's workload from the same seeded device state:
+    observables (FP64 arithmetic) every `every` steps."""
+    import torch
+
+    from spacetime_gb300 import capi
+    from spacetime_gb300.stepper import Stepper
+
+    bs = BOX / (w["dims"][0] * lat.block_width[0])
+    runs = {}
+    for prec in (capi.FP32, capi.FP64):
+        p = capi.make_params(components=w["C"], scheme=w["scheme"], precision=prec, dims=w["dims"], block_scale=bs,
+                             dt=w["dt"], trap_offset=100.0, c0=w["c0"], c2=w["c2"], c4=w["c4"], sigma=w["sigma"],
+                             lattice=lat)
+        s = Stepper(lat, p)
+        s.init_state(capi.PSI_ODD, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
+                                                  noise_rel=w["noise_rel"], seed=w["seed"]))
+        s.start()
+        e = [s.observe(s.current, 0.0)]
+        done = 0
+        while done < nsteps:
+            k = min(every, nsteps - done)
+            s.step(k)
+            done += k
+            e.append(s.observe(s.current, done * w["dt"]))
+        torch.cuda.synchronize()
+        runs[prec] = e
+        s.close()
+    e32, e64 = runs[capi.FP32], runs[capi.FP64]
+    return {"steps": nsteps, "every": every,
+            "energy_rel_diff_max": max(abs(a["energy"] - b["energy"]) / abs(b["energy"]) for a, b in zip(e32, e64)),
+            "norm_rel_diff_max": max(abs(a["norm"] - b["norm"]) / abs(b["norm"]) for a, b in zip(e32, e64)),
+            "energy_rel_drift_fp32": abs(e32[-1]["energy"] - e32[0]["energy"]) / abs(e32[0]["energy"]),
+            "energy_rel_drift_fp64": abs(e64[-1]["energy"] - e64[0]["energy"]) / abs(e64[0]["energy"])}
 
 
 # Adjoint ramp control: spin-1, BCC 64^3 cells, 2000 steps, Bz(t) and Bq(t) with 16
@@ -727,6 +766,8 @@ def main():
     ap.add_argument("--workload", default="spin1-bcc96", choices=["spin1-bcc96", "adjoint-bcc64", "ensemble-256"] + sorted(LEGS))
     ap.add_argument("--inner", type=int, default=0, help="leapfrog steps per bench step for --workload legs")
     ap.add_argument("--observe-fp64", action="store_true", help="FP64 arithmetic for the per-step observables")
+    ap.add_argument("--leg-drift", action="store_true",
+                    help="--workload legs: FP32 vs FP64 observables over --drift-steps steps (every 100)")
     ap.add_argument("--adjoint-steps", type=int, default=ADJ["steps"], help="adjoint-bcc64: steps of the recorded run")
     ap.add_argument("--fd-knots", type=int, default=ADJ["fd_knots"], help="adjoint-bcc64: knots checked by central differences")
     ap.add_argument("--members", type=int, default=ENS["members"], help="ensemble-256: members of the ensemble (a prefix)")
