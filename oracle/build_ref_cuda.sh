@@ -23,6 +23,7 @@ build Spin1GpeBCC/Spin1GpeBCC spin1_bcc &
 build Spin2GpeBCC/Spin2GpeBCC spin2_bcc &
 build RelativisticSpin2Gpe/RelativisticSpin2Gpe rel_spin2_bcc &
 build RelativisticSpin1Gpe/RelativisticSpin1Gpe rel_spin1_bcc &
+build RelativisticGpeBCC/RelativisticGpeBCC rel_scalar_bcc &
 build GrossPitaevskiiGpuBcc/GPUGrossPitaevskii_BCC scalar_bcc &
 build GrossPitaevskiiGpuC15/GPUGrossPitaevskii_C15 scalar_c15 &
 build GrossPitaevskiiGpuA15/GPUGrossPitaevskii_A15 scalar_a15 &

@@ -15,6 +15,8 @@ Kernels (names as the compiler exports them):
   spin1_bcc      leapfrog / forwardEuler       Spin1GpeBCC/Spin1GpeBCC.cu:667-917
   spin2_bcc      leapfrog / forwardEuler       Spin2GpeBCC/Spin2GpeBCC.cu:698-990
   rel_spin2_bcc  update_psi / update_q          RelativisticSpin2Gpe/RelativisticSpin2Gpe.cu:971-1132
+  rel_spin1_bcc  update_psi / update_q_hyper    RelativisticSpin1Gpe/common_kernels.h:176-255, hyper_kernels.h:80-116
+  rel_scalar_bcc update_psi / update_q          RelativisticGpeBCC/RelativisticGpeBCC.cu:179-255 (sigma = 0.001 compiled in)
   scalar_bcc     update                         GrossPitaevskiiGpuBcc/GPUGrossPitaevskii_BCC.cu:176-202, 327-347
   scalar_c15/a15 update (dt folded in)          GrossPitaevskiiGpuC15/GPUGrossPitaevskii_C15.cu:104-146
   scalar_fcc     update (CSR node table)        GrossPitaevskiiGpuFcc/GPUGrossPitaevskii_FCC.cu:104-150
@@ -38,6 +40,7 @@ QUAD_CENTER = (-0.20590789, -0.48902826, -0.27353409)     # Spin1GpeBCC.cu:124-1
 SPIN2_DT = 1e-5                                           # Spin2GpeBCC.cu:159
 TB_X, TB_Y = 16, 2                                        # THREAD_BLOCK_X/Y of the spinor programs
 SCALAR_TB = 8                                             # THREAD_BLOCK_X/Y of the scalar programs
+REL_SCALAR_SIGMA = 0.001                                  # RelativisticGpeBCC.cu:18
 
 NAMES = {
     ("spin1_bcc", "leapfrog"): "_Z8leapfrog10PitchedPtrS_PK4int4PKd9MagFields5uint3d7double3dddbbbdd",
@@ -46,6 +49,10 @@ NAMES = {
     ("spin2_bcc", "euler"): "_Z12forwardEuler10PitchedPtrS_P4int4Pd9MagFields5uint3d7double3ddddd",
     ("rel_spin2_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_PK4int2PKd9MagFields5uint3d7double3ddddbd",
     ("rel_spin2_bcc", "update_q"): "_Z8update_q10PitchedPtrS_S_P4int35uint3db",
+    ("rel_spin1_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_PK4int2PKd9MagFields5uint3d7double3dddbd",
+    ("rel_spin1_bcc", "update_q_hyper"): "_Z14update_q_hyper10PitchedPtrS_S_P4int35uint3d",
+    ("rel_scalar_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_S_P4int2Pdd5uint3d",
+    ("rel_scalar_bcc", "update_q"): "_Z8update_q10PitchedPtrS_S_P4int35uint3d",
     ("scalar_bcc", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3d",
     ("scalar_c15", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3",
     ("scalar_a15", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3",

@@ -8,7 +8,9 @@ oracle/ref_cuda.py with per-step fields and times, and stores the parameters,
 the inputs and the outputs (interior cells only).  tests/test_ref_cuda_golden.py
 replays every sequence with the oracle (CPU) and with libgpe's kernels (GPU).
 
-    python tests/golden/make_ref_cuda_golden.py [outdir]
+    python tests/golden/make_ref_cuda_golden.py [outdir] [--all]
+
+Cases whose file already exists in outdir are kept unless --all is given.
 """
 from __future__ import annotations
 
@@ -85,13 +87,18 @@ def spinor_case(drv, name, program, lattice, C, dims, flags, dt, c0, c2, c4, alp
                 in_even=interior(even0), in_odd=interior(odd0), **{"out_" + k: v for k, v in out.items()})
 
 
-def rel_case(drv, name, lattice, dims, dt, sigma, c0, c2, c4, seed):
+def rel_case(drv, name, lattice, dims, dt, sigma, c0, c2, c4, seed, program="rel_spin2_bcc", C=5):
     """NSTEPS hyperbolic steps: update_psi then update_q per step
-    (RelativisticSpin2Gpe.cu:1859-1899)."""
+    (RelativisticSpin2Gpe.cu:1859-1899; RelativisticSpin1Gpe.cu:830-850;
+    RelativisticGpeBCC.cu:683-687).  The scalar program's psi increment is
+    dt_ref (-i H) and its q increment i (dt_ref/sigma)(q + d0 psi): libgpe's
+    2 dt and 2 dt/sigma with dt = dt_ref/2; its potential array holds the trap
+    values libgpe computes."""
     lat = capi.Lattice(lattice)
-    p = capi.make_params(components=5, scheme=capi.SCHEME_HYPERBOLIC, precision=capi.FP64, dims=dims, block_scale=0.3,
-                         dt=dt, trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, c4=c4,
-                         sigma=sigma, lattice=lat)
+    scalar = program == "rel_scalar_bcc"
+    p = capi.make_params(components=C, scheme=capi.SCHEME_HYPERBOLIC, precision=capi.FP64, dims=dims, block_scale=0.3,
+                         dt=dt, trap_lambda=(1.0, 1.1, 1.3) if scalar else (1.0, 1.0, R.LAMBDA_Z),
+                         trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, c4=c4, sigma=sigma, lattice=lat)
     s = Stepper(lat, p)
     shape, qshape = capi.buffer_shape(lat, p), capi.buffer_shape(lat, p, edges=True)
     ins = {"in_even": 0.2 * states.random_state(shape, seed=seed), "in_odd": 0.2 * states.random_state(shape, seed=seed + 1),
@@ -104,18 +111,34 @@ def rel_case(drv, name, lattice, dims, dt, sigma, c0, c2, c4, seed):
     d0, d1, w = R.edge_tables(lat, s, p.block_scale)
     d_d0, d_d1, d_w = drv.upload(d0), drv.upload(d1), drv.upload(w)
     grid, pblock = R.spinor_grid(p, lat.nodes)
-    _, eblock = R.edge_grid(p, lat.edges)
-    F = fields_table(NSTEPS, seed + 7)
+    egrid, eblock = grid, R.edge_grid(p, lat.edges)[1]
+    if scalar:
+        grid, pblock = R.scalar_grid(p, lat.nodes)
+        egrid, eblock = R.scalar_grid(p, lat.edges)
+        d_pot = R.pitched_upload(drv, R.node_potential(lat, p))
+    F = fields_table(NSTEPS, seed + 7) if not scalar else np.zeros((NSTEPS, 8))
     psi = [R.pitched(s, capi.PSI_EVEN), R.pitched(s, capi.PSI_ODD)]
     q = [R.pitched(s, capi.Q_EVEN), R.pitched(s, capi.Q_ODD)]
     for j in range(NSTEPS):
         a, b = j % 2, (j + 1) % 2  # prev parity, next parity
-        drv.launch(drv.function("rel_spin2_bcc", "update_psi"), grid, pblock,
-                   [psi[b], psi[a], q[a], R.C.c_void_p(d_d1), R.C.c_void_p(d_w), R.mag_fields(as_fields(F[j])),
-                    R.uint3(p), R.C.c_double(p.block_scale), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2),
-                    R.C.c_double(c4), R.C.c_double(dt), R.C.c_bool(True), R.C.c_double(sigma)])
-        drv.launch(drv.function("rel_spin2_bcc", "update_q"), grid, eblock,
-                   [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(dt / sigma), R.C.c_bool(True)])
+        if scalar:
+            drv.launch(drv.function(program, "update_psi"), grid, pblock,
+                       [psi[b], psi[a], q[a], d_pot, R.C.c_void_p(d_d1), R.C.c_void_p(d_w), R.C.c_double(c0), R.uint3(p),
+                        R.C.c_double(2 * dt)])
+            drv.launch(drv.function(program, "update_q"), egrid, eblock,
+                       [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(2 * dt / sigma)])
+            continue
+        head = [psi[b], psi[a], q[a], R.C.c_void_p(d_d1), R.C.c_void_p(d_w), R.mag_fields(as_fields(F[j])),
+                R.uint3(p), R.C.c_double(p.block_scale), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2)]
+        tail = [R.C.c_double(dt), R.C.c_bool(True), R.C.c_double(sigma)]
+        drv.launch(drv.function(program, "update_psi"), grid, pblock,
+                   head + ([R.C.c_double(c4)] if C == 5 else []) + tail)
+        if C == 5:
+            drv.launch(drv.function(program, "update_q"), egrid, eblock,
+                       [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(dt / sigma), R.C.c_bool(True)])
+        else:
+            drv.launch(drv.function(program, "update_q_hyper"), egrid, eblock,
+                       [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(dt / sigma)])
     out = {"out_even": interior(s.download(capi.PSI_EVEN)), "out_odd": interior(s.download(capi.PSI_ODD)),
            "out_qeven": interior(s.download(capi.Q_EVEN)), "out_qodd": interior(s.download(capi.Q_ODD))}
     s.close()
@@ -173,6 +196,10 @@ CASES = [
     ("spin2_bcc", lambda d: spinor_case(d, "spin2_bcc", "spin2_bcc", "bcc", 5, (5, 3, 2), capi.FLAG_THREE_BODY_LOSS,
                                         R.SPIN2_DT, 120.0, -7.0, 3.0, 2.0, 31)),
     ("rel_spin2_bcc", lambda d: rel_case(d, "rel_spin2_bcc", "bcc", (4, 3, 2), 2e-4, 0.01, 120.0, -7.0, 3.0, 41)),
+    ("rel_spin1_bcc", lambda d: rel_case(d, "rel_spin1_bcc", "bcc", (4, 3, 2), 2e-4, 0.01, 120.0, -7.0, 0.0, 43,
+                                         program="rel_spin1_bcc", C=3)),
+    ("rel_scalar_bcc", lambda d: rel_case(d, "rel_scalar_bcc", "bcc", (5, 3, 2), 1e-4, R.REL_SCALAR_SIGMA, 150.0, 0.0,
+                                          0.0, 45, program="rel_scalar_bcc", C=1)),
     ("scalar_bcc", lambda d: scalar_case(d, "scalar_bcc", "scalar_bcc", "bcc", (5, 3, 2), 2e-4, 150.0, 51)),
     ("scalar_c15", lambda d: scalar_case(d, "scalar_c15", "scalar_c15", "c15", (2, 2, 2), 2e-4, 150.0, 61)),
     ("scalar_a15", lambda d: scalar_case(d, "scalar_a15", "scalar_a15", "a15", (3, 2, 2), 2e-4, 150.0, 71)),
@@ -188,6 +215,8 @@ def main(outdir):
     try:
         for name, fn in CASES:
             program = name.replace("_toggles", "")
+            if os.path.exists(os.path.join(outdir, "ref_cuda_%s.npz" % name)) and "--all" not in sys.argv:
+                continue  # keep the vectors already made
             if not R.available(program):
                 print("skip %s: %s.cubin not built" % (name, program))
                 continue
@@ -202,4 +231,5 @@ def main(outdir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden"))
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(args[0] if args else os.path.join(ROOT, "tests", "golden"))
