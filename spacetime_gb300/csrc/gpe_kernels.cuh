@@ -1587,8 +1587,10 @@ namespace gpe {
 // C15 tile (16 KB of psi+q per cell) small enough for several blocks per SM.
 // Both updated tiles go back by bulk stores.  Requires cell_bytes and
 // qcell_bytes to be multiples of 16.
+constexpr uint32_t kHyperTileThreads = 224;
 template <typename R, int C>
-__global__ void __launch_bounds__(256) hyper_tile_kernel(StepArgs a, uint32_t T, uint32_t tiles_per_row) {
+__global__ void __launch_bounds__(kHyperTileThreads, sizeof(R) == 4 ? 5 : 2)
+    hyper_tile_kernel(StepArgs a, uint32_t T, uint32_t tiles_per_row) {
     extern __shared__ __align__(128) unsigned char dyn[];
     __shared__ __align__(8) uint64_t bar;
     using V2 = typename Vec2<R>::type;
@@ -1757,15 +1759,18 @@ template <typename R, int C>
 cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
     const uint32_t tiles = (a.g.X + T - 1) / T;
     const uint32_t tasks = T * (a.g.V + a.g.E);
-    // at most 256 threads; the tasks split evenly into passes of the block
-    const uint32_t passes = (tasks + 255) / 256;
-    const uint32_t threads = (((tasks + passes - 1) / passes) + 31) / 32 * 32;
+    // at most kHyperTileThreads threads (five blocks per SM in FP32); the tasks split
+    // evenly into passes of the block
+    const uint32_t passes = (tasks + kHyperTileThreads - 1) / kHyperTileThreads;
+    const uint32_t threads = std::min(kHyperTileThreads, (((tasks + passes - 1) / passes) + 31) / 32 * 32);
     const size_t smem = hyper_tile_smem_bytes<R, C>(a, T);
     if (smem > 220 * 1024) return cudaErrorInvalidValue;
     static size_t configured = 0;
     if (smem > configured) {
         cudaError_t e = cudaFuncSetAttribute(hyper_tile_kernel<R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
+        // all of the unified L1 as shared memory: five ~44 KB C15 tiles per SM
+        cudaFuncSetAttribute(hyper_tile_kernel<R, C>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         configured = smem;
     }
     const uint64_t blocks = (uint64_t)tiles * a.g.Y * a.g.Z;
