@@ -156,7 +156,7 @@ __device__ __forceinline__ void block_partials(T (&v)[K], double scale, double* 
 // One reverse step: lambda_j = lambda_{j+2} + factor [L^T b + (dh/du)^T b] and the
 // field gradients factor (dh/dB)^T b, b = i lambda_{j+1}.  One thread per node.
 template <typename R, int C>
-__global__ void __launch_bounds__(256) adjoint_step_kernel(StepArgs a, AdjArgs j) {
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoint_step_kernel(StepArgs a, AdjArgs j) {
     __shared__ SmemTables<R> st;
     __shared__ R wT[kMaxEntries];
     load_tables<R>(st, a);

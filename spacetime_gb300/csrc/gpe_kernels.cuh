@@ -516,7 +516,14 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
 #pragma unroll
     for (int k = 0; k < OBS_COUNT; ++k) acc[k] = 0.0;
     // grid-stride: each thread sums many nodes, so the FP64 warp reduction (which
-    // runs on GB300's narrow FP64 pipe) is paid once per thread, not per node
+    // runs on GB300's narrow FP64 pipe) is paid once per thread, not per node.  With
+    // FP32 node terms, groups of kGroup nodes are summed in FP32 first and each group
+    // sum is added in FP64 (the group sum's rounding is that of its FP32 terms).
+    constexpr int kGroup = sizeof(A) == 4 ? 8 : 1;
+    A grp[OBS_COUNT];
+#pragma unroll
+    for (int k = 0; k < OBS_COUNT; ++k) grp[k] = (A)0;
+    int in_group = 0;
     for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
          gid += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)gid;
@@ -569,32 +576,57 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
             hl += ps[s].x * Hl[s].x + ps[s].y * Hl[s].y;
             hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
         }
-        acc[OBS_NORM] += rho;
-        acc[OBS_HEXP] += (double)kin + (double)hl;
-        acc[OBS_EINT] += hn;
-        acc[OBS_COMX] += (double)rho * r[0];
-        acc[OBS_COMY] += (double)rho * r[1];
-        acc[OBS_COMZ] += (double)rho * r[2];
-        acc[OBS_MAXABS] = fmax(acc[OBS_MAXABS], (double)maxabs);
-        acc[OBS_NONFINITE] += bad;
+        A v[OBS_COUNT];
+#pragma unroll
+        for (int k = 0; k < OBS_COUNT; ++k) v[k] = (A)0;
+        v[OBS_NORM] = rho;
+        v[OBS_HEXP] = kin + hl;
+        v[OBS_EINT] = hn;
+        v[OBS_COMX] = rho * r[0];
+        v[OBS_COMY] = rho * r[1];
+        v[OBS_COMZ] = rho * r[2];
         if constexpr (C == 3) {
             const Cx<A> m = (A)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
             const A fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
-            acc[OBS_MAGX] += m.x;
-            acc[OBS_MAGY] += m.y;
-            acc[OBS_MAGZ] += fz;
-            acc[OBS_SPIN] += sqrt(m.x * m.x + m.y * m.y + fz * fz);
+            v[OBS_MAGX] = m.x;
+            v[OBS_MAGY] = m.y;
+            v[OBS_MAGZ] = fz;
+            v[OBS_SPIN] = sqrt(m.x * m.x + m.y * m.y + fz * fz);
         } else if constexpr (C == 5) {
             const Cx<A> fp = (A)2 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
                              (A)2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
             A n[5];
             for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
             const A fz = (A)2 * n[0] + n[1] - n[3] - (A)2 * n[4];
-            acc[OBS_MAGX] += fp.x;
-            acc[OBS_MAGY] += fp.y;
-            acc[OBS_MAGZ] += fz;
-            acc[OBS_SPIN] += sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
+            v[OBS_MAGX] = fp.x;
+            v[OBS_MAGY] = fp.y;
+            v[OBS_MAGZ] = fz;
+            v[OBS_SPIN] = sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
         }
+        acc[OBS_MAXABS] = fmax(acc[OBS_MAXABS], (double)maxabs);
+        acc[OBS_NONFINITE] += bad;
+        if constexpr (kGroup == 1) {
+            // FP64 node terms: the sums as they were (kin + hl added in FP64)
+#pragma unroll
+            for (int k = 0; k < OBS_COUNT; ++k)
+                if (k != OBS_MAXABS && k != OBS_NONFINITE) acc[k] += (double)v[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < OBS_COUNT; ++k) grp[k] += v[k];
+            if (++in_group == kGroup) {
+#pragma unroll
+                for (int k = 0; k < OBS_COUNT; ++k)
+                    if (k != OBS_MAXABS && k != OBS_NONFINITE) acc[k] += (double)grp[k];
+#pragma unroll
+                for (int k = 0; k < OBS_COUNT; ++k) grp[k] = (A)0;
+                in_group = 0;
+            }
+        }
+    }
+    if constexpr (kGroup > 1) {
+#pragma unroll
+        for (int k = 0; k < OBS_COUNT; ++k)
+            if (k != OBS_MAXABS && k != OBS_NONFINITE) acc[k] += (double)grp[k];
     }
     // warp reduction
 #pragma unroll
