@@ -655,15 +655,6 @@ static cudaError_t dispatch_march(const gpe_handle* h, const StepArgs& a, const 
     }
 }
 
-static uint32_t auto_tile_length(const gpe_handle* h) {
-    const uint32_t V = h->g.V, X = h->g.X;
-    uint32_t tmax = 256 / V;
-    if (tmax == 0) tmax = 1;
-    if (tmax >= X) return X;
-    for (uint32_t t = tmax; t * 2 > tmax; --t)
-        if (X % t == 0) return t;
-    return tmax;
-}
 
 // Row buffers a block of RY x RZ output rows needs: the distinct (y, z) rows
 // (relative to the block origin) reached by the stencil's (dy, dz) offsets.

@@ -18,3 +18,13 @@ def test_fp32_vs_reference_fp64(gpu):
     assert r["energy_rel_diff_max"] <= 1e-6, r
     assert r["norm_rel_diff_max"] <= 1e-6, r
     assert r["psi_max_abs_err"] <= 1e-4 * r["psi_max_abs"], r
+
+
+def test_scalar_fp32_vs_reference_fp64(gpu):
+    if not ref_cuda.available("scalar_bcc"):
+        pytest.skip("reference cubins not built (oracle/build_ref_cuda.sh needs the reference tree)")
+    from oracle.ref_cuda_drift import run_scalar
+
+    r = run_scalar(cells=16, steps=300, every=100)
+    assert r["energy_rel_diff_max"] <= 1e-6, r
+    assert r["psi_max_abs_err"] <= 1e-4 * r["psi_max_abs"], r
