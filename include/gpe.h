@@ -383,7 +383,18 @@ gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, double* grad,
  *   one counter, so a block that finishes early takes more.
  *   `report` receives a JSON list of the timings. */
 typedef struct gpe_batch gpe_batch;
-enum { GPE_BATCH_ITEM_NODES = 0, GPE_BATCH_STEPS_PER_LAUNCH = 1, GPE_BATCH_BLOCKS_PER_SM = 2 };
+/* Batch tuning keys.  GPE_BATCH_BARRIER_TIMEOUT_MS bounds each grid-barrier wait
+ * (default 10000).  GPE_BATCH_TEST_EXTRA_ARRIVALS is a test hook for the failure
+ * path: the barrier then waits for that many arrivals that never come, every wait
+ * runs out, the kernel returns and the call reports GPE_ERR_TIMEOUT (set it back
+ * to 0 to step again). */
+enum {
+    GPE_BATCH_ITEM_NODES = 0,
+    GPE_BATCH_STEPS_PER_LAUNCH = 1,
+    GPE_BATCH_BLOCKS_PER_SM = 2,
+    GPE_BATCH_BARRIER_TIMEOUT_MS = 3,
+    GPE_BATCH_TEST_EXTRA_ARRIVALS = 4
+};
 gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count, gpe_batch** out);
 gpe_status gpe_batch_destroy(gpe_batch* b);
 gpe_status gpe_batch_step(gpe_batch* b, int32_t n, void* stream);

@@ -67,11 +67,12 @@ struct BatchArgs {
     uint32_t step_base;        // steps of this call taken by earlier launches
     unsigned* bar;             // grid barrier: arrivals, generation
     int* err;
+    unsigned expect;           // arrivals that release the barrier (gridDim.x; more only in tests)
+    unsigned long long timeout_ns;
 };
 
 constexpr unsigned kBatchThreads = 256;
 constexpr int32_t kMaxStepsPerLaunch = 4096;  // item counters held for one launch
-constexpr unsigned long long kBarrierTimeoutNs = 10ull * 1000 * 1000 * 1000;
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -80,9 +81,9 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Grid-wide barrier of a cooperative launch (all blocks co-resident).  The wait
-// is bounded; false means it ran out (or another block's did) and the error flag
-// is set.
-__device__ bool grid_barrier(unsigned* bar, int* err) {
+// is bounded by the global timer; false means it ran out (or another block's did)
+// and the error flag is set.
+__device__ bool grid_barrier(unsigned* bar, int* err, unsigned expect, unsigned long long timeout_ns) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -90,7 +91,7 @@ __device__ bool grid_barrier(unsigned* bar, int* err) {
         volatile unsigned* vgen = bar + 1;
         const unsigned gen = *vgen;
         __threadfence();
-        if (atomicAdd(bar, 1u) + 1 == gridDim.x) {
+        if (atomicAdd(bar, 1u) + 1 == expect) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);
@@ -101,7 +102,7 @@ __device__ bool grid_barrier(unsigned* bar, int* err) {
                     ok = 0;
                     break;
                 }
-                if (global_ns() - t0 > kBarrierTimeoutNs) {
+                if (global_ns() - t0 > timeout_ns) {
                     atomicExch(err, 2);
                     ok = 0;
                     break;
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs A) {
     const uint32_t gtid = blockIdx.x * kBatchThreads + threadIdx.x;
     const uint32_t gthreads = gridDim.x * kBatchThreads;
     for (uint32_t m = gtid; m < A.nmembers; m += gthreads) batch_fields(A, m, A.step_base, A.fields);
-    if (!grid_barrier(A.bar, A.err)) return;
+    if (!grid_barrier(A.bar, A.err, A.expect, A.timeout_ns)) return;
     for (uint32_t s = 0; s < A.nsteps; ++s) {
         const uint32_t k = A.step_base + s;
         const StepFieldsD* F = A.fields + (size_t)(s & 1) * A.nmembers;
@@ -224,7 +225,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs A) {
             StepFieldsD* G = A.fields + (size_t)((s + 1) & 1) * A.nmembers;
             for (uint32_t m = gtid; m < A.nmembers; m += gthreads) batch_fields(A, m, k + 1, G);
         }
-        if (!grid_barrier(A.bar, A.err)) return;
+        if (!grid_barrier(A.bar, A.err, A.expect, A.timeout_ns)) return;
     }
 }
 
@@ -261,6 +262,8 @@ struct gpe_batch {
     int32_t steps_per_launch = 0;    // 0: all steps of a call in one launch
     std::vector<std::pair<uint64_t, int32_t>> item_nodes_by_lattice;  // (lattice key, target nodes per item)
     int32_t item_nodes = 16384;
+    int32_t barrier_timeout_ms = 10000;
+    int32_t extra_arrivals = 0;       // test hook: the barrier waits for arrivals that never come
     BatchMember* d_members = nullptr;
     BatchState* d_state = nullptr;
     BatchState* h_state = nullptr;   // pinned
@@ -415,6 +418,8 @@ gpe_status enqueue_steps(gpe_batch* b, int32_t n, cudaStream_t s, const BatchMem
         A.step_base = (uint32_t)done;
         A.bar = b->d_bar;
         A.err = b->d_err;
+        A.expect = (unsigned)(grid + b->extra_arrivals);
+        A.timeout_ns = (unsigned long long)b->barrier_timeout_ms * 1000000ull;
         void* args[] = {&A};
         cudaLaunchConfig_t cfg;
         std::memset(&cfg, 0, sizeof cfg);
@@ -615,6 +620,16 @@ extern "C" gpe_status gpe_batch_set_tuning(gpe_batch* b, int32_t key, int32_t va
         b->steps_per_launch = value;
         return GPE_OK;
     }
+    if (key == GPE_BATCH_BARRIER_TIMEOUT_MS) {
+        if (value < 1) return fail(GPE_ERR_INVALID_ARG, "barrier timeout");
+        b->barrier_timeout_ms = value;
+        return GPE_OK;
+    }
+    if (key == GPE_BATCH_TEST_EXTRA_ARRIVALS) {
+        if (value < 0) return fail(GPE_ERR_INVALID_ARG, "extra arrivals");
+        b->extra_arrivals = value;
+        return GPE_OK;
+    }
     if (key == GPE_BATCH_BLOCKS_PER_SM) {
         if (value < 0) return fail(GPE_ERR_INVALID_ARG, "blocks per SM");
         b->tune_blocks_per_sm = value;
@@ -628,6 +643,8 @@ extern "C" gpe_status gpe_batch_get_tuning(const gpe_batch* b, int32_t key, int3
     if (key == GPE_BATCH_ITEM_NODES) *value = b->item_nodes;
     else if (key == GPE_BATCH_STEPS_PER_LAUNCH) *value = b->steps_per_launch;
     else if (key == GPE_BATCH_BLOCKS_PER_SM) *value = b->grid / (b->sms ? b->sms : 1);
+    else if (key == GPE_BATCH_BARRIER_TIMEOUT_MS) *value = b->barrier_timeout_ms;
+    else if (key == GPE_BATCH_TEST_EXTRA_ARRIVALS) *value = b->extra_arrivals;
     else return fail(GPE_ERR_INVALID_ARG, "unknown batch tuning key");
     return GPE_OK;
 }

@@ -144,3 +144,32 @@ def test_batch_rejects(gpu):
     finally:
         a.close()
         b2.close()
+
+
+def test_batch_barrier_timeout_is_reported(gpu):
+    """The grid barrier's bounded wait: with one arrival that never comes every
+    wait runs out after the set limit, the kernel returns, the call reports
+    GPE_ERR_TIMEOUT, and the batch steps normally afterwards."""
+    prec = capi.FP32
+    mem, ref = _pair(prec)
+    try:
+        with Batch(mem) as b:
+            b.set_tuning(capi.BATCH_BARRIER_TIMEOUT_MS, 50)
+            b.set_tuning(capi.BATCH_TEST_EXTRA_ARRIVALS, 1)
+            with pytest.raises(capi.GpeError) as e:
+                b.step(2)
+            assert e.value.status == 4  # GPE_ERR_TIMEOUT
+            b.set_tuning(capi.BATCH_TEST_EXTRA_ARRIVALS, 0)
+            for m in mem:  # the timed-out call left the members' states undefined: restart them
+                m.upload(capi.PSI_ODD, 0.2 * states.random_state(capi.buffer_shape(m.lattice, m.params), seed=5))
+            for r in ref:
+                r.upload(capi.PSI_ODD, 0.2 * states.random_state(capi.buffer_shape(r.lattice, r.params), seed=5))
+            for m, r in zip(mem, ref):
+                m.start()
+                r.start()
+            b.step(3)
+        for r in ref:
+            r.step(3)
+        _compare(mem, ref, prec)
+    finally:
+        _close(mem + ref)
