@@ -233,13 +233,22 @@ gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream);
 /* One step with explicit fields instead of the ramp: next <- prev, the
  * per-launch form of the reference loop (leapfrog<<<>>>(next, prev, ..., Bs, t),
  * Spin1GpeBCC.cu:1588).  mode: 0 leapfrog, 1 forward Euler, 2 imaginary time
- * (next = prev - dt*H prev, H prev stored in GPE_HPSI; Spin1GpeBCC.cu:554-662). */
+ * (next = prev - dt*H prev, H prev stored in GPE_HPSI; Spin1GpeBCC.cu:554-662).
+ * Hyperbolic scheme: modes 0 and 2; mode 2 is the ground-state pair itp_q +
+ * itp_psi (RelativisticSpin2Gpe.cu:558-599, 706-807; RelativisticSpin1Gpe/
+ * hyper_kernels.h:4-40, common_kernels.h:17-94): q_next = q_prev -
+ * (dt/sigma)(q_prev - d0 psi_prev), psi_next = psi_prev - dt H(psi_prev, q_prev)
+ * with B = 0 and H psi_prev stored in GPE_HPSI (get_Hpsi, :602-704).
+ * next_slot and prev_slot must differ (GPE_ERR_INVALID_ARG). */
 enum { GPE_MODE_LEAPFROG = 0, GPE_MODE_EULER = 1, GPE_MODE_ITP = 2 };
 gpe_status gpe_step_explicit(gpe_handle* h, int32_t next_slot, int32_t prev_slot,
                              const gpe_fields* fields, double t, int32_t mode, void* stream);
 
 /* Imaginary-time ground-state iterations: itp + renormalisation to norm 1, n
- * times, on PSI_EVEN (Spin1GpeBCC.cu:1470-1478; GPUGrossPitaevskii_BCC.cu:845-849).
+ * times, from the newest psi slot (Spin1GpeBCC.cu:1470-1478;
+ * GPUGrossPitaevskii_BCC.cu:845-849).  Hyperbolic scheme: each iteration is the
+ * mode-2 step of gpe_step_explicit on the (psi, q) pair, then normalize_h of the
+ * new psi (RelativisticSpin2Gpe.cu:1712-1715); q is not renormalised.
  * If mu_out != NULL it receives <psi|H psi> of the last iteration (FP64, synchronises). */
 gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* stream);
 

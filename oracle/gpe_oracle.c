@@ -287,7 +287,7 @@ int orc_parabolic_step(const gpe_lattice_desc* lat, const gpe_params* p, const g
 /* --------------------------------------------------------- q-based psi step */
 
 int orc_q_psi_step(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_fields* Bs, double t, int mode,
-                   int hyperb, double* next, const double* prev, const double* q, int threads) {
+                   int hyperb, double* next, const double* prev, const double* q, double* hpsi, int threads) {
     int st = check_args(lat, p);
     if (st) return st;
     if (lat->edges <= 0 || !lat->incidence) return GPE_ERR_UNSUPPORTED;
@@ -372,7 +372,7 @@ int orc_q_psi_step(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_f
                         }
                         local_spin2(p, B, ab, n, prv, H);
                     }
-                    write_update(&g, mode, p->dt, next, NULL, cell, l, prv, H);
+                    write_update(&g, mode, p->dt, next, hpsi, cell, l, prv, H);
                 }
             }
         }
@@ -414,6 +414,11 @@ int orc_q_step(const gpe_lattice_desc* lat, const gpe_params* p, int qmode, doub
                             cplx nq = load_c(next_q, cell, g.qcell_vals, e, C, s);
                             nq = c_add(nq, c_make(-qq.y, qq.x));
                             store_c(next_q, cell, g.qcell_vals, e, C, s, nq);
+                        } else if (qmode == ORC_Q_ITP) {
+                            /* itp_q, :589-599: q = (dt/sigma)(-d0 psi + prev_q); next_q = prev_q - q */
+                            const cplx pq = load_c(prev_q, cell, g.qcell_vals, e, C, s);
+                            const cplx qq = c_scale(dt_per_sigma, c_add(c_scale(-1.0, d0psi), pq));
+                            store_c(next_q, cell, g.qcell_vals, e, C, s, c_sub(pq, qq));
                         } else {
                             /* forwardEuler_q, :841-851 */
                             const cplx pq = load_c(prev_q, cell, g.qcell_vals, e, C, s);

@@ -31,7 +31,8 @@ enum {
 enum {
     ORC_Q_HYPER = 0,      /* next_q += i 2 (dt/sigma) (prev_q + d0 psi)       */
     ORC_Q_PARA = 1,       /* next_q  = d0 psi                                  */
-    ORC_Q_EULER_HYPER = 2 /* next_q  = prev_q + i (dt/sigma) (prev_q + d0 psi) */
+    ORC_Q_EULER_HYPER = 2, /* next_q  = prev_q + i (dt/sigma) (prev_q + d0 psi) */
+    ORC_Q_ITP = 3          /* next_q  = prev_q - (dt/sigma) (prev_q - d0 psi)  */
 };
 
 /* Parabolic step for C = 1, 3, 5 (scalar GPUGrossPitaevskii_BCC.cu:327-347;
@@ -43,14 +44,18 @@ int orc_parabolic_step(const gpe_lattice_desc* lat, const gpe_params* p, const g
 
 /* Hyperbolic / q-based psi update for C = 1, 3, 5 (update_psi and forwardEuler:
  * RelativisticGpeBCC.cu:212-255, RelativisticSpin1Gpe/common_kernels.h:95-255,
- * RelativisticSpin2Gpe.cu:859-969, 1022-1132).  hyperb selects the -c_K scaling. */
+ * RelativisticSpin2Gpe.cu:859-969, 1022-1132).  hyperb selects the -c_K scaling.
+ * mode ORC_ITP with hyperb = 0 is the imaginary-time itp_psi (B = 0; hpsi, when
+ * not NULL, receives H prev: RelativisticSpin2Gpe.cu:706-807 and get_Hpsi :602-704,
+ * RelativisticSpin1Gpe/common_kernels.h:17-94). */
 int orc_q_psi_step(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_fields* B,
                    double t, int mode, int hyperb, double* next, const double* prev,
-                   const double* q, int threads);
+                   const double* q, double* hpsi, int threads);
 
-/* Dual-edge update (update_q / forwardEuler_q / update_q_para:
- * RelativisticSpin2Gpe.cu:808-857, 971-1020; RelativisticSpin1Gpe/hyper_kernels.h:80-116,
- * para_kernels.h:4-31; RelativisticGpeBCC.cu:154-210). */
+/* Dual-edge update (update_q / forwardEuler_q / update_q_para / itp_q:
+ * RelativisticSpin2Gpe.cu:558-599, 808-857, 971-1020; RelativisticSpin1Gpe/hyper_kernels.h:4-40,
+ * 80-116, para_kernels.h:4-31; RelativisticGpeBCC.cu:154-210).  next_q may equal
+ * prev_q (each edge reads only its own prev_q). */
 int orc_q_step(const gpe_lattice_desc* lat, const gpe_params* p, int qmode,
                double* next_q, const double* prev_q, const double* psi, int threads);
 

@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD_DIR, "libgpe_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 LEAPFROG, EULER, ITP = 0, 1, 2
-Q_HYPER, Q_PARA, Q_EULER_HYPER = 0, 1, 2
+Q_HYPER, Q_PARA, Q_EULER_HYPER, Q_ITP = 0, 1, 2, 3
 
 
 def build(force: bool = False) -> str:
@@ -50,7 +50,7 @@ def lib():
         P = C.POINTER
         dp = P(C.c_double)
         L.orc_parabolic_step.argtypes = [P(capi.LatticeDesc), P(capi.Params), P(capi.Fields), C.c_double, C.c_int, dp, dp, dp, C.c_int]
-        L.orc_q_psi_step.argtypes = [P(capi.LatticeDesc), P(capi.Params), P(capi.Fields), C.c_double, C.c_int, C.c_int, dp, dp, dp, C.c_int]
+        L.orc_q_psi_step.argtypes = [P(capi.LatticeDesc), P(capi.Params), P(capi.Fields), C.c_double, C.c_int, C.c_int, dp, dp, dp, dp, C.c_int]
         L.orc_q_step.argtypes = [P(capi.LatticeDesc), P(capi.Params), C.c_int, dp, dp, dp, C.c_int]
         L.orc_normalize.argtypes = [P(capi.LatticeDesc), P(capi.Params), dp]
         L.orc_normalize.restype = C.c_double
@@ -81,8 +81,8 @@ def parabolic_step(lat, params, fields, t, mode, nxt, prev, hpsi=None, threads=0
     _check(lib().orc_parabolic_step(C.byref(lat.desc), C.byref(params), C.byref(fields), t, mode, _dp(nxt), _dp(prev), _dp(hpsi), threads), "orc_parabolic_step")
 
 
-def q_psi_step(lat, params, fields, t, mode, hyperb, nxt, prev, q, threads=0):
-    _check(lib().orc_q_psi_step(C.byref(lat.desc), C.byref(params), C.byref(fields), t, mode, int(hyperb), _dp(nxt), _dp(prev), _dp(q), threads), "orc_q_psi_step")
+def q_psi_step(lat, params, fields, t, mode, hyperb, nxt, prev, q, threads=0, hpsi=None):
+    _check(lib().orc_q_psi_step(C.byref(lat.desc), C.byref(params), C.byref(fields), t, mode, int(hyperb), _dp(nxt), _dp(prev), _dp(q), _dp(hpsi), threads), "orc_q_psi_step")
 
 
 def q_step(lat, params, qmode, next_q, prev_q, psi, threads=0):
@@ -141,6 +141,23 @@ def hyper_run(lat, params, psi_even, psi_odd, q_even, q_odd, nsteps, ramp=None, 
         else:
             q_step(lat, params, Q_PARA, qs[b], qs[b], ps[b], threads)
     return ps[nsteps % 2], qs[nsteps % 2]
+
+
+def hyper_itp_run(lat, params, psi_even, psi_odd, q_even, q_odd, niter, hpsi=None, threads=0):
+    """Imaginary-time loop of the hyperbolic scheme (RelativisticSpin2Gpe.cu:1712-1719;
+    RelativisticSpin1Gpe.cu:687-697): per iteration itp_q and itp_psi both read the
+    current (psi, q) pair and write the other one, then the new psi is renormalised.
+    Starts from the even pair; returns the newest (psi, q).  hpsi, if given, holds
+    H psi of the last iteration's input."""
+    ps = [psi_even, psi_odd]
+    qs = [q_even, q_odd]
+    f = capi.make_fields()
+    for n in range(niter):
+        a, b = n % 2, (n + 1) % 2
+        q_step(lat, params, Q_ITP, qs[b], qs[a], ps[a], threads)
+        q_psi_step(lat, params, f, 0.0, ITP, False, ps[b], ps[a], qs[a], threads, hpsi=hpsi)
+        normalize(lat, params, ps[b])
+    return ps[niter % 2], qs[niter % 2]
 
 
 def gpblocks_run(X, Y, Z, V, deg, lapind, lapfac, lapfac0, g, pot, even, odd, steps):

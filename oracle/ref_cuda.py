@@ -51,6 +51,11 @@ NAMES = {
     ("rel_spin2_bcc", "update_q"): "_Z8update_q10PitchedPtrS_S_P4int35uint3db",
     ("rel_spin1_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_PK4int2PKd9MagFields5uint3d7double3dddbd",
     ("rel_spin1_bcc", "update_q_hyper"): "_Z14update_q_hyper10PitchedPtrS_S_P4int35uint3d",
+    ("rel_spin1_bcc", "itp_q_hyper"): "_Z11itp_q_hyper10PitchedPtrS_S_P4int35uint3d",
+    ("rel_spin1_bcc", "itp_psi"): "_Z7itp_psi10PitchedPtrS_S_S_PK4int2PKd9MagFields5uint3d7double3ddd",
+    ("rel_spin2_gs", "itp_q"): "_Z5itp_q10PitchedPtrS_S_P4int35uint3d",
+    ("rel_spin2_gs", "itp_psi"): "_Z7itp_psi10PitchedPtrS_S_PK4int2PKd5uint3d7double3dddd",
+    ("rel_spin2_gs", "get_Hpsi"): "_Z8get_Hpsi10PitchedPtrS_S_PK4int2PKd5uint3d7double3ddd",
     ("rel_scalar_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_S_P4int2Pdd5uint3d",
     ("rel_scalar_bcc", "update_q"): "_Z8update_q10PitchedPtrS_S_P4int35uint3d",
     ("scalar_bcc", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3d",
@@ -98,6 +103,7 @@ class Driver:
         self.cu.cuMemAlloc_v2.argtypes = [C.POINTER(C.c_uint64), C.c_size_t]
         self.cu.cuMemFree_v2.argtypes = [C.c_uint64]
         self.cu.cuMemcpyHtoD_v2.argtypes = [C.c_uint64, C.c_void_p, C.c_size_t]
+        self.cu.cuMemcpyDtoH_v2.argtypes = [C.c_void_p, C.c_uint64, C.c_size_t]
         self.cu.cuLaunchKernel.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
                                            C.c_uint, C.c_void_p, C.POINTER(C.c_void_p), C.c_void_p]
         self.modules = {}
@@ -126,6 +132,11 @@ class Driver:
         self.allocs.append(p.value)
         self._check(self.cu.cuMemcpyHtoD_v2(p.value, a.ctypes.data, a.nbytes), "cuMemcpyHtoD")
         return p.value
+
+    def download(self, ptr: int, nbytes: int) -> np.ndarray:
+        out = np.empty(nbytes, dtype=np.uint8)
+        self._check(self.cu.cuMemcpyDtoH_v2(out.ctypes.data, ptr, nbytes), "cuMemcpyDtoH")
+        return out
 
     def launch(self, fn, grid, block, args):
         params = (C.c_void_p * len(args))(*[C.addressof(a) for a in args])
@@ -212,6 +223,17 @@ def pitched_upload(drv: Driver, host: np.ndarray, row_align: int = 256) -> Pitch
     return PitchedPtr(base + slice_pitch + pitch + cell, pitch, slice_pitch)
 
 
+def pitched_download(drv: Driver, pp: PitchedPtr, shape, dtype=np.float64) -> np.ndarray:
+    """Reads back a buffer made by pitched_upload: shape is the full
+    (Z+2, Y+2, X+2, ...) host shape."""
+    Z2, Y2, X2 = shape[:3]
+    itemsize = np.dtype(dtype).itemsize
+    cell = int(np.prod(shape[3:])) * itemsize
+    base = pp.ptr - pp.slicePitch - pp.pitch - cell
+    raw = drv.download(base, Z2 * pp.slicePitch).reshape(Z2, Y2, pp.pitch)
+    return np.ascontiguousarray(raw[:, :, : X2 * cell]).view(dtype).reshape(shape)
+
+
 def spinor_grid(params, V):
     X, Y, Z = (int(params.dims[i]) for i in range(3))
     return ((X + TB_X - 1) // TB_X, (Y + TB_Y - 1) // TB_Y, Z), (TB_X * V, TB_Y, 1)
@@ -236,5 +258,5 @@ def double3(v) -> Double3:
 
 
 __all__ = ["Driver", "available", "mag_fields", "pitched", "stencil_int4", "stencil_int2", "edge_tables",
-           "node_potential", "pitched_upload", "spinor_grid", "edge_grid", "scalar_grid", "uint3", "double3",
+           "node_potential", "pitched_upload", "pitched_download", "spinor_grid", "edge_grid", "scalar_grid", "uint3", "double3",
            "LAMBDA_Z", "TRAP_OFFSET", "QUAD_CENTER", "SPIN2_DT", "math"]

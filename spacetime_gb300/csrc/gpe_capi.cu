@@ -44,7 +44,8 @@ enum HyperKind {
     HK_PSI_PARA_ITP,
     HK_Q_PARA,
     HK_Q_EULER_HYPER,
-    HK_Q_HYPER
+    HK_Q_HYPER,
+    HK_FUSED_ITP
 };
 }  // namespace gpe
 
@@ -858,19 +859,28 @@ gpe_status gpe::step_buffers(gpe_handle* h, char* next, const char* prev, const 
     return GPE_OK;
 }
 
-// psi[next] <- psi[prev] (and q when hyperbolic), one step at time t.
+// psi[next] <- psi[prev] (and q when hyperbolic), one step at time t.  The
+// hyperbolic imaginary-time step is itp_q + itp_psi of the ground-state loop
+// (RelativisticSpin2Gpe.cu:1712-1713), both reading the (psi, q) pair of prev,
+// in one launch that also stores H psi_prev in GPE_HPSI.
 static gpe_status one_step(gpe_handle* h, int next, int prev, const gpe_fields& B, double t, int mode, cudaStream_t s) {
     if (h->p.scheme == GPE_SCHEME_PARABOLIC) return step_buffers(h, h->interior[next], h->interior[prev], B, t, mode, s);
     StepArgs a = make_args(h, B, t);
     a.prev = h->interior[prev];
     a.next = h->interior[next];
-    if (mode != GPE_MODE_LEAPFROG) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme: explicit steps are leapfrog only");
+    if (mode == GPE_MODE_EULER) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme: explicit steps are leapfrog or imaginary time");
     const int qprev = prev == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
     const int qnext = next == GPE_PSI_EVEN ? GPE_Q_EVEN : GPE_Q_ODD;
     a.q = h->interior[qprev];
     a.qnext = h->interior[qnext];
-    const uint32_t T = hyper_tile_cells(h);
-    cudaError_t e = T > 0 ? dispatch_hyper_tile(h, a, T, s) : dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
+    cudaError_t e;
+    if (mode == GPE_MODE_ITP) {
+        a.hpsi = h->interior[GPE_HPSI];
+        e = dispatch_hyper(h, a, HK_FUSED_ITP, s);
+    } else {
+        const uint32_t T = hyper_tile_cells(h);
+        e = T > 0 ? dispatch_hyper_tile(h, a, T, s) : dispatch_hyper(h, a, HK_FUSED_LEAPFROG, s);
+    }
     h->launches += 1;
     h->epoch += 1;
     if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
@@ -882,7 +892,8 @@ extern "C" gpe_status gpe_step_explicit(gpe_handle* h, int32_t next_slot, int32_
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
     if ((next_slot != GPE_PSI_EVEN && next_slot != GPE_PSI_ODD) || (prev_slot != GPE_PSI_EVEN && prev_slot != GPE_PSI_ODD))
         return fail(GPE_ERR_INVALID_ARG, "psi slots must be PSI_EVEN or PSI_ODD");
-    if (mode == GPE_MODE_LEAPFROG && next_slot == prev_slot) return fail(GPE_ERR_INVALID_ARG, "leapfrog needs two buffers");
+    // every mode reads neighbours of prev while it writes next
+    if (next_slot == prev_slot) return fail(GPE_ERR_INVALID_ARG, "next and prev must be different buffers");
     if (mode < 0 || mode > 2) return fail(GPE_ERR_INVALID_ARG, "mode");
     if (mode == GPE_MODE_ITP) {
         gpe_status st = ensure_hpsi(h);
@@ -976,7 +987,6 @@ extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_obs
 
 extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* stream) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
-    if (h->p.scheme != GPE_SCHEME_PARABOLIC) return fail(GPE_ERR_UNSUPPORTED, "imaginary time is built for the parabolic scheme");
     gpe_status st = ensure_hpsi(h);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -985,7 +995,8 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
     const double dv = cell_dv(h);
     for (int32_t k = 0; k < n; ++k) {
         const int prev = h->cur, next = h->cur == GPE_PSI_EVEN ? GPE_PSI_ODD : GPE_PSI_EVEN;
-        // itp(H psi, next <- prev) then normalize(next) (Spin1GpeBCC.cu:1470-1473)
+        // itp(H psi, next <- prev) then normalize(next) (Spin1GpeBCC.cu:1470-1473;
+        // hyperbolic: itp_q + itp_psi, normalize_h, RelativisticSpin2Gpe.cu:1712-1715)
         st = one_step(h, next, prev, zero, 0.0, GPE_MODE_ITP, s);
         if (st) return st;
         StepArgs a = make_args(h, zero, 0.0);

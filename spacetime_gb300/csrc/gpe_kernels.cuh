@@ -353,10 +353,11 @@ struct SmemHyper {
     R pos[kMaxNodes * 3];
 };
 
-// Edge (q) update of one dual edge (RelativisticSpin2Gpe.cu:986-1019, :823-856).
+// Edge (q) update of one dual edge (RelativisticSpin2Gpe.cu:986-1019, :823-856, :573-598).
 // QM: 0 hyperbolic leapfrog  next_q += i 2(dt/sigma)(prev_q + d0 psi)
 //     1 parabolic            next_q  = d0 psi
 //     2 forward Euler        next_q  = prev_q + i (dt/sigma)(prev_q + d0 psi)
+//     3 imaginary time       next_q  = prev_q - (dt/sigma)(prev_q - d0 psi)
 template <typename R, int C, int QM>
 __device__ __forceinline__ void q_update(const StepArgs& a, const SmemHyper<R>& sh, uint32_t x, uint32_t y,
                                          uint32_t z, uint32_t e) {
@@ -380,6 +381,9 @@ __device__ __forceinline__ void q_update(const StepArgs& a, const SmemHyper<R>& 
             Cx<R> v = ldc_rw<R>(qn);
             v += cx<R>(-qq.y, qq.x);
             stc<R>(qn, v);
+        } else if constexpr (QM == 3) {
+            const Cx<R> pq = ldc_rw<R>(qprev + s * 2 * sizeof(R));
+            stc<R>(qn, pq - dts * (pq - d0psi));
         } else {
             const Cx<R> pq = ldc_rw<R>(qprev + s * 2 * sizeof(R));
             const Cx<R> qq = dts * (pq + d0psi);
@@ -465,7 +469,8 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
         } else {
             local_spin2<R>(P, r, pot, MODE != GPE_MODE_ITP, false, HYPERB, prv, H);
         }
-        write_update<R, C>(MODE, P.dt, a.next + cell_off + l * node_bytes, nullptr, prv, H);
+        char* hp = (MODE == GPE_MODE_ITP && a.hpsi) ? a.hpsi + cell_off + l * node_bytes : nullptr;
+        write_update<R, C>(MODE, P.dt, a.next + cell_off + l * node_bytes, hp, prv, H);
     } else if constexpr (QM >= 0) {
         const uint32_t eb = (DO_PSI ? group * ratio : 0) + (sub - 1);
         const uint32_t i = eb * blockDim.x + threadIdx.x;
@@ -725,7 +730,8 @@ enum HyperKind {
     HK_PSI_PARA_ITP,         // psi only, parabolic, imaginary time
     HK_Q_PARA,               // q = d0 psi
     HK_Q_EULER_HYPER,        // q = q + i dt/sigma (q + d0 psi)
-    HK_Q_HYPER               // q += i 2 dt/sigma (q + d0 psi)
+    HK_Q_HYPER,              // q += i 2 dt/sigma (q + d0 psi)
+    HK_FUSED_ITP             // psi (parabolic kinetic from q, imaginary time, H psi out) + q relaxation
 };
 
 template <typename R, int C>
@@ -739,6 +745,11 @@ cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
             // every group of (1 + ratio) blocks holds one node block and `ratio` edge blocks
             const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
             hyper_step_kernel<R, C, true, GPE_MODE_LEAPFROG, true, 0><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio);
+            break;
+        }
+        case HK_FUSED_ITP: {
+            const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
+            hyper_step_kernel<R, C, true, GPE_MODE_ITP, false, 3><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio);
             break;
         }
         case HK_PSI_PARA_LEAPFROG:

@@ -5,7 +5,8 @@ tree).  For every case it uploads seeded random states into an FP64 libgpe
 handle (whose buffers have the reference's BlockPsis / BlockEdges layout), runs
 a short sequence of the reference's kernels on those buffers through
 oracle/ref_cuda.py with per-step fields and times, and stores the parameters,
-the inputs and the outputs (interior cells only).  tests/test_ref_cuda_golden.py
+the inputs and the outputs (interior cells only).  The ground-state (imaginary-time)
+kernels of the hyperbolic spin-2 program come from rel_spin2_gs.cubin.  tests/test_ref_cuda_golden.py
 replays every sequence with the oracle (CPU) and with libgpe's kernels (GPU).
 
     python tests/golden/make_ref_cuda_golden.py [outdir] [--all]
@@ -146,6 +147,59 @@ def rel_case(drv, name, lattice, dims, dt, sigma, c0, c2, c4, seed, program="rel
                 **{k: interior(v) for k, v in ins.items()}, **out)
 
 
+def itp_case(drv, name, program, C, dims, dt, sigma, c0, c2, c4, seed):
+    """NSTEPS imaginary-time steps of the hyperbolic ground-state loop without the
+    renormalisation: itp_q then itp_psi per step, both reading the previous (psi, q)
+    pair (RelativisticSpin2Gpe.cu:1712-1713 with rel_spin2_gs.cubin;
+    RelativisticSpin1Gpe.cu:687-688).  out_hpsi is H psi of the last step's input:
+    get_Hpsi on it for spin-2 (:1677), itp_psi's own H psi output for spin-1."""
+    lat = capi.Lattice("bcc")
+    p = capi.make_params(components=C, scheme=capi.SCHEME_HYPERBOLIC, precision=capi.FP64, dims=dims, block_scale=0.3,
+                         dt=dt, trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, c4=c4,
+                         sigma=sigma, lattice=lat)
+    s = Stepper(lat, p)
+    shape, qshape = capi.buffer_shape(lat, p), capi.buffer_shape(lat, p, edges=True)
+    ins = {"in_even": 0.2 * states.random_state(shape, seed=seed), "in_odd": 0.2 * states.random_state(shape, seed=seed + 1),
+           "in_qeven": 0.2 * states.random_state(qshape, seed=seed + 2),
+           "in_qodd": 0.2 * states.random_state(qshape, seed=seed + 3)}
+    s.upload(capi.PSI_EVEN, ins["in_even"])
+    s.upload(capi.PSI_ODD, ins["in_odd"])
+    s.upload(capi.Q_EVEN, ins["in_qeven"])
+    s.upload(capi.Q_ODD, ins["in_qodd"])
+    d0, d1, w = R.edge_tables(lat, s, p.block_scale)
+    d_d0, d_d1, d_w = drv.upload(d0), drv.upload(d1), drv.upload(w)
+    grid, pblock = R.spinor_grid(p, lat.nodes)
+    eblock = R.edge_grid(p, lat.edges)[1]
+    d_h = R.pitched_upload(drv, np.zeros(shape))
+    psi = [R.pitched(s, capi.PSI_EVEN), R.pitched(s, capi.PSI_ODD)]
+    q = [R.pitched(s, capi.Q_EVEN), R.pitched(s, capi.Q_ODD)]
+    geo = [R.uint3(p), R.C.c_double(p.block_scale), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2)]
+    for j in range(NSTEPS):
+        a, b = j % 2, (j + 1) % 2
+        if C == 5:
+            drv.launch(drv.function(program, "itp_q"), grid, eblock,
+                       [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(dt / sigma)])
+            drv.launch(drv.function(program, "itp_psi"), grid, pblock,
+                       [psi[b], psi[a], q[a], R.C.c_void_p(d_d1), R.C.c_void_p(d_w)] + geo +
+                       [R.C.c_double(c4), R.C.c_double(dt)])
+        else:
+            drv.launch(drv.function(program, "itp_q_hyper"), grid, eblock,
+                       [q[b], q[a], psi[a], R.C.c_void_p(d_d0), R.uint3(p), R.C.c_double(dt / sigma)])
+            drv.launch(drv.function(program, "itp_psi"), grid, pblock,
+                       [d_h, psi[b], psi[a], q[a], R.C.c_void_p(d_d1), R.C.c_void_p(d_w),
+                        R.mag_fields(capi.make_fields())] + geo + [R.C.c_double(dt)])
+    if C == 5:
+        a = (NSTEPS - 1) % 2
+        drv.launch(drv.function(program, "get_Hpsi"), grid, pblock,
+                   [d_h, psi[a], q[a], R.C.c_void_p(d_d1), R.C.c_void_p(d_w)] + geo + [R.C.c_double(c4)])
+    out = {"out_even": interior(s.download(capi.PSI_EVEN)), "out_odd": interior(s.download(capi.PSI_ODD)),
+           "out_qeven": interior(s.download(capi.Q_EVEN)), "out_qodd": interior(s.download(capi.Q_ODD)),
+           "out_hpsi": interior(R.pitched_download(drv, d_h, shape))}
+    s.close()
+    return dict(kind="itp", lattice="bcc", params=params_dict(p), fields=np.zeros((NSTEPS, 8)), times=np.zeros(NSTEPS),
+                **{k: interior(v) for k, v in ins.items()}, **out)
+
+
 def scalar_case(drv, name, program, lattice, dims, dt, g, seed):
     """NSTEPS leapfrog updates of the scalar programs.  Their update is
     next += dt_ref (-i H) (GPUGrossPitaevskii_BCC.cu:345-346); the C15/A15/FCC
@@ -200,6 +254,10 @@ CASES = [
                                          program="rel_spin1_bcc", C=3)),
     ("rel_scalar_bcc", lambda d: rel_case(d, "rel_scalar_bcc", "bcc", (5, 3, 2), 1e-4, R.REL_SCALAR_SIGMA, 150.0, 0.0,
                                           0.0, 45, program="rel_scalar_bcc", C=1)),
+    ("itp_rel_spin2_gs", lambda d: itp_case(d, "itp_rel_spin2_gs", "rel_spin2_gs", 5, (4, 3, 2), 1e-3, 0.1, 120.0, -7.0,
+                                            3.0, 91)),
+    ("itp_rel_spin1_bcc", lambda d: itp_case(d, "itp_rel_spin1_bcc", "rel_spin1_bcc", 3, (4, 3, 2), 1e-3, 0.1, 120.0,
+                                             -7.0, 0.0, 93)),
     ("scalar_bcc", lambda d: scalar_case(d, "scalar_bcc", "scalar_bcc", "bcc", (5, 3, 2), 2e-4, 150.0, 51)),
     ("scalar_c15", lambda d: scalar_case(d, "scalar_c15", "scalar_c15", "c15", (2, 2, 2), 2e-4, 150.0, 61)),
     ("scalar_a15", lambda d: scalar_case(d, "scalar_a15", "scalar_a15", "a15", (3, 2, 2), 2e-4, 150.0, 71)),
@@ -214,7 +272,7 @@ def main(outdir):
     drv = R.Driver()
     try:
         for name, fn in CASES:
-            program = name.replace("_toggles", "")
+            program = name.replace("_toggles", "").replace("itp_", "")
             if os.path.exists(os.path.join(outdir, "ref_cuda_%s.npz" % name)) and "--all" not in sys.argv:
                 continue  # keep the vectors already made
             if not R.available(program):

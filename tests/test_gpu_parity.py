@@ -248,6 +248,73 @@ def test_imaginary_time(gpu, prec):
     assert mu == pytest.approx(mu_ref, rel=1e-11 if prec == capi.FP64 else 1e-5)
 
 
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C", [("bcc", 1), ("bcc", 3), ("bcc", 5), ("c15", 5), ("cube", 3)])
+def test_hyperbolic_imaginary_time(gpu, name, C, prec):
+    """gpe_itp on a hyperbolic handle: itp_q + itp_psi in one launch, then
+    normalize_h, per iteration (RelativisticSpin2Gpe.cu:1712-1715), and H psi /
+    mu of the last iteration."""
+    lat = capi.Lattice(name)
+    dims = (4, 3, 3) if lat.nodes > 40 else (6, 5, 4)
+    p = _params(lat, C, prec, dims, dt=1e-3, scheme=capi.SCHEME_HYPERBOLIC, sigma=0.1)
+    po = states.normalize(_rand(lat, p, 81), lat, p)
+    qo = _rand(lat, p, 82, edges=True)
+    with Stepper(lat, p) as s:
+        assert s.current == capi.PSI_ODD
+        s.upload(capi.PSI_ODD, po)
+        s.upload(capi.Q_ODD, qo)
+        mu = s.itp(5)
+        assert s.current == capi.PSI_EVEN
+        got_p, got_q, got_h = s.download(capi.PSI_EVEN), s.download(capi.Q_EVEN), s.download(capi.HPSI)
+        obs = s.observe(capi.PSI_EVEN)
+    hp = np.zeros_like(po)
+    rp, rq = oracle.hyper_itp_run(lat, p, po.copy(), np.zeros_like(po), qo.copy(), np.zeros_like(qo), 5, hpsi=hp)
+    dv = p.block_scale ** 3 * lat.volume
+    mu_ref = float(np.sum(rp[1:-1, 1:-1, 1:-1] * hp[1:-1, 1:-1, 1:-1])) * dv
+    _close(got_p, rp, prec, "psi")
+    _close(got_q, rq, prec, "q")
+    _close(got_h, hp, prec, "H psi")
+    assert obs["norm"] == pytest.approx(1.0, rel=1e-10 if prec == capi.FP64 else 1e-6)
+    assert mu == pytest.approx(mu_ref, rel=1e-11 if prec == capi.FP64 else 1e-5)
+
+
+def test_hyperbolic_itp_reaches_the_parabolic_ground_state(gpu):
+    """Property at a size the oracle loop would take minutes for: the fixed point of
+    the hyperbolic imaginary-time loop has q = d0 psi and H psi = mu psi with the
+    d1 * d0 operator, which on BCC is the parabolic stencil away from the boundary;
+    with the state confined well inside the grid both loops reach the same ground
+    state (mu within 1e-8, overlap within 1e-5, q - d0 psi within 1e-5) from the
+    same start after 8000 iterations."""
+    lat = capi.Lattice("bcc")
+    kw = dict(dims=(12, 12, 12), dt=1e-3, trap_offset=0.0, trap_lambda=(2.0, 2.0, 2.0), c0=50.0)
+    pp = _params(lat, 1, capi.FP64, **kw)
+    ph = _params(lat, 1, capi.FP64, scheme=capi.SCHEME_HYPERBOLIC, sigma=0.1, **kw)
+    psi0 = np.abs(_rand(lat, pp, 7))
+    for ax in range(3):
+        idx = [slice(None)] * 3
+        for end in (0, -1):
+            idx[ax] = end
+            psi0[tuple(idx)] = 0.0
+    psi0 = states.normalize(psi0, lat, pp)
+    n = 8000
+    with Stepper(lat, pp) as s:
+        s.upload(capi.PSI_ODD, psi0)
+        s.itp(n - 1, want_mu=False)
+        mu_p = s.itp(1)
+        psi_p = s.download(s.current)
+    with Stepper(lat, ph) as s:
+        s.upload(capi.PSI_ODD, psi0)
+        s.itp(n - 1, want_mu=False)
+        mu_h = s.itp(1)
+        psi_h, q_h = s.download(s.current), s.download(capi.Q_EVEN if s.current == capi.PSI_EVEN else capi.Q_ODD)
+    dv = pp.block_scale ** 3 * lat.volume
+    assert mu_h == pytest.approx(mu_p, rel=1e-8)
+    assert float(np.sum(psi_h * psi_p)) * dv == pytest.approx(1.0, abs=1e-5)
+    d0 = np.zeros_like(q_h)
+    oracle.q_step(lat, ph, oracle.Q_PARA, d0, d0, psi_h)
+    assert float(np.max(np.abs(q_h - d0))) <= 1e-5 * float(np.max(np.abs(d0)))  # q lags psi by ~sigma/dt steps
+
+
 def test_leapfrog_run_with_ramp_matches_oracle(gpu):
     """gpe_start + gpe_step(n) with the device-side schedule of a ramp (config-2 shape:
     linear Bz ramp plus a quadrupole gradient) against the oracle time loop."""

@@ -4,7 +4,10 @@ tests/golden/ref_cuda_*.npz hold short runs of the reference's unmodified
 kernels -- spin-1 leapfrog/forwardEuler with and without loss, quadratic Zeeman
 and quadrupole offset (Spin1GpeBCC.cu:667-917), spin-2 (Spin2GpeBCC.cu:698-990),
 relativistic spin-2 update_psi + update_q (RelativisticSpin2Gpe.cu:971-1132),
-and the scalar BCC / C15 / A15 / FCC updates -- made by
+the hyperbolic imaginary-time pair itp_q + itp_psi and get_Hpsi of the spin-2 and
+spin-1 ground-state loops (RelativisticSpin2Gpe.cu:558-807;
+RelativisticSpin1Gpe/hyper_kernels.h:4-40, common_kernels.h:17-94), and the
+scalar BCC / C15 / A15 / FCC updates -- made by
 tests/golden/make_ref_cuda_golden.py on a GB300 from seeded inputs.
 
 CPU: the FP64 oracle replays each run: max |oracle - reference| <= 1e-12 * max|reference|
@@ -63,7 +66,7 @@ def _check(got, want, tol, what):
 
 
 def test_golden_files_present():
-    assert len(FILES) >= 8, "reference-kernel golden vectors missing"
+    assert len(FILES) >= 12, "reference-kernel golden vectors missing"
 
 
 @pytest.mark.parametrize("path", FILES, ids=IDS)
@@ -82,7 +85,7 @@ def test_oracle_vs_reference_cuda(path):
         bufs = [even, odd]
         for j in range(n):
             oracle.parabolic_step(lat, p, capi.make_fields(), 0.0, oracle.LEAPFROG, bufs[(j + 1) % 2], bufs[j % 2])
-    else:
+    elif d["kind"] == "hyper":
         ps = [_embed(d["in_even"]), _embed(d["in_odd"])]
         qs = [_embed(d["in_qeven"]), _embed(d["in_qodd"])]
         for j in range(n):
@@ -92,6 +95,18 @@ def test_oracle_vs_reference_cuda(path):
         even, odd = ps
         _check(qs[0], d["out_qeven"], 1e-12, "q even")
         _check(qs[1], d["out_qodd"], 1e-12, "q odd")
+    else:  # itp: itp_q + itp_psi per step, H psi of the last step's input
+        ps = [_embed(d["in_even"]), _embed(d["in_odd"])]
+        qs = [_embed(d["in_qeven"]), _embed(d["in_qodd"])]
+        hpsi = np.zeros_like(ps[0])
+        for j in range(n):
+            a, b = j % 2, (j + 1) % 2
+            oracle.q_step(lat, p, oracle.Q_ITP, qs[b], qs[a], ps[a])
+            oracle.q_psi_step(lat, p, capi.make_fields(), 0.0, oracle.ITP, False, ps[b], ps[a], qs[a], hpsi=hpsi)
+        even, odd = ps
+        _check(qs[0], d["out_qeven"], 1e-12, "q even")
+        _check(qs[1], d["out_qodd"], 1e-12, "q odd")
+        _check(hpsi, d["out_hpsi"], 1e-12, "H psi")
     _check(even, d["out_even"], 1e-12, "even")
     _check(odd, d["out_odd"], 1e-12, "odd")
 
@@ -109,11 +124,14 @@ def test_kernels_vs_reference_cuda(gpu, path, prec):
     with Stepper(lat, p) as s:
         s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
         s.upload(capi.PSI_ODD, _embed(d["in_odd"]))
-        if d["kind"] == "hyper":
+        if d["kind"] in ("hyper", "itp"):
             s.upload(capi.Q_EVEN, _embed(d["in_qeven"]))
             s.upload(capi.Q_ODD, _embed(d["in_qodd"]))
         for j in range(n):
-            if d["kind"] == "spinor":
+            if d["kind"] == "itp":
+                slots = [capi.PSI_EVEN, capi.PSI_ODD]
+                s.step_explicit(slots[(j + 1) % 2], slots[j % 2], capi.make_fields(), 0.0, capi.MODE_ITP)
+            elif d["kind"] == "spinor":
                 slots = [capi.PSI_ODD, capi.PSI_EVEN]
                 mode = capi.MODE_EULER if j == 0 else capi.MODE_LEAPFROG
                 s.step_explicit(slots[(j + 1) % 2], slots[j % 2], _fields(d["fields"][j]), float(d["times"][j]), mode)
@@ -123,6 +141,8 @@ def test_kernels_vs_reference_cuda(gpu, path, prec):
                 s.step_explicit(slots[(j + 1) % 2], slots[j % 2], f, 0.0, capi.MODE_LEAPFROG)
         _check(s.download(capi.PSI_EVEN), d["out_even"], tol, "even")
         _check(s.download(capi.PSI_ODD), d["out_odd"], tol, "odd")
-        if d["kind"] == "hyper":
+        if d["kind"] in ("hyper", "itp"):
             _check(s.download(capi.Q_EVEN), d["out_qeven"], tol, "q even")
             _check(s.download(capi.Q_ODD), d["out_qodd"], tol, "q odd")
+        if d["kind"] == "itp":
+            _check(s.download(capi.HPSI), d["out_hpsi"], tol, "H psi")
