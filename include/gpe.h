@@ -94,7 +94,13 @@ void gpe_lattice_destroy(gpe_lattice* lat);
 
 /* ----------------------------------------------------------------- physics */
 
-enum { GPE_SCHEME_PARABOLIC = 0, GPE_SCHEME_HYPERBOLIC = 1 };
+/* PARABOLIC: node stencil, leapfrog (Spin1GpeBCC.cu, Spin2GpeBCC.cu, GrossPitaevskiiGpu*).
+ * HYPERBOLIC: psi + dual-edge q, leapfrog (Relativistic{GpeBCC,Spin1Gpe,Spin2Gpe}).
+ * SPLIT: scalar psi = R + iI and q = q_R + i q_I with R and I staggered by half a
+ * step (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:90-155, loop :477-482); C = 1,
+ * state in PSI_EVEN / Q_EVEN (the real part holds R, the imaginary part I); gpe_start
+ * is the loop's q_R initialisation (:469), gpe_step two launches per step. */
+enum { GPE_SCHEME_PARABOLIC = 0, GPE_SCHEME_HYPERBOLIC = 1, GPE_SCHEME_SPLIT = 2 };
 enum { GPE_FP32 = 0, GPE_FP64 = 1 };
 enum {
     GPE_FLAG_THREE_BODY_LOSS = 1,     /* -i alpha rho^2 (Spin1GpeBCC.cu:877-880) */

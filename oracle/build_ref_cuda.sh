@@ -42,6 +42,7 @@ build RelativisticSpin2Gpe/RelativisticSpin2Gpe rel_spin2_bcc &
 build_gs RelativisticSpin2Gpe/RelativisticSpin2Gpe rel_spin2_gs &
 build RelativisticSpin1Gpe/RelativisticSpin1Gpe rel_spin1_bcc &
 build RelativisticGpeBCC/RelativisticGpeBCC rel_scalar_bcc &
+build RelativisticGpeC15/GPUGrossPitaevskii_C15 rel_scalar_c15 &
 build GrossPitaevskiiGpuBcc/GPUGrossPitaevskii_BCC scalar_bcc &
 build GrossPitaevskiiGpuC15/GPUGrossPitaevskii_C15 scalar_c15 &
 build GrossPitaevskiiGpuA15/GPUGrossPitaevskii_A15 scalar_a15 &

@@ -433,6 +433,76 @@ int orc_q_step(const gpe_lattice_desc* lat, const gpe_params* p, int qmode, doub
     return GPE_OK;
 }
 
+/* ------------------------------------------------------- split scheme (C15) */
+
+/* RelativisticGpeC15/GPUGrossPitaevskii_C15.cu: psi = R + iI, q = q_R + i q_I stored
+ * as complex pairs.  The reference folds dt into the potential, g and the Hodge
+ * weights (:282-286) and updates next += sign ((pot + g (prev^2 + next^2)) prev - d1q)
+ * (update_psi :116-155) and next_q += sign dts (prev_q + d0 psi) (update_q :90-114);
+ * the time loop (:477-482) is part 0 = (I, q_I) from (R, q_R) with sign -1 / +1 and
+ * part 1 = (R, q_R) from (I, q_I) with sign +1 / -1; part 2 is the start (:469),
+ * q_R += c (q_R + d0 R) with c = dts / (dt - dts). */
+int orc_split_step(const gpe_lattice_desc* lat, const gpe_params* p, int part, double* psi, double* q, int threads) {
+    int st = check_args(lat, p);
+    if (st) return st;
+    if (p->components != 1 || lat->edges <= 0 || !lat->incidence || !lat->edge_table) return GPE_ERR_UNSUPPORTED;
+    if (part < 0 || part > 2) return GPE_ERR_INVALID_ARG;
+    const geom g = make_geom(lat, p);
+    const int F = lat->faces_per_node;
+    const double dt = p->dt;
+    const double dts = p->dt / p->sigma;
+    const double bs2 = p->block_scale * p->block_scale;
+    const double gdt = p->c0 * dt;
+    const int rd = part == 1 ? 1 : 0; /* the half read: 0 = R / q_R, 1 = I / q_I */
+    const int wr = 1 - rd;
+    const int nt = nthreads(threads);
+    (void)nt;
+    if (part != 2) {
+        const double sign = part == 0 ? -1.0 : 1.0;
+#pragma omp parallel for schedule(static) num_threads(nt)
+        for (int z = 0; z < g.Z; ++z)
+            for (int y = 0; y < g.Y; ++y)
+                for (int x = 0; x < g.X; ++x) {
+                    const size_t cell = cell_index(&g, x, y, z);
+                    for (int l = 0; l < g.V; ++l) {
+                        double* own = psi + cell * g.cell_vals + 2 * l;
+                        double d1q = 0;
+                        for (int k = 0; k < F; ++k) {
+                            const gpe_incidence* e = &lat->incidence[l * F + k];
+                            const size_t qcell = cell_index(&g, x + e->dx, y + e->dy, z + e->dz);
+                            const double hodge = -0.5 * e->hodge / bs2 * dt;
+                            d1q += hodge * q[qcell * g.qcell_vals + 2 * e->edge + rd];
+                        }
+                        double r[3];
+                        node_pos(lat, p, x, y, z, l, r);
+                        const double pot = trap(p, r, 0.0) * dt;
+                        const double prev = own[rd];
+                        double next = own[wr];
+                        const double normsq = prev * prev + next * next;
+                        next += sign * ((pot + gdt * normsq) * prev - d1q);
+                        own[wr] = next;
+                    }
+                }
+    }
+    const double qsign = part == 1 ? -1.0 : 1.0;
+    const double coef = part == 2 ? dts / (dt - dts) : dts;
+    const int qwr = part == 2 ? 0 : wr;
+#pragma omp parallel for schedule(static) num_threads(nt)
+    for (int z = 0; z < g.Z; ++z)
+        for (int y = 0; y < g.Y; ++y)
+            for (int x = 0; x < g.X; ++x) {
+                const size_t cell = cell_index(&g, x, y, z);
+                for (int e = 0; e < g.E; ++e) {
+                    const gpe_edge* d0 = &lat->edge_table[e];
+                    const size_t ocell = cell_index(&g, x + d0->dx, y + d0->dy, z + d0->dz);
+                    const double d0psi = psi[ocell * g.cell_vals + 2 * d0->to + rd] - psi[cell * g.cell_vals + 2 * d0->from + rd];
+                    double* qv = q + cell * g.qcell_vals + 2 * e;
+                    qv[qwr] += qsign * coef * (qv[rd] + d0psi);
+                }
+            }
+    return GPE_OK;
+}
+
 /* ------------------------------------------------------------ reductions */
 
 static double cell_volume(const gpe_lattice_desc* lat, const gpe_params* p) {

@@ -59,6 +59,13 @@ int orc_q_psi_step(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_f
 int orc_q_step(const gpe_lattice_desc* lat, const gpe_params* p, int qmode,
                double* next_q, const double* prev_q, const double* psi, int threads);
 
+/* Real/imaginary split scalar scheme (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:
+ * 90-155, 469, 477-482) on complex-pair buffers psi = R + iI, q = q_R + i q_I, in
+ * place.  part 0: I and q_I from R and q_R; part 1: R and q_R from I and q_I; part 2:
+ * the start q_R += c (q_R + d0 R), c = (dt/sigma) / (dt - dt/sigma). */
+int orc_split_step(const gpe_lattice_desc* lat, const gpe_params* p, int part, double* psi, double* q,
+                   int threads);
+
 /* Renormalise psi to unit norm, sum |psi|^2 dv = 1 (density + integrate + normalize,
  * Spin1GpeBCC.cu:191-211, 328-348, 412-434).  Returns the norm before scaling. */
 double orc_normalize(const gpe_lattice_desc* lat, const gpe_params* p, double* psi);

@@ -57,6 +57,8 @@ def lib():
         L.orc_observe.argtypes = [P(capi.LatticeDesc), P(capi.Params), P(capi.Fields), C.c_double, dp, P(capi.Observables)]
         L.orc_ramp_eval.argtypes = [P(capi.Ramp), C.c_double, P(capi.Fields)]
         L.orc_ramp_eval.restype = None
+        L.orc_split_step.argtypes = [P(capi.LatticeDesc), P(capi.Params), C.c_int, dp, dp, C.c_int]
+        L.orc_split_step.restype = C.c_int
         L.orc_gpblocks_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int64), C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
         L.orc_gpblocks_run.restype = None
         L.orc_gpblocks_norm.argtypes = [C.c_size_t, C.c_size_t, dp, dp, C.c_double, dp]
@@ -141,6 +143,21 @@ def hyper_run(lat, params, psi_even, psi_odd, q_even, q_odd, nsteps, ramp=None, 
         else:
             q_step(lat, params, Q_PARA, qs[b], qs[b], ps[b], threads)
     return ps[nsteps % 2], qs[nsteps % 2]
+
+
+def split_step(lat, params, part, psi, q, threads=0):
+    _check(lib().orc_split_step(C.byref(lat.desc), C.byref(params), part, _dp(psi), _dp(q), threads), "orc_split_step")
+
+
+def split_run(lat, params, psi, q, nsteps, start=True, threads=0):
+    """Time loop of the real/imaginary split scheme (RelativisticGpeC15/
+    GPUGrossPitaevskii_C15.cu:469-482): the q_R start, then per step the I half
+    and the R half, in place on psi = R + iI and q = q_R + i q_I."""
+    if start:
+        split_step(lat, params, 2, psi, q, threads)
+    for _ in range(nsteps):
+        split_step(lat, params, 0, psi, q, threads)
+        split_step(lat, params, 1, psi, q, threads)
 
 
 def hyper_itp_run(lat, params, psi_even, psi_odd, q_even, q_odd, niter, hpsi=None, threads=0):

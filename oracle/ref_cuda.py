@@ -58,6 +58,8 @@ NAMES = {
     ("rel_spin2_gs", "get_Hpsi"): "_Z8get_Hpsi10PitchedPtrS_S_PK4int2PKd5uint3d7double3ddd",
     ("rel_scalar_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_S_P4int2Pdd5uint3d",
     ("rel_scalar_bcc", "update_q"): "_Z8update_q10PitchedPtrS_S_P4int35uint3d",
+    ("rel_scalar_c15", "update_psi"): "_Z10update_psi10PitchedPtrS_S_S_P4int2Pdd5uint3d",
+    ("rel_scalar_c15", "update_q"): "_Z8update_q10PitchedPtrS_S_P4int35uint3dd",
     ("scalar_bcc", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3d",
     ("scalar_c15", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3",
     ("scalar_a15", "update"): "_Z6update10PitchedPtrS_S_P4int2Pdd5uint3",
@@ -187,10 +189,17 @@ def edge_tables(lat, stepper, bs) -> tuple:
     host-scaled incidence weights -0.5 * h / bs^2 (RelativisticSpin2Gpe.cu:1399)."""
     pp, cb = stepper.buffer(0)
     qp, qcb = stepper.buffer(2)
-    d0 = np.array([[int(f), cell_offset(dx, dy, dz, cb, pp.pitch, pp.slice_pitch), int(t)]
+    return edge_tables_for(lat, bs, (cb, pp.pitch, pp.slice_pitch), (qcb, qp.pitch, qp.slice_pitch))
+
+
+def edge_tables_for(lat, bs, psi_geom, q_geom) -> tuple:
+    """edge_tables for buffers of the given (cell bytes, pitch, slice pitch)."""
+    cb, pitch, slice_pitch = psi_geom
+    qcb, qpitch, qslice = q_geom
+    d0 = np.array([[int(f), cell_offset(dx, dy, dz, cb, pitch, slice_pitch), int(t)]
                    for f, dx, dy, dz, t in lat.data["edges"]], dtype=np.int32)  # rows (from, dx, dy, dz, to)
     inc = lat.data["incidence"]  # rows (dx, dy, dz, edge, hodge)
-    d1 = np.array([[cell_offset(dx, dy, dz, qcb, qp.pitch, qp.slice_pitch), int(e)] for dx, dy, dz, e, _ in inc],
+    d1 = np.array([[cell_offset(dx, dy, dz, qcb, qpitch, qslice), int(e)] for dx, dy, dz, e, _ in inc],
                   dtype=np.int32)
     w = np.array([-0.5 * float(h) / (bs * bs) for *_, h in inc])
     return d0, d1, w
@@ -258,5 +267,5 @@ def double3(v) -> Double3:
 
 
 __all__ = ["Driver", "available", "mag_fields", "pitched", "stencil_int4", "stencil_int2", "edge_tables",
-           "node_potential", "pitched_upload", "pitched_download", "spinor_grid", "edge_grid", "scalar_grid", "uint3", "double3",
+           "edge_tables_for", "node_potential", "pitched_upload", "pitched_download", "spinor_grid", "edge_grid", "scalar_grid", "uint3", "double3",
            "LAMBDA_Z", "TRAP_OFFSET", "QUAD_CENTER", "SPIN2_DT", "math"]

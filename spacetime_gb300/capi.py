@@ -28,7 +28,7 @@ STATUS_NAMES = {
     7: "GPE_ERR_NO_DEVICE",
 }
 
-SCHEME_PARABOLIC, SCHEME_HYPERBOLIC = 0, 1
+SCHEME_PARABOLIC, SCHEME_HYPERBOLIC, SCHEME_SPLIT = 0, 1, 2
 FP32, FP64 = 0, 1
 FLAG_THREE_BODY_LOSS, FLAG_QUADRATIC_ZEEMAN, FLAG_QUADRUPOLE_OFFSET, FLAG_TRAP_OFF_AFTER = 1, 2, 4, 8
 RAMP_CONSTANT, RAMP_LINEAR, RAMP_SQRT = 0, 1, 2

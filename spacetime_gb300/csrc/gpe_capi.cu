@@ -34,6 +34,8 @@ cudaError_t launch_leapfrog_rows(const StepArgs& a, uint32_t T, uint32_t RY, uin
                                  const int32_t* blk, uint32_t threads, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s);
+template <typename R>
+cudaError_t launch_split(const StepArgs& a, int part, double qinit, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads, cudaStream_t s);
 enum HyperKind {
@@ -287,11 +289,14 @@ extern "C" gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* p, gp
     if (p->components != 1 && p->components != 3 && p->components != 5)
         return fail(GPE_ERR_INVALID_ARG, "components must be 1, 3 or 5");
     if (p->precision != GPE_FP32 && p->precision != GPE_FP64) return fail(GPE_ERR_INVALID_ARG, "precision");
-    if (p->scheme != GPE_SCHEME_PARABOLIC && p->scheme != GPE_SCHEME_HYPERBOLIC) return fail(GPE_ERR_INVALID_ARG, "scheme");
+    if (p->scheme != GPE_SCHEME_PARABOLIC && p->scheme != GPE_SCHEME_HYPERBOLIC && p->scheme != GPE_SCHEME_SPLIT)
+        return fail(GPE_ERR_INVALID_ARG, "scheme");
     if (p->dims[0] == 0 || p->dims[1] == 0 || p->dims[2] == 0) return fail(GPE_ERR_INVALID_ARG, "empty grid");
     if (!(p->block_scale > 0) || !std::isfinite(p->dt)) return fail(GPE_ERR_INVALID_ARG, "block_scale/dt");
     if (p->scheme == GPE_SCHEME_HYPERBOLIC && (lat->E == 0 || !(p->sigma > 0)))
         return fail(GPE_ERR_UNSUPPORTED, "hyperbolic scheme needs edge tables and sigma > 0");
+    if (p->scheme == GPE_SCHEME_SPLIT && (lat->E == 0 || !(p->sigma > 0) || p->components != 1))
+        return fail(GPE_ERR_UNSUPPORTED, "split scheme needs C = 1, edge tables and sigma > 0");
     if (p->components == 5 && (p->flags & GPE_FLAG_QUADRATIC_ZEEMAN))
         return fail(GPE_ERR_UNSUPPORTED, "quadratic Zeeman is not built for spin-2");
     const uint64_t sites = (uint64_t)p->dims[0] * p->dims[1] * p->dims[2] * (uint64_t)lat->V;
@@ -320,7 +325,7 @@ extern "C" gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* p, gp
     g.qpitch = g.E ? round_up((size_t)(g.X + 2) * g.qcell_bytes, 256) : 0;
     g.qslice = g.qpitch * (g.Y + 2);
 
-    const bool hyper = p->scheme == GPE_SCHEME_HYPERBOLIC;
+    const bool hyper = p->scheme != GPE_SCHEME_PARABOLIC;  // q buffers
     for (int slot = 0; slot < 5; ++slot) {
         const bool is_q = slot == GPE_Q_EVEN || slot == GPE_Q_ODD;
         if (is_q && !hyper) continue;
@@ -357,7 +362,9 @@ extern "C" gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* p, gp
         delete h;
         return cuda_fail(e, "gpe_create");
     }
-    h->cur = GPE_PSI_ODD;  // the reference loads the initial state into the odd buffer (Spin1GpeBCC.cu:1236)
+    // the reference loads the initial state into the odd buffer (Spin1GpeBCC.cu:1236);
+    // the split scheme keeps R + iI in PSI_EVEN and q_R + i q_I in Q_EVEN
+    h->cur = p->scheme == GPE_SCHEME_SPLIT ? GPE_PSI_EVEN : GPE_PSI_ODD;
     *out = h;
     return GPE_OK;
 }
@@ -568,6 +575,21 @@ static cudaError_t dispatch_hyper(const gpe_handle* h, const StepArgs& a, int ki
         default: return dispatch_hyper_c<5>(h, a, kind, s);
     }
 }
+// One launch of the split scheme on PSI_EVEN / Q_EVEN (part 0, 1: half-steps; 2: start).
+static gpe_status split_launch(gpe_handle* h, int part, double t, cudaStream_t s) {
+    gpe_fields zero;
+    std::memset(&zero, 0, sizeof zero);
+    StepArgs a = make_args(h, zero, t);
+    a.prev = a.next = h->interior[GPE_PSI_EVEN];
+    a.q = a.qnext = h->interior[GPE_Q_EVEN];
+    const double dts = h->p.dt / h->p.sigma;
+    const double qinit = dts / (h->p.dt - dts);
+    cudaError_t e = h->real_bytes == 8 ? launch_split<double>(a, part, qinit, s) : launch_split<float>(a, part, qinit, s);
+    h->launches += 1;
+    if (e != cudaSuccess) return cuda_fail(e, "split-scheme launch");
+    return GPE_OK;
+}
+
 template <int C>
 static cudaError_t dispatch_observe_c(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
     return h->real_bytes == 8 ? launch_observe<double, C>(a, out, false, s)
@@ -895,6 +917,7 @@ extern "C" gpe_status gpe_step_explicit(gpe_handle* h, int32_t next_slot, int32_
     // every mode reads neighbours of prev while it writes next
     if (next_slot == prev_slot) return fail(GPE_ERR_INVALID_ARG, "next and prev must be different buffers");
     if (mode < 0 || mode > 2) return fail(GPE_ERR_INVALID_ARG, "mode");
+    if (h->p.scheme == GPE_SCHEME_SPLIT) return fail(GPE_ERR_UNSUPPORTED, "the split scheme steps in place: use gpe_step");
     if (mode == GPE_MODE_ITP) {
         gpe_status st = ensure_hpsi(h);
         if (st) return st;
@@ -910,7 +933,13 @@ extern "C" gpe_status gpe_start(gpe_handle* h, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const double t = h->t0;
     const gpe_fields B = fields_at(h, t);
-    if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
+    if (h->p.scheme == GPE_SCHEME_SPLIT) {
+        // q_R += c (q_R + d0 R), c = (dt/sigma) / (dt - dt/sigma)
+        // (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:469)
+        gpe_status st = split_launch(h, 2, t, s);
+        if (st) return st;
+        h->epoch += 1;
+    } else if (h->p.scheme == GPE_SCHEME_PARABOLIC) {
         // forwardEuler(even <- odd) at t0 (Spin1GpeBCC.cu:1428-1433)
         gpe_status st = one_step(h, GPE_PSI_EVEN, GPE_PSI_ODD, B, t, GPE_MODE_EULER, s);
         if (st) return st;
@@ -941,6 +970,19 @@ extern "C" gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
     if (n < 0) return fail(GPE_ERR_INVALID_ARG, "negative step count");
     cudaStream_t s = (cudaStream_t)stream;
+    if (h->p.scheme == GPE_SCHEME_SPLIT) {
+        // update_psi(I) + update_q(q_I), then update_psi(R) + update_q(q_R)
+        // (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:477-482), one launch each
+        for (int32_t k = 0; k < n; ++k) {
+            const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
+            gpe_status st = split_launch(h, 0, t, s);
+            if (!st) st = split_launch(h, 1, t, s);
+            if (st) return st;
+            h->epoch += 1;
+            h->nstep++;
+        }
+        return GPE_OK;
+    }
     for (int32_t k = 0; k < n; ++k) {
         const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
         const gpe_fields B = fields_at(h, t);
@@ -987,6 +1029,7 @@ extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_obs
 
 extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* stream) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (h->p.scheme == GPE_SCHEME_SPLIT) return fail(GPE_ERR_UNSUPPORTED, "imaginary time is not built for the split scheme");
     gpe_status st = ensure_hpsi(h);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1106,6 +1149,7 @@ extern "C" uint64_t gpe_sites(const gpe_handle* h) {
 // is saved before and restored after the trials.
 extern "C" gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, size_t report_len, void* stream) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (h->p.scheme == GPE_SCHEME_SPLIT) return fail(GPE_ERR_UNSUPPORTED, "the split scheme has one kernel: nothing to tune");
     if (steps <= 0) steps = 10;
     cudaStream_t s = (cudaStream_t)stream;
     struct Cand {
@@ -1129,15 +1173,18 @@ extern "C" gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, s
     }
     const int saved_k = h->tune_kernel, saved_t = h->tune_tile, saved_r = h->tune_rows, saved_z = h->tune_zchunk,
               saved_th = h->tune_threads;
-    // save the two psi buffers
-    const size_t bytes = h->alloc_bytes[GPE_PSI_EVEN];
-    void* save[2] = {nullptr, nullptr};
-    if (cudaMalloc(&save[0], bytes) != cudaSuccess || cudaMalloc(&save[1], bytes) != cudaSuccess) {
-        if (save[0]) cudaFree(save[0]);
-        return fail(GPE_ERR_OOM, "cudaMalloc (autotune save)");
+    // save the state buffers the trial steps overwrite: psi even/odd and, for the
+    // hyperbolic scheme, q even/odd
+    void* save[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int slot = GPE_PSI_EVEN; slot <= GPE_Q_ODD; ++slot) {
+        if (!h->alloc[slot]) continue;
+        if (cudaMalloc(&save[slot], h->alloc_bytes[slot]) != cudaSuccess) {
+            for (void* p : save)
+                if (p) cudaFree(p);
+            return fail(GPE_ERR_OOM, "cudaMalloc (autotune save)");
+        }
+        CUDA_TRY(cudaMemcpyAsync(save[slot], h->alloc[slot], h->alloc_bytes[slot], cudaMemcpyDeviceToDevice, s));
     }
-    CUDA_TRY(cudaMemcpyAsync(save[0], h->alloc[GPE_PSI_EVEN], bytes, cudaMemcpyDeviceToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(save[1], h->alloc[GPE_PSI_ODD], bytes, cudaMemcpyDeviceToDevice, s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1185,11 +1232,12 @@ extern "C" gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, s
     h->tune_rows = best.rows;
     h->tune_zchunk = best.zchunk;
     h->tune_threads = best.threads;
-    CUDA_TRY(cudaMemcpyAsync(h->alloc[GPE_PSI_EVEN], save[0], bytes, cudaMemcpyDeviceToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(h->alloc[GPE_PSI_ODD], save[1], bytes, cudaMemcpyDeviceToDevice, s));
+    for (int slot = GPE_PSI_EVEN; slot <= GPE_Q_ODD; ++slot)
+        if (save[slot])
+            CUDA_TRY(cudaMemcpyAsync(h->alloc[slot], save[slot], h->alloc_bytes[slot], cudaMemcpyDeviceToDevice, s));
     CUDA_TRY(cudaStreamSynchronize(s));
-    cudaFree(save[0]);
-    cudaFree(save[1]);
+    for (void* p : save)
+        if (p) cudaFree(p);
     if (report && report_len) {
         std::snprintf(report, report_len, "%s", rep.c_str());
     }

@@ -15,6 +15,8 @@ GPE_INSTANTIATE_INIT(float, 1)
 GPE_INSTANTIATE_INIT(double, 1)
 GPE_INSTANTIATE_HYPER_TILE(float, 1)
 GPE_INSTANTIATE_HYPER_TILE(double, 1)
+template cudaError_t launch_split<float>(const StepArgs&, int, double, cudaStream_t);
+template cudaError_t launch_split<double>(const StepArgs&, int, double, cudaStream_t);
 
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s) {
     if (precision == GPE_FP64) {

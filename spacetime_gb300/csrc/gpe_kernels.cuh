@@ -773,6 +773,114 @@ cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// Real/imaginary split scalar scheme on the dual edges (RelativisticGpeC15/
+// GPUGrossPitaevskii_C15.cu:90-155, time loop :477-482).  psi = R + iI and q = q_R +
+// i q_I are the two halves of one complex value (R and I staggered by half a step);
+// a.next is the psi buffer and a.qnext the q buffer, both updated in place.
+//   PART 0 (first half of a step):  I   -= dt [(V + g(R^2 + I^2)) R - sum_f w_f q_R],
+//                                   q_I += (dt/sigma)(q_R + d0 R)
+//   PART 1 (second half):           R   += dt [(V + g(I^2 + R^2)) I - sum_f w_f q_I],
+//                                   q_R -= (dt/sigma)(q_I + d0 I)
+//   PART 2 (start, :469):           q_R += c (q_R + d0 R),  c = qinit
+// with w_f = -0.5 h_f / bs^2 (the reference folds dt into V, g and the Hodge weights).
+// A half-step reads one half of every value and writes the other (a node also reads
+// the half it writes, of its own value only), so the node and edge updates of a
+// half-step share one launch, laid out in groups of 1 + E/V blocks as the hyperbolic
+// step is.  Plain loads: lines read here are written by the same launch.
+template <typename R, int PART>
+__global__ void __launch_bounds__(256) split_step_kernel(StepArgs a, uint32_t node_items, uint32_t edge_items,
+                                                         uint32_t ratio, R qinit) {
+    __shared__ SmemHyper<R> sh;
+    const int V = a.g.V, E = a.g.E, F = a.tab.faces;
+    for (int i = threadIdx.x; i < V * F; i += blockDim.x) {
+        sh.inc_off[i] = a.tab.inc_off[i];
+        if constexpr (sizeof(R) == 4) sh.inc_w[i] = a.tab.inc_w32[i];
+        else sh.inc_w[i] = a.tab.inc_w64[i];
+    }
+    for (int i = threadIdx.x; i < E; i += blockDim.x) {
+        sh.e_from[i] = a.tab.e_from_off[i];
+        sh.e_to[i] = a.tab.e_to_off[i];
+    }
+    for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
+        if constexpr (sizeof(R) == 4) sh.pos[i] = a.tab.pos32[i];
+        else sh.pos[i] = a.tab.pos64[i];
+    }
+    __syncthreads();
+    constexpr bool kNodes = PART != 2;
+    uint32_t group, sub;
+    if (kNodes) {
+        group = blockIdx.x / (1 + ratio);
+        sub = blockIdx.x - group * (1 + ratio);
+    } else {
+        group = 0;
+        sub = 1 + blockIdx.x;
+    }
+    const PhysR<R>& P = make_phys<R>(a);
+    // the half read by the psi update and by d0 (R for PARTs 0 and 2, I for PART 1)
+    constexpr uint32_t rd = PART == 1 ? sizeof(R) : 0;
+    constexpr uint32_t wr = sizeof(R) - rd;
+    if (kNodes && sub == 0) {
+        const uint32_t i = group * blockDim.x + threadIdx.x;
+        if (i >= node_items) return;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+        const size_t qcell_off = (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x * a.g.qcell_bytes;
+        char* own = a.next + cell_off + l * 2 * sizeof(R);
+        const Cx<R> v = ldc_rw<R>(own);
+        const char* qb = a.qnext + qcell_off + rd;
+        R d1q = (R)0;
+        for (int k = 0; k < F; ++k) d1q += sh.inc_w[l * F + k] * *reinterpret_cast<const R*>(qb + sh.inc_off[l * F + k]);
+        R r[3];
+        r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + sh.pos[3 * l + 0]);
+        r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + sh.pos[3 * l + 1]);
+        r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + sh.pos[3 * l + 2]);
+        const R tp = trap<R>(P, r) + P.c0 * (v.x * v.x + v.y * v.y);
+        if constexpr (PART == 0) *reinterpret_cast<R*>(own + wr) = v.y - P.dt * (tp * v.x - d1q);
+        else *reinterpret_cast<R*>(own + wr) = v.x + P.dt * (tp * v.y - d1q);
+    } else {
+        const uint32_t eb = (kNodes ? group * ratio : 0) + (sub - 1);
+        const uint32_t i = eb * blockDim.x + threadIdx.x;
+        if (i >= edge_items) return;
+        const uint32_t row = fdiv(i, a.divRowE);
+        const uint32_t within = i - row * a.row_items_e;
+        const uint32_t x = fdiv(within, a.divE);
+        const uint32_t e = within - x * E;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
+        const size_t qcell_off = (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x * a.g.qcell_bytes;
+        const char* pb = a.next + cell_off + rd;
+        const R d0 = *reinterpret_cast<const R*>(pb + sh.e_to[e]) - *reinterpret_cast<const R*>(pb + sh.e_from[e]);
+        char* qe = a.qnext + qcell_off + e * 2 * sizeof(R);
+        const R qr = *reinterpret_cast<const R*>(qe + rd);
+        if constexpr (PART == 0) *reinterpret_cast<R*>(qe + wr) += P.dts * (qr + d0);
+        else if constexpr (PART == 1) *reinterpret_cast<R*>(qe + wr) -= P.dts * (qr + d0);
+        else *reinterpret_cast<R*>(qe) = qr + qinit * (qr + d0);
+    }
+}
+
+// part: 0/1 the two half-steps, 2 the start; qinit is PART 2's coefficient.
+template <typename R>
+cudaError_t launch_split(const StepArgs& a, int part, double qinit, cudaStream_t s) {
+    const uint32_t nn = (uint32_t)((uint64_t)a.g.X * a.g.Y * a.g.Z * a.g.V);
+    const uint32_t ne = (uint32_t)((uint64_t)a.g.X * a.g.Y * a.g.Z * a.g.E);
+    const uint32_t ratio = a.g.V ? (a.g.E + a.g.V - 1) / a.g.V : 1;
+    const unsigned nbn = nblocks(nn, 256), nbe = nblocks(ne, 256);
+    const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
+    if (nn == 0) return cudaSuccess;
+    switch (part) {
+        case 0: split_step_kernel<R, 0><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio, (R)0); break;
+        case 1: split_step_kernel<R, 1><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio, (R)0); break;
+        default: split_step_kernel<R, 2><<<nbe, 256, 0, s>>>(a, nn, ne, ratio, (R)qinit); break;
+    }
+    return cudaGetLastError();
+}
+
 // node_fp32: per-node terms in FP32 (FP32 storage only); sums are FP64 either way.
 template <typename R, int C>
 cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaStream_t s) {

@@ -200,6 +200,55 @@ def itp_case(drv, name, program, C, dims, dt, sigma, c0, c2, c4, seed):
                 **{k: interior(v) for k, v in ins.items()}, **out)
 
 
+def split_case(drv, name, dims, dt, sigma, g, seed, program="rel_scalar_c15"):
+    """The C15 real/imaginary split program: its q_R start, then NSTEPS steps of
+    update_psi(I) + update_q(q_I) + update_psi(R) + update_q(q_R)
+    (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:469-482) on separate R, I, q_R,
+    q_I arrays, with dt folded into the potential, g and the Hodge weights as the
+    program does (:282-286).  The potential array holds the trap values libgpe
+    computes (lambda = 1, no offset: potentialV3).  Stored as complex pairs
+    psi = R + iI, q = q_R + i q_I, libgpe's split-scheme layout."""
+    lat = capi.Lattice("c15")
+    p = capi.make_params(components=1, scheme=capi.SCHEME_SPLIT, precision=capi.FP64, dims=dims, block_scale=0.3,
+                         dt=dt, trap_lambda=(1.0, 1.0, 1.0), trap_offset=0.0, c0=g, sigma=sigma, lattice=lat)
+    shape, qshape = capi.buffer_shape(lat, p), capi.buffer_shape(lat, p, edges=True)
+    psi = 0.2 * states.random_state(shape, seed=seed)
+    q = 0.2 * states.random_state(qshape, seed=seed + 2)
+    parts = [np.ascontiguousarray(psi[..., 0, 0]), np.ascontiguousarray(psi[..., 0, 1]),
+             np.ascontiguousarray(q[..., 0, 0]), np.ascontiguousarray(q[..., 0, 1])]
+    dR, dI, dqR, dqI = (R.pitched_upload(drv, a) for a in parts)
+    d_pot = R.pitched_upload(drv, R.node_potential(lat, p) * dt)
+    V, E = lat.nodes, lat.edges
+    d0, d1, w = R.edge_tables_for(lat, p.block_scale, (V * 8, dR.pitch, dR.slicePitch), (E * 8, dqR.pitch, dqR.slicePitch))
+    d_d0, d_d1, d_w = drv.upload(d0), drv.upload(d1), drv.upload(w * dt)
+    grid, block = R.scalar_grid(p, V)
+    egrid, eblock = R.scalar_grid(p, E)
+    dts = dt / sigma
+    dbl = R.C.c_double
+    fq, fpsi = drv.function(program, "update_q"), drv.function(program, "update_psi")
+
+    def upd_q(nq, pq, ps, coef, sign):
+        drv.launch(fq, egrid, eblock, [nq, pq, ps, R.C.c_void_p(d_d0), R.uint3(p), dbl(coef), dbl(sign)])
+
+    def upd_psi(nx, pv, qs, sign):
+        drv.launch(fpsi, grid, block, [nx, pv, qs, d_pot, R.C.c_void_p(d_d1), R.C.c_void_p(d_w), dbl(g * dt), R.uint3(p),
+                                       dbl(sign)])
+
+    upd_q(dqR, dqR, dR, dts / (dt - dts), 1.0)
+    for _ in range(NSTEPS):
+        upd_psi(dI, dR, dqR, -1.0)
+        upd_q(dqI, dqR, dR, dts, 1.0)
+        upd_psi(dR, dI, dqI, 1.0)
+        upd_q(dqR, dqI, dI, dts, -1.0)
+    outp, outq = np.zeros_like(psi), np.zeros_like(q)
+    outp[..., 0, 0] = R.pitched_download(drv, dR, parts[0].shape)
+    outp[..., 0, 1] = R.pitched_download(drv, dI, parts[1].shape)
+    outq[..., 0, 0] = R.pitched_download(drv, dqR, parts[2].shape)
+    outq[..., 0, 1] = R.pitched_download(drv, dqI, parts[3].shape)
+    return dict(kind="split", lattice="c15", params=params_dict(p), fields=np.zeros((NSTEPS, 8)), times=np.zeros(NSTEPS),
+                in_even=interior(psi), in_qeven=interior(q), out_even=interior(outp), out_qeven=interior(outq))
+
+
 def scalar_case(drv, name, program, lattice, dims, dt, g, seed):
     """NSTEPS leapfrog updates of the scalar programs.  Their update is
     next += dt_ref (-i H) (GPUGrossPitaevskii_BCC.cu:345-346); the C15/A15/FCC
@@ -258,6 +307,7 @@ CASES = [
                                             3.0, 91)),
     ("itp_rel_spin1_bcc", lambda d: itp_case(d, "itp_rel_spin1_bcc", "rel_spin1_bcc", 3, (4, 3, 2), 1e-3, 0.1, 120.0,
                                              -7.0, 0.0, 93)),
+    ("rel_scalar_c15", lambda d: split_case(d, "rel_scalar_c15", (2, 2, 2), 1e-3, 0.01, 300.0, 95)),
     ("scalar_bcc", lambda d: scalar_case(d, "scalar_bcc", "scalar_bcc", "bcc", (5, 3, 2), 2e-4, 150.0, 51)),
     ("scalar_c15", lambda d: scalar_case(d, "scalar_c15", "scalar_c15", "c15", (2, 2, 2), 2e-4, 150.0, 61)),
     ("scalar_a15", lambda d: scalar_case(d, "scalar_a15", "scalar_a15", "a15", (3, 2, 2), 2e-4, 150.0, 71)),

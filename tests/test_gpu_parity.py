@@ -315,6 +315,43 @@ def test_hyperbolic_itp_reaches_the_parabolic_ground_state(gpu):
     assert float(np.max(np.abs(q_h - d0))) <= 1e-5 * float(np.max(np.abs(d0)))  # q lags psi by ~sigma/dt steps
 
 
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("dims", [(2, 2, 2), (3, 1, 2), (1, 1, 1)])
+def test_split_scheme(gpu, dims, prec):
+    """C15 real/imaginary split scheme (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:
+    90-155, 469-482): gpe_start's q_R start then 5 steps of two half-step launches."""
+    lat = capi.Lattice("c15")
+    p = _params(lat, 1, prec, dims, scheme=capi.SCHEME_SPLIT, sigma=0.01, dt=1e-3, trap_offset=0.0,
+                trap_lambda=(1.0, 1.0, 1.0), c0=300.0)
+    psi, q = _rand(lat, p, 91), _rand(lat, p, 92, edges=True)
+    with Stepper(lat, p) as s:
+        assert s.current == capi.PSI_EVEN
+        s.upload(capi.PSI_EVEN, psi)
+        s.upload(capi.Q_EVEN, q)
+        n0 = s.launches
+        s.start()
+        s.step(5)
+        assert s.launches - n0 == 11
+        got_p, got_q = s.download(capi.PSI_EVEN), s.download(capi.Q_EVEN)
+    oracle.split_run(lat, p, psi, q, 5)
+    _close(got_p, psi, prec, "psi")
+    _close(got_q, q, prec, "q")
+
+
+def test_split_scheme_rejects(gpu):
+    lat = capi.Lattice("c15")
+    with pytest.raises(capi.GpeError):  # scalar only
+        Stepper(lat, _params(lat, 3, capi.FP64, (2, 2, 2), scheme=capi.SCHEME_SPLIT, sigma=0.01))
+    with pytest.raises(capi.GpeError):  # needs edge tables
+        Stepper(capi.Lattice("fcc"), _params(capi.Lattice("fcc"), 1, capi.FP64, (2, 2, 2), scheme=capi.SCHEME_SPLIT,
+                                             sigma=0.01))
+    with Stepper(lat, _params(lat, 1, capi.FP64, (2, 2, 2), scheme=capi.SCHEME_SPLIT, sigma=0.01)) as s:
+        with pytest.raises(capi.GpeError):
+            s.itp(1)
+        with pytest.raises(capi.GpeError):
+            s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN)
+
+
 def test_leapfrog_run_with_ramp_matches_oracle(gpu):
     """gpe_start + gpe_step(n) with the device-side schedule of a ramp (config-2 shape:
     linear Bz ramp plus a quadrupole gradient) against the oracle time loop."""
@@ -524,6 +561,28 @@ def test_autotune_keeps_state_and_picks_a_kernel(gpu):
         got = s.download(capi.PSI_ODD)
     oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, odd, even)
     _close(got, odd, capi.FP32)
+
+
+def test_autotune_keeps_hyperbolic_state(gpu):
+    """gpe_autotune on a hyperbolic handle restores q even/odd as well as psi (its
+    trial steps write both), and stepping after it still matches the oracle."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 5, capi.FP32, (8, 4, 4), scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01)
+    pe, po = _rand(lat, p, 141), _rand(lat, p, 142)
+    qe, qo = _rand(lat, p, 143, edges=True), _rand(lat, p, 144, edges=True)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        for slot, a in ((capi.PSI_EVEN, pe), (capi.PSI_ODD, po), (capi.Q_EVEN, qe), (capi.Q_ODD, qo)):
+            s.upload(slot, a)
+        s.autotune(steps=2)
+        for slot, a in ((capi.PSI_EVEN, pe), (capi.PSI_ODD, po), (capi.Q_EVEN, qe), (capi.Q_ODD, qo)):
+            np.testing.assert_array_equal(s.download(slot), a.astype(np.float32).astype(np.float64))
+        s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN, f, t=0.2)
+        got_p, got_q = s.download(capi.PSI_ODD), s.download(capi.Q_ODD)
+    oracle.q_psi_step(lat, p, f, 0.2, oracle.LEAPFROG, True, po, pe, qe)
+    oracle.q_step(lat, p, oracle.Q_HYPER, qo, qe, pe)
+    _close(got_p, po, capi.FP32, "psi")
+    _close(got_q, qo, capi.FP32, "q")
 
 
 @pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])

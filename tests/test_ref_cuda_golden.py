@@ -4,7 +4,9 @@ tests/golden/ref_cuda_*.npz hold short runs of the reference's unmodified
 kernels -- spin-1 leapfrog/forwardEuler with and without loss, quadratic Zeeman
 and quadrupole offset (Spin1GpeBCC.cu:667-917), spin-2 (Spin2GpeBCC.cu:698-990),
 relativistic spin-2 update_psi + update_q (RelativisticSpin2Gpe.cu:971-1132),
-the hyperbolic imaginary-time pair itp_q + itp_psi and get_Hpsi of the spin-2 and
+the C15 real/imaginary split scalar program (RelativisticGpeC15/
+GPUGrossPitaevskii_C15.cu:90-155, 469-482), the hyperbolic imaginary-time pair
+itp_q + itp_psi and get_Hpsi of the spin-2 and
 spin-1 ground-state loops (RelativisticSpin2Gpe.cu:558-807;
 RelativisticSpin1Gpe/hyper_kernels.h:4-40, common_kernels.h:17-94), and the
 scalar BCC / C15 / A15 / FCC updates -- made by
@@ -66,7 +68,7 @@ def _check(got, want, tol, what):
 
 
 def test_golden_files_present():
-    assert len(FILES) >= 12, "reference-kernel golden vectors missing"
+    assert len(FILES) >= 13, "reference-kernel golden vectors missing"
 
 
 @pytest.mark.parametrize("path", FILES, ids=IDS)
@@ -95,6 +97,12 @@ def test_oracle_vs_reference_cuda(path):
         even, odd = ps
         _check(qs[0], d["out_qeven"], 1e-12, "q even")
         _check(qs[1], d["out_qodd"], 1e-12, "q odd")
+    elif d["kind"] == "split":  # the q_R start, then NSTEPS (I, q_I), (R, q_R) half-step pairs
+        even, q = _embed(d["in_even"]), _embed(d["in_qeven"])
+        oracle.split_run(lat, p, even, q, n)
+        _check(q, d["out_qeven"], 1e-12, "q")
+        _check(even, d["out_even"], 1e-12, "psi")
+        return
     else:  # itp: itp_q + itp_psi per step, H psi of the last step's input
         ps = [_embed(d["in_even"]), _embed(d["in_odd"])]
         qs = [_embed(d["in_qeven"]), _embed(d["in_qodd"])]
@@ -122,6 +130,14 @@ def test_kernels_vs_reference_cuda(gpu, path, prec):
     tol = 1e-12 if prec == capi.FP64 else 2e-5
     n = d["fields"].shape[0]
     with Stepper(lat, p) as s:
+        if d["kind"] == "split":
+            s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
+            s.upload(capi.Q_EVEN, _embed(d["in_qeven"]))
+            s.start()
+            s.step(n)
+            _check(s.download(capi.PSI_EVEN), d["out_even"], tol, "psi")
+            _check(s.download(capi.Q_EVEN), d["out_qeven"], tol, "q")
+            return
         s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
         s.upload(capi.PSI_ODD, _embed(d["in_odd"]))
         if d["kind"] in ("hyper", "itp"):
