@@ -274,6 +274,41 @@ typedef struct {
 } gpe_observables;
 gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream);
 
+/* Per-node output fields of a psi slot (PSI_EVEN, PSI_ODD or HPSI), FP64, interior
+ * nodes in the reference's order idx = V (z X Y + y X + x) + l, K values per node:
+ *   DENSITY (K = 1): |psi|^2 (density, Spin1GpeBCC.cu:191-211).
+ *   SPIN (K = 5, C = 3 or 5): spin norm, local average spin x, y, z, density
+ *     (localAvgSpinAndDensity, Spin1GpeBCC.cu:235-271; spin-2 Spin2GpeBCC.cu:214-254,
+ *     which uses s1, s0, s_1).  As in the reference, x and y come from the spinor
+ *     normalised by sqrt(density) and z = |s1|^2 - |s_1|^2 from the unnormalised one.
+ *   UV_THETA (K = 7, C = 3 or 5): u x, y, z, v x, y, z, theta of a = m + i n
+ *     (uvTheta, Spin1GpeBCC.cu:273-326, theta in [0, pi); Spin2GpeBCC.cu:256-306).
+ *   MAX_HAMILTON (K = 1, C = 3): the local bound of maxHamilton (Spin1GpeBCC.cu:
+ *     144-189) with the fields of the installed ramp at time t.
+ *   PROJ_X, PROJ_Y (K = 3, C = 3): |component|^2 in the x- or y-quantised basis
+ *     (the BASIS switch of the picture writer, Spin1GpeBCC/utils.h:177-193).
+ * gpe_node_field_count gives K and the count of doubles `out` must hold.
+ * gpe_node_fields copies the field to host memory and synchronises the stream.
+ * gpe_node_fields_reduce integrates it (x dv = bs^3 VOLUME, FP64 sums, fixed
+ * order): DENSITY -> out[1] = total norm; SPIN -> out[5] = spin, magnetisation
+ * x, y, z, density, the quantities of integrateSpinAndDensity (Spin1GpeBCC.cu:
+ * 992-1020; the magnetisation sums density x local average spin, so its z is
+ * sum rho (|s1|^2 - |s_1|^2) dv there and here, unlike gpe_observe's sum F dv);
+ * MAX_HAMILTON -> out[1] = the maximum over nodes (getMaxHamilton, :1022-1037,
+ * the reference's dt bound). */
+enum {
+    GPE_FIELD_DENSITY = 0,
+    GPE_FIELD_SPIN = 1,
+    GPE_FIELD_UV_THETA = 2,
+    GPE_FIELD_MAX_HAMILTON = 3,
+    GPE_FIELD_PROJ_X = 4,
+    GPE_FIELD_PROJ_Y = 5
+};
+gpe_status gpe_node_field_count(const gpe_handle* h, int32_t kind, size_t* per_node, size_t* count);
+gpe_status gpe_node_fields(gpe_handle* h, int32_t slot, int32_t kind, double t, double* out, size_t count,
+                           void* stream);
+gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, double t, double* out, void* stream);
+
 /* Kernel selection and tile shape (the autotuner's knobs).
  * GPE_TUNE_KERNEL: 0 = automatic, 1 = one-node-per-thread gather kernel,
  *                  2 = row-tile kernel (TMA bulk copies of a row of cells into shared

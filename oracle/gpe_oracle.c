@@ -433,6 +433,123 @@ int orc_q_step(const gpe_lattice_desc* lat, const gpe_params* p, int qmode, doub
     return GPE_OK;
 }
 
+/* ------------------------------------------------------------ node fields */
+
+/* Per-node output fields, interior nodes in the reference's order
+ * idx = V (z X Y + y X + x) + l, GPE_FIELD_* values per node (see gpe.h).
+ * DENSITY: density kernels (Spin1GpeBCC.cu:191-211, Spin2GpeBCC.cu:192-212).
+ * SPIN: localAvgSpinAndDensity (Spin1GpeBCC.cu:235-271; Spin2GpeBCC.cu:214-254,
+ *   which applies the spin-1 formula to s1, s0, s_1): psi normalised by sqrt(rho)
+ *   for x, y, while z = |s1|^2 - |s_1|^2 of the unnormalised psi, as there.
+ * UV_THETA: uvTheta (Spin1GpeBCC.cu:273-326, theta wrapped into [0, pi);
+ *   Spin2GpeBCC.cu:256-306 on s1, s0, s_1, unwrapped).
+ * MAX_HAMILTON: maxHamilton (Spin1GpeBCC.cu:144-189), field without quadrupole offset.
+ * PROJ_X / PROJ_Y: |components|^2 in the x- / y-quantised basis (Spin1GpeBCC/utils.h:177-193). */
+int orc_node_fields(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_fields* Bs, double t, int kind,
+                    const double* psi, double* out) {
+    int st = check_args(lat, p);
+    if (st) return st;
+    const int C = p->components;
+    const int per = kind == GPE_FIELD_DENSITY ? 1 : kind == GPE_FIELD_SPIN ? 5 : kind == GPE_FIELD_UV_THETA ? 7
+                  : kind == GPE_FIELD_MAX_HAMILTON ? 1 : (kind == GPE_FIELD_PROJ_X || kind == GPE_FIELD_PROJ_Y) ? 3 : 0;
+    if (per == 0) return GPE_ERR_INVALID_ARG;
+    if ((kind == GPE_FIELD_SPIN || kind == GPE_FIELD_UV_THETA) && C == 1) return GPE_ERR_UNSUPPORTED;
+    if ((kind == GPE_FIELD_MAX_HAMILTON || kind == GPE_FIELD_PROJ_X || kind == GPE_FIELD_PROJ_Y) && C != 3)
+        return GPE_ERR_UNSUPPORTED;
+    const geom g = make_geom(lat, p);
+    const int o = C == 5 ? 1 : 0; /* s1, s0, s_1 */
+    for (int z = 0; z < g.Z; ++z)
+        for (int y = 0; y < g.Y; ++y)
+            for (int x = 0; x < g.X; ++x) {
+                const size_t cell = cell_index(&g, x, y, z);
+                for (int l = 0; l < g.V; ++l) {
+                    const size_t idx = (size_t)g.V * (((size_t)z * g.Y + y) * g.X + x) + l;
+                    double* v = out + idx * per;
+                    cplx ps[5];
+                    double rho = 0;
+                    for (int s = 0; s < C; ++s) {
+                        ps[s] = load_c(psi, cell, g.cell_vals, l, C, s);
+                        rho += ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+                    }
+                    if (kind == GPE_FIELD_DENSITY) {
+                        v[0] = rho;
+                    } else if (kind == GPE_FIELD_SPIN) {
+                        const double n1 = ps[o].x * ps[o].x + ps[o].y * ps[o].y;
+                        const double nm1 = ps[o + 2].x * ps[o + 2].x + ps[o + 2].y * ps[o + 2].y;
+                        const double sq = sqrt(rho);
+                        const cplx a = c_make(ps[o].x / sq, ps[o].y / sq);
+                        const cplx b = c_make(ps[o + 1].x / sq, ps[o + 1].y / sq);
+                        const cplx c = c_make(ps[o + 2].x / sq, ps[o + 2].y / sq);
+                        const cplx tmp = c_scale(REF_SQRT_2, c_add(c_mul(c_conj(a), b), c_mul(c_conj(b), c)));
+                        const double sz = n1 - nm1;
+                        v[0] = rho * sqrt(tmp.x * tmp.x + tmp.y * tmp.y + sz * sz);
+                        v[1] = tmp.x;
+                        v[2] = tmp.y;
+                        v[3] = sz;
+                        v[4] = rho;
+                    } else if (kind == GPE_FIELD_UV_THETA) {
+                        const cplx s1 = ps[o], s0 = ps[o + 1], sm1 = ps[o + 2];
+                        const cplx ax = c_make((sm1.x - s1.x) / REF_SQRT_2, (sm1.y - s1.y) / REF_SQRT_2);
+                        const cplx sum = c_add(sm1, s1);
+                        const cplx ay = c_make(sum.y / REF_SQRT_2, -sum.x / REF_SQRT_2); /* -i (s_1 + s1) / sqrt2 */
+                        const double m[3] = {ax.x, ay.x, s0.x}, n[3] = {ax.y, ay.y, s0.y};
+                        const double mn = m[0] * n[0] + m[1] * n[1] + m[2] * n[2];
+                        const double mm = m[0] * m[0] + m[1] * m[1] + m[2] * m[2];
+                        const double nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+                        double th = atan2(-2 * mn, mm - nn) / 2;
+                        if (C == 3 && th < 0) th += 3.1415926535897932385;
+                        const double sn = sin(th), cs = cos(th);
+                        double u[3], w[3];
+                        for (int k = 0; k < 3; ++k) {
+                            u[k] = m[k] * cs - sn * n[k];
+                            w[k] = m[k] * sn + cs * n[k];
+                        }
+                        const double un = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+                        const double wn = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+                        const double* first = un >= wn ? u : w;
+                        const double* second = un >= wn ? w : u;
+                        for (int k = 0; k < 3; ++k) {
+                            v[k] = first[k];
+                            v[3 + k] = second[k];
+                        }
+                        v[6] = th;
+                    } else if (kind == GPE_FIELD_MAX_HAMILTON) {
+                        double r[3];
+                        node_pos(lat, p, x, y, z, l, r);
+                        const double n1 = ps[0].x * ps[0].x + ps[0].y * ps[0].y;
+                        const double nm1 = ps[2].x * ps[2].x + ps[2].y * ps[2].y;
+                        const double pot = trap(p, r, t) + p->c0 * rho;
+                        const cplx tmp = c_scale(REF_SQRT_2, c_add(c_mul(c_conj(ps[0]), ps[1]), c_mul(c_conj(ps[1]), ps[2])));
+                        double B[3] = {Bs->bq * r[0] + Bs->bb[0], Bs->bq * r[1] + Bs->bb[1], -2 * Bs->bq * r[2] + Bs->bb[2]};
+                        B[0] += p->c2 * tmp.x;
+                        B[1] += p->c2 * tmp.y;
+                        B[2] += p->c2 * (n1 - nm1);
+                        const double hx = pot + fabs(REF_INV_SQRT_2 * B[0]);
+                        const double hy = pot + fabs(REF_INV_SQRT_2 * B[1]);
+                        const double hz = pot + fabs(B[2]);
+                        v[0] = fmax(hx, fmax(hy, hz));
+                    } else {
+                        const cplx s1 = ps[0], s0 = ps[1], sm1 = ps[2];
+                        const double r2 = sqrt(2.0);
+                        cplx q[3];
+                        if (kind == GPE_FIELD_PROJ_X) {
+                            q[0] = c_sub(c_scale(0.5, c_add(s1, sm1)), c_make(s0.x / r2, s0.y / r2));
+                            q[1] = c_make((s1.x - sm1.x) / r2, (s1.y - sm1.y) / r2);
+                            q[2] = c_add(c_scale(0.5, c_add(sm1, s1)), c_make(s0.x / r2, s0.y / r2));
+                        } else {
+                            const cplx ms0 = c_mul(s0, c_make(0, -1)); /* s0 (0, -1) */
+                            const cplx ms = c_mul(c_add(s1, sm1), c_make(0, -1));
+                            q[0] = c_add(c_scale(0.5, c_sub(s1, sm1)), c_make(ms0.x / r2, ms0.y / r2));
+                            q[1] = c_make(ms.x / r2, ms.y / r2);
+                            q[2] = c_add(c_scale(0.5, c_sub(sm1, s1)), c_make(ms0.x / r2, ms0.y / r2));
+                        }
+                        for (int k = 0; k < 3; ++k) v[k] = q[k].x * q[k].x + q[k].y * q[k].y;
+                    }
+                }
+            }
+    return GPE_OK;
+}
+
 /* ------------------------------------------------------- split scheme (C15) */
 
 /* RelativisticGpeC15/GPUGrossPitaevskii_C15.cu: psi = R + iI, q = q_R + i q_I stored

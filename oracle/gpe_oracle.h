@@ -59,6 +59,11 @@ int orc_q_psi_step(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_f
 int orc_q_step(const gpe_lattice_desc* lat, const gpe_params* p, int qmode,
                double* next_q, const double* prev_q, const double* psi, int threads);
 
+/* Per-node output fields (GPE_FIELD_*; gpe_node_fields), interior nodes in the
+ * reference's order idx = V (z X Y + y X + x) + l. */
+int orc_node_fields(const gpe_lattice_desc* lat, const gpe_params* p, const gpe_fields* B, double t, int kind,
+                    const double* psi, double* out);
+
 /* Real/imaginary split scalar scheme (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:
  * 90-155, 469, 477-482) on complex-pair buffers psi = R + iI, q = q_R + i q_I, in
  * place.  part 0: I and q_I from R and q_R; part 1: R and q_R from I and q_I; part 2:

@@ -57,6 +57,8 @@ def lib():
         L.orc_observe.argtypes = [P(capi.LatticeDesc), P(capi.Params), P(capi.Fields), C.c_double, dp, P(capi.Observables)]
         L.orc_ramp_eval.argtypes = [P(capi.Ramp), C.c_double, P(capi.Fields)]
         L.orc_ramp_eval.restype = None
+        L.orc_node_fields.argtypes = [P(capi.LatticeDesc), P(capi.Params), P(capi.Fields), C.c_double, C.c_int, dp, dp]
+        L.orc_node_fields.restype = C.c_int
         L.orc_split_step.argtypes = [P(capi.LatticeDesc), P(capi.Params), C.c_int, dp, dp, C.c_int]
         L.orc_split_step.restype = C.c_int
         L.orc_gpblocks_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int64), C.c_double, C.c_double, C.c_double, dp, dp, dp, C.c_int]
@@ -143,6 +145,18 @@ def hyper_run(lat, params, psi_even, psi_odd, q_even, q_odd, nsteps, ramp=None, 
         else:
             q_step(lat, params, Q_PARA, qs[b], qs[b], ps[b], threads)
     return ps[nsteps % 2], qs[nsteps % 2]
+
+
+FIELD_WIDTH = {0: 1, 1: 5, 2: 7, 3: 1, 4: 3, 5: 3}
+
+
+def node_fields(lat, params, fields, t, kind, psi) -> np.ndarray:
+    """Per-node output field, shape (Z, Y, X, V, K) (orc_node_fields)."""
+    X, Y, Z = (int(params.dims[i]) for i in range(3))
+    out = np.zeros((Z, Y, X, lat.nodes, FIELD_WIDTH[kind]))
+    _check(lib().orc_node_fields(C.byref(lat.desc), C.byref(params), C.byref(fields), t, kind, _dp(psi), _dp(out)),
+           "orc_node_fields")
+    return out
 
 
 def split_step(lat, params, part, psi, q, threads=0):

@@ -36,6 +36,7 @@ RAMP_MAX_SEGMENTS = 32
 PSI_EVEN, PSI_ODD, Q_EVEN, Q_ODD, HPSI = 0, 1, 2, 3, 4
 MODE_LEAPFROG, MODE_EULER, MODE_ITP = 0, 1, 2
 TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS, TUNE_OBSERVE_ARITH, TUNE_CARVEOUT = 0, 1, 2, 3, 4, 5, 6
+FIELD_DENSITY, FIELD_SPIN, FIELD_UV_THETA, FIELD_MAX_HAMILTON, FIELD_PROJ_X, FIELD_PROJ_Y = 0, 1, 2, 3, 4, 5
 KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS = 0, 1, 2, 3, 4
 BATCH_ITEM_NODES, BATCH_STEPS_PER_LAUNCH, BATCH_BLOCKS_PER_SM, BATCH_BARRIER_TIMEOUT_MS, BATCH_TEST_EXTRA_ARRIVALS = 0, 1, 2, 3, 4
 
@@ -309,6 +310,9 @@ def load_library(path: str = LIB_PATH):
         "gpe_step_explicit": (C.c_int, [vp, C.c_int32, C.c_int32, P(Fields), C.c_double, C.c_int32, vp]),
         "gpe_itp": (C.c_int, [vp, C.c_int32, P(C.c_double), vp]),
         "gpe_observe": (C.c_int, [vp, C.c_int32, C.c_double, P(Observables), vp]),
+        "gpe_node_field_count": (C.c_int, [vp, C.c_int32, P(C.c_size_t), P(C.c_size_t)]),
+        "gpe_node_fields": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_double, P(C.c_double), C.c_size_t, vp]),
+        "gpe_node_fields_reduce": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_double, P(C.c_double), vp]),
         "gpe_launch_count": (C.c_uint64, [vp]),
         "gpe_current_slot": (C.c_int32, [vp]),
         "gpe_set_tuning": (C.c_int, [vp, C.c_int32, C.c_int32]),

@@ -183,6 +183,7 @@ static void release(gpe_handle* h) {
     if (h->partials) cudaFree(h->partials);
     if (h->obs_out) cudaFree(h->obs_out);
     if (h->stage) cudaFree(h->stage);
+    if (h->field_buf) cudaFree(h->field_buf);
     if (h->err) cudaFree(h->err);
     if (h->blk) cudaFree(h->blk);
     adjoint_release(h);

@@ -59,6 +59,8 @@ struct gpe_handle {
     size_t partial_blocks = 0;
     double* obs_out = nullptr;
     double* stage = nullptr;   // FP64 staging for uploads/downloads (allocated on first use)
+    double* field_buf = nullptr;  // per-node output fields (gpe_node_fields; allocated on first use)
+    size_t field_count = 0;
     size_t stage_count = 0;
     gpe_ramp ramp{};
     bool has_ramp = false;

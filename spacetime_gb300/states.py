@@ -168,3 +168,25 @@ def random_state(shape, seed=7) -> np.ndarray:
     inner = (Z, Y, X) + tuple(shape[3:])
     v = 2.0 * uniform01(seed, int(np.prod(inner))).reshape(inner) - 1.0
     return _embed(v)
+
+
+def read_state_file(path, lat: "capi.Lattice", params: "capi.Params", edges: bool = False) -> np.ndarray:
+    """A state file of the reference programs: the raw host array of BlockPsis
+    (or BlockEdges for q) cells with the one-cell zero halo, x fastest, written with
+    ``fs.write`` and read back with ``fs.read`` (Spin1GpeBCC.cu:1215-1237, 1690-1699;
+    RelativisticSpin2Gpe.cu:1428-1441, 1695-1706).  Returns the array in the layout
+    gpe_upload takes, shape (Z+2, Y+2, X+2, V or E, C, 2).  The file must hold
+    exactly that many little-endian doubles."""
+    shape = capi.buffer_shape(lat, params, edges)
+    data = np.fromfile(path, dtype="<f8")
+    if data.size != int(np.prod(shape)):
+        raise ValueError("%s holds %d doubles; a (%s) state of this grid has %d" %
+                         (path, data.size, ", ".join(map(str, shape)), int(np.prod(shape))))
+    return data.reshape(shape).astype(np.float64)
+
+
+def write_state_file(path, state: np.ndarray) -> None:
+    """Writes a state array (the layout gpe_download returns) as the reference's
+    raw state file: the same bytes the reference's ``fs.write`` of its host array
+    produces, so its programs can load it."""
+    np.ascontiguousarray(state, dtype="<f8").tofile(path)

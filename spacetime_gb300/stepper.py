@@ -133,6 +133,35 @@ class Stepper:
         capi.check(self.lib.gpe_observe(self._h, slot, t, C.byref(o), self.stream), "gpe_observe")
         return o.as_dict()
 
+    def load_state(self, slot: int, path: str):
+        """Uploads a reference state file (states.read_state_file) into a slot."""
+        from . import states
+
+        self.upload(slot, states.read_state_file(path, self.lattice, self.params, slot in (capi.Q_EVEN, capi.Q_ODD)))
+
+    def save_state(self, slot: int, path: str):
+        """Writes a slot as a reference state file (states.write_state_file)."""
+        from . import states
+
+        states.write_state_file(path, self.download(slot))
+
+    def node_fields(self, slot: int, kind: int, t: float = 0.0) -> np.ndarray:
+        """Per-node output field (gpe_node_fields): shape (Z, Y, X, V, K)."""
+        per, count = C.c_size_t(), C.c_size_t()
+        capi.check(self.lib.gpe_node_field_count(self._h, kind, C.byref(per), C.byref(count)), "gpe_node_field_count")
+        out = np.zeros(count.value)
+        capi.check(self.lib.gpe_node_fields(self._h, slot, kind, t, out.ctypes.data_as(C.POINTER(C.c_double)), out.size,
+                                            self.stream), "gpe_node_fields")
+        X, Y, Z = (int(self.params.dims[i]) for i in range(3))
+        return out.reshape(Z, Y, X, self.lattice.nodes, per.value)
+
+    def node_fields_reduce(self, slot: int, kind: int, t: float = 0.0) -> np.ndarray:
+        """Integral (or maximum, for FIELD_MAX_HAMILTON) of a field (gpe_node_fields_reduce)."""
+        out = np.zeros(5)
+        capi.check(self.lib.gpe_node_fields_reduce(self._h, slot, kind, t, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                   self.stream), "gpe_node_fields_reduce")
+        return out[:5 if kind == capi.FIELD_SPIN else 1]
+
     def set_tuning(self, key: int, value: int):
         capi.check(self.lib.gpe_set_tuning(self._h, key, value), "gpe_set_tuning")
 

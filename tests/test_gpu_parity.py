@@ -352,6 +352,68 @@ def test_split_scheme_rejects(gpu):
             s.step_explicit(capi.PSI_ODD, capi.PSI_EVEN)
 
 
+FIELD_CASES = [(3, k) for k in (capi.FIELD_DENSITY, capi.FIELD_SPIN, capi.FIELD_UV_THETA, capi.FIELD_MAX_HAMILTON,
+                                 capi.FIELD_PROJ_X, capi.FIELD_PROJ_Y)] + \
+              [(5, capi.FIELD_SPIN), (5, capi.FIELD_UV_THETA), (1, capi.FIELD_DENSITY)]
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("C,kind", FIELD_CASES)
+def test_node_fields(gpu, C, kind, prec):
+    """gpe_node_fields against the oracle on the same stored values (FP64 fields
+    from FP32 or FP64 storage): localAvgSpinAndDensity, uvTheta, maxHamilton,
+    projections (Spin1GpeBCC.cu:144-326, Spin2GpeBCC.cu:192-306)."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, C, prec, (5, 4, 3))
+    psi = _rand(lat, p, 151)
+    if prec == capi.FP32:
+        psi = psi.astype(np.float32).astype(np.float64)
+    f = capi.make_fields(**FIELDS)
+    ramp = capi.make_ramp(bq_segments=[(f.bq, 1e9, capi.RAMP_CONSTANT)], bb_segments=[(tuple(f.bb), 1e9, capi.RAMP_CONSTANT)])
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_EVEN, psi)
+        s.set_ramp(ramp, 0.0)
+        got = s.node_fields(capi.PSI_EVEN, kind, t=0.0)
+    want = oracle.node_fields(lat, p, oracle.ramp_eval(ramp, 0.0), 0.0, kind, psi)
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12 * float(np.max(np.abs(want))))
+
+
+@pytest.mark.parametrize("C,kind", [(3, capi.FIELD_DENSITY), (3, capi.FIELD_SPIN), (5, capi.FIELD_SPIN),
+                                    (3, capi.FIELD_MAX_HAMILTON)])
+def test_node_fields_reduce(gpu, C, kind):
+    """gpe_node_fields_reduce: integrateSpinAndDensity's spin, density-weighted
+    magnetisation and density (Spin1GpeBCC.cu:992-1020) and getMaxHamilton's
+    maximum (:1022-1037), from the oracle's per-node fields."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, C, capi.FP64, (6, 5, 4))
+    psi = _rand(lat, p, 152)
+    with Stepper(lat, p) as s:
+        s.upload(capi.PSI_ODD, psi)
+        got = s.node_fields_reduce(capi.PSI_ODD, kind)
+    v = oracle.node_fields(lat, p, capi.make_fields(), 0.0, kind, psi).reshape(-1, oracle.FIELD_WIDTH[kind])
+    dv = p.block_scale ** 3 * lat.volume
+    if kind == capi.FIELD_SPIN:
+        want = np.array([v[:, 0].sum(), (v[:, 4] * v[:, 1]).sum(), (v[:, 4] * v[:, 2]).sum(), (v[:, 4] * v[:, 3]).sum(),
+                         v[:, 4].sum()]) * dv
+    elif kind == capi.FIELD_MAX_HAMILTON:
+        want = np.array([v[:, 0].max()])
+    else:
+        want = np.array([v[:, 0].sum() * dv])
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-14)
+
+
+def test_node_fields_rejects(gpu):
+    lat = capi.Lattice("bcc")
+    with Stepper(lat, _params(lat, 1, capi.FP64, (2, 2, 2))) as s:
+        with pytest.raises(capi.GpeError):
+            s.node_fields(capi.PSI_EVEN, capi.FIELD_SPIN)
+        with pytest.raises(capi.GpeError):
+            s.node_fields_reduce(capi.PSI_EVEN, capi.FIELD_UV_THETA)
+        with pytest.raises(capi.GpeError):
+            s.node_fields(capi.PSI_EVEN, 99)
+
+
 def test_leapfrog_run_with_ramp_matches_oracle(gpu):
     """gpe_start + gpe_step(n) with the device-side schedule of a ramp (config-2 shape:
     linear Bz ramp plus a quadrupole gradient) against the oracle time loop."""
