@@ -224,6 +224,19 @@ gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init* init, voi
 /* Install the field ramp used by gpe_step / gpe_start (device-side getSignal). */
 gpe_status gpe_set_ramp(gpe_handle* h, const gpe_ramp* ramp, double t0);
 
+/* Condensate expansion (Spin1GpeBCC.cu:1576-1582, 1590-1596): from t_start on,
+ * every step at time t uses the block scale bs(t) = bs0 (1 + rate (t - t_start)),
+ * for the node positions and the Laplacian weights h / bs^2, as the reference
+ * passes its growing expansionBlockScale to leapfrog.  gpe_observe uses bs(t) for
+ * positions and kinetic energy and keeps dv = bs0^3 VOLUME, as the reference's
+ * volume.  The reference adds dt k bs0 per step from the first step whose time is
+ * at or after EXPANSION_START: rate = k times its ms per code time unit, and
+ * t_start = that step's time minus dt.  Pair it with GPE_FLAG_TRAP_OFF_AFTER at
+ * the same time for the reference's trap switch-off (:112-116).  rate = 0 turns it
+ * off.  Parabolic scheme only; the adjoint and batched stepping refuse handles
+ * with expansion (GPE_ERR_UNSUPPORTED). */
+gpe_status gpe_set_expansion(gpe_handle* h, double t_start, double rate);
+
 /* Forward-Euler start step from PSI_ODD into PSI_EVEN at t0
  * (forwardEuler, Spin1GpeBCC.cu:667-791, launched at :1433; hyperbolic start
  * RelativisticSpin2Gpe.cu:1628-1630). */

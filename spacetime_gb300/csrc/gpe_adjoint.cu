@@ -544,6 +544,7 @@ extern "C" gpe_status gpe_adjoint_forward(gpe_handle* h, int32_t n_steps, const 
                                           const double* target, size_t count, double* out, void* stream) {
     if (!h || !fields || !target || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
     if (h->p.scheme != GPE_SCHEME_PARABOLIC) return fail(GPE_ERR_UNSUPPORTED, "the adjoint is built for the parabolic scheme");
+    if (h->exp_rate != 0) return fail(GPE_ERR_UNSUPPORTED, "the adjoint does not follow condensate expansion");
     if (n_steps < 1) return fail(GPE_ERR_INVALID_ARG, "n_steps must be at least 1");
     if (count != host_count(h, false)) return fail(GPE_ERR_INVALID_ARG, "target size does not match the grid");
     if (stride <= 0) stride = (int32_t)std::ceil(std::sqrt((double)n_steps));

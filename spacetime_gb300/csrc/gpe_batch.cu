@@ -364,9 +364,13 @@ gpe_status rebuild_items(gpe_batch* b) {
     return upload_items(b, build_items(b, all), member_grids(b));
 }
 
-void fill_state(gpe_batch* b) {
+// Refreshes the per-member state; members stepped with condensate expansion
+// (a block scale that changes in time) are refused, since the batch kernel
+// keeps each member's block scale fixed.
+gpe_status fill_state(gpe_batch* b) {
     for (size_t m = 0; m < b->members.size(); ++m) {
         const gpe_handle* h = b->members[m];
+        if (h->exp_rate != 0) return fail(GPE_ERR_UNSUPPORTED, "batched stepping does not follow condensate expansion");
         BatchState& S = b->h_state[m];
         S.ramp = h->ramp;
         S.has_ramp = h->has_ramp ? 1 : 0;
@@ -378,6 +382,7 @@ void fill_state(gpe_batch* b) {
         S.flags = h->p.flags;
         S.pad = 0;
     }
+    return GPE_OK;
 }
 
 gpe_status grid_size(gpe_batch* b) {
@@ -553,7 +558,7 @@ extern "C" gpe_status gpe_batch_step(gpe_batch* b, int32_t n, void* stream) {
     // may still feed a copy of an earlier call
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "batch step");
-    fill_state(b);
+    if (gpe_status st = fill_state(b)) return st;
     gpe_status st = enqueue_steps(b, n, s, b->d_members, (uint32_t)b->members.size(), b->h_state, b->grid);
     if (st) return st;
     advance_members(b, n);
@@ -598,7 +603,7 @@ extern "C" gpe_status gpe_batch_replay(gpe_batch* b, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaDeviceSynchronize();  // see gpe_batch_step
     if (e != cudaSuccess) return cuda_fail(e, "batch replay");
-    fill_state(b);
+    if (gpe_status st = fill_state(b)) return st;
     e = cudaGraphLaunch(b->exec, s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
     const int32_t K = b->steps_per_launch > 0 ? b->steps_per_launch : b->graph_steps;
@@ -667,7 +672,7 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
     for (const gpe_handle* h : b->members) full_cost += (uint64_t)h->g.X * h->g.Y * h->g.Z * h->g.V * h->g.C;
     std::string rep = "[";
     std::vector<std::pair<uint64_t, int32_t>> best_by_lattice;
-    fill_state(b);
+    if (gpe_status st = fill_state(b)) return st;
     for (uint64_t key : keys) {
         const uint32_t V = (uint32_t)(key >> 32);
         std::vector<uint32_t> which;

@@ -510,6 +510,7 @@ static void fill_phys(PhysR<R>& P, const Phys& ph, const gpe_fields& B, double t
     P.bqq = (R)B.bq_quad;
     P.dt = (R)ph.dt;
     P.dts = ph.sigma > 0 ? (R)(ph.dt / ph.sigma) : (R)0;
+    P.ks = (R)ph.ks;
     P.flags = ph.flags;
     P.trap_on = !((ph.flags & GPE_FLAG_TRAP_OFF_AFTER) && t >= ph.trap_off_time);
 }
@@ -526,7 +527,14 @@ StepArgs gpe::make_args(const gpe_handle* h, const gpe_fields& B, double t) {
         a.ph.lambda[i] = p.trap_lambda[i];
         a.ph.quad_center[i] = p.quad_center[i];
     }
+    // condensate expansion (Spin1GpeBCC.cu:1579-1582): block scale bs(t) = bs0 (1 +
+    // rate (t - t_start)) from t_start on; positions use bs(t), the Laplacian h / bs^2
     a.ph.bs = p.block_scale;
+    a.ph.ks = 1.0;
+    if (h->exp_rate != 0 && t >= h->exp_t0) {
+        a.ph.bs = p.block_scale * (1.0 + h->exp_rate * (t - h->exp_t0));
+        a.ph.ks = (p.block_scale / a.ph.bs) * (p.block_scale / a.ph.bs);
+    }
     a.ph.dt = p.dt;
     a.ph.trap_offset = p.trap_offset;
     a.ph.trap_off_time = p.trap_off_time;
@@ -927,6 +935,16 @@ extern "C" gpe_status gpe_step_explicit(gpe_handle* h, int32_t next_slot, int32_
     std::memset(&B, 0, sizeof B);
     if (fields) B = *fields;
     return one_step(h, next_slot, prev_slot, B, t, mode, (cudaStream_t)stream);
+}
+
+extern "C" gpe_status gpe_set_expansion(gpe_handle* h, double t_start, double rate) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (h->p.scheme != GPE_SCHEME_PARABOLIC) return fail(GPE_ERR_UNSUPPORTED, "expansion is built for the parabolic scheme");
+    if (!std::isfinite(t_start) || !std::isfinite(rate) || rate < 0)
+        return fail(GPE_ERR_INVALID_ARG, "expansion: finite t_start and rate >= 0");
+    h->exp_t0 = t_start;
+    h->exp_rate = rate;
+    return GPE_OK;
 }
 
 extern "C" gpe_status gpe_start(gpe_handle* h, void* stream) {

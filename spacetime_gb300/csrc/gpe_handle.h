@@ -64,6 +64,7 @@ struct gpe_handle {
     size_t stage_count = 0;
     gpe_ramp ramp{};
     bool has_ramp = false;
+    double exp_t0 = 0, exp_rate = 0;  // condensate expansion (gpe_set_expansion)
     double t0 = 0;
     int cur = 0;          // psi slot holding the newest state
     uint64_t nstep = 0;   // leapfrog steps since gpe_start / gpe_set_ramp

@@ -87,6 +87,7 @@ struct Phys {
     double trap_off_time;
     double c0, c2, c4, alpha, sigma;
     double quad_center[3];
+    double ks;       // kinetic scale (bs0 / bs)^2 of the step's block scale bs (1 without expansion)
     int flags;
 };
 
@@ -97,6 +98,7 @@ struct PhysR {
     R p0[3], bs, bw[3], lambda[3], trap_offset, c0, c2, c4, alpha, sigma, qc[3];
     R bq, bb[3], bqq, bbq[3];
     R dt, dts;       // dt and dt/sigma
+    R ks;            // kinetic scale (bs0 / bs)^2; bs above is the step's block scale
     int trap_on;     // trap() is zero after trap_off_time (Spin1GpeBCC.cu:114)
     int flags;
 };

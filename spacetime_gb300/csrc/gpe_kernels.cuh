@@ -255,11 +255,12 @@ template <typename R>
 __device__ __forceinline__ void load_tables(SmemTables<R>& s, const StepArgs& a) {
     const int V = a.g.V;
     const int n = a.tab.entries;
+    const R ks = make_phys<R>(a).ks;  // condensate expansion: weights h / bs^2 of the step's bs
     for (int i = threadIdx.x; i <= V; i += blockDim.x) s.row_ptr[i] = a.tab.row_ptr[i];
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         s.nb_off[i] = a.tab.nb_off[i];
-        if constexpr (sizeof(R) == 4) s.w[i] = a.tab.w32[i];
-        else s.w[i] = a.tab.w64[i];
+        if constexpr (sizeof(R) == 4) s.w[i] = a.tab.w32[i] * ks;
+        else s.w[i] = a.tab.w64[i] * ks;
     }
     for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
         if constexpr (sizeof(R) == 4) s.pos[i] = a.tab.pos32[i];
@@ -508,8 +509,9 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
         for (int i = threadIdx.x; i <= V; i += blockDim.x) st.row_ptr[i] = a.tab.row_ptr[i];
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             st.nb_off[i] = a.tab.nb_off[i];
-            if constexpr (sizeof(A) == 4) st.w[i] = a.tab.w32[i];
-            else st.w[i] = a.tab.w64[i];
+            // condensate expansion: weights h / bs^2 of the step's bs
+            if constexpr (sizeof(A) == 4) st.w[i] = a.tab.w32[i] * make_phys<A>(a).ks;
+            else st.w[i] = a.tab.w64[i] * make_phys<A>(a).ks;
         }
         for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
             if constexpr (sizeof(A) == 4) st.pos[i] = a.tab.pos32[i];
@@ -1087,8 +1089,9 @@ __global__ void __launch_bounds__(256) leapfrog_tile_kernel(StepArgs a, uint32_t
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         s_goff[i] = a.tab.nb_off[i];
         s_soff[i] = a.tab.nb_soff[i];
-        if constexpr (sizeof(R) == 4) s_w[i] = a.tab.w32[i];
-        else s_w[i] = a.tab.w64[i];
+        // condensate expansion: weights h / bs^2 of the step's bs
+        if constexpr (sizeof(R) == 4) s_w[i] = a.tab.w32[i] * make_phys<R>(a).ks;
+        else s_w[i] = a.tab.w64[i] * make_phys<R>(a).ks;
     }
     for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
         if constexpr (sizeof(R) == 4) s_pos[i] = a.tab.pos32[i];
@@ -1279,8 +1282,9 @@ __global__ void __launch_bounds__(1024) leapfrog_march_kernel(StepArgs a, MarchA
         MarchEntry<R> e;
         e.soff = (q.y * (int)(m.T + 2) + q.x) * (int)cb + q.w * (int)node_bytes;
         e.dz = q.z;
-        if constexpr (sizeof(R) == 4) e.w = a.tab.w32[i];
-        else e.w = a.tab.w64[i];
+        // condensate expansion: weights h / bs^2 of the step's bs
+        if constexpr (sizeof(R) == 4) e.w = a.tab.w32[i] * make_phys<R>(a).ks;
+        else e.w = a.tab.w64[i] * make_phys<R>(a).ks;
         s_ent[i] = e;
     }
     for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {
@@ -1519,8 +1523,9 @@ __global__ void __launch_bounds__(RowsLB<R, C>::threads, RowsLB<R, C>::blocks) l
         RowsEntry<R> e;
         // offset k of (dy, dz) in the high byte, in-row byte offset below
         e.off = (a.tab.ent_row[i] << 24) + (q.x * (int)cb + q.w * (int)node_bytes + (1 << 23));
-        if constexpr (sizeof(R) == 4) e.w = a.tab.w32[i];
-        else e.w = a.tab.w64[i];
+        // condensate expansion: weights h / bs^2 of the step's bs
+        if constexpr (sizeof(R) == 4) e.w = a.tab.w32[i] * make_phys<R>(a).ks;
+        else e.w = a.tab.w64[i] * make_phys<R>(a).ks;
         s_ent[i] = e;
     }
     for (int i = threadIdx.x; i < 3 * V; i += blockDim.x) {

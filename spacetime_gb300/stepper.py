@@ -133,6 +133,10 @@ class Stepper:
         capi.check(self.lib.gpe_observe(self._h, slot, t, C.byref(o), self.stream), "gpe_observe")
         return o.as_dict()
 
+    def set_expansion(self, t_start: float, rate: float):
+        """Condensate expansion: block scale bs0 (1 + rate (t - t_start)) from t_start on."""
+        capi.check(self.lib.gpe_set_expansion(self._h, t_start, rate), "gpe_set_expansion")
+
     def load_state(self, slot: int, path: str):
         """Uploads a reference state file (states.read_state_file) into a slot."""
         from . import states

@@ -51,8 +51,11 @@ def params_dict(p):
             "alpha": p.alpha, "sigma": p.sigma, "quad_center": list(p.quad_center)}
 
 
-def spinor_case(drv, name, program, lattice, C, dims, flags, dt, c0, c2, c4, alpha, seed):
-    """forwardEuler (odd -> even) then NSTEPS-1 leapfrog steps (Spin1GpeBCC.cu:1428-1603)."""
+def spinor_case(drv, name, program, lattice, C, dims, flags, dt, c0, c2, c4, alpha, seed, expansion=None):
+    """forwardEuler (odd -> even) then NSTEPS-1 leapfrog steps (Spin1GpeBCC.cu:1428-1603).
+    expansion = (t_start, rate): the block scale passed to each launch grows as
+    bs0 (1 + rate (t - t_start)) from t_start on, as the program's expansion phase
+    passes its growing expansionBlockScale (:1576-1588)."""
     lat = capi.Lattice(lattice)
     p = capi.make_params(components=C, precision=capi.FP64, dims=dims, block_scale=0.3, dt=dt,
                          trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, c4=c4,
@@ -72,8 +75,11 @@ def spinor_case(drv, name, program, lattice, C, dims, flags, dt, c0, c2, c4, alp
     for j in range(NSTEPS):
         kern = "euler" if j == 0 else "leapfrog"
         nxt, prv = bufs[(j + 1) % 2], bufs[j % 2]
+        bs = p.block_scale
+        if expansion is not None and times[j] >= expansion[0]:
+            bs = p.block_scale * (1.0 + expansion[1] * (times[j] - expansion[0]))
         common = [nxt, prv, R.C.c_void_p(d_ent), R.C.c_void_p(d_w), R.mag_fields(as_fields(F[j])), R.uint3(p),
-                  R.C.c_double(p.block_scale), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2)]
+                  R.C.c_double(bs), R.double3(p.p0), R.C.c_double(c0), R.C.c_double(c2)]
         if program == "spin1_bcc":
             args = common + [R.C.c_double(alpha), R.C.c_bool(bool(flags & capi.FLAG_THREE_BODY_LOSS)),
                              R.C.c_bool(bool(flags & capi.FLAG_QUADRATIC_ZEEMAN)),
@@ -84,8 +90,9 @@ def spinor_case(drv, name, program, lattice, C, dims, flags, dt, c0, c2, c4, alp
         drv.launch(drv.function(program, kern), grid, block, args)
     out = {"even": interior(s.download(capi.PSI_EVEN)), "odd": interior(s.download(capi.PSI_ODD))}
     s.close()
+    extra = {} if expansion is None else {"expansion": np.array(expansion, dtype=np.float64)}
     return dict(kind="spinor", lattice=lattice, params=params_dict(p), fields=F, times=times,
-                in_even=interior(even0), in_odd=interior(odd0), **{"out_" + k: v for k, v in out.items()})
+                in_even=interior(even0), in_odd=interior(odd0), **{"out_" + k: v for k, v in out.items()}, **extra)
 
 
 def rel_case(drv, name, lattice, dims, dt, sigma, c0, c2, c4, seed, program="rel_spin2_bcc", C=5):
@@ -296,6 +303,8 @@ CASES = [
     ("spin1_bcc_toggles", lambda d: spinor_case(d, "spin1_bcc_toggles", "spin1_bcc", "bcc", 3, (4, 3, 3),
                                                 capi.FLAG_THREE_BODY_LOSS | capi.FLAG_QUADRATIC_ZEEMAN | capi.FLAG_QUADRUPOLE_OFFSET,
                                                 2e-4, 120.0, -7.0, 0.0, 2.0, 21)),
+    ("spin1_bcc_expansion", lambda d: spinor_case(d, "spin1_bcc_expansion", "spin1_bcc", "bcc", 3, (4, 3, 3), 0, 2e-4,
+                                                  120.0, -7.0, 0.0, 0.0, 23, expansion=(0.2501, 50.0))),
     ("spin2_bcc", lambda d: spinor_case(d, "spin2_bcc", "spin2_bcc", "bcc", 5, (5, 3, 2), capi.FLAG_THREE_BODY_LOSS,
                                         R.SPIN2_DT, 120.0, -7.0, 3.0, 2.0, 31)),
     ("rel_spin2_bcc", lambda d: rel_case(d, "rel_spin2_bcc", "bcc", (4, 3, 2), 2e-4, 0.01, 120.0, -7.0, 3.0, 41)),
@@ -322,7 +331,7 @@ def main(outdir):
     drv = R.Driver()
     try:
         for name, fn in CASES:
-            program = name.replace("_toggles", "").replace("itp_", "")
+            program = name.replace("_toggles", "").replace("_expansion", "").replace("itp_", "")
             if os.path.exists(os.path.join(outdir, "ref_cuda_%s.npz" % name)) and "--all" not in sys.argv:
                 continue  # keep the vectors already made
             if not R.available(program):

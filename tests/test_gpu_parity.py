@@ -414,6 +414,68 @@ def test_node_fields_rejects(gpu):
             s.node_fields(capi.PSI_EVEN, 99)
 
 
+def _bs_at(p, t, t0, rate):
+    q = capi.Params.from_buffer_copy(p)
+    if t >= t0:
+        q.block_scale = p.block_scale * (1.0 + rate * (t - t0))
+    return q
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("kernel", [capi.KERNEL_TILE, capi.KERNEL_GATHER, capi.KERNEL_ROWS])
+def test_expansion_run(gpu, kernel, prec):
+    """gpe_set_expansion: 8 leapfrog steps with a ramp, the block scale growing from
+    the 3rd step on (Spin1GpeBCC.cu:1576-1588) and the trap off from then too
+    (:112-116), against the oracle stepping with each step's block scale."""
+    lat = capi.Lattice("bcc")
+    dt = 2e-4
+    t_exp, rate = 2.5 * dt, 40.0
+    p = _params(lat, 3, prec, (8, 4, 4), dt=dt, flags=capi.FLAG_TRAP_OFF_AFTER, trap_off_time=t_exp)
+    even, odd = _rand(lat, p, 161), _rand(lat, p, 162)
+    ramp = capi.make_ramp(bq_segments=[(0.3, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0.1, 0.0, 0.5), 0.0, capi.RAMP_CONSTANT), ((0.0, 0.2, -0.5), 6 * dt, capi.RAMP_LINEAR)])
+    with Stepper(lat, p) as s:
+        try:
+            s.set_tuning(capi.TUNE_KERNEL, kernel)
+        except capi.GpeError:
+            pytest.skip("kernel not available for this shape")
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        s.set_ramp(ramp, 0.0)
+        s.set_expansion(t_exp, rate)
+        s.step(8)
+        got = s.download(s.current)
+        obs = s.observe(s.current, t=8 * dt)
+    bufs = [odd, even]  # a new handle's newest state is PSI_ODD: step 0 writes PSI_EVEN
+    for n in range(8):
+        t = (n + 1) * dt
+        oracle.parabolic_step(lat, _bs_at(p, t, t_exp, rate), oracle.ramp_eval(ramp, ramp.time_scale * t), t, oracle.LEAPFROG,
+                              bufs[(n + 1) % 2], bufs[n % 2])
+    _close(got, bufs[8 % 2], prec, "psi")
+    pe = _bs_at(p, 8 * dt, t_exp, rate)
+    want = oracle.observe(lat, pe, oracle.ramp_eval(ramp, ramp.time_scale * 8 * dt), 8 * dt, bufs[0].astype(np.float32).astype(np.float64)
+                          if prec == capi.FP32 else bufs[0])
+    vol = (p.block_scale / pe.block_scale) ** 3  # dv stays bs0^3 VOLUME, as in the reference
+    tol = 1e-10 if prec == capi.FP64 else 1e-4
+    for k in ("norm", "energy", "h_expect"):
+        assert obs[k] == pytest.approx(want[k] * vol, rel=tol), k
+
+
+def test_expansion_rejects(gpu):
+    lat = capi.Lattice("bcc")
+    p = _params(lat, 3, capi.FP32, (4, 4, 4))
+    with Stepper(lat, p) as s:
+        with pytest.raises(capi.GpeError):
+            s.set_expansion(0.0, -1.0)
+        s.set_expansion(0.0, 10.0)
+        with pytest.raises(capi.GpeError):
+            s.adjoint_forward(np.zeros((2, 4)), _rand(lat, p, 1))
+    ph = _params(lat, 3, capi.FP32, (4, 4, 4), scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01)
+    with Stepper(lat, ph) as s:
+        with pytest.raises(capi.GpeError):
+            s.set_expansion(0.0, 10.0)
+
+
 def test_leapfrog_run_with_ramp_matches_oracle(gpu):
     """gpe_start + gpe_step(n) with the device-side schedule of a ramp (config-2 shape:
     linear Bz ramp plus a quadrupole gradient) against the oracle time loop."""

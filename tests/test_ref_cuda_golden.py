@@ -2,7 +2,8 @@
 
 tests/golden/ref_cuda_*.npz hold short runs of the reference's unmodified
 kernels -- spin-1 leapfrog/forwardEuler with and without loss, quadratic Zeeman
-and quadrupole offset (Spin1GpeBCC.cu:667-917), spin-2 (Spin2GpeBCC.cu:698-990),
+and quadrupole offset (Spin1GpeBCC.cu:667-917) and with a growing block scale
+(the expansion phase, :1576-1588), spin-2 (Spin2GpeBCC.cu:698-990),
 relativistic spin-2 update_psi + update_q (RelativisticSpin2Gpe.cu:971-1132),
 the C15 real/imaginary split scalar program (RelativisticGpeC15/
 GPUGrossPitaevskii_C15.cu:90-155, 469-482), the hyperbolic imaginary-time pair
@@ -60,6 +61,18 @@ def _fields(row):
     return capi.make_fields(bq=row[0], bb=tuple(row[1:4]), bq_quad=row[4], bb_quad=tuple(row[5:8]))
 
 
+def _expanded(p, d, t):
+    """The parameters of a step at time t of a run with condensate expansion: the
+    oracle takes the step's block scale as the reference's launch does."""
+    if "expansion" not in d:
+        return p
+    t0, rate = (float(v) for v in d["expansion"])
+    q = capi.Params.from_buffer_copy(p)
+    if t >= t0:
+        q.block_scale = p.block_scale * (1.0 + rate * (t - t0))
+    return q
+
+
 def _check(got, want, tol, what):
     g = got[1:-1, 1:-1, 1:-1] if got.shape != want.shape else got
     scale = float(np.max(np.abs(want)))
@@ -68,7 +81,7 @@ def _check(got, want, tol, what):
 
 
 def test_golden_files_present():
-    assert len(FILES) >= 13, "reference-kernel golden vectors missing"
+    assert len(FILES) >= 14, "reference-kernel golden vectors missing"
 
 
 @pytest.mark.parametrize("path", FILES, ids=IDS)
@@ -81,7 +94,8 @@ def test_oracle_vs_reference_cuda(path):
         bufs = [odd, even]
         for j in range(n):
             mode = oracle.EULER if j == 0 else oracle.LEAPFROG
-            oracle.parabolic_step(lat, p, _fields(d["fields"][j]), float(d["times"][j]), mode, bufs[(j + 1) % 2], bufs[j % 2])
+            pj = _expanded(p, d, float(d["times"][j]))
+            oracle.parabolic_step(lat, pj, _fields(d["fields"][j]), float(d["times"][j]), mode, bufs[(j + 1) % 2], bufs[j % 2])
     elif d["kind"] == "scalar":
         even, odd = _embed(d["in_even"]), _embed(d["in_odd"])
         bufs = [even, odd]
@@ -140,6 +154,8 @@ def test_kernels_vs_reference_cuda(gpu, path, prec):
             return
         s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
         s.upload(capi.PSI_ODD, _embed(d["in_odd"]))
+        if "expansion" in d:
+            s.set_expansion(*(float(v) for v in d["expansion"]))
         if d["kind"] in ("hyper", "itp"):
             s.upload(capi.Q_EVEN, _embed(d["in_qeven"]))
             s.upload(capi.Q_ODD, _embed(d["in_qodd"]))
