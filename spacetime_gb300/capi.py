@@ -167,10 +167,14 @@ class Lattice:
     """Lattice tables loaded from ``lattices/<name>.json`` with ctypes views that
     stay alive as long as this object does."""
 
-    def __init__(self, name: str):
-        path = os.path.join(LATTICE_DIR, name + ".json")
-        with open(path) as f:
-            d = json.load(f)
+    def __init__(self, name: str, tables: dict | None = None):
+        """tables: tables in the same layout (e.g. lattices.generate.generate())
+        instead of the file."""
+        if tables is None:
+            with open(os.path.join(LATTICE_DIR, name + ".json")) as f:
+                d = json.load(f)
+        else:
+            d = tables
         self.name = name
         self.data = d
         self.nodes = int(d["nodes"])
