@@ -24,7 +24,7 @@ to rounding (tests/test_lattice_generate.py), in the node order given by
 position.  The dual-edge tables follow the reference generator's rule: an edge
 runs from the lower-numbered node to the higher (a node's edges to its own
 periodic images get one orientation), and both of its incidences carry the weight
-seen from the edge's first node (:201-248).  Where cell volumes differ (A15, C15,
+seen from the edge's first node (:240-248).  Where cell volumes differ (A15, C15,
 Z) the edge form therefore differs from the node stencil, as the reference's
 tables do.
 """
