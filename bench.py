@@ -516,13 +516,14 @@ def run_reference(args):
 # ------------------------------------------------------------------ GPU arm
 
 
-def traffic_from_profile():
+def traffic_from_profile(kernel):
+    """DRAM bytes per launch from the committed ncu capture, if it is of `kernel`."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(path):
         try:
             with open(path) as f:
                 d = json.load(f)
-            return d.get("bytes_per_launch")
+            return d.get("bytes_per_launch") if d.get("kernel") == kernel else None
         except Exception:
             return None
     return None
@@ -576,7 +577,7 @@ def run_gpu(args):
         s.step(INNER)
         s._nsteps += INNER
 
-    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_step_kernel<float,3,LEAPFROG>",
+    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_step_kernel<float,3,LEAPFROG,4>",
                    capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
@@ -624,7 +625,7 @@ def run_gpu(args):
     algo_bytes = BYTES_PER_SITE_FP32 * sites
     achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = traffic_from_profile()
+    traffic = traffic_from_profile(kernel_name[chosen])
 
     # ---- end to end through the C ABI with host buffers: H2D of the FP64 host state
     # (reference file layout, pinned), start + 100 leapfrog steps + FP64 observables

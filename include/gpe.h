@@ -323,7 +323,7 @@ gpe_status gpe_node_fields(gpe_handle* h, int32_t slot, int32_t kind, double t, 
 gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, double t, double* out, void* stream);
 
 /* Kernel selection and tile shape (the autotuner's knobs).
- * GPE_TUNE_KERNEL: 0 = automatic, 1 = one-node-per-thread gather kernel,
+ * GPE_TUNE_KERNEL: 0 = automatic, 1 = gather kernel (one node per thread per pass),
  *                  2 = row-tile kernel (TMA bulk copies of a row of cells into shared
  *                      memory; needs a cell size that is a multiple of 16 bytes),
  *                  3 = 2.5-D z-march kernel (tiles of T cells x TY rows streamed
@@ -332,8 +332,8 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  *                  4 = row-block kernel (a block of RY x RZ output rows; bulk copies
  *                      of every row the block's stencil touches; all gathers from
  *                      shared memory; needs 16-byte cells, RY | Y, RZ | Z).  The
- *                      automatic choice is 2 where cells are 16-byte multiples, else
- *                      1; gpe_autotune may pick any of them.
+ *                      automatic choice is 1 (grid-stride, whole-record loads); 2-4 on
+ *                      request, and gpe_autotune may pick any of them.
  * GPE_TUNE_TILE_CELLS: cells per tile row (0 = automatic).
  * GPE_TUNE_TILE_ROWS: rows per tile along y (z-march TY, row-block RY; 0 = automatic).
  * GPE_TUNE_ZCHUNK: z-march planes per block, or row-block RZ (0 = automatic).

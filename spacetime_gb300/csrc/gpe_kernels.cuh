@@ -90,6 +90,67 @@ __device__ __forceinline__ void stc(char* p, Cx<R> c) {
     }
 }
 
+// A whole node record of C complex values.  FP32 records of odd C > 1 (24 or 40
+// bytes) start 8-byte aligned at a stride of 8C bytes, so each is (C-1)/2 aligned
+// 16-byte loads plus one 8-byte load, in an order set by bit 3 of the address
+// (which half of the record is 16-byte aligned): a warp's load instructions, and
+// with them the L1 wavefronts they cost, drop from C to (C+1)/2 per record.
+// NC: the read-only path (buffers the kernel does not write).
+template <typename R, int C, bool NC>
+__device__ __forceinline__ void ld_node(const char* p, Cx<R>* v) {
+    if constexpr (sizeof(R) == 4 && C > 1 && (C % 2) == 1) {
+        const bool odd = (reinterpret_cast<uintptr_t>(p) & 8) != 0;
+        const char* q = p + (odd ? 8 : 0);
+        const char* r = p + (odd ? 0 : 8 * (C - 1));
+        float4 a[(C - 1) / 2];
+#pragma unroll
+        for (int k = 0; k < (C - 1) / 2; ++k) {
+            if constexpr (NC) a[k] = __ldg(reinterpret_cast<const float4*>(q + 16 * k));
+            else a[k] = *reinterpret_cast<const float4*>(q + 16 * k);
+        }
+        float2 b;
+        if constexpr (NC) b = __ldg(reinterpret_cast<const float2*>(r));
+        else b = *reinterpret_cast<const float2*>(r);
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            // even: a[0].xy a[0].zw a[1].xy ... b;  odd: b a[0].xy a[0].zw ...
+            const int te = s, to = s - 1;
+            const Cx<R> ve = s == C - 1 ? cx<R>(b.x, b.y)
+                                        : ((te & 1) ? cx<R>(a[te / 2].z, a[te / 2].w) : cx<R>(a[te / 2].x, a[te / 2].y));
+            const Cx<R> vo = s == 0 ? cx<R>(b.x, b.y)
+                                    : ((to & 1) ? cx<R>(a[to / 2].z, a[to / 2].w) : cx<R>(a[to / 2].x, a[to / 2].y));
+            v[s] = odd ? vo : ve;
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < C; ++s) v[s] = NC ? ldc<R>(p + s * 2 * sizeof(R)) : ldc_rw<R>(p + s * 2 * sizeof(R));
+    }
+}
+
+template <typename R, int C>
+__device__ __forceinline__ void st_node(char* p, const Cx<R>* v) {
+    if constexpr (sizeof(R) == 4 && C > 1 && (C % 2) == 1) {
+        const bool odd = (reinterpret_cast<uintptr_t>(p) & 8) != 0;
+        char* q = p + (odd ? 8 : 0);
+        char* r = p + (odd ? 0 : 8 * (C - 1));
+#pragma unroll
+        for (int k = 0; k < (C - 1) / 2; ++k) {
+            // component o + 2k and o + 2k + 1 (selected without dynamic indexing)
+            Cx<R> lo = v[2 * k], hi = v[2 * k + 1];
+            if (odd) {
+                lo = v[2 * k + 1];
+                hi = v[2 * k + 2];
+            }
+            *reinterpret_cast<float4*>(q + 16 * k) = make_float4(lo.x, lo.y, hi.x, hi.y);
+        }
+        const Cx<R> b = odd ? v[0] : v[C - 1];
+        *reinterpret_cast<float2*>(r) = make_float2(b.x, b.y);
+    } else {
+#pragma unroll
+        for (int s = 0; s < C; ++s) stc<R>(p + s * 2 * sizeof(R), v[s]);
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ const PhysR<R>& make_phys(const StepArgs& a) {
     if constexpr (sizeof(R) == 4) return a.pf;
@@ -244,11 +305,11 @@ __device__ __forceinline__ void local_terms(const PhysR<R>& P, const R r[3], R p
 
 // Shared-memory copy of the per-handle tables.
 template <typename R>
-struct SmemTables {
-    int32_t row_ptr[kMaxNodes + 1];
-    int32_t nb_off[kMaxEntries];
+struct __align__(16) SmemTables {
+    int32_t nb_off[kMaxEntries];  // first and 16-byte aligned: a node's 4 entries load as one vector
     R w[kMaxEntries];
     R pos[kMaxNodes * 3];
+    int32_t row_ptr[kMaxNodes + 1];
 };
 
 template <typename R>
@@ -291,8 +352,9 @@ __device__ __forceinline__ void write_update(int mode, R dt, char* nxt, char* hp
 
 // One node of a parabolic step: the DEC Laplacian gather, the local terms and the
 // time update (Spin1GpeBCC.cu:835-916).  prev/next/hpsi are the buffers' interior
-// pointers; (x, y, z) the cell, l the node.
-template <typename R, int C, int MODE>
+// pointers; (x, y, z) the cell, l the node.  D > 0: every node has D stencil
+// entries, and all D neighbour loads are issued before they are used.
+template <typename R, int C, int MODE, int D = 0>
 __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R>& st, const PhysR<R>& P, const char* prev,
                                                char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l) {
     const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
@@ -301,18 +363,49 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
     const char* own = base + l * node_bytes;
 
     Cx<R> prv[C], H[C];
+    ld_node<R, C, true>(own, prv);
 #pragma unroll
-    for (int s = 0; s < C; ++s) {
-        prv[s] = ldc<R>(own + s * 2 * sizeof(R));
-        H[s] = cx<R>((R)0, (R)0);
-    }
+    for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
     // DEC Laplacian, sum_f w_f (psi_nb - psi) (Spin1GpeBCC.cu:835-865)
-    const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
-    for (int f = f0; f < f1; ++f) {
-        const char* nb = base + st.nb_off[f];
-        const R w = st.w[f];
+    if constexpr (D > 0) {
+        int32_t off[D];
+        R wt[D];
+        if constexpr (D == 4) {
+            // one 16-byte shared load for the offsets, one or two for the weights
+            const int4 o4 = *reinterpret_cast<const int4*>(st.nb_off + l * 4);
+            off[0] = o4.x; off[1] = o4.y; off[2] = o4.z; off[3] = o4.w;
+            if constexpr (sizeof(R) == 4) {
+                const float4 w4 = *reinterpret_cast<const float4*>(st.w + l * 4);
+                wt[0] = w4.x; wt[1] = w4.y; wt[2] = w4.z; wt[3] = w4.w;
+            } else {
+                const double2 wa = *reinterpret_cast<const double2*>(st.w + l * 4);
+                const double2 wb = *reinterpret_cast<const double2*>(st.w + l * 4 + 2);
+                wt[0] = wa.x; wt[1] = wa.y; wt[2] = wb.x; wt[3] = wb.y;
+            }
+        } else {
 #pragma unroll
-        for (int s = 0; s < C; ++s) H[s] += w * (ldc<R>(nb + s * 2 * sizeof(R)) - prv[s]);
+            for (int k = 0; k < D; ++k) {
+                off[k] = st.nb_off[l * D + k];
+                wt[k] = st.w[l * D + k];
+            }
+        }
+        Cx<R> v[D][C];
+#pragma unroll
+        for (int k = 0; k < D; ++k) ld_node<R, C, true>(base + off[k], v[k]);
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+#pragma unroll
+            for (int s = 0; s < C; ++s) H[s] += wt[k] * (v[k][s] - prv[s]);
+        }
+    } else {
+        const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
+        for (int f = f0; f < f1; ++f) {
+            Cx<R> v[C];
+            ld_node<R, C, true>(base + st.nb_off[f], v);
+            const R w = st.w[f];
+#pragma unroll
+            for (int s = 0; s < C; ++s) H[s] += w * (v[s] - prv[s]);
+        }
     }
     R r[3];
     r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
@@ -321,26 +414,52 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
     const R pot = trap<R>(P, r);
     local_terms<R, C>(P, r, pot, MODE, false, prv, H);
     char* nxt = next + cell_off + l * node_bytes;
-    char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
-    write_update<R, C>(MODE, P.dt, nxt, hp, prv, H);
+    if constexpr (MODE == GPE_MODE_LEAPFROG) {
+        // next += 2 dt (-i H), the whole record read and written at once
+        Cx<R> nv[C];
+        ld_node<R, C, false>(nxt, nv);
+#pragma unroll
+        for (int s = 0; s < C; ++s) nv[s] += ((R)2 * P.dt) * cx<R>(H[s].y, -H[s].x);
+        st_node<R, C>(nxt, nv);
+    } else {
+        char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
+        write_update<R, C>(MODE, P.dt, nxt, hp, prv, H);
+    }
 }
 
-// MODE: GPE_MODE_LEAPFROG / EULER / ITP.  One thread per (node, cell).
-template <typename R, int C, int MODE>
+// MODE: GPE_MODE_LEAPFROG / EULER / ITP.  Grid-stride over the nodes, one node
+// per thread per pass, on a fixed grid, so that each block stages the tables once.
+template <typename R, int C, int MODE, int D>
 __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
     __shared__ SmemTables<R> st;
     load_tables<R>(st, a);
     __syncthreads();
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= a.total) return;
-    const uint32_t i = (uint32_t)gid;
-    const uint32_t row = fdiv(i, a.divRow);
-    const uint32_t within = i - row * a.row_items;
-    const uint32_t x = fdiv(within, a.divV);
-    const uint32_t l = within - x * a.g.V;
-    const uint32_t z = fdiv(row, a.divY);
-    const uint32_t y = row - z * a.g.Y;
-    parabolic_node<R, C, MODE>(a.g, st, make_phys<R>(a), a.prev, a.next, a.hpsi, x, y, z, l);
+    const PhysR<R>& P = make_phys<R>(a);
+    for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
+         gid += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)gid;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * a.g.V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        parabolic_node<R, C, MODE, D>(a.g, st, P, a.prev, a.next, a.hpsi, x, y, z, l);
+    }
+}
+
+// SM count of the current device (cached per device).
+inline int device_sm_count() {
+    static int cache[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (cache[dev] == 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = sms > 0 ? sms : 1;
+    }
+    return cache[dev];
 }
 
 // ---------------------------------------------------------------- hyperbolic
@@ -711,16 +830,37 @@ __global__ void __launch_bounds__(256) scale_kernel(StepArgs a, const double* no
 
 inline unsigned nblocks(uint64_t items, unsigned bs) { return (unsigned)((items + bs - 1) / bs); }
 
+// One wave of resident blocks (the kernel's occupancy x SMs), fewer for small grids.
+template <typename R, int C, int MODE, int D>
+cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s) {
+    static int occ = 0;
+    if (occ == 0) {
+        // a small shared-memory share leaves the rest of L1 to cache the gathers
+        cudaFuncSetAttribute(parabolic_step_kernel<R, C, MODE, D>, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, parabolic_step_kernel<R, C, MODE, D>, 256, 0);
+        if (occ < 1) occ = 1;
+    }
+    const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), (unsigned)occ * (unsigned)device_sm_count());
+    if (nb) parabolic_step_kernel<R, C, MODE, D><<<nb, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename R, int C, int D>
+cudaError_t launch_parabolic_d(const StepArgs& a, int mode, cudaStream_t s) {
+    switch (mode) {
+        case GPE_MODE_LEAPFROG: return launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, D>(a, s);
+        case GPE_MODE_EULER: return launch_parabolic_m<R, C, GPE_MODE_EULER, D>(a, s);
+        default: return launch_parabolic_m<R, C, GPE_MODE_ITP, D>(a, s);
+    }
+}
+
 template <typename R, int C>
 cudaError_t launch_parabolic(const StepArgs& a, int mode, cudaStream_t s) {
-    const unsigned nb = nblocks(a.total, 256);
-    if (nb == 0) return cudaSuccess;
-    switch (mode) {
-        case GPE_MODE_LEAPFROG: parabolic_step_kernel<R, C, GPE_MODE_LEAPFROG><<<nb, 256, 0, s>>>(a); break;
-        case GPE_MODE_EULER: parabolic_step_kernel<R, C, GPE_MODE_EULER><<<nb, 256, 0, s>>>(a); break;
-        default: parabolic_step_kernel<R, C, GPE_MODE_ITP><<<nb, 256, 0, s>>>(a); break;
+    if (a.total == 0) return cudaSuccess;
+    if constexpr (C <= 3) {
+        if (a.tab.uniform_deg == 4) return launch_parabolic_d<R, C, 4>(a, mode, s);
     }
-    return cudaGetLastError();
+    return launch_parabolic_d<R, C, 0>(a, mode, s);
 }
 
 // kinds of hyperbolic launches

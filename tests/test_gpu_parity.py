@@ -611,11 +611,22 @@ def test_march_kernel(gpu, name, C, dims, shape, prec):
     _close(go, odd, prec, "odd")
 
 
+@pytest.mark.parametrize("name,C,want", [("bcc", 1, capi.KERNEL_GATHER), ("bcc", 5, capi.KERNEL_GATHER),
+                                         ("fcc", 3, capi.KERNEL_GATHER), ("a15", 3, capi.KERNEL_GATHER),
+                                         ("c15", 5, capi.KERNEL_GATHER), ("fcc", 1, capi.KERNEL_GATHER)])
+def test_automatic_kernel_choice(gpu, name, C, want):
+    """The automatic choice is the grid-stride gather kernel on every lattice."""
+    lat = capi.Lattice(name)
+    with Stepper(lat, _params(lat, C, capi.FP32, (6, 4, 4))) as s:
+        assert s.get_tuning(capi.TUNE_KERNEL) == want
+
+
 def test_kernel_choice_on_config2_shape(gpu):
     lat = capi.Lattice("bcc")
     p = _params(lat, 3, capi.FP32, (96, 96, 96))
     with Stepper(lat, p) as s:
-        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_TILE
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER  # the grid-stride gather kernel
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_TILE)
         assert s.get_tuning(capi.TUNE_TILE_CELLS) == 16
         s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_ROWS)
         assert s.get_tuning(capi.TUNE_TILE_CELLS) == 8
