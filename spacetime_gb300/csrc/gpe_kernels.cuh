@@ -366,6 +366,10 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
     ld_node<R, C, true>(own, prv);
 #pragma unroll
     for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
+    char* nxt = next + cell_off + l * node_bytes;
+    // leapfrog: the old next record is loaded up front, in flight with the gathers
+    Cx<R> nv[C];
+    if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
     // DEC Laplacian, sum_f w_f (psi_nb - psi) (Spin1GpeBCC.cu:835-865)
     if constexpr (D > 0) {
         int32_t off[D];
@@ -399,12 +403,32 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
         }
     } else {
         const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
-        for (int f = f0; f < f1; ++f) {
-            Cx<R> v[C];
-            ld_node<R, C, true>(base + st.nb_off[f], v);
-            const R w = st.w[f];
+        if constexpr (C == 1) {
+            // scalars: groups of 4 entries, the loads of a group issued together (rows
+            // of mixed length, e.g. FCC's 4 and 8; for spinors the registers this
+            // takes cost more occupancy than it gains)
+            for (int f = f0; f < f1; f += 4) {
+                Cx<R> v[4][C];
 #pragma unroll
-            for (int s = 0; s < C; ++s) H[s] += w * (v[s] - prv[s]);
+                for (int k = 0; k < 4; ++k)
+                    if (f + k < f1) ld_node<R, C, true>(base + st.nb_off[f + k], v[k]);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (f + k < f1) {
+                        const R w = st.w[f + k];
+#pragma unroll
+                        for (int s = 0; s < C; ++s) H[s] += w * (v[k][s] - prv[s]);
+                    }
+                }
+            }
+        } else {
+            for (int f = f0; f < f1; ++f) {
+                Cx<R> v[C];
+                ld_node<R, C, true>(base + st.nb_off[f], v);
+                const R w = st.w[f];
+#pragma unroll
+                for (int s = 0; s < C; ++s) H[s] += w * (v[s] - prv[s]);
+            }
         }
     }
     R r[3];
@@ -413,11 +437,8 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
     r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + st.pos[3 * l + 2]);
     const R pot = trap<R>(P, r);
     local_terms<R, C>(P, r, pot, MODE, false, prv, H);
-    char* nxt = next + cell_off + l * node_bytes;
     if constexpr (MODE == GPE_MODE_LEAPFROG) {
-        // next += 2 dt (-i H), the whole record read and written at once
-        Cx<R> nv[C];
-        ld_node<R, C, false>(nxt, nv);
+        // next += 2 dt (-i H), the whole record written at once
 #pragma unroll
         for (int s = 0; s < C; ++s) nv[s] += ((R)2 * P.dt) * cx<R>(H[s].y, -H[s].x);
         st_node<R, C>(nxt, nv);
