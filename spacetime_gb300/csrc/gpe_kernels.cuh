@@ -350,6 +350,93 @@ __device__ __forceinline__ void write_update(int mode, R dt, char* nxt, char* hp
 
 // ---------------------------------------------------------------- parabolic
 
+// A node's stencil entries and position, for nodes with D entries each.
+template <typename R, int D>
+struct NodeTab {
+    int32_t off[D];
+    R w[D];
+    R pos[3];
+};
+
+template <typename R, int D>
+__device__ __forceinline__ NodeTab<R, D> node_tab(const SmemTables<R>& st, uint32_t l) {
+    NodeTab<R, D> t;
+    if constexpr (D == 4) {
+        // one 16-byte shared load for the offsets, one or two for the weights
+        const int4 o4 = *reinterpret_cast<const int4*>(st.nb_off + l * 4);
+        t.off[0] = o4.x; t.off[1] = o4.y; t.off[2] = o4.z; t.off[3] = o4.w;
+        if constexpr (sizeof(R) == 4) {
+            const float4 w4 = *reinterpret_cast<const float4*>(st.w + l * 4);
+            t.w[0] = w4.x; t.w[1] = w4.y; t.w[2] = w4.z; t.w[3] = w4.w;
+        } else {
+            const double2 wa = *reinterpret_cast<const double2*>(st.w + l * 4);
+            const double2 wb = *reinterpret_cast<const double2*>(st.w + l * 4 + 2);
+            t.w[0] = wa.x; t.w[1] = wa.y; t.w[2] = wb.x; t.w[3] = wb.y;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            t.off[k] = st.nb_off[l * D + k];
+            t.w[k] = st.w[l * D + k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) t.pos[k] = st.pos[3 * l + k];
+    return t;
+}
+
+// The local terms and the time update of one node, given its Laplacian sum in H
+// (Spin1GpeBCC.cu:867-916).  nv: the old next record (leapfrog).
+template <typename R, int C, int MODE>
+__device__ __forceinline__ void node_finish(const PhysR<R>& P, const R pos[3], uint32_t x, uint32_t y, uint32_t z,
+                                            const Cx<R>* prv, Cx<R>* H, Cx<R>* nv, char* nxt, char* hp) {
+    R r[3];
+    r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + pos[0]);
+    r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + pos[1]);
+    r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + pos[2]);
+    const R pot = trap<R>(P, r);
+    local_terms<R, C>(P, r, pot, MODE, false, prv, H);
+    if constexpr (MODE == GPE_MODE_LEAPFROG) {
+        // next += 2 dt (-i H), the whole record written at once
+#pragma unroll
+        for (int s = 0; s < C; ++s) nv[s] += ((R)2 * P.dt) * cx<R>(H[s].y, -H[s].x);
+        st_node<R, C>(nxt, nv);
+    } else {
+        write_update<R, C>(MODE, P.dt, nxt, hp, prv, H);
+    }
+}
+
+// One node of a parabolic step whose D (> 0) stencil entries are given: the DEC
+// Laplacian gather with all D neighbour loads issued together, the local terms
+// and the time update.  prev/next/hpsi are the buffers' interior pointers;
+// (x, y, z) the cell, l the node.
+template <typename R, int C, int MODE, int D>
+__device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R, D>& t, const PhysR<R>& P,
+                                                 const char* prev, char* next, char* hpsi, uint32_t x, uint32_t y,
+                                                 uint32_t z, uint32_t l) {
+    const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
+    const char* base = prev + cell_off;
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    Cx<R> prv[C], H[C], nv[C];
+    ld_node<R, C, true>(base + l * node_bytes, prv);
+    char* nxt = next + cell_off + l * node_bytes;
+    // leapfrog: the old next record is loaded up front, in flight with the gathers
+    if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
+    // DEC Laplacian, sum_f w_f (psi_nb - psi) (Spin1GpeBCC.cu:835-865)
+    Cx<R> v[D][C];
+#pragma unroll
+    for (int k = 0; k < D; ++k) ld_node<R, C, true>(base + t.off[k], v[k]);
+#pragma unroll
+    for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+#pragma unroll
+        for (int s = 0; s < C; ++s) H[s] += t.w[k] * (v[k][s] - prv[s]);
+    }
+    char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
+    node_finish<R, C, MODE>(P, t.pos, x, y, z, prv, H, nv, nxt, hp);
+}
+
 // One node of a parabolic step: the DEC Laplacian gather, the local terms and the
 // time update (Spin1GpeBCC.cu:835-916).  prev/next/hpsi are the buffers' interior
 // pointers; (x, y, z) the cell, l the node.  D > 0: every node has D stencil
@@ -357,51 +444,18 @@ __device__ __forceinline__ void write_update(int mode, R dt, char* nxt, char* hp
 template <typename R, int C, int MODE, int D = 0>
 __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R>& st, const PhysR<R>& P, const char* prev,
                                                char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l) {
-    const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
-    const char* base = prev + cell_off;
-    const uint32_t node_bytes = C * 2 * sizeof(R);
-    const char* own = base + l * node_bytes;
-
-    Cx<R> prv[C], H[C];
-    ld_node<R, C, true>(own, prv);
-#pragma unroll
-    for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
-    char* nxt = next + cell_off + l * node_bytes;
-    // leapfrog: the old next record is loaded up front, in flight with the gathers
-    Cx<R> nv[C];
-    if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
-    // DEC Laplacian, sum_f w_f (psi_nb - psi) (Spin1GpeBCC.cu:835-865)
     if constexpr (D > 0) {
-        int32_t off[D];
-        R wt[D];
-        if constexpr (D == 4) {
-            // one 16-byte shared load for the offsets, one or two for the weights
-            const int4 o4 = *reinterpret_cast<const int4*>(st.nb_off + l * 4);
-            off[0] = o4.x; off[1] = o4.y; off[2] = o4.z; off[3] = o4.w;
-            if constexpr (sizeof(R) == 4) {
-                const float4 w4 = *reinterpret_cast<const float4*>(st.w + l * 4);
-                wt[0] = w4.x; wt[1] = w4.y; wt[2] = w4.z; wt[3] = w4.w;
-            } else {
-                const double2 wa = *reinterpret_cast<const double2*>(st.w + l * 4);
-                const double2 wb = *reinterpret_cast<const double2*>(st.w + l * 4 + 2);
-                wt[0] = wa.x; wt[1] = wa.y; wt[2] = wb.x; wt[3] = wb.y;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < D; ++k) {
-                off[k] = st.nb_off[l * D + k];
-                wt[k] = st.w[l * D + k];
-            }
-        }
-        Cx<R> v[D][C];
-#pragma unroll
-        for (int k = 0; k < D; ++k) ld_node<R, C, true>(base + off[k], v[k]);
-#pragma unroll
-        for (int k = 0; k < D; ++k) {
-#pragma unroll
-            for (int s = 0; s < C; ++s) H[s] += wt[k] * (v[k][s] - prv[s]);
-        }
+        parabolic_node_t<R, C, MODE, D>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l);
     } else {
+        const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
+        const char* base = prev + cell_off;
+        const uint32_t node_bytes = C * 2 * sizeof(R);
+        Cx<R> prv[C], H[C], nv[C];
+        ld_node<R, C, true>(base + l * node_bytes, prv);
+#pragma unroll
+        for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
+        char* nxt = next + cell_off + l * node_bytes;
+        if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
         const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
         if constexpr (C == 1) {
             // scalars: groups of 4 entries, the loads of a group issued together (rows
@@ -430,21 +484,9 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
                 for (int s = 0; s < C; ++s) H[s] += w * (v[s] - prv[s]);
             }
         }
-    }
-    R r[3];
-    r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
-    r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + st.pos[3 * l + 1]);
-    r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + st.pos[3 * l + 2]);
-    const R pot = trap<R>(P, r);
-    local_terms<R, C>(P, r, pot, MODE, false, prv, H);
-    if constexpr (MODE == GPE_MODE_LEAPFROG) {
-        // next += 2 dt (-i H), the whole record written at once
-#pragma unroll
-        for (int s = 0; s < C; ++s) nv[s] += ((R)2 * P.dt) * cx<R>(H[s].y, -H[s].x);
-        st_node<R, C>(nxt, nv);
-    } else {
+        const R pos[3] = {st.pos[3 * l + 0], st.pos[3 * l + 1], st.pos[3 * l + 2]};
         char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
-        write_update<R, C>(MODE, P.dt, nxt, hp, prv, H);
+        node_finish<R, C, MODE>(P, pos, x, y, z, prv, H, nv, nxt, hp);
     }
 }
 
@@ -466,6 +508,30 @@ __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
         const uint32_t z = fdiv(row, a.divY);
         const uint32_t y = row - z * a.g.Y;
         parabolic_node<R, C, MODE, D>(a.g, st, P, a.prev, a.next, a.hpsi, x, y, z, l);
+    }
+}
+
+// The same update for nodes of D stencil entries, on a grid whose stride is a
+// multiple of V: a thread keeps one node index l on every pass, so its entries
+// and position are loaded once into registers instead of from shared memory for
+// every node.
+template <typename R, int C, int MODE, int D>
+__global__ void __launch_bounds__(256) parabolic_fixed_kernel(StepArgs a) {
+    __shared__ SmemTables<R> st;
+    load_tables<R>(st, a);
+    __syncthreads();
+    const PhysR<R>& P = make_phys<R>(a);
+    uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= a.total) return;
+    const uint32_t l = (uint32_t)gid - fdiv((uint32_t)gid, a.divV) * a.g.V;
+    const NodeTab<R, D> t = node_tab<R, D>(st, l);
+    for (; gid < a.total; gid += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)gid;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t x = fdiv(i - row * a.row_items, a.divV);
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        parabolic_node_t<R, C, MODE, D>(a.g, t, P, a.prev, a.next, a.hpsi, x, y, z, l);
     }
 }
 
@@ -854,6 +920,29 @@ inline unsigned nblocks(uint64_t items, unsigned bs) { return (unsigned)((items 
 // One wave of resident blocks (the kernel's occupancy x SMs), fewer for small grids.
 template <typename R, int C, int MODE, int D>
 cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s) {
+    if constexpr (D > 0) {
+        // the largest multiple of V / gcd(V, 256) blocks within one wave: the grid
+        // stride is then a multiple of V
+        static int occ_f = 0;
+        if (occ_f == 0) {
+            cudaFuncSetAttribute(parabolic_fixed_kernel<R, C, MODE, D>, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, parabolic_fixed_kernel<R, C, MODE, D>, 256, 0);
+            if (occ_f < 1) occ_f = 1;
+        }
+        uint32_t gv = a.g.V, gb = 256;
+        while (gb) {
+            const uint32_t r = gv % gb;
+            gv = gb;
+            gb = r;
+        }
+        const uint32_t m = a.g.V / gv;
+        const uint64_t wave = std::min<uint64_t>((uint64_t)occ_f * (unsigned)device_sm_count(), (a.total + 255) / 256);
+        const unsigned nb = (unsigned)(wave / m * m);
+        if (nb > 0) {
+            parabolic_fixed_kernel<R, C, MODE, D><<<nb, 256, 0, s>>>(a);
+            return cudaGetLastError();
+        }
+    }
     static int occ = 0;
     if (occ == 0) {
         // a small shared-memory share leaves the rest of L1 to cache the gathers
