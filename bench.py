@@ -577,7 +577,7 @@ def run_gpu(args):
         s.step(INNER)
         s._nsteps += INNER
 
-    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_step_kernel<float,3,LEAPFROG,4>",
+    kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_fixed_kernel<float,3,LEAPFROG,4>",
                    capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
