@@ -174,12 +174,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoi
         const uint32_t node_bytes = C * 2 * sizeof(R);
         const char* abase = j.a_prev + cell_off;
         Cx<R> b[C], u[C];
+        ld_node<R, C, true>(abase + l * node_bytes, b);  // whole records: (C+1)/2 loads in FP32
+        ld_node<R, C, true>(j.psi + cell_off + l * node_bytes, u);
 #pragma unroll
-        for (int c = 0; c < C; ++c) {
-            const Cx<R> av = ldc<R>(abase + l * node_bytes + c * 2 * sizeof(R));
-            b[c] = cx<R>(-av.y, av.x);
-            u[c] = ldc<R>(j.psi + cell_off + l * node_bytes + c * 2 * sizeof(R));
-        }
+        for (int c = 0; c < C; ++c) b[c] = cx<R>(-b[c].y, b[c].x);
         const PhysR<R>& P = make_phys<R>(a);
         R r[3];
         r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + st.pos[3 * l + 0]);
@@ -192,14 +190,27 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoi
 #pragma unroll
             for (int c = 0; c < C; ++c) K[c] = cx<R>((R)0, (R)0);
             R diag = 0;
-            for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
-                const char* nb = abase + st.nb_off[f];
-                diag += st.w[f];
-                const R wt = wT[f];
+            const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
+            if (a.tab.uniform_deg == 4 && C <= 3) {
+                // 4 entries: the 4 neighbour records are loaded before they are used
+                Cx<R> v[4][C];
 #pragma unroll
-                for (int c = 0; c < C; ++c) {
-                    const Cx<R> av = ldc<R>(nb + c * 2 * sizeof(R));
-                    K[c] += wt * cx<R>(-av.y, av.x);
+                for (int k = 0; k < 4; ++k) ld_node<R, C, true>(abase + st.nb_off[f0 + k], v[k]);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    diag += st.w[f0 + k];
+                    const R wt = wT[f0 + k];
+#pragma unroll
+                    for (int c = 0; c < C; ++c) K[c] += wt * cx<R>(-v[k][c].y, v[k][c].x);
+                }
+            } else {
+                for (int f = f0; f < f1; ++f) {
+                    Cx<R> av[C];
+                    ld_node<R, C, true>(abase + st.nb_off[f], av);
+                    diag += st.w[f];
+                    const R wt = wT[f];
+#pragma unroll
+                    for (int c = 0; c < C; ++c) K[c] += wt * cx<R>(-av[c].y, av[c].x);
                 }
             }
             // (dh/du)^T b.  Apart from three-body loss, h = dE/d(conj u) for a real
@@ -235,13 +246,14 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoi
             R fac;
             if constexpr (sizeof(R) == 4) fac = j.factor32;
             else fac = j.factor;
+            Cx<R> v[C];
+            ld_node<R, C, false>(o, v);
 #pragma unroll
             for (int c = 0; c < C; ++c) {
-                Cx<R> v = ldc_rw<R>(o + c * 2 * sizeof(R));
-                v.x += fac * (K[c].x - diag * b[c].x + g[c].x);
-                v.y += fac * (K[c].y - diag * b[c].y + g[c].y);
-                stc<R>(o + c * 2 * sizeof(R), v);
+                v[c].x += fac * (K[c].x - diag * b[c].x + g[c].x);
+                v[c].y += fac * (K[c].y - diag * b[c].y + g[c].y);
             }
+            st_node<R, C>(o, v);
         }
         // field parameters.  h depends on Bb only through the Zeeman term (B.F) u,
         // so dh/dBb_k = F_k u: the local terms with every coefficient zero except
