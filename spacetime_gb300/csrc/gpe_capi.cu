@@ -216,6 +216,13 @@ static gpe_status build_tables(gpe_handle* h) {
     for (int l = 0; l < L.V; ++l)
         if (L.row_ptr[l + 1] - L.row_ptr[l] != udeg) udeg = 0;
     h->tab.uniform_deg = udeg;
+    // rows of different lengths, all multiples of 4 (FCC's 4 and 8): read in vectors of 4
+    bool quad = udeg == 0;
+    for (int l = 0; l < L.V && quad; ++l) {
+        const int len = L.row_ptr[l + 1] - L.row_ptr[l];
+        quad = len > 0 && len % 4 == 0;
+    }
+    h->tab.quad_rows = quad ? 1 : 0;
     // rows (dy, dz) touched by the stencil, the own row first
     h->nrows = 1;
     h->rdy[0] = h->rdz[0] = 0;

@@ -125,6 +125,7 @@ struct DevTables {
     int entries;
     int faces;
     int uniform_deg;      // > 0 when every node has the same number of entries
+    int quad_rows;        // 1 when rows differ in length and every row is a positive multiple of 4 long
 };
 
 struct StepArgs {

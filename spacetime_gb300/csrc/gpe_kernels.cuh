@@ -359,30 +359,39 @@ struct NodeTab {
 };
 
 template <typename R, int D>
-__device__ __forceinline__ NodeTab<R, D> node_tab(const SmemTables<R>& st, uint32_t l) {
+__device__ __forceinline__ NodeTab<R, D> node_tab(const SmemTables<R>& st, uint32_t l, int f0) {
     NodeTab<R, D> t;
-    if constexpr (D == 4) {
-        // one 16-byte shared load for the offsets, one or two for the weights
-        const int4 o4 = *reinterpret_cast<const int4*>(st.nb_off + l * 4);
-        t.off[0] = o4.x; t.off[1] = o4.y; t.off[2] = o4.z; t.off[3] = o4.w;
-        if constexpr (sizeof(R) == 4) {
-            const float4 w4 = *reinterpret_cast<const float4*>(st.w + l * 4);
-            t.w[0] = w4.x; t.w[1] = w4.y; t.w[2] = w4.z; t.w[3] = w4.w;
-        } else {
-            const double2 wa = *reinterpret_cast<const double2*>(st.w + l * 4);
-            const double2 wb = *reinterpret_cast<const double2*>(st.w + l * 4 + 2);
-            t.w[0] = wa.x; t.w[1] = wa.y; t.w[2] = wb.x; t.w[3] = wb.y;
+    if constexpr (D % 4 == 0) {
+        // f0 a multiple of 4: one 16-byte shared load per 4 offsets, one or two per 4 weights
+#pragma unroll
+        for (int q = 0; q < D; q += 4) {
+            const int4 o4 = *reinterpret_cast<const int4*>(st.nb_off + f0 + q);
+            t.off[q] = o4.x; t.off[q + 1] = o4.y; t.off[q + 2] = o4.z; t.off[q + 3] = o4.w;
+            if constexpr (sizeof(R) == 4) {
+                const float4 w4 = *reinterpret_cast<const float4*>(st.w + f0 + q);
+                t.w[q] = w4.x; t.w[q + 1] = w4.y; t.w[q + 2] = w4.z; t.w[q + 3] = w4.w;
+            } else {
+                const double2 wa = *reinterpret_cast<const double2*>(st.w + f0 + q);
+                const double2 wb = *reinterpret_cast<const double2*>(st.w + f0 + q + 2);
+                t.w[q] = wa.x; t.w[q + 1] = wa.y; t.w[q + 2] = wb.x; t.w[q + 3] = wb.y;
+            }
         }
     } else {
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-            t.off[k] = st.nb_off[l * D + k];
-            t.w[k] = st.w[l * D + k];
+            t.off[k] = st.nb_off[f0 + k];
+            t.w[k] = st.w[f0 + k];
         }
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) t.pos[k] = st.pos[3 * l + k];
     return t;
+}
+
+// Node l of a lattice whose nodes all have D entries.
+template <typename R, int D>
+__device__ __forceinline__ NodeTab<R, D> node_tab(const SmemTables<R>& st, uint32_t l) {
+    return node_tab<R, D>(st, l, (int)l * D);
 }
 
 // The local terms and the time update of one node, given its Laplacian sum in H
@@ -406,14 +415,17 @@ __device__ __forceinline__ void node_finish(const PhysR<R>& P, const R pos[3], u
     }
 }
 
-// One node of a parabolic step whose D (> 0) stencil entries are given: the DEC
-// Laplacian gather with all D neighbour loads issued together, the local terms
-// and the time update.  prev/next/hpsi are the buffers' interior pointers;
-// (x, y, z) the cell, l the node.
-template <typename R, int C, int MODE, int D>
+// One node of a parabolic step whose first D (> 0) stencil entries are given in t:
+// the DEC Laplacian gather, the neighbour loads issued G at a time, then the local
+// terms and the time update.  MORE: the node's further entries f_more .. f_end - 1
+// (a multiple of 4 of them, f_more a multiple of 4) come from the shared tables, 4
+// loads at a time (FCC's octahedra: 8 entries beside the tetrahedra's 4).
+// prev/next/hpsi are the buffers' interior pointers; (x, y, z) the cell, l the node.
+template <typename R, int C, int MODE, int D, int G = D, bool MORE = false>
 __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R, D>& t, const PhysR<R>& P,
                                                  const char* prev, char* next, char* hpsi, uint32_t x, uint32_t y,
-                                                 uint32_t z, uint32_t l) {
+                                                 uint32_t z, uint32_t l, const SmemTables<R>* st = nullptr,
+                                                 int f_more = 0, int f_end = 0) {
     const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
     const char* base = prev + cell_off;
     const uint32_t node_bytes = C * 2 * sizeof(R);
@@ -422,16 +434,49 @@ __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R,
     char* nxt = next + cell_off + l * node_bytes;
     // leapfrog: the old next record is loaded up front, in flight with the gathers
     if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
-    // DEC Laplacian, sum_f w_f (psi_nb - psi) (Spin1GpeBCC.cu:835-865)
-    Cx<R> v[D][C];
-#pragma unroll
-    for (int k = 0; k < D; ++k) ld_node<R, C, true>(base + t.off[k], v[k]);
+    // DEC Laplacian, sum_f w_f (psi_nb - psi) in entry order (Spin1GpeBCC.cu:835-865)
 #pragma unroll
     for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
+    for (int k0 = 0; k0 < D; k0 += G) {
+        Cx<R> v[G][C];
 #pragma unroll
-        for (int s = 0; s < C; ++s) H[s] += t.w[k] * (v[k][s] - prv[s]);
+        for (int k = 0; k < G; ++k)
+            if (k0 + k < D) ld_node<R, C, true>(base + t.off[k0 + k], v[k]);
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+            if (k0 + k < D) {
+#pragma unroll
+                for (int s = 0; s < C; ++s) H[s] += t.w[k0 + k] * (v[k][s] - prv[s]);
+            }
+        }
+    }
+    if constexpr (MORE) {
+        static_assert(4 % G == 0, "MORE: groups of 4 entries issued G at a time");
+        for (int f = f_more; f < f_end; f += 4) {
+            const int4 o4 = *reinterpret_cast<const int4*>(st->nb_off + f);
+            const int32_t o[4] = {o4.x, o4.y, o4.z, o4.w};
+            R w[4];
+            if constexpr (sizeof(R) == 4) {
+                const float4 w4 = *reinterpret_cast<const float4*>(st->w + f);
+                w[0] = w4.x; w[1] = w4.y; w[2] = w4.z; w[3] = w4.w;
+            } else {
+                const double2 wa = *reinterpret_cast<const double2*>(st->w + f);
+                const double2 wb = *reinterpret_cast<const double2*>(st->w + f + 2);
+                w[0] = wa.x; w[1] = wa.y; w[2] = wb.x; w[3] = wb.y;
+            }
+#pragma unroll
+            for (int h = 0; h < 4; h += G) {
+                Cx<R> v[G][C];
+#pragma unroll
+                for (int k = 0; k < G; ++k) ld_node<R, C, true>(base + o[h + k], v[k]);
+#pragma unroll
+                for (int k = 0; k < G; ++k) {
+#pragma unroll
+                    for (int s = 0; s < C; ++s) H[s] += w[h + k] * (v[k][s] - prv[s]);
+                }
+            }
+        }
     }
     char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
     node_finish<R, C, MODE>(P, t.pos, x, y, z, prv, H, nv, nxt, hp);
@@ -511,11 +556,12 @@ __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
     }
 }
 
-// The same update for nodes of D stencil entries, on a grid whose stride is a
-// multiple of V: a thread keeps one node index l on every pass, so its entries
-// and position are loaded once into registers instead of from shared memory for
-// every node.
-template <typename R, int C, int MODE, int D>
+// The same update on a grid whose stride is a multiple of V: a thread keeps one
+// node index l on every pass, so its first D entries and its position are loaded
+// once into registers instead of from shared memory for every node.  Every node has
+// D entries, or (MORE) a multiple of 4 of them, the entries past the first D read
+// from the shared tables.  G: neighbour loads issued together.
+template <typename R, int C, int MODE, int D, int G, bool MORE>
 __global__ void __launch_bounds__(256) parabolic_fixed_kernel(StepArgs a) {
     __shared__ SmemTables<R> st;
     load_tables<R>(st, a);
@@ -524,14 +570,16 @@ __global__ void __launch_bounds__(256) parabolic_fixed_kernel(StepArgs a) {
     uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= a.total) return;
     const uint32_t l = (uint32_t)gid - fdiv((uint32_t)gid, a.divV) * a.g.V;
-    const NodeTab<R, D> t = node_tab<R, D>(st, l);
+    const int f0 = MORE ? st.row_ptr[l] : (int)l * D;
+    const int f_end = MORE ? st.row_ptr[l + 1] : 0;
+    const NodeTab<R, D> t = node_tab<R, D>(st, l, f0);
     for (; gid < a.total; gid += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)gid;
         const uint32_t row = fdiv(i, a.divRow);
         const uint32_t x = fdiv(i - row * a.row_items, a.divV);
         const uint32_t z = fdiv(row, a.divY);
         const uint32_t y = row - z * a.g.Y;
-        parabolic_node_t<R, C, MODE, D>(a.g, t, P, a.prev, a.next, a.hpsi, x, y, z, l);
+        parabolic_node_t<R, C, MODE, D, G, MORE>(a.g, t, P, a.prev, a.next, a.hpsi, x, y, z, l, &st, f0 + D, f_end);
     }
 }
 
@@ -918,15 +966,17 @@ __global__ void __launch_bounds__(256) scale_kernel(StepArgs a, const double* no
 inline unsigned nblocks(uint64_t items, unsigned bs) { return (unsigned)((items + bs - 1) / bs); }
 
 // One wave of resident blocks (the kernel's occupancy x SMs), fewer for small grids.
-template <typename R, int C, int MODE, int D>
+// D > 0: the fixed-node kernel (see parabolic_fixed_kernel for D, G, MORE).
+template <typename R, int C, int MODE, int D, int G, bool MORE>
 cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s) {
     if constexpr (D > 0) {
         // the largest multiple of V / gcd(V, 256) blocks within one wave: the grid
         // stride is then a multiple of V
         static int occ_f = 0;
         if (occ_f == 0) {
-            cudaFuncSetAttribute(parabolic_fixed_kernel<R, C, MODE, D>, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, parabolic_fixed_kernel<R, C, MODE, D>, 256, 0);
+            cudaFuncSetAttribute(parabolic_fixed_kernel<R, C, MODE, D, G, MORE>,
+                                 cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, parabolic_fixed_kernel<R, C, MODE, D, G, MORE>, 256, 0);
             if (occ_f < 1) occ_f = 1;
         }
         uint32_t gv = a.g.V, gb = 256;
@@ -939,36 +989,48 @@ cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s) {
         const uint64_t wave = std::min<uint64_t>((uint64_t)occ_f * (unsigned)device_sm_count(), (a.total + 255) / 256);
         const unsigned nb = (unsigned)(wave / m * m);
         if (nb > 0) {
-            parabolic_fixed_kernel<R, C, MODE, D><<<nb, 256, 0, s>>>(a);
+            parabolic_fixed_kernel<R, C, MODE, D, G, MORE><<<nb, 256, 0, s>>>(a);
             return cudaGetLastError();
         }
     }
+    // grids smaller than V / gcd(V, 256) blocks: the grid-stride kernel (the
+    // 4-entry form where every node has 4 entries)
+    constexpr int DS = (D == 4 && !MORE) ? 4 : 0;
     static int occ = 0;
     if (occ == 0) {
         // a small shared-memory share leaves the rest of L1 to cache the gathers
-        cudaFuncSetAttribute(parabolic_step_kernel<R, C, MODE, D>, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, parabolic_step_kernel<R, C, MODE, D>, 256, 0);
+        cudaFuncSetAttribute(parabolic_step_kernel<R, C, MODE, DS>, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, parabolic_step_kernel<R, C, MODE, DS>, 256, 0);
         if (occ < 1) occ = 1;
     }
     const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), (unsigned)occ * (unsigned)device_sm_count());
-    if (nb) parabolic_step_kernel<R, C, MODE, D><<<nb, 256, 0, s>>>(a);
+    if (nb) parabolic_step_kernel<R, C, MODE, DS><<<nb, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-template <typename R, int C, int D>
+template <typename R, int C, int D, int G = D, bool MORE = false>
 cudaError_t launch_parabolic_d(const StepArgs& a, int mode, cudaStream_t s) {
     switch (mode) {
-        case GPE_MODE_LEAPFROG: return launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, D>(a, s);
-        case GPE_MODE_EULER: return launch_parabolic_m<R, C, GPE_MODE_EULER, D>(a, s);
-        default: return launch_parabolic_m<R, C, GPE_MODE_ITP, D>(a, s);
+        case GPE_MODE_LEAPFROG: return launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, D, G, MORE>(a, s);
+        case GPE_MODE_EULER: return launch_parabolic_m<R, C, GPE_MODE_EULER, D, G, MORE>(a, s);
+        default: return launch_parabolic_m<R, C, GPE_MODE_ITP, D, G, MORE>(a, s);
     }
 }
 
+// The kernel form by the lattice's row lengths: every node 4 entries (BCC, A15,
+// C15, Z), every row a multiple of 4 long (FCC: 4 and 8), every node 6 entries
+// (the cube); others the general grid-stride kernel.
 template <typename R, int C>
 cudaError_t launch_parabolic(const StepArgs& a, int mode, cudaStream_t s) {
     if (a.total == 0) return cudaSuccess;
     if constexpr (C <= 3) {
         if (a.tab.uniform_deg == 4) return launch_parabolic_d<R, C, 4>(a, mode, s);
+        if (a.tab.quad_rows) return launch_parabolic_d<R, C, 4, 4, true>(a, mode, s);
+        if (a.tab.uniform_deg == 6) return launch_parabolic_d<R, C, 6, (C == 1 ? 6 : 3)>(a, mode, s);
+    } else {
+        if (a.tab.uniform_deg == 4) return launch_parabolic_d<R, C, 4, 2>(a, mode, s);
+        if (a.tab.quad_rows) return launch_parabolic_d<R, C, 4, 2, true>(a, mode, s);
+        if (a.tab.uniform_deg == 6) return launch_parabolic_d<R, C, 6, 2>(a, mode, s);
     }
     return launch_parabolic_d<R, C, 0>(a, mode, s);
 }

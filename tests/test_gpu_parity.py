@@ -39,8 +39,8 @@ def _close(gpu, ref, prec, what=""):
 
 CASES = [
     ("bcc", 1), ("bcc", 3), ("bcc", 5),
-    ("bcc227", 1), ("cube", 1), ("cube", 3),
-    ("fcc", 1), ("fcc", 3), ("a15", 1), ("a15", 3), ("c15", 1), ("c15", 5), ("z", 1), ("z", 3),
+    ("bcc227", 1), ("cube", 1), ("cube", 3), ("cube", 5),
+    ("fcc", 1), ("fcc", 3), ("fcc", 5), ("a15", 1), ("a15", 3), ("a15", 5), ("c15", 1), ("c15", 5), ("z", 1), ("z", 3),
 ]
 
 
