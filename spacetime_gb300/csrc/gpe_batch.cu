@@ -148,7 +148,7 @@ __device__ __forceinline__ void set_fields(PhysR<R>& P, const StepFieldsD& f) {
     P.trap_on = f.trap_on;
 }
 
-template <typename R, int C, int D>
+template <typename R, int C, int D, int G = D, bool MORE = false>
 __device__ __forceinline__ void batch_rows(const BatchMember& M, const SmemTables<R>& st, const PhysR<R>& P,
                                            const char* prev, char* next, uint32_t row0, uint32_t rows) {
     const uint32_t n = rows * M.row_items;
@@ -160,7 +160,7 @@ __device__ __forceinline__ void batch_rows(const BatchMember& M, const SmemTable
         const uint32_t row = row0 + rr;
         const uint32_t z = fdiv(row, M.divY);
         const uint32_t y = row - z * M.g.Y;
-        parabolic_node<R, C, GPE_MODE_LEAPFROG, D>(M.g, st, P, prev, next, nullptr, x, y, z, l);
+        parabolic_node<R, C, GPE_MODE_LEAPFROG, D, G, MORE>(M.g, st, P, prev, next, nullptr, x, y, z, l);
     }
 }
 
@@ -217,16 +217,20 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs A) {
             const int prev_slot = A.state[w.member].cur ^ (int)(k & 1);
             const char* prev = M.psi[prev_slot];
             char* next = M.psi[prev_slot ^ 1];
-            // members whose nodes all have 4 neighbours issue the 4 loads together
-            const bool d4 = M.tab.uniform_deg == 4;
+            // members whose nodes all have 4 neighbours issue the 4 loads together;
+            // rows of 4 and 8 (FCC) take their entries in vectors of 4
+            const bool d4 = M.tab.uniform_deg == 4, quad = M.tab.quad_rows != 0;
             if ((CMASK & 1) && M.C == 1) {
                 if (d4) batch_rows<R, 1, 4>(M, st, P, prev, next, w.row0, w.rows);
+                else if (quad) batch_rows<R, 1, 4, 4, true>(M, st, P, prev, next, w.row0, w.rows);
                 else batch_rows<R, 1, 0>(M, st, P, prev, next, w.row0, w.rows);
             } else if ((CMASK & 2) && M.C == 3) {
                 if (d4) batch_rows<R, 3, 4>(M, st, P, prev, next, w.row0, w.rows);
+                else if (quad) batch_rows<R, 3, 4, 4, true>(M, st, P, prev, next, w.row0, w.rows);
                 else batch_rows<R, 3, 0>(M, st, P, prev, next, w.row0, w.rows);
             } else if (CMASK & 4) {
-                batch_rows<R, 5, 0>(M, st, P, prev, next, w.row0, w.rows);
+                if (d4) batch_rows<R, 5, 4, 2>(M, st, P, prev, next, w.row0, w.rows);
+                else batch_rows<R, 5, 0>(M, st, P, prev, next, w.row0, w.rows);
             }
         }
         if (s + 1 < A.nsteps) {

@@ -485,12 +485,17 @@ __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R,
 // One node of a parabolic step: the DEC Laplacian gather, the local terms and the
 // time update (Spin1GpeBCC.cu:835-916).  prev/next/hpsi are the buffers' interior
 // pointers; (x, y, z) the cell, l the node.  D > 0: every node has D stencil
-// entries, and all D neighbour loads are issued before they are used.
-template <typename R, int C, int MODE, int D = 0>
+// entries (MORE: a multiple of 4, the first D taken as the node's table), the
+// neighbour loads issued G at a time.
+template <typename R, int C, int MODE, int D = 0, int G = D, bool MORE = false>
 __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R>& st, const PhysR<R>& P, const char* prev,
                                                char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l) {
-    if constexpr (D > 0) {
-        parabolic_node_t<R, C, MODE, D>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l);
+    if constexpr (D > 0 && MORE) {
+        const int f0 = st.row_ptr[l];
+        parabolic_node_t<R, C, MODE, D, G, true>(g, node_tab<R, D>(st, l, f0), P, prev, next, hpsi, x, y, z, l, &st,
+                                                 f0 + D, st.row_ptr[l + 1]);
+    } else if constexpr (D > 0) {
+        parabolic_node_t<R, C, MODE, D, G>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l);
     } else {
         const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
         const char* base = prev + cell_off;
