@@ -165,9 +165,10 @@ __device__ __forceinline__ void batch_rows(const BatchMember& M, const SmemTable
 }
 
 // CMASK: which component counts the batch holds (bit 0: 1, bit 1: 3, bit 2: 5), so
-// that a batch of scalar and spin-1 members does not carry spin-2 registers.
+// that a batch of scalar and spin-1 members does not carry spin-2 registers; such
+// FP32 batches fit 64 registers, 4 blocks per SM.
 template <typename R, int CMASK>
-__global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs A) {
+__global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4) ? 3 : 4) batch_kernel(BatchArgs A) {
     __shared__ SmemTables<R> st;
     __shared__ PhysR<R> P;
     __shared__ BatchMember M;
@@ -229,8 +230,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchArgs A) {
                 else if (quad) batch_rows<R, 3, 4, 4, true>(M, st, P, prev, next, w.row0, w.rows);
                 else batch_rows<R, 3, 0>(M, st, P, prev, next, w.row0, w.rows);
             } else if (CMASK & 4) {
-                if (d4) batch_rows<R, 5, 4, 2>(M, st, P, prev, next, w.row0, w.rows);
-                else batch_rows<R, 5, 0>(M, st, P, prev, next, w.row0, w.rows);
+                batch_rows<R, 5, 0>(M, st, P, prev, next, w.row0, w.rows);
             }
         }
         if (s + 1 < A.nsteps) {
