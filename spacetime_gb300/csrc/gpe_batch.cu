@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "gpe_handle.h"
@@ -45,7 +46,21 @@ struct BatchMember {
     FastDiv divV, divRow, divY;
     uint32_t row_items; // X * V
     int32_t C;
+    int32_t cslot;      // slot of the member's MemberConst, or -1
 };
+
+// The values an FP32 member's node loop reads for every node, kept in constant
+// memory: read through the constant cache, they cost none of the L1 bandwidth the
+// gathers are bound by (from shared memory they took about as many L1 wavefronts
+// as the gathers).  The step's fields stay in shared memory.
+struct MemberConst {
+    PhysR<float> p;
+    Grid g;
+    FastDiv divV, divRow, divY;
+    uint32_t row_items;
+};
+constexpr int kConstSlots = 256;
+__constant__ MemberConst c_members[kConstSlots];
 
 struct StepFieldsD {
     double bq, bb[3], bqq, bbq[3];
@@ -148,9 +163,13 @@ __device__ __forceinline__ void set_fields(PhysR<R>& P, const StepFieldsD& f) {
     P.trap_on = f.trap_on;
 }
 
-template <typename R, int C, int D, int G = D, bool MORE = false>
-__device__ __forceinline__ void batch_rows(const BatchMember& M, const SmemTables<R>& st, const PhysR<R>& P,
-                                           const char* prev, char* next, uint32_t row0, uint32_t rows) {
+// Rows row0 .. row0 + rows - 1 of a member.  K: the member's grid and divisors
+// (BatchMember in shared memory, or MemberConst in constant memory); P its
+// constants; F where the step's fields are read from (P if null).
+template <typename R, int C, int D, int G = D, bool MORE = false, typename MK>
+__device__ __forceinline__ void batch_rows(const MK& M, const SmemTables<R>& st, const PhysR<R>& P,
+                                           const PhysR<R>* F, const char* prev, char* next, uint32_t row0,
+                                           uint32_t rows) {
     const uint32_t n = rows * M.row_items;
     for (uint32_t i = threadIdx.x; i < n; i += kBatchThreads) {
         const uint32_t rr = fdiv(i, M.divRow);
@@ -160,15 +179,38 @@ __device__ __forceinline__ void batch_rows(const BatchMember& M, const SmemTable
         const uint32_t row = row0 + rr;
         const uint32_t z = fdiv(row, M.divY);
         const uint32_t y = row - z * M.g.Y;
-        parabolic_node<R, C, GPE_MODE_LEAPFROG, D, G, MORE>(M.g, st, P, prev, next, nullptr, x, y, z, l);
+        parabolic_node<R, C, GPE_MODE_LEAPFROG, D, G, MORE>(M.g, st, P, prev, next, nullptr, x, y, z, l, F);
+    }
+}
+
+// One work item: the member's kernel form by its spin and row lengths.  Members
+// whose nodes all have 4 neighbours issue the 4 loads together; rows of 4 and 8
+// (FCC) take their entries in vectors of 4.
+template <typename R, int CMASK, typename MK>
+__device__ __forceinline__ void batch_item(const BatchMember& M, const MK& K, const SmemTables<R>& st,
+                                           const PhysR<R>& P, const PhysR<R>* F, const char* prev, char* next,
+                                           uint32_t row0, uint32_t rows) {
+    const bool d4 = M.tab.uniform_deg == 4, quad = M.tab.quad_rows != 0;
+    if ((CMASK & 1) && M.C == 1) {
+        if (d4) batch_rows<R, 1, 4>(K, st, P, F, prev, next, row0, rows);
+        else if (quad) batch_rows<R, 1, 4, 4, true>(K, st, P, F, prev, next, row0, rows);
+        else batch_rows<R, 1, 0>(K, st, P, F, prev, next, row0, rows);
+    } else if ((CMASK & 2) && M.C == 3) {
+        if (d4) batch_rows<R, 3, 4>(K, st, P, F, prev, next, row0, rows);
+        else if (quad) batch_rows<R, 3, 4, 4, true>(K, st, P, F, prev, next, row0, rows);
+        else batch_rows<R, 3, 0>(K, st, P, F, prev, next, row0, rows);
+    } else if (CMASK & 4) {
+        batch_rows<R, 5, 0>(K, st, P, F, prev, next, row0, rows);
     }
 }
 
 // CMASK: which component counts the batch holds (bit 0: 1, bit 1: 3, bit 2: 5), so
 // that a batch of scalar and spin-1 members does not carry spin-2 registers; such
-// FP32 batches fit 64 registers, 4 blocks per SM.
-template <typename R, int CMASK>
+// FP32 batches fit 64 registers, 4 blocks per SM.  CONSTP (FP32): every member has
+// a MemberConst slot.
+template <typename R, int CMASK, bool CONSTP>
 __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4) ? 3 : 4) batch_kernel(BatchArgs A) {
+    static_assert(!CONSTP || sizeof(R) == 4, "constant-memory members are FP32");
     __shared__ SmemTables<R> st;
     __shared__ PhysR<R> P;
     __shared__ BatchMember M;
@@ -218,19 +260,11 @@ __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4
             const int prev_slot = A.state[w.member].cur ^ (int)(k & 1);
             const char* prev = M.psi[prev_slot];
             char* next = M.psi[prev_slot ^ 1];
-            // members whose nodes all have 4 neighbours issue the 4 loads together;
-            // rows of 4 and 8 (FCC) take their entries in vectors of 4
-            const bool d4 = M.tab.uniform_deg == 4, quad = M.tab.quad_rows != 0;
-            if ((CMASK & 1) && M.C == 1) {
-                if (d4) batch_rows<R, 1, 4>(M, st, P, prev, next, w.row0, w.rows);
-                else if (quad) batch_rows<R, 1, 4, 4, true>(M, st, P, prev, next, w.row0, w.rows);
-                else batch_rows<R, 1, 0>(M, st, P, prev, next, w.row0, w.rows);
-            } else if ((CMASK & 2) && M.C == 3) {
-                if (d4) batch_rows<R, 3, 4>(M, st, P, prev, next, w.row0, w.rows);
-                else if (quad) batch_rows<R, 3, 4, 4, true>(M, st, P, prev, next, w.row0, w.rows);
-                else batch_rows<R, 3, 0>(M, st, P, prev, next, w.row0, w.rows);
-            } else if (CMASK & 4) {
-                batch_rows<R, 5, 0>(M, st, P, prev, next, w.row0, w.rows);
+            if constexpr (CONSTP) {
+                const MemberConst& K = c_members[M.cslot];
+                batch_item<R, CMASK>(M, K, st, K.p, &P, prev, next, w.row0, w.rows);
+            } else {
+                batch_item<R, CMASK>(M, M, st, P, nullptr, prev, next, w.row0, w.rows);
             }
         }
         if (s + 1 < A.nsteps) {
@@ -241,21 +275,51 @@ __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4
     }
 }
 
-template <typename R, int CMASK>
+template <typename R, int CMASK, bool CONSTP>
 static void* batch_kernel_ptr() {
-    return reinterpret_cast<void*>(&batch_kernel<R, CMASK>);
+    return reinterpret_cast<void*>(&batch_kernel<R, CMASK, CONSTP>);
 }
 
-static void* batch_kernel_for(int precision, int cmask) {
+static void* batch_kernel_for(int precision, int cmask, bool constp) {
     typedef void* (*Fn)();
-    static const Fn f32[8] = {nullptr, batch_kernel_ptr<float, 1>, batch_kernel_ptr<float, 2>, batch_kernel_ptr<float, 3>,
-                              batch_kernel_ptr<float, 4>, batch_kernel_ptr<float, 5>, batch_kernel_ptr<float, 6>,
-                              batch_kernel_ptr<float, 7>};
-    static const Fn f64[8] = {nullptr, batch_kernel_ptr<double, 1>, batch_kernel_ptr<double, 2>, batch_kernel_ptr<double, 3>,
-                              batch_kernel_ptr<double, 4>, batch_kernel_ptr<double, 5>, batch_kernel_ptr<double, 6>,
-                              batch_kernel_ptr<double, 7>};
+    static const Fn f32[8] = {nullptr, batch_kernel_ptr<float, 1, false>, batch_kernel_ptr<float, 2, false>,
+                              batch_kernel_ptr<float, 3, false>, batch_kernel_ptr<float, 4, false>,
+                              batch_kernel_ptr<float, 5, false>, batch_kernel_ptr<float, 6, false>,
+                              batch_kernel_ptr<float, 7, false>};
+    static const Fn f32c[8] = {nullptr, batch_kernel_ptr<float, 1, true>, batch_kernel_ptr<float, 2, true>,
+                               batch_kernel_ptr<float, 3, true>, batch_kernel_ptr<float, 4, true>,
+                               batch_kernel_ptr<float, 5, true>, batch_kernel_ptr<float, 6, true>,
+                               batch_kernel_ptr<float, 7, true>};
+    static const Fn f64[8] = {nullptr, batch_kernel_ptr<double, 1, false>, batch_kernel_ptr<double, 2, false>,
+                              batch_kernel_ptr<double, 3, false>, batch_kernel_ptr<double, 4, false>,
+                              batch_kernel_ptr<double, 5, false>, batch_kernel_ptr<double, 6, false>,
+                              batch_kernel_ptr<double, 7, false>};
     if (cmask < 1 || cmask > 7) return nullptr;
-    return (precision == GPE_FP64 ? f64 : f32)[cmask]();
+    if (precision == GPE_FP64) return f64[cmask]();
+    return (constp ? f32c : f32)[cmask]();
+}
+
+// Constant-memory slots of FP32 members, per device.
+std::mutex g_slot_mu;
+constexpr int kSlotDevices = 64;
+bool g_slot_used[kSlotDevices][kConstSlots];
+
+// n free slots of the device, or none when fewer are free.
+std::vector<int> take_slots(int device, int n) {
+    std::vector<int> got;
+    if (device < 0 || device >= kSlotDevices) return got;
+    std::lock_guard<std::mutex> lock(g_slot_mu);
+    for (int i = 0; i < kConstSlots && (int)got.size() < n; ++i)
+        if (!g_slot_used[device][i]) got.push_back(i);
+    if ((int)got.size() < n) return {};
+    for (int i : got) g_slot_used[device][i] = true;
+    return got;
+}
+
+void give_slots(int device, const std::vector<int>& slots) {
+    if (device < 0 || device >= kSlotDevices) return;
+    std::lock_guard<std::mutex> lock(g_slot_mu);
+    for (int i : slots) g_slot_used[device][i] = false;
 }
 
 }  // namespace gpe
@@ -287,6 +351,7 @@ struct gpe_batch {
     unsigned* d_next = nullptr;       // per-step item counters of one launch
     unsigned* d_bar = nullptr;
     int* d_err = nullptr;
+    std::vector<int> cslots;         // FP32: one constant-memory slot per member, or none
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int32_t graph_steps = 0;
@@ -312,6 +377,7 @@ void member_constants(const gpe_handle* h, BatchMember& M) {
     M.divY = a.divY;
     M.row_items = a.row_items;
     M.C = h->g.C;
+    M.cslot = -1;
 }
 
 // A lattice is told apart by its node and stencil-entry counts per cell.
@@ -398,7 +464,7 @@ gpe_status fill_state(gpe_batch* b) {
 }
 
 gpe_status grid_size(gpe_batch* b) {
-    void* fn = batch_kernel_for(b->precision, b->cmask);
+    void* fn = batch_kernel_for(b->precision, b->cmask, !b->cslots.empty());
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kBatchThreads, 0);
     if (e != cudaSuccess) return batch_fail_cuda(e, "occupancy of the batch kernel");
@@ -416,7 +482,7 @@ gpe_status enqueue_steps(gpe_batch* b, int32_t n, cudaStream_t s, const BatchMem
                          const BatchState* h_state, int grid) {
     cudaError_t e = cudaMemcpyAsync(b->d_state, h_state, nmembers * sizeof(BatchState), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return batch_fail_cuda(e, "batch state upload");
-    void* fn = batch_kernel_for(b->precision, b->cmask);
+    void* fn = batch_kernel_for(b->precision, b->cmask, !b->cslots.empty());
     const int32_t K = std::min(b->steps_per_launch > 0 ? b->steps_per_launch : n, kMaxStepsPerLaunch);
     for (int32_t done = 0; done < n; done += K) {
         const int32_t steps = std::min(K, n - done);
@@ -486,6 +552,8 @@ void release_batch(gpe_batch* b) {
     if (b->d_next) cudaFree(b->d_next);
     if (b->d_bar) cudaFree(b->d_bar);
     if (b->d_err) cudaFree(b->d_err);
+    give_slots(b->device, b->cslots);
+    b->cslots.clear();
 }
 
 }  // namespace
@@ -530,6 +598,27 @@ extern "C" gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count
     std::vector<BatchMember> hm(count);
     for (int32_t i = 0; i < count; ++i) member_constants(members[i], hm[i]);
     gpe_status st = GPE_OK;
+    if (b->precision == GPE_FP32) {
+        // the members' per-node constants into constant memory, where slots are free
+        b->cslots = take_slots(b->device, count);
+        for (int32_t i = 0; i < (int32_t)b->cslots.size(); ++i) {
+            MemberConst mc;
+            std::memset(&mc, 0, sizeof mc);
+            mc.p = hm[i].pf;
+            mc.g = hm[i].g;
+            mc.divV = hm[i].divV;
+            mc.divRow = hm[i].divRow;
+            mc.divY = hm[i].divY;
+            mc.row_items = hm[i].row_items;
+            hm[i].cslot = b->cslots[i];
+            cudaError_t ce = cudaMemcpyToSymbol(c_members, &mc, sizeof mc, (size_t)b->cslots[i] * sizeof(MemberConst));
+            if (ce != cudaSuccess) {
+                release_batch(b);
+                delete b;
+                return cuda_fail(ce, "batch member constants");
+            }
+        }
+    }
     if (cudaMalloc(&b->d_members, count * sizeof(BatchMember)) != cudaSuccess ||
         cudaMalloc(&b->d_state, count * sizeof(BatchState)) != cudaSuccess ||
         cudaMallocHost(&b->h_state, count * sizeof(BatchState)) != cudaSuccess ||
@@ -698,6 +787,7 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
         for (size_t i = 0; i < which.size() && ok; ++i) {
             const gpe_handle* h = b->members[which[i]];
             member_constants(h, hm[i]);
+            if (!b->cslots.empty()) hm[i].cslot = b->cslots[which[i]];
             hs[i] = b->h_state[which[i]];
             for (int slot = 0; slot < 2 && ok; ++slot) {
                 void* p = nullptr;

@@ -157,10 +157,15 @@ __device__ __forceinline__ const PhysR<R>& make_phys(const StepArgs& a) {
     else return a.pd;
 }
 
+// The per-step values of a PhysR (external fields bq, bb, bqq, bbq and the trap
+// switch) are read from F where it is given, the constants from P: the batch
+// kernel keeps its members' constants in constant memory and the fields of the
+// step in shared memory.
+
 // trap (Spin1GpeBCC.cu:112-122)
 template <typename R>
-__device__ __forceinline__ R trap(const PhysR<R>& P, const R r[3]) {
-    if (!P.trap_on) return (R)0;
+__device__ __forceinline__ R trap(const PhysR<R>& P, const R r[3], const PhysR<R>* F = nullptr) {
+    if (!(F ? F->trap_on : P.trap_on)) return (R)0;
     R x = r[0] * P.lambda[0];
     R y = r[1] * P.lambda[1];
     R z = r[2] * P.lambda[2];
@@ -187,7 +192,8 @@ __device__ __forceinline__ void mag_field(const PhysR<R>& P, const R r[3], R Bq,
 // allowed.  totalPot_out receives trap + c0 rho for the hyperbolic c_K.
 template <typename R>
 __device__ __forceinline__ void local_spin1(const PhysR<R>& P, const R r[3], R pot, bool ext, bool lossqz,
-                                            bool hyper, const Cx<R>* ps, Cx<R>* H) {
+                                            bool hyper, const Cx<R>* ps, Cx<R>* H, const PhysR<R>* F = nullptr) {
+    const PhysR<R>& Fs = F ? *F : P;
     const R n1 = ps[0].x * ps[0].x + ps[0].y * ps[0].y;
     const R n_1 = ps[2].x * ps[2].x + ps[2].y * ps[2].y;
     const R normSq = n1 + (ps[1].x * ps[1].x + ps[1].y * ps[1].y) + n_1;
@@ -204,7 +210,7 @@ __device__ __forceinline__ void local_spin1(const PhysR<R>& P, const R r[3], R p
     const Cx<R> magXY = (R)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
     R B[3];
     if (ext) {
-        mag_field(P, r, P.bq, P.bb, B);
+        mag_field(P, r, Fs.bq, Fs.bb, B);
         B[0] += P.c2 * magXY.x;
         B[1] += P.c2 * magXY.y;
         B[2] += P.c2 * (n1 - n_1);
@@ -221,7 +227,7 @@ __device__ __forceinline__ void local_spin1(const PhysR<R>& P, const R r[3], R p
     if (lossqz && (P.flags & GPE_FLAG_QUADRATIC_ZEEMAN)) {
         // Spin1GpeBCC.cu:897-912
         R Q[3];
-        mag_field(P, r, P.bqq, P.bbq, Q);
+        mag_field(P, r, Fs.bqq, Fs.bbq, Q);
         Bxy = (R)GPE_REF_INV_SQRT_2 * cx<R>(Q[0], Q[1]);
         BxyConj = conj(Bxy);
         const R BxyNormSq = (BxyConj * Bxy).x;
@@ -239,7 +245,8 @@ __device__ __forceinline__ void local_spin1(const PhysR<R>& P, const R r[3], R p
 // Local part of H for spin-2 (Spin2GpeBCC.cu:923-970; RelativisticSpin2Gpe.cu:1068-1125).
 template <typename R>
 __device__ __forceinline__ void local_spin2(const PhysR<R>& P, const R r[3], R pot, bool ext, bool loss, bool hyper,
-                                            const Cx<R>* ps, Cx<R>* H) {
+                                            const Cx<R>* ps, Cx<R>* H, const PhysR<R>* F = nullptr) {
+    const PhysR<R>& Fs = F ? *F : P;
     R n[5];
     for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
     const R normSq = n[0] + n[1] + n[2] + n[3] + n[4];
@@ -250,7 +257,7 @@ __device__ __forceinline__ void local_spin2(const PhysR<R>& P, const R r[3], R p
         for (int s = 0; s < 5; ++s) H[s] = (-cK) * H[s];
     }
     R B[3] = {(R)0, (R)0, (R)0};
-    if (ext) mag_field(P, r, P.bq, P.bb, B);
+    if (ext) mag_field(P, r, Fs.bq, Fs.bb, B);
     const R c2 = P.c2, c4 = P.c4;
     const R Fz = c2 * ((R)2 * n[0] + n[1] - n[3] - (R)2 * n[4]);
     Cx<R> d[5];
@@ -292,14 +299,14 @@ __device__ __forceinline__ void local_scalar(const PhysR<R>& P, R pot, bool loss
 
 template <typename R, int C>
 __device__ __forceinline__ void local_terms(const PhysR<R>& P, const R r[3], R pot, int mode, bool hyper, const Cx<R>* ps,
-                                            Cx<R>* H) {
+                                            Cx<R>* H, const PhysR<R>* F = nullptr) {
     const bool ext = (mode != GPE_MODE_ITP);
     if constexpr (C == 1) {
         local_scalar<R>(P, pot, ext, hyper, ps, H);
     } else if constexpr (C == 3) {
-        local_spin1<R>(P, r, pot, ext, ext, hyper, ps, H);
+        local_spin1<R>(P, r, pot, ext, ext, hyper, ps, H, F);
     } else {
-        local_spin2<R>(P, r, pot, ext, true, hyper, ps, H);
+        local_spin2<R>(P, r, pot, ext, true, hyper, ps, H, F);
     }
 }
 
@@ -398,13 +405,14 @@ __device__ __forceinline__ NodeTab<R, D> node_tab(const SmemTables<R>& st, uint3
 // (Spin1GpeBCC.cu:867-916).  nv: the old next record (leapfrog).
 template <typename R, int C, int MODE>
 __device__ __forceinline__ void node_finish(const PhysR<R>& P, const R pos[3], uint32_t x, uint32_t y, uint32_t z,
-                                            const Cx<R>* prv, Cx<R>* H, Cx<R>* nv, char* nxt, char* hp) {
+                                            const Cx<R>* prv, Cx<R>* H, Cx<R>* nv, char* nxt, char* hp,
+                                            const PhysR<R>* F = nullptr) {
     R r[3];
     r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + pos[0]);
     r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + pos[1]);
     r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + pos[2]);
-    const R pot = trap<R>(P, r);
-    local_terms<R, C>(P, r, pot, MODE, false, prv, H);
+    const R pot = trap<R>(P, r, F);
+    local_terms<R, C>(P, r, pot, MODE, false, prv, H, F);
     if constexpr (MODE == GPE_MODE_LEAPFROG) {
         // next += 2 dt (-i H), the whole record written at once
 #pragma unroll
@@ -425,7 +433,7 @@ template <typename R, int C, int MODE, int D, int G = D, bool MORE = false>
 __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R, D>& t, const PhysR<R>& P,
                                                  const char* prev, char* next, char* hpsi, uint32_t x, uint32_t y,
                                                  uint32_t z, uint32_t l, const SmemTables<R>* st = nullptr,
-                                                 int f_more = 0, int f_end = 0) {
+                                                 int f_more = 0, int f_end = 0, const PhysR<R>* F = nullptr) {
     const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
     const char* base = prev + cell_off;
     const uint32_t node_bytes = C * 2 * sizeof(R);
@@ -479,23 +487,25 @@ __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R,
         }
     }
     char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
-    node_finish<R, C, MODE>(P, t.pos, x, y, z, prv, H, nv, nxt, hp);
+    node_finish<R, C, MODE>(P, t.pos, x, y, z, prv, H, nv, nxt, hp, F);
 }
 
 // One node of a parabolic step: the DEC Laplacian gather, the local terms and the
 // time update (Spin1GpeBCC.cu:835-916).  prev/next/hpsi are the buffers' interior
 // pointers; (x, y, z) the cell, l the node.  D > 0: every node has D stencil
 // entries (MORE: a multiple of 4, the first D taken as the node's table), the
-// neighbour loads issued G at a time.
+// neighbour loads issued G at a time.  F: where the step's fields come from (P if
+// null).
 template <typename R, int C, int MODE, int D = 0, int G = D, bool MORE = false>
 __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R>& st, const PhysR<R>& P, const char* prev,
-                                               char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l) {
+                                               char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l,
+                                               const PhysR<R>* F = nullptr) {
     if constexpr (D > 0 && MORE) {
         const int f0 = st.row_ptr[l];
         parabolic_node_t<R, C, MODE, D, G, true>(g, node_tab<R, D>(st, l, f0), P, prev, next, hpsi, x, y, z, l, &st,
-                                                 f0 + D, st.row_ptr[l + 1]);
+                                                 f0 + D, st.row_ptr[l + 1], F);
     } else if constexpr (D > 0) {
-        parabolic_node_t<R, C, MODE, D, G>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l);
+        parabolic_node_t<R, C, MODE, D, G>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l, nullptr, 0, 0, F);
     } else {
         const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
         const char* base = prev + cell_off;
@@ -536,7 +546,7 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
         }
         const R pos[3] = {st.pos[3 * l + 0], st.pos[3 * l + 1], st.pos[3 * l + 2]};
         char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
-        node_finish<R, C, MODE>(P, pos, x, y, z, prv, H, nv, nxt, hp);
+        node_finish<R, C, MODE>(P, pos, x, y, z, prv, H, nv, nxt, hp, F);
     }
 }
 
