@@ -154,9 +154,11 @@ __device__ __forceinline__ void block_partials(T (&v)[K], double scale, double* 
 }
 
 // One reverse step: lambda_j = lambda_{j+2} + factor [L^T b + (dh/du)^T b] and the
-// field gradients factor (dh/dB)^T b, b = i lambda_{j+1}.  One thread per node.
+// field gradients factor (dh/dB)^T b, b = i lambda_{j+1}.  Grid-stride over the
+// nodes on one wave of blocks: the tables are staged, and the gradient sums
+// reduced, once per block rather than once per 256 nodes.
 template <typename R, int C>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoint_step_kernel(StepArgs a, AdjArgs j) {
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 4 : 1) adjoint_step_kernel(StepArgs a, AdjArgs j) {
     __shared__ SmemTables<R> st;
     __shared__ R wT[kMaxEntries];
     load_tables<R>(st, a);
@@ -166,8 +168,8 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoi
     }
     __syncthreads();
     R gsum[kGradCount] = {(R)0, (R)0, (R)0, (R)0};
-    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid < a.total) {
+    for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
+         gid += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t x, y, z, l;
         node_coords(a, (uint32_t)gid, x, y, z, l);
         const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
@@ -280,10 +282,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 5 : 1) adjoi
             const R zero3[3] = {(R)0, (R)0, (R)0};
             R w[3];
             mag_field<R>(P, r, (R)1, zero3, w);
-            gsum[0] = w[0] * s3[0] + w[1] * s3[1] + w[2] * s3[2];
-            gsum[1] = s3[0];
-            gsum[2] = s3[1];
-            gsum[3] = s3[2];
+            gsum[0] += w[0] * s3[0] + w[1] * s3[1] + w[2] * s3[2];
+            gsum[1] += s3[0];
+            gsum[2] += s3[1];
+            gsum[3] += s3[2];
         }
     }
     block_partials<kGradCount, R>(gsum, j.factor, a.partials);
@@ -389,10 +391,23 @@ __global__ void __launch_bounds__(256) adjoint_seed_kernel(StepArgs a, const cha
     for (int c = 0; c < C; ++c) stc<R>(a.next + off + c * 2 * sizeof(R), cx<R>((R)(dv * g[c].x), (R)(dv * g[c].y)));
 }
 
-// One reverse step; its block partials go to a.partials (nblocks x kGradCount).
+// Blocks of a reverse step: one wave (the kernel's occupancy x SMs), fewer for
+// small grids.  Its partials are that many blocks x kGradCount.
 template <typename R, int C>
-static cudaError_t launch_adjoint_step(const StepArgs& a, const AdjArgs& j, cudaStream_t s) {
-    adjoint_step_kernel<R, C><<<nblocks(a.total, 256), 256, 0, s>>>(a, j);
+static unsigned adjoint_step_blocks(uint64_t total) {
+    static int occ = 0;
+    if (occ == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adjoint_step_kernel<R, C>, 256, 0);
+        if (occ < 1) occ = 1;
+    }
+    return std::min<unsigned>(nblocks(total, 256), (unsigned)occ * (unsigned)device_sm_count());
+}
+
+// One reverse step on nb blocks (adjoint_step_blocks); its block partials go to
+// a.partials (nb x kGradCount).
+template <typename R, int C>
+static cudaError_t launch_adjoint_step(const StepArgs& a, const AdjArgs& j, unsigned nb, cudaStream_t s) {
+    adjoint_step_kernel<R, C><<<nb, 256, 0, s>>>(a, j);
     return cudaGetLastError();
 }
 
@@ -651,7 +666,7 @@ extern "C" gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, do
                                    A.t0 + jj * dt, GPE_MODE_LEAPFROG, s)))
                 return st;
         }
-        const unsigned nb = nblocks(h->g.X * (uint64_t)h->g.Y * h->g.Z * h->g.V, 256);
+        const unsigned nb = GPE_ADJ_DISPATCH(adjoint_step_blocks, h, h->g.X * (uint64_t)h->g.Y * h->g.Z * h->g.V);
         for (int j = hi - 1; j >= lo; --j) {
             StepArgs a = make_args(h, A.fields[j], A.t0 + j * dt);
             a.partials = A.part + (size_t)(j - lo) * nb * kGradCount;
@@ -664,7 +679,7 @@ extern "C" gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, do
             aj.factor = j >= 1 ? 2.0 * dt : dt;
             aj.factor32 = (float)aj.factor;
             aj.update = j >= 1 ? 1 : 0;
-            e = GPE_ADJ_DISPATCH(launch_adjoint_step, h, a, aj, s);
+            e = GPE_ADJ_DISPATCH(launch_adjoint_step, h, a, aj, nb, s);
             if (e != cudaSuccess) return cuda_fail(e, "adjoint step kernel");
             h->launches += 1;
             if (j >= 1) std::swap(P, Q);
