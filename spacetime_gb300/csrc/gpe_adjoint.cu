@@ -109,6 +109,24 @@ __device__ __forceinline__ void local_mag(const Cx<R>* ps, R M[3]) {
     }
 }
 
+// Re(b^H (e_k . F) u) for k = x, y, z: the spin-1 Zeeman term of local_spin1
+// (Spin1GpeBCC.cu:884-896: H0 += Bz u0 + conj(Bxy) u1, H1 += Bxy u0 + conj(Bxy) u2,
+// H2 += Bxy u1 - Bz u2 with Bxy = (Bx + i By)/sqrt2) for a unit field along each
+// axis and every other coefficient zero, projected on b.  The generic form runs
+// local_terms three times on mostly zero coefficients.
+template <typename R>
+__device__ __forceinline__ void zeeman_proj_spin1(const Cx<R>* b, const Cx<R>* u, R s3[3]) {
+    const R h = (R)GPE_REF_INV_SQRT_2;
+    // Bx = 1: H = (u1, u0 + u2, u1) / sqrt2
+    s3[0] = h * (b[0].x * u[1].x + b[0].y * u[1].y + b[1].x * (u[0].x + u[2].x) + b[1].y * (u[0].y + u[2].y) +
+                 b[2].x * u[1].x + b[2].y * u[1].y);
+    // By = 1: H = (-i u1, i (u0 - u2), i u1) / sqrt2
+    s3[1] = h * (b[0].x * u[1].y - b[0].y * u[1].x + b[1].x * (u[2].y - u[0].y) + b[1].y * (u[0].x - u[2].x) -
+                 b[2].x * u[1].y + b[2].y * u[1].x);
+    // Bz = 1: H = (u0, 0, -u2)
+    s3[2] = b[0].x * u[0].x + b[0].y * u[0].y - (b[2].x * u[2].x + b[2].y * u[2].y);
+}
+
 struct AdjArgs {
     const char* a_prev;     // lambda_{j+1}: neighbours read
     char* a_next;           // lambda_{j+2} -> lambda_j: read-modify-write
@@ -261,11 +279,14 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 4 : 1) adjoi
         // so dh/dBb_k = F_k u: the local terms with every coefficient zero except
         // Bb = e_k.  dB/dBq is mag_field's B at Bq = 1, Bb = 0.
         if constexpr (C > 1) {
+            R s3[3];
+            if constexpr (C == 3) {
+                zeeman_proj_spin1<R>(b, u, s3);
+            } else {
             PhysR<R> Z = P;
             Z.c0 = Z.c2 = Z.c4 = Z.alpha = Z.bq = Z.bqq = (R)0;
             Z.flags = 0;
             Z.trap_on = 0;
-            R s3[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
 #pragma unroll
@@ -278,6 +299,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 4 : 1) adjoi
 #pragma unroll
                 for (int c = 0; c < C; ++c) d += b[c].x * H[c].x + b[c].y * H[c].y;
                 s3[k] = d;
+            }
             }
             const R zero3[3] = {(R)0, (R)0, (R)0};
             R w[3];
