@@ -540,6 +540,8 @@ static gpe_status ensure_adjoint_buffers(gpe_handle* h, int n, int stride) {
             void* p = nullptr;
             if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
             v.push_back(p);
+            // zero halos: the out-of-place recomputation writes only the interior
+            if (cudaMemset(p, 0, bytes) != cudaSuccess) return false;
         }
         return true;
     };
@@ -547,8 +549,9 @@ static gpe_status ensure_adjoint_buffers(gpe_handle* h, int n, int stride) {
         adjoint_release(h);
         return fail(GPE_ERR_OOM, "cudaMalloc (adjoint checkpoints)");
     }
-    // recompute and adjoint buffers keep zero halos: checkpoint copies carry the
-    // (zero) halo of a handle buffer and every kernel writes the interior only
+    // recompute and adjoint buffers keep zero halos: they are zeroed when
+    // allocated, checkpoint copies carry the (zero) halo of a handle buffer, and
+    // every kernel writes the interior only
     for (void*& p : A.adj)
         if (!p && cudaMalloc(&p, bytes) != cudaSuccess) return fail(GPE_ERR_OOM, "cudaMalloc (adjoint state)");
     if (!A.target) {
@@ -676,14 +679,25 @@ extern "C" gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, do
     char* P = interior_of(h, A.adj[0]);  // lambda_{j+1}
     char* Q = interior_of(h, A.adj[1]);  // lambda_{j+2} -> lambda_j
     std::vector<void*> state((size_t)S, nullptr);
+    // the gather kernel recomputes a segment out of place; the tile kernels (which
+    // the forward run then used) in place after a state copy, so that the states
+    // stay bit-identical to the forward run's
+    const bool oop = leapfrog_from_supported(h);
     for (int k = A.segments - 1; k >= 0; --k) {
         const int lo = k * S, hi = std::min(lo + S, n), len = hi - lo;
         state[0] = A.ckpt[2 * k];
         if (len > 1) state[1] = A.ckpt[2 * k + 1];
         for (int m = 2; m < len; ++m) {
             state[m] = A.seg[m - 2];
-            if ((st = copy_state(h, state[m], state[m - 2], s))) return st;
             const int jj = lo + m - 1;
+            if (oop) {
+                // u_{jj+1} = u_{jj-1} + F(u_jj) into a fresh buffer: no state copy
+                if ((st = leapfrog_from(h, interior_of(h, state[m]), interior_of(h, state[m - 1]),
+                                        interior_of(h, state[m - 2]), A.fields[jj], A.t0 + jj * dt, s)))
+                    return st;
+                continue;
+            }
+            if ((st = copy_state(h, state[m], state[m - 2], s))) return st;
             if ((st = step_buffers(h, interior_of(h, state[m]), interior_of(h, state[m - 1]), A.fields[jj],
                                    A.t0 + jj * dt, GPE_MODE_LEAPFROG, s)))
                 return st;

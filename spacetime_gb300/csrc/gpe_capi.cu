@@ -899,6 +899,24 @@ gpe_status gpe::step_buffers(gpe_handle* h, char* next, const char* prev, const 
     return GPE_OK;
 }
 
+bool gpe::leapfrog_from_supported(const gpe_handle* h) {
+    return h->p.scheme == GPE_SCHEME_PARABOLIC && rows_shape(h).T == 0 && march_shape(h).T == 0 && tile_cells(h) == 0;
+}
+
+gpe_status gpe::leapfrog_from(gpe_handle* h, char* next, const char* cur, const char* old, const gpe_fields& B,
+                              double t, cudaStream_t s) {
+    if (!leapfrog_from_supported(h)) return fail(GPE_ERR_UNSUPPORTED, "out-of-place leapfrog needs the gather kernel");
+    StepArgs a = make_args(h, B, t);
+    a.prev = cur;
+    a.next = next;
+    a.hpsi = const_cast<char*>(old);  // read only, by the kModeLeapfrogFrom kernels
+    const cudaError_t e = dispatch_parabolic(h, a, kModeLeapfrogFrom, s);
+    h->launches += 1;
+    h->epoch += 1;
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    return GPE_OK;
+}
+
 // psi[next] <- psi[prev] (and q when hyperbolic), one step at time t.  The
 // hyperbolic imaginary-time step is itp_q + itp_psi of the ground-state loop
 // (RelativisticSpin2Gpe.cu:1712-1713), both reading the (psi, q) pair of prev,

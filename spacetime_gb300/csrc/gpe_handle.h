@@ -93,6 +93,12 @@ StepArgs make_args(const gpe_handle* h, const gpe_fields& B, double t);
 // pointers), with the same kernel choice as the slot-based steps.
 gpe_status step_buffers(gpe_handle* h, char* next, const char* prev, const gpe_fields& B, double t, int mode,
                         cudaStream_t s);
+// The leapfrog step next <- old + F(cur), leaving old as it was.  Only where the
+// handle's step kernel is the gather kernel, whose in-place and out-of-place forms
+// give identical states (false otherwise: nothing is launched).
+bool leapfrog_from_supported(const gpe_handle* h);
+gpe_status leapfrog_from(gpe_handle* h, char* next, const char* cur, const char* old, const gpe_fields& B, double t,
+                         cudaStream_t s);
 double cell_dv(const gpe_handle* h);
 size_t host_count(const gpe_handle* h, bool is_q);
 gpe_status ensure_stage(gpe_handle* h, size_t count);

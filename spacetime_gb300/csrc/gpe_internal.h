@@ -13,6 +13,11 @@ namespace gpe {
 
 // Largest tables the kernels stage in shared memory.  C15 (V=136, 544 stencil
 // entries, E=272) is the largest lattice of the reference.
+// Internal step mode beside GPE_MODE_LEAPFROG / EULER / ITP: a leapfrog step that
+// reads the old value from StepArgs::hpsi and writes next, leaving the old buffer
+// as it was (the adjoint's recomputation keeps every state of a segment).
+constexpr int kModeLeapfrogFrom = 3;
+
 constexpr int kMaxNodes = 160;
 constexpr int kMaxEntries = 640;
 constexpr int kMaxEdges = 320;

@@ -413,8 +413,8 @@ __device__ __forceinline__ void node_finish(const PhysR<R>& P, const R pos[3], u
     r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + pos[2]);
     const R pot = trap<R>(P, r, F);
     local_terms<R, C>(P, r, pot, MODE, false, prv, H, F);
-    if constexpr (MODE == GPE_MODE_LEAPFROG) {
-        // next += 2 dt (-i H), the whole record written at once
+    if constexpr (MODE == GPE_MODE_LEAPFROG || MODE == kModeLeapfrogFrom) {
+        // next = old + 2 dt (-i H), the whole record written at once
 #pragma unroll
         for (int s = 0; s < C; ++s) nv[s] += ((R)2 * P.dt) * cx<R>(H[s].y, -H[s].x);
         st_node<R, C>(nxt, nv);
@@ -442,6 +442,7 @@ __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R,
     char* nxt = next + cell_off + l * node_bytes;
     // leapfrog: the old next record is loaded up front, in flight with the gathers
     if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
+    if constexpr (MODE == kModeLeapfrogFrom) ld_node<R, C, true>(hpsi + cell_off + l * node_bytes, nv);
     // DEC Laplacian, sum_f w_f (psi_nb - psi) in entry order (Spin1GpeBCC.cu:835-865)
 #pragma unroll
     for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
@@ -516,6 +517,7 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
         for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
         char* nxt = next + cell_off + l * node_bytes;
         if constexpr (MODE == GPE_MODE_LEAPFROG) ld_node<R, C, false>(nxt, nv);
+        if constexpr (MODE == kModeLeapfrogFrom) ld_node<R, C, true>(hpsi + cell_off + l * node_bytes, nv);
         const int f0 = st.row_ptr[l], f1 = st.row_ptr[l + 1];
         if constexpr (C == 1) {
             // scalars: groups of 4 entries, the loads of a group issued together (rows
@@ -1028,6 +1030,7 @@ cudaError_t launch_parabolic_d(const StepArgs& a, int mode, cudaStream_t s) {
     switch (mode) {
         case GPE_MODE_LEAPFROG: return launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, D, G, MORE>(a, s);
         case GPE_MODE_EULER: return launch_parabolic_m<R, C, GPE_MODE_EULER, D, G, MORE>(a, s);
+        case kModeLeapfrogFrom: return launch_parabolic_m<R, C, kModeLeapfrogFrom, D, G, MORE>(a, s);
         default: return launch_parabolic_m<R, C, GPE_MODE_ITP, D, G, MORE>(a, s);
     }
 }
