@@ -21,7 +21,8 @@
 //
 // Checkpointing: the forward run keeps (u_{kS}, u_{kS+1}) for every segment k of
 // S steps; the reverse run recomputes one segment at a time from its pair with the
-// forward step kernel itself (bit-identical states) and walks it backwards.
+// forward step kernel itself (bit-identical states; with the gather kernel out of
+// place, u_{j+1} = u_{j-1} + F(u_j) into a fresh buffer) and walks it backwards.
 // Memory: 2 ceil(N/S) + S - 2 state buffers; S = ceil(sqrt(N)) by default.
 #include <algorithm>
 #include <cmath>
