@@ -128,6 +128,50 @@ __device__ __forceinline__ void zeeman_proj_spin1(const Cx<R>* b, const Cx<R>* u
     s3[2] = b[0].x * u[0].x + b[0].y * u[0].y - (b[2].x * u[2].x + b[2].y * u[2].y);
 }
 
+// J b for the spin-1 local terms of local_spin1 (external fields, quadratic Zeeman,
+// no loss; Spin1GpeBCC.cu:867-912): the directional derivative along b of
+//   h0 = T u0 + Bz u0 + conj(Bxy) u1,  h1 = T u1 + Bxy u0 + conj(Bxy) u2,
+//   h2 = T u2 + Bxy u1 - Bz u2  (+ the quadratic Zeeman matrix times u),
+// T = pot + c0 n, B = B_ext + c2 (Re m, Im m, n1 - n_-1), m = sqrt2 (u0* u1 + u1* u2),
+// Bxy = (Bx + i By) / sqrt2.  The same values as a dual-number evaluation of
+// local_terms along b, without the arithmetic on the constants' zero derivatives.
+template <typename R>
+__device__ __forceinline__ void jvp_spin1(const PhysR<R>& P, const R r[3], R pot, const Cx<R>* u, const Cx<R>* b,
+                                          Cx<R>* g) {
+    const R n1 = u[0].x * u[0].x + u[0].y * u[0].y;
+    const R n_1 = u[2].x * u[2].x + u[2].y * u[2].y;
+    const R n = n1 + (u[1].x * u[1].x + u[1].y * u[1].y) + n_1;
+    const R d1 = (R)2 * (u[0].x * b[0].x + u[0].y * b[0].y);
+    const R d_1 = (R)2 * (u[2].x * b[2].x + u[2].y * b[2].y);
+    const R dn = d1 + (R)2 * (u[1].x * b[1].x + u[1].y * b[1].y) + d_1;
+    const R T = pot + P.c0 * n, dT = P.c0 * dn;
+    const Cx<R> m = (R)GPE_REF_SQRT_2 * (conj(u[0]) * u[1] + conj(u[1]) * u[2]);
+    const Cx<R> dm = (R)GPE_REF_SQRT_2 * (conj(b[0]) * u[1] + conj(u[0]) * b[1] + conj(b[1]) * u[2] + conj(u[1]) * b[2]);
+    R B[3];
+    mag_field(P, r, P.bq, P.bb, B);
+    B[0] += P.c2 * m.x;
+    B[1] += P.c2 * m.y;
+    B[2] += P.c2 * (n1 - n_1);
+    const R dBz = P.c2 * (d1 - d_1);
+    const Cx<R> Bxy = (R)GPE_REF_INV_SQRT_2 * cx<R>(B[0], B[1]);
+    const Cx<R> dBxy = ((R)GPE_REF_INV_SQRT_2 * P.c2) * dm;
+    g[0] = (dT + dBz) * u[0] + (T + B[2]) * b[0] + conj(dBxy) * u[1] + conj(Bxy) * b[1];
+    g[1] = dT * u[1] + T * b[1] + dBxy * u[0] + Bxy * b[0] + conj(dBxy) * u[2] + conj(Bxy) * b[2];
+    g[2] = (dT - dBz) * u[2] + (T - B[2]) * b[2] + dBxy * u[1] + Bxy * b[1];
+    if (P.flags & GPE_FLAG_QUADRATIC_ZEEMAN) {
+        // linear in u: the same matrix applied to b
+        R Q[3];
+        mag_field(P, r, P.bqq, P.bbq, Q);
+        const Cx<R> qxy = (R)GPE_REF_INV_SQRT_2 * cx<R>(Q[0], Q[1]);
+        const Cx<R> qc = conj(qxy);
+        const R nsq = (qc * qxy).x;
+        const R bz2 = Q[2] * Q[2];
+        g[0] += (bz2 + nsq) * b[0] + (Q[2] * qc) * b[1] + (qc * qc) * b[2];
+        g[1] += (Q[2] * qxy) * b[0] + ((R)2 * nsq) * b[1] - (Q[2] * qc) * b[2];
+        g[2] += (qxy * qxy) * b[0] - (Q[2] * qxy) * b[1] + (bz2 + nsq) * b[2];
+    }
+}
+
 struct AdjArgs {
     const char* a_prev;     // lambda_{j+1}: neighbours read
     char* a_next;           // lambda_{j+2} -> lambda_j: read-modify-write
@@ -238,19 +282,23 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4 && C <= 3) ? 4 : 1) adjoi
             // energy E (trap, c0 n^2/2, Zeeman B.<F>, c2 <F>^2/2, quadratic Zeeman,
             // spin-2 singlet |A00|^2), so its real Jacobian is half the Hessian of E,
             // symmetric: J^T b = J b, one dual evaluation along b.
-            PhysR<Dual<R>> PD = dual_phys<R>(P);
-            PD.flags &= ~GPE_FLAG_THREE_BODY_LOSS;
-            const Dual<R> rD[3] = {cd<R>(r[0]), cd<R>(r[1]), cd<R>(r[2])};
-            Cx<Dual<R>> psD[C], H[C];
-#pragma unroll
-            for (int c = 0; c < C; ++c) {
-                psD[c] = cx<Dual<R>>(Dual<R>(u[c].x, b[c].x), Dual<R>(u[c].y, b[c].y));
-                H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
-            }
-            local_terms<Dual<R>, C>(PD, rD, cd<R>(pot), GPE_MODE_LEAPFROG, false, psD, H);
             Cx<R> g[C];
+            if constexpr (C == 3) {
+                jvp_spin1<R>(P, r, pot, u, b, g);
+            } else {
+                PhysR<Dual<R>> PD = dual_phys<R>(P);
+                PD.flags &= ~GPE_FLAG_THREE_BODY_LOSS;
+                const Dual<R> rD[3] = {cd<R>(r[0]), cd<R>(r[1]), cd<R>(r[2])};
+                Cx<Dual<R>> psD[C], H[C];
 #pragma unroll
-            for (int c = 0; c < C; ++c) g[c] = cx<R>(H[c].x.d, H[c].y.d);
+                for (int c = 0; c < C; ++c) {
+                    psD[c] = cx<Dual<R>>(Dual<R>(u[c].x, b[c].x), Dual<R>(u[c].y, b[c].y));
+                    H[c] = cx<Dual<R>>(cd<R>((R)0), cd<R>((R)0));
+                }
+                local_terms<Dual<R>, C>(PD, rD, cd<R>(pot), GPE_MODE_LEAPFROG, false, psD, H);
+#pragma unroll
+                for (int c = 0; c < C; ++c) g[c] = cx<R>(H[c].x.d, H[c].y.d);
+            }
             if (P.flags & GPE_FLAG_THREE_BODY_LOSS) {
                 // h_loss = -i alpha n^2 u: J^T b = i alpha n^2 b + 4 alpha n Im(b^H u) u
                 R n = 0, im = 0;
