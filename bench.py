@@ -50,6 +50,19 @@ LEGS = {
                           noise_rel=1e-3, bytes_fp32=360, seed=3),
 }
 LEGS["spin2-c15-48"] = dict(LEGS["spin2-c15-128"], dims=(48, 48, 48))   # small case for profiling
+#  scalar-hyper-bcc128: scalar hyperbolic psi+q (RelativisticGpeBCC), BCC 128^3 cells, c0 = 2000,
+#                       sigma = 0.00225, dt = 2e-5; 72 B per site (psi 24 B + q 2 x 24 B, E/V = 2)
+#  scalar-split-c15-64: the C15 real/imaginary split scheme (RelativisticGpeC15), C15 64^3 cells,
+#                       two in-place half-step launches per step; 72 B per site (each half of
+#                       psi and q read once and written once per step, E/V = 2)
+LEGS["scalar-hyper-bcc128"] = dict(lattice="bcc", C=1, dims=(128, 128, 128), c0=2000.0, c2=0.0, c4=0.0, dt=2e-5,
+                                   scheme=1, sigma=0.00225, zeta=(1.0,), kappa=1, noise_abs=1e-3, noise_rel=0.0,
+                                   bytes_fp32=72, seed=6)
+LEGS["scalar-split-c15-64"] = dict(lattice="c15", C=1, dims=(64, 64, 64), c0=2000.0, c2=0.0, c4=0.0, dt=2e-5,
+                                   scheme=2, sigma=0.00225, zeta=(1.0,), kappa=1, noise_abs=1e-3, noise_rel=0.0,
+                                   bytes_fp32=72, seed=7)
+KERNEL_OF_SCHEME = {0: "leapfrog kernel (auto) C=%d", 1: "hyper_tile_kernel<float,%d>",
+                    2: "split_step_kernel<float,PART> (C=%d, two launches per step)"}
 
 
 def workload(precision):
@@ -86,8 +99,8 @@ def run_leg(args):
     s.stream = C.c_void_p(stream.cuda_stream)
     inner = args.inner or INNER
     with torch.cuda.stream(stream):
-        s.init_state(capi.PSI_ODD, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
-                                                  noise_rel=w["noise_rel"], seed=w["seed"]))
+        s.init_state(s.current, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
+                                               noise_rel=w["noise_rel"], seed=w["seed"]))
         s.start()
         e0 = s.observe(s.current, 0.0)
         for _ in range(args.warmup):
@@ -116,7 +129,7 @@ def run_leg(args):
     launch_ms = step_ms / (inner * args.steps)
     algo = w["bytes_fp32"] * sites
     peak, kind = measured_peak()
-    name = "hyper_tile_kernel<float,%d>" % w["C"] if w["scheme"] else "leapfrog kernel (auto) C=%d" % w["C"]
+    name = KERNEL_OF_SCHEME[w["scheme"]] % w["C"]
     res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
            "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -148,8 +161,8 @@ def leg_drift(w, lat, nsteps, every=100):
                              dt=w["dt"], trap_offset=100.0, c0=w["c0"], c2=w["c2"], c4=w["c4"], sigma=w["sigma"],
                              lattice=lat)
         s = Stepper(lat, p)
-        s.init_state(capi.PSI_ODD, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
-                                                  noise_rel=w["noise_rel"], seed=w["seed"]))
+        s.init_state(s.current, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
+                                               noise_rel=w["noise_rel"], seed=w["seed"]))
         s.start()
         e = [s.observe(s.current, 0.0)]
         done = 0

@@ -1117,11 +1117,13 @@ cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
 // with w_f = -0.5 h_f / bs^2 (the reference folds dt into V, g and the Hodge weights).
 // A half-step reads one half of every value and writes the other (a node also reads
 // the half it writes, of its own value only), so the node and edge updates of a
-// half-step share one launch, laid out in groups of 1 + E/V blocks as the hyperbolic
-// step is.  Plain loads: lines read here are written by the same launch.
+// half-step share one launch, laid out in groups of 1 + E/V blocks of 256 items as
+// the hyperbolic step is.  The grid strides over these `vblocks` item blocks on one
+// wave, so that each block stages the tables once.  Plain loads: lines read here
+// are written by the same launch.
 template <typename R, int PART>
 __global__ void __launch_bounds__(256) split_step_kernel(StepArgs a, uint32_t node_items, uint32_t edge_items,
-                                                         uint32_t ratio, R qinit) {
+                                                         uint32_t ratio, R qinit, uint32_t vblocks) {
     __shared__ SmemHyper<R> sh;
     const int V = a.g.V, E = a.g.E, F = a.tab.faces;
     for (int i = threadIdx.x; i < V * F; i += blockDim.x) {
@@ -1139,21 +1141,22 @@ __global__ void __launch_bounds__(256) split_step_kernel(StepArgs a, uint32_t no
     }
     __syncthreads();
     constexpr bool kNodes = PART != 2;
-    uint32_t group, sub;
-    if (kNodes) {
-        group = blockIdx.x / (1 + ratio);
-        sub = blockIdx.x - group * (1 + ratio);
-    } else {
-        group = 0;
-        sub = 1 + blockIdx.x;
-    }
     const PhysR<R>& P = make_phys<R>(a);
     // the half read by the psi update and by d0 (R for PARTs 0 and 2, I for PART 1)
     constexpr uint32_t rd = PART == 1 ? sizeof(R) : 0;
     constexpr uint32_t wr = sizeof(R) - rd;
+    for (uint32_t vb = blockIdx.x; vb < vblocks; vb += gridDim.x) {
+    uint32_t group, sub;
+    if (kNodes) {
+        group = vb / (1 + ratio);
+        sub = vb - group * (1 + ratio);
+    } else {
+        group = 0;
+        sub = 1 + vb;
+    }
     if (kNodes && sub == 0) {
         const uint32_t i = group * blockDim.x + threadIdx.x;
-        if (i >= node_items) return;
+        if (i >= node_items) continue;
         const uint32_t row = fdiv(i, a.divRow);
         const uint32_t within = i - row * a.row_items;
         const uint32_t x = fdiv(within, a.divV);
@@ -1177,7 +1180,7 @@ __global__ void __launch_bounds__(256) split_step_kernel(StepArgs a, uint32_t no
     } else {
         const uint32_t eb = (kNodes ? group * ratio : 0) + (sub - 1);
         const uint32_t i = eb * blockDim.x + threadIdx.x;
-        if (i >= edge_items) return;
+        if (i >= edge_items) continue;
         const uint32_t row = fdiv(i, a.divRowE);
         const uint32_t within = i - row * a.row_items_e;
         const uint32_t x = fdiv(within, a.divE);
@@ -1194,6 +1197,7 @@ __global__ void __launch_bounds__(256) split_step_kernel(StepArgs a, uint32_t no
         else if constexpr (PART == 1) *reinterpret_cast<R*>(qe + wr) -= P.dts * (qr + d0);
         else *reinterpret_cast<R*>(qe) = qr + qinit * (qr + d0);
     }
+    }
 }
 
 // part: 0/1 the two half-steps, 2 the start; qinit is PART 2's coefficient.
@@ -1205,10 +1209,18 @@ cudaError_t launch_split(const StepArgs& a, int part, double qinit, cudaStream_t
     const unsigned nbn = nblocks(nn, 256), nbe = nblocks(ne, 256);
     const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
     if (nn == 0) return cudaSuccess;
+    static int occ = 0;
+    if (occ == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, split_step_kernel<R, 0>, 256, 0);
+        if (occ < 1) occ = 1;
+    }
+    const unsigned wave = (unsigned)occ * (unsigned)device_sm_count();
+    const unsigned vb = part == 2 ? nbe : groups * (1 + ratio);
+    const unsigned nb = std::min(vb, wave);
     switch (part) {
-        case 0: split_step_kernel<R, 0><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio, (R)0); break;
-        case 1: split_step_kernel<R, 1><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio, (R)0); break;
-        default: split_step_kernel<R, 2><<<nbe, 256, 0, s>>>(a, nn, ne, ratio, (R)qinit); break;
+        case 0: split_step_kernel<R, 0><<<nb, 256, 0, s>>>(a, nn, ne, ratio, (R)0, vb); break;
+        case 1: split_step_kernel<R, 1><<<nb, 256, 0, s>>>(a, nn, ne, ratio, (R)0, vb); break;
+        default: split_step_kernel<R, 2><<<nb, 256, 0, s>>>(a, nn, ne, ratio, (R)qinit, vb); break;
     }
     return cudaGetLastError();
 }
