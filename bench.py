@@ -97,6 +97,8 @@ def run_leg(args):
     stream = torch.cuda.Stream()
     s = Stepper(lat, p)
     s.stream = C.c_void_p(stream.cuda_stream)
+    if args.kernel:
+        s.set_tuning(capi.TUNE_KERNEL, args.kernel)
     inner = args.inner or INNER
     with torch.cuda.stream(stream):
         s.init_state(s.current, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
@@ -124,12 +126,15 @@ def run_leg(args):
         total_ms = a.elapsed_time(b)
         launches = s.launches - n0
     sites = s.sites
+    gather = s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER
     s.close()
     drift = leg_drift(w, lat, args.drift_steps) if args.leg_drift else None
     launch_ms = step_ms / (inner * args.steps)
     algo = w["bytes_fp32"] * sites
     peak, kind = measured_peak()
     name = KERNEL_OF_SCHEME[w["scheme"]] % w["C"]
+    if w["scheme"] == 1 and gather:
+        name = "hyper_step_kernel<float,%d> (gather form)" % w["C"]
     res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
            "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

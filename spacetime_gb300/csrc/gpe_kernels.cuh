@@ -668,11 +668,13 @@ __device__ __forceinline__ void q_update(const StepArgs& a, const SmemHyper<R>& 
 // reading the previous (psi, q) (RelativisticSpin2Gpe.cu:1873-1874); here one
 // launch does both.  Blocks are interleaved in groups of 1 + E/V: the first block
 // of a group updates 256 nodes, the next E/V blocks update the 256*E/V edges of
-// the same cells, so both halves of a group read the same psi/q lines from L2.
+// the same cells, so both halves of a group read the same psi/q lines from L2.  The
+// grid strides over these `vblocks` item blocks on one wave, so that each block
+// stages the tables once.
 // DO_PSI: psi update with MODE and HYPERB (-c_K scaling); QM < 0: no q update.
 template <typename R, int C, bool DO_PSI, int MODE, bool HYPERB, int QM>
 __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t node_items, uint32_t edge_items,
-                                                         uint32_t ratio) {
+                                                         uint32_t ratio, uint32_t vblocks) {
     __shared__ SmemHyper<R> sh;
     const int V = a.g.V, E = a.g.E, F = a.tab.faces;
     for (int i = threadIdx.x; i < V * F; i += blockDim.x) {
@@ -690,20 +692,21 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
     }
     __syncthreads();
 
+    for (uint32_t vb = blockIdx.x; vb < vblocks; vb += gridDim.x) {
     uint32_t group, sub;
     if (DO_PSI && QM >= 0) {
-        group = blockIdx.x / (1 + ratio);
-        sub = blockIdx.x - group * (1 + ratio);
+        group = vb / (1 + ratio);
+        sub = vb - group * (1 + ratio);
     } else if (DO_PSI) {
-        group = blockIdx.x;
+        group = vb;
         sub = 0;
     } else {
         group = 0;
-        sub = 1 + blockIdx.x;  // edge block index = sub - 1
+        sub = 1 + vb;  // edge block index = sub - 1
     }
     if (DO_PSI && sub == 0) {
         const uint32_t i = group * blockDim.x + threadIdx.x;
-        if (i >= node_items) return;
+        if (i >= node_items) continue;
         const PhysR<R>& P = make_phys<R>(a);
         const uint32_t node_bytes = C * 2 * sizeof(R);
         const uint32_t row = fdiv(i, a.divRow);
@@ -746,7 +749,7 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
     } else if constexpr (QM >= 0) {
         const uint32_t eb = (DO_PSI ? group * ratio : 0) + (sub - 1);
         const uint32_t i = eb * blockDim.x + threadIdx.x;
-        if (i >= edge_items) return;
+        if (i >= edge_items) continue;
         const uint32_t row = fdiv(i, a.divRowE);
         const uint32_t within = i - row * a.row_items_e;
         const uint32_t x = fdiv(within, a.divE);
@@ -754,6 +757,7 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
         const uint32_t z = fdiv(row, a.divY);
         const uint32_t y = row - z * a.g.Y;
         q_update<R, C, QM>(a, sh, x, y, z, e);
+    }
     }
 }
 
@@ -1066,43 +1070,40 @@ enum HyperKind {
     HK_FUSED_ITP             // psi (parabolic kinetic from q, imaginary time, H psi out) + q relaxation
 };
 
+// One hyper_step_kernel launch over vb item blocks, on at most one wave.
+template <typename R, int C, bool DO_PSI, int MODE, bool HYPERB, int QM>
+cudaError_t launch_hyper_k(const StepArgs& a, uint32_t nn, uint32_t ne, uint32_t ratio, unsigned vb, cudaStream_t s) {
+    static int occ = 0;
+    if (occ == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hyper_step_kernel<R, C, DO_PSI, MODE, HYPERB, QM>, 256, 0);
+        if (occ < 1) occ = 1;
+    }
+    const unsigned nb = std::min(vb, (unsigned)occ * (unsigned)device_sm_count());
+    if (nb) hyper_step_kernel<R, C, DO_PSI, MODE, HYPERB, QM><<<nb, 256, 0, s>>>(a, nn, ne, ratio, vb);
+    return cudaGetLastError();
+}
+
 template <typename R, int C>
 cudaError_t launch_hyper(const StepArgs& a, int kind, cudaStream_t s) {
     const uint32_t nn = (uint32_t)((uint64_t)a.g.X * a.g.Y * a.g.Z * a.g.V);
     const uint32_t ne = (uint32_t)((uint64_t)a.g.X * a.g.Y * a.g.Z * a.g.E);
     const uint32_t ratio = a.g.V ? (a.g.E + a.g.V - 1) / a.g.V : 1;
     const unsigned nbn = nblocks(nn, 256), nbe = nblocks(ne, 256);
+    // every group of (1 + ratio) blocks holds one node block and `ratio` edge blocks
+    const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
     switch (kind) {
-        case HK_FUSED_LEAPFROG: {
-            // every group of (1 + ratio) blocks holds one node block and `ratio` edge blocks
-            const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
-            hyper_step_kernel<R, C, true, GPE_MODE_LEAPFROG, true, 0><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        }
-        case HK_FUSED_ITP: {
-            const unsigned groups = nbn > (nbe + ratio - 1) / ratio ? nbn : (nbe + ratio - 1) / ratio;
-            hyper_step_kernel<R, C, true, GPE_MODE_ITP, false, 3><<<groups * (1 + ratio), 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        }
-        case HK_PSI_PARA_LEAPFROG:
-            hyper_step_kernel<R, C, true, GPE_MODE_LEAPFROG, false, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        case HK_PSI_PARA_EULER:
-            hyper_step_kernel<R, C, true, GPE_MODE_EULER, false, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        case HK_PSI_HYPER_EULER:
-            hyper_step_kernel<R, C, true, GPE_MODE_EULER, true, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        case HK_PSI_PARA_ITP:
-            hyper_step_kernel<R, C, true, GPE_MODE_ITP, false, -1><<<nbn, 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        case HK_Q_PARA: hyper_step_kernel<R, C, false, GPE_MODE_LEAPFROG, false, 1><<<nbe, 256, 0, s>>>(a, nn, ne, ratio); break;
-        case HK_Q_EULER_HYPER:
-            hyper_step_kernel<R, C, false, GPE_MODE_LEAPFROG, false, 2><<<nbe, 256, 0, s>>>(a, nn, ne, ratio);
-            break;
-        default: hyper_step_kernel<R, C, false, GPE_MODE_LEAPFROG, false, 0><<<nbe, 256, 0, s>>>(a, nn, ne, ratio); break;
+        case HK_FUSED_LEAPFROG:
+            return launch_hyper_k<R, C, true, GPE_MODE_LEAPFROG, true, 0>(a, nn, ne, ratio, groups * (1 + ratio), s);
+        case HK_FUSED_ITP:
+            return launch_hyper_k<R, C, true, GPE_MODE_ITP, false, 3>(a, nn, ne, ratio, groups * (1 + ratio), s);
+        case HK_PSI_PARA_LEAPFROG: return launch_hyper_k<R, C, true, GPE_MODE_LEAPFROG, false, -1>(a, nn, ne, ratio, nbn, s);
+        case HK_PSI_PARA_EULER: return launch_hyper_k<R, C, true, GPE_MODE_EULER, false, -1>(a, nn, ne, ratio, nbn, s);
+        case HK_PSI_HYPER_EULER: return launch_hyper_k<R, C, true, GPE_MODE_EULER, true, -1>(a, nn, ne, ratio, nbn, s);
+        case HK_PSI_PARA_ITP: return launch_hyper_k<R, C, true, GPE_MODE_ITP, false, -1>(a, nn, ne, ratio, nbn, s);
+        case HK_Q_PARA: return launch_hyper_k<R, C, false, GPE_MODE_LEAPFROG, false, 1>(a, nn, ne, ratio, nbe, s);
+        case HK_Q_EULER_HYPER: return launch_hyper_k<R, C, false, GPE_MODE_LEAPFROG, false, 2>(a, nn, ne, ratio, nbe, s);
+        default: return launch_hyper_k<R, C, false, GPE_MODE_LEAPFROG, false, 0>(a, nn, ne, ratio, nbe, s);
     }
-    return cudaGetLastError();
 }
 
 // Real/imaginary split scalar scheme on the dual edges (RelativisticGpeC15/
