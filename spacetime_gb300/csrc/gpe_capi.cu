@@ -835,6 +835,10 @@ static cudaError_t dispatch_tile(const gpe_handle* h, const StepArgs& a, uint32_
 // Hyperbolic row-tile kernel eligibility and tile length (0 = gather kernel).
 static uint32_t hyper_tile_cells(const gpe_handle* h) {
     if (h->tune_kernel == 1 || h->g.E == 0) return 0;
+    // scalars: the gather kernel is faster (fraction of peak, gather against tile:
+    // BCC 128^3 0.61 / 0.45, C15 40^3 0.60 / 0.39); the tile on request only.
+    // Spinors keep the tile (C15 spin-2 128^3 0.69 against 0.61).
+    if (h->g.C == 1 && h->tune_kernel != 2) return 0;
     if (h->g.cell_bytes % 16 != 0 || h->g.qcell_bytes % 16 != 0) return 0;
     const uint32_t per = h->g.V + h->g.E;
     const size_t tables = (size_t)h->g.V * h->lat.F * (8 + h->real_bytes) + (size_t)(3 * h->g.E + 1) * 4 +
@@ -1169,6 +1173,12 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
     if (!h || !value) return fail(GPE_ERR_INVALID_ARG, "null argument");
     const MarchShape ms = march_shape(h);
     const uint32_t tr = rows_cells(h);
+    if (h->p.scheme == GPE_SCHEME_HYPERBOLIC && (key == GPE_TUNE_KERNEL || key == GPE_TUNE_TILE_CELLS)) {
+        // hyperbolic handles: the fused tile kernel or the gather kernel
+        const uint32_t T = hyper_tile_cells(h);
+        *value = key == GPE_TUNE_KERNEL ? (T > 0 ? 2 : 1) : (int32_t)T;
+        return GPE_OK;
+    }
     if (key == GPE_TUNE_KERNEL) *value = tr > 0 ? 4 : ms.T > 0 ? 3 : (tile_cells(h) > 0 ? 2 : 1);
     else if (key == GPE_TUNE_TILE_CELLS) *value = (int32_t)(tr > 0 ? tr : ms.T > 0 ? ms.T : tile_cells(h));
     else if (key == GPE_TUNE_TILE_ROWS) *value = (int32_t)(tr > 0 ? rows_shape(h).RY : ms.TY);

@@ -642,26 +642,28 @@ __device__ __forceinline__ void q_update(const StepArgs& a, const SmemHyper<R>& 
     const char* qprev = a.q + qcell_off + e * edge_bytes;
     char* qnext = a.qnext + qcell_off + e * edge_bytes;
     const R dts = make_phys<R>(a).dts;
+    // whole records: (C+1)/2 loads each in FP32
+    Cx<R> to[C], from[C], pq[C], v[C];
+    ld_node<R, C, true>(otherp, to);
+    ld_node<R, C, true>(thisp, from);
+    if constexpr (QM != 1) ld_node<R, C, false>(qprev, pq);
+    if constexpr (QM == 0) ld_node<R, C, false>(qnext, v);
 #pragma unroll
     for (int s = 0; s < C; ++s) {
-        const Cx<R> d0psi = ldc<R>(otherp + s * 2 * sizeof(R)) - ldc<R>(thisp + s * 2 * sizeof(R));
-        char* qn = qnext + s * 2 * sizeof(R);
+        const Cx<R> d0psi = to[s] - from[s];
         if constexpr (QM == 1) {
-            stc<R>(qn, d0psi);
+            v[s] = d0psi;
         } else if constexpr (QM == 0) {
-            const Cx<R> qq = ((R)2 * dts) * (ldc_rw<R>(qprev + s * 2 * sizeof(R)) + d0psi);
-            Cx<R> v = ldc_rw<R>(qn);
-            v += cx<R>(-qq.y, qq.x);
-            stc<R>(qn, v);
+            const Cx<R> qq = ((R)2 * dts) * (pq[s] + d0psi);
+            v[s] += cx<R>(-qq.y, qq.x);
         } else if constexpr (QM == 3) {
-            const Cx<R> pq = ldc_rw<R>(qprev + s * 2 * sizeof(R));
-            stc<R>(qn, pq - dts * (pq - d0psi));
+            v[s] = pq[s] - dts * (pq[s] - d0psi);
         } else {
-            const Cx<R> pq = ldc_rw<R>(qprev + s * 2 * sizeof(R));
-            const Cx<R> qq = dts * (pq + d0psi);
-            stc<R>(qn, pq + cx<R>(-qq.y, qq.x));
+            const Cx<R> qq = dts * (pq[s] + d0psi);
+            v[s] = pq[s] + cx<R>(-qq.y, qq.x);
         }
     }
+    st_node<R, C>(qnext, v);
 }
 
 // Fused psi + q step.  The reference launches update_psi then update_q, both
@@ -719,18 +721,17 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
         const size_t qcell_off = (size_t)z * a.g.qslice + (size_t)y * a.g.qpitch + (size_t)x * a.g.qcell_bytes;
         const char* own = a.prev + cell_off + l * node_bytes;
         Cx<R> prv[C], H[C];
+        ld_node<R, C, true>(own, prv);
 #pragma unroll
-        for (int s = 0; s < C; ++s) {
-            prv[s] = ldc<R>(own + s * 2 * sizeof(R));
-            H[s] = cx<R>((R)0, (R)0);
-        }
-        // d1 of q (RelativisticSpin2Gpe.cu:1051-1066)
+        for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
+        // d1 of q (RelativisticSpin2Gpe.cu:1051-1066), whole edge records
         const char* qb = a.q + qcell_off;
         for (int k = 0; k < F; ++k) {
-            const char* qp = qb + sh.inc_off[l * F + k];
+            Cx<R> qv[C];
+            ld_node<R, C, true>(qb + sh.inc_off[l * F + k], qv);
             const R w = sh.inc_w[l * F + k];
 #pragma unroll
-            for (int s = 0; s < C; ++s) H[s] += w * ldc<R>(qp + s * 2 * sizeof(R));
+            for (int s = 0; s < C; ++s) H[s] += w * qv[s];
         }
         R r[3];
         r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + sh.pos[3 * l + 0]);

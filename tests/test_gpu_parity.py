@@ -146,10 +146,12 @@ def test_hyperbolic_fused_step(gpu, name, C, prec, kernel, tile):
         _close(g, r, prec, w)
 
 
+@pytest.mark.parametrize("kernel", [capi.KERNEL_AUTO, capi.KERNEL_GATHER, capi.KERNEL_TILE])
 @pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
 @pytest.mark.parametrize("C", [1, 3, 5])
-def test_hyperbolic_start_and_run(gpu, C, prec):
-    """gpe_start (RelativisticSpin2Gpe.cu:1628-1630) then 6 fused steps with a ramp."""
+def test_hyperbolic_start_and_run(gpu, C, prec, kernel):
+    """gpe_start (RelativisticSpin2Gpe.cu:1628-1630) then 6 fused steps with a ramp,
+    with the automatic kernel choice, the gather kernel and the fused tile kernel."""
     lat = capi.Lattice("bcc")
     p = _params(lat, C, prec, (6, 4, 5), scheme=capi.SCHEME_HYPERBOLIC, sigma=0.02)
     psi = _rand(lat, p, 51)
@@ -157,6 +159,8 @@ def test_hyperbolic_start_and_run(gpu, C, prec):
                           bb_segments=[((0, 0, 0.5), 0.0, capi.RAMP_CONSTANT), ((0, 0, -0.5), 4 * p.dt, capi.RAMP_LINEAR),
                                        ((0, 0, -0.5), 1e9, capi.RAMP_CONSTANT)])
     with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_KERNEL, kernel)
+        assert s.get_tuning(capi.TUNE_KERNEL) == (kernel or (1 if C == 1 else 2))
         s.upload(capi.PSI_ODD, psi)
         s.set_ramp(ramp, 0.0)
         s.start()
