@@ -807,6 +807,10 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
 #pragma unroll
     for (int k = 0; k < OBS_COUNT; ++k) grp[k] = (A)0;
     int in_group = 0;
+    // the thread's max |psi_s| and non-finite count, in A and an integer (exact), so
+    // that no FP64 operation is paid per node for them
+    A tmax = (A)0;
+    uint32_t nbad = 0;
     for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
          gid += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)gid;
@@ -820,25 +824,25 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
         const char* base = a.prev + cell_off;
         const uint32_t node_bytes = C * 2 * sizeof(R);
         Cx<A> ps[C], L[C], Hl[C], Hn[C];
-        A rho = 0, maxabs = 0;
-        double bad = 0;
-#pragma unroll
-        for (int s = 0; s < C; ++s) {
-            const Cx<R> v = ldc<R>(base + l * node_bytes + s * 2 * sizeof(R));
-            ps[s] = cx<A>((A)v.x, (A)v.y);
-            L[s] = Hl[s] = Hn[s] = cx<A>((A)0, (A)0);
-            const A n2 = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
-            rho += n2;
-            maxabs = fmax(maxabs, sqrt(n2));
-            if (!isfinite(ps[s].x) || !isfinite(ps[s].y)) bad += 1;
-        }
-        for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
-            const char* nb = base + st.nb_off[f];
+        A rho = 0;
+        {
+            Cx<R> pv[C];
+            ld_node<R, C, true>(base + l * node_bytes, pv);  // whole records
 #pragma unroll
             for (int s = 0; s < C; ++s) {
-                const Cx<R> v = ldc<R>(nb + s * 2 * sizeof(R));
-                L[s] += st.w[f] * (cx<A>((A)v.x, (A)v.y) - ps[s]);
+                ps[s] = cx<A>((A)pv[s].x, (A)pv[s].y);
+                L[s] = Hl[s] = Hn[s] = cx<A>((A)0, (A)0);
+                const A n2 = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+                rho += n2;
+                tmax = fmax(tmax, sqrt(n2));
+                if (!isfinite(ps[s].x) || !isfinite(ps[s].y)) ++nbad;
             }
+        }
+        for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
+            Cx<R> nv[C];
+            ld_node<R, C, true>(base + st.nb_off[f], nv);
+#pragma unroll
+            for (int s = 0; s < C; ++s) L[s] += st.w[f] * (cx<A>((A)nv[s].x, (A)nv[s].y) - ps[s]);
         }
         const PhysR<A>& P = make_phys<A>(a);
         A r[3];
@@ -886,8 +890,6 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
             v[OBS_MAGZ] = fz;
             v[OBS_SPIN] = sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
         }
-        acc[OBS_MAXABS] = fmax(acc[OBS_MAXABS], (double)maxabs);
-        acc[OBS_NONFINITE] += bad;
         if constexpr (kGroup == 1) {
             // FP64 node terms: the sums as they were (kin + hl added in FP64)
 #pragma unroll
@@ -911,6 +913,8 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
         for (int k = 0; k < OBS_COUNT; ++k)
             if (k != OBS_MAXABS && k != OBS_NONFINITE) acc[k] += (double)grp[k];
     }
+    acc[OBS_MAXABS] = (double)tmax;
+    acc[OBS_NONFINITE] = (double)nbad;
     // warp reduction
 #pragma unroll
     for (int k = 0; k < OBS_COUNT; ++k) {
@@ -1230,13 +1234,19 @@ cudaError_t launch_split(const StepArgs& a, int part, double qinit, cudaStream_t
 // node_fp32: per-node terms in FP32 (FP32 storage only); sums are FP64 either way.
 template <typename R, int C>
 cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaStream_t s) {
-    // a fixed grid of 8 blocks per SM (fewer for small grids); the partial sums are
-    // added in an order that depends only on the grid size
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), 8u * (unsigned)(sms > 0 ? sms : 1));
-    if (sizeof(R) == 4 && node_fp32) observe_kernel<R, C, float><<<nb, 256, 0, s>>>(a);
+    // one wave of resident blocks (fewer for small grids); the partial sums are added
+    // in an order that depends only on the grid size
+    static int occ32 = 0, occ64 = 0;
+    if (occ32 == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ32, observe_kernel<R, C, float>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ64, observe_kernel<R, C, double>, 256, 0);
+        occ32 = std::max(occ32, 1);
+        occ64 = std::max(occ64, 1);
+    }
+    const bool f32 = sizeof(R) == 4 && node_fp32;
+    const unsigned nb =
+        std::min<unsigned>(nblocks(a.total, 256), (unsigned)(f32 ? occ32 : occ64) * (unsigned)device_sm_count());
+    if (f32) observe_kernel<R, C, float><<<nb, 256, 0, s>>>(a);
     else observe_kernel<R, C, double><<<nb, 256, 0, s>>>(a);
     observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
     return cudaGetLastError();
