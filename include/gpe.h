@@ -444,7 +444,12 @@ gpe_status gpe_adjoint_backward(gpe_handle* h, const double* seed, double* grad,
  *   whole batch, for item sizes of 4K..256K nodes, and keeps the fastest; the
  *   members' states are untouched.  Within a step the blocks take items from
  *   one counter, so a block that finishes early takes more.
- *   `report` receives a JSON list of the timings. */
+ *   `report` receives a JSON list of the timings.
+ * An FP32 batch keeps its members' per-node constants in constant memory, one of
+ * 256 slots per device and member, held until gpe_batch_destroy.  A batch created
+ * while fewer slots are free (or an FP64 batch) reads them from shared memory
+ * instead: the same results, about 5 % slower.  The members' parameters are read
+ * once, at gpe_batch_create. */
 typedef struct gpe_batch gpe_batch;
 /* Batch tuning keys.  GPE_BATCH_BARRIER_TIMEOUT_MS bounds each grid-barrier wait
  * (default 10000).  GPE_BATCH_TEST_EXTRA_ARRIVALS is a test hook for the failure
