@@ -173,3 +173,29 @@ def test_batch_barrier_timeout_is_reported(gpu):
         _compare(mem, ref, prec)
     finally:
         _close(mem + ref)
+
+
+def test_batch_constant_slots_exhausted(gpu):
+    """An FP32 batch created while another live batch holds all 256 constant-memory
+    slots of the device reads its members' constants from shared memory instead:
+    the same states, bit for bit, as the constant-memory form."""
+    lat = capi.Lattice("bcc")
+    p = capi.make_params(components=1, precision=capi.FP32, dims=(2, 2, 2), block_scale=0.3, dt=2e-4, lattice=lat)
+    fillers = [Stepper(lat, p) for _ in range(256)]
+    outs = []
+    try:
+        for hold in (True, False):
+            mem = [_member(sp, capi.FP32, i) for i, sp in enumerate(SPECS)]
+            holder = Batch(fillers) if hold else None
+            try:
+                with Batch(mem) as b:
+                    b.step(7)
+                outs.append([m.download(m.current) for m in mem])
+            finally:
+                if holder is not None:
+                    holder.close()
+                _close(mem)
+    finally:
+        _close(fillers)
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
