@@ -1,14 +1,15 @@
 """Benchmark: lattice site-updates/s of the fused FP32 stepper on one GB300.
 
-Workload (the north-star's spin-1 configuration): spin-1 GPE on a BCC mesh of
+Workload (the headline spin-1 configuration): spin-1 GPE on a BCC mesh of
 96^3 block cells (10,616,832 dual nodes), box [-8, 8]^3, c0 = 2000, c2 = -50,
 seeded polar state (0, 1, 0) with 1e-3 relative noise, linear Zeeman ramp
 Bz 0.5 -> -0.5 over 4000 steps plus quadrupole gradient Bq = 0.2, dt = 5e-5.
 Each psi buffer is 255 MB (FP32), larger than the 129 MB L2, so no L2 flush is
 needed between iterations.
 
-One bench "step" = 100 leapfrog steps (one fused kernel each) + one FP64
-observables pass (norm, energy, magnetisation).  value = sites * 100 * K / time.
+One bench "step" = 100 leapfrog steps (one fused kernel each) + one observables
+pass (norm, energy, magnetisation; FP32 node terms, FP64 sums).  value = sites *
+100 * K / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
