@@ -448,19 +448,29 @@ static gpe_status transfer(gpe_handle* h, int32_t slot, double* host, size_t cou
     if (!slot_ok(h, slot)) return fail(GPE_ERR_INVALID_ARG, "slot not allocated");
     const bool is_q = slot == GPE_Q_EVEN || slot == GPE_Q_ODD;
     if (count != host_count(h, is_q)) return fail(GPE_ERR_INVALID_ARG, "host buffer size does not match the grid");
-    gpe_status st = ensure_stage(h, count);
-    if (st) return st;
     const Grid& g = h->g;
     const uint32_t vals = (uint32_t)((is_q ? g.qcell_bytes : g.cell_bytes) / h->real_bytes);
     const size_t pitch = is_q ? g.qpitch : g.pitch;
     const size_t slice = is_q ? g.qslice : g.slice;
     cudaStream_t s = (cudaStream_t)stream;
-    if (up) CUDA_TRY(cudaMemcpyAsync(h->stage, host, count * sizeof(double), cudaMemcpyHostToDevice, s));
-    cudaError_t e = launch_pack_any(h->p.precision, h->stage, static_cast<char*>(h->alloc[slot]), g.X, g.Y, g.Z, vals,
-                                    pitch, slice, up, s);
+    // pinned (page-locked, device-mapped) host arrays are read or written by the
+    // pack kernel itself over the host link, without the staging copy
+    double* mapped = nullptr;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer)
+        mapped = static_cast<double*>(attr.devicePointer);
+    else
+        cudaGetLastError();  // an unregistered pointer is not an error here
+    if (!mapped) {
+        gpe_status st = ensure_stage(h, count);
+        if (st) return st;
+    }
+    if (up && !mapped) CUDA_TRY(cudaMemcpyAsync(h->stage, host, count * sizeof(double), cudaMemcpyHostToDevice, s));
+    cudaError_t e = launch_pack_any(h->p.precision, mapped ? mapped : h->stage, static_cast<char*>(h->alloc[slot]), g.X,
+                                    g.Y, g.Z, vals, pitch, slice, up, s);
     if (e != cudaSuccess) return cuda_fail(e, "pack kernel");
     h->launches += 1;
-    if (!up) CUDA_TRY(cudaMemcpyAsync(host, h->stage, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (!up && !mapped) CUDA_TRY(cudaMemcpyAsync(host, h->stage, count * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     return up ? GPE_OK : check_device_error(h, s);
 }

@@ -1318,17 +1318,31 @@ namespace gpe {
 // ((Z+2)(Y+2)(X+2) cells of `vals` doubles, halo included) and a pitched device
 // buffer of storage type R.  TO_DEVICE: interior cells are converted, the device
 // halo is left untouched (zero).  Otherwise the packed array receives the
-// interior values and zeros in the halo.
-template <typename R, bool TO_DEVICE>
+// interior values and zeros in the halo.  `packed` may be device memory or pinned
+// host memory (read and written over the host link).  W32: the element count
+// fits 32 bits, and the index arithmetic uses 32-bit multiply-shift divisions.
+template <typename R, bool TO_DEVICE, bool W32>
 __global__ void __launch_bounds__(256) pack_kernel(double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
-                                                   uint32_t vals, size_t pitch, size_t slice, uint64_t total) {
+                                                   uint32_t vals, size_t pitch, size_t slice, uint64_t total,
+                                                   FastDiv dvals, FastDiv dx, FastDiv dy) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t cell = i / vals;
-        const uint32_t within = (uint32_t)(i - cell * vals);
-        const uint32_t x = (uint32_t)(cell % (X + 2));
-        const uint64_t yz = cell / (X + 2);
-        const uint32_t y = (uint32_t)(yz % (Y + 2));
-        const uint32_t z = (uint32_t)(yz / (Y + 2));
+        uint32_t x, y, z, within;
+        if constexpr (W32) {
+            const uint32_t i32 = (uint32_t)i;
+            const uint32_t cell = fdiv(i32, dvals);
+            within = i32 - cell * vals;
+            const uint32_t yz = fdiv(cell, dx);
+            x = cell - yz * (X + 2);
+            z = fdiv(yz, dy);
+            y = yz - z * (Y + 2);
+        } else {
+            const uint64_t cell = i / vals;
+            within = (uint32_t)(i - cell * vals);
+            x = (uint32_t)(cell % (X + 2));
+            const uint64_t yz = cell / (X + 2);
+            y = (uint32_t)(yz % (Y + 2));
+            z = (uint32_t)(yz / (Y + 2));
+        }
         const bool halo = x == 0 || y == 0 || z == 0 || x == X + 1 || y == Y + 1 || z == Z + 1;
         R* d = reinterpret_cast<R*>(dev_base + (size_t)z * slice + (size_t)y * pitch + (size_t)x * vals * sizeof(R)) + within;
         if (TO_DEVICE) {
@@ -1344,8 +1358,14 @@ cudaError_t launch_pack(double* packed, char* dev_base, uint32_t X, uint32_t Y, 
                         size_t slice, bool to_device, cudaStream_t s) {
     const uint64_t total = (uint64_t)(X + 2) * (Y + 2) * (Z + 2) * vals;
     const unsigned nb = (unsigned)((total + 255) / 256 < 152u * 64u ? (total + 255) / 256 : 152u * 64u);
-    if (to_device) pack_kernel<R, true><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total);
-    else pack_kernel<R, false><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total);
+    const FastDiv dv = make_fastdiv(vals), dx = make_fastdiv(X + 2), dy = make_fastdiv(Y + 2);
+    if (total < (1ull << 32)) {
+        if (to_device) pack_kernel<R, true, true><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total, dv, dx, dy);
+        else pack_kernel<R, false, true><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total, dv, dx, dy);
+    } else {
+        if (to_device) pack_kernel<R, true, false><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total, dv, dx, dy);
+        else pack_kernel<R, false, false><<<nb, 256, 0, s>>>(packed, dev_base, X, Y, Z, vals, pitch, slice, total, dv, dx, dy);
+    }
     return cudaGetLastError();
 }
 
