@@ -617,13 +617,29 @@ inline int device_sm_count() {
 // ---------------------------------------------------------------- hyperbolic
 
 template <typename R>
-struct SmemHyper {
-    int32_t inc_off[kMaxNodes * kMaxFaces];
+struct __align__(16) SmemHyper {
+    int32_t inc_off[kMaxNodes * kMaxFaces];  // first and 16-byte aligned: a node's 4 faces load as one vector
     R inc_w[kMaxNodes * kMaxFaces];
     int32_t e_from[kMaxEdges];
     int32_t e_to[kMaxEdges];
     R pos[kMaxNodes * 3];
 };
+
+// The 4 incidences of node l (offsets and weights) as two 16-byte shared loads
+// (one 16-byte and two for FP64 weights), for lattices of 4 faces per node.
+template <typename R>
+__device__ __forceinline__ void incidences4(const SmemHyper<R>& sh, uint32_t l, int32_t off[4], R w[4]) {
+    const int4 o = *reinterpret_cast<const int4*>(sh.inc_off + 4 * l);
+    off[0] = o.x; off[1] = o.y; off[2] = o.z; off[3] = o.w;
+    if constexpr (sizeof(R) == 4) {
+        const float4 v = *reinterpret_cast<const float4*>(sh.inc_w + 4 * l);
+        w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+    } else {
+        const double2 a = *reinterpret_cast<const double2*>(sh.inc_w + 4 * l);
+        const double2 b = *reinterpret_cast<const double2*>(sh.inc_w + 4 * l + 2);
+        w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+    }
+}
 
 // Edge (q) update of one dual edge (RelativisticSpin2Gpe.cu:986-1019, :823-856, :573-598).
 // QM: 0 hyperbolic leapfrog  next_q += i 2(dt/sigma)(prev_q + d0 psi)
@@ -726,12 +742,25 @@ __global__ void __launch_bounds__(256) hyper_step_kernel(StepArgs a, uint32_t no
         for (int s = 0; s < C; ++s) H[s] = cx<R>((R)0, (R)0);
         // d1 of q (RelativisticSpin2Gpe.cu:1051-1066), whole edge records
         const char* qb = a.q + qcell_off;
-        for (int k = 0; k < F; ++k) {
-            Cx<R> qv[C];
-            ld_node<R, C, true>(qb + sh.inc_off[l * F + k], qv);
-            const R w = sh.inc_w[l * F + k];
+        if (F == 4) {
+            int32_t off[4];
+            R w[4];
+            incidences4<R>(sh, l, off, w);
 #pragma unroll
-            for (int s = 0; s < C; ++s) H[s] += w * qv[s];
+            for (int k = 0; k < 4; ++k) {
+                Cx<R> qv[C];
+                ld_node<R, C, true>(qb + off[k], qv);
+#pragma unroll
+                for (int s = 0; s < C; ++s) H[s] += w[k] * qv[s];
+            }
+        } else {
+            for (int k = 0; k < F; ++k) {
+                Cx<R> qv[C];
+                ld_node<R, C, true>(qb + sh.inc_off[l * F + k], qv);
+                const R w = sh.inc_w[l * F + k];
+#pragma unroll
+                for (int s = 0; s < C; ++s) H[s] += w * qv[s];
+            }
         }
         R r[3];
         r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + sh.pos[3 * l + 0]);
@@ -1175,7 +1204,18 @@ __global__ void __launch_bounds__(256) split_step_kernel(StepArgs a, uint32_t no
         const Cx<R> v = ldc_rw<R>(own);
         const char* qb = a.qnext + qcell_off + rd;
         R d1q = (R)0;
-        for (int k = 0; k < F; ++k) d1q += sh.inc_w[l * F + k] * *reinterpret_cast<const R*>(qb + sh.inc_off[l * F + k]);
+        if (F == 4) {
+            // the 4 incident q values loaded together, tables as vectors
+            int32_t off[4];
+            R w[4], qv[4];
+            incidences4<R>(sh, l, off, w);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) qv[k] = *reinterpret_cast<const R*>(qb + off[k]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) d1q += w[k] * qv[k];
+        } else {
+            for (int k = 0; k < F; ++k) d1q += sh.inc_w[l * F + k] * *reinterpret_cast<const R*>(qb + sh.inc_off[l * F + k]);
+        }
         R r[3];
         r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + sh.pos[3 * l + 0]);
         r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + sh.pos[3 * l + 1]);
