@@ -62,7 +62,7 @@ LEGS["scalar-hyper-bcc128"] = dict(lattice="bcc", C=1, dims=(128, 128, 128), c0=
 LEGS["scalar-split-c15-64"] = dict(lattice="c15", C=1, dims=(64, 64, 64), c0=2000.0, c2=0.0, c4=0.0, dt=2e-5,
                                    scheme=2, sigma=0.00225, zeta=(1.0,), kappa=1, noise_abs=1e-3, noise_rel=0.0,
                                    bytes_fp32=72, seed=7)
-KERNEL_OF_SCHEME = {0: "leapfrog kernel (auto) C=%d", 1: "hyper_tile_kernel<float,%d>",
+KERNEL_OF_SCHEME = {0: "leapfrog kernel (auto) C=%d", 1: "hyper_tile_kernel<float,%d> (fused tile)",
                     2: "split_step_kernel<float,PART> (C=%d, two launches per step)"}
 
 

@@ -845,10 +845,12 @@ static cudaError_t dispatch_tile(const gpe_handle* h, const StepArgs& a, uint32_
 // Hyperbolic row-tile kernel eligibility and tile length (0 = gather kernel).
 static uint32_t hyper_tile_cells(const gpe_handle* h) {
     if (h->tune_kernel == 1 || h->g.E == 0) return 0;
-    // scalars: the gather kernel is faster (fraction of peak, gather against tile:
-    // BCC 128^3 0.61 / 0.45, C15 40^3 0.60 / 0.39); the tile on request only.
-    // Spinors keep the tile (C15 spin-2 128^3 0.69 against 0.61).
-    if (h->g.C == 1 && h->tune_kernel != 2) return 0;
+    // the automatic choice, by measurement (fraction of peak, gather against tile):
+    // scalars BCC 128^3 0.64 / 0.45, C15 40^3 0.60 / 0.39; spin-2 C15 128^3 0.69 /
+    // 0.69, C15 48^3 0.75 / 0.71, BCC 96^3 0.77 / 0.69; spin-1 C15 40^3 0.55 / 0.51
+    // -- the gather kernel; spin-1 BCC 96^3 0.56 / 0.74 -- the tile.  The tile
+    // is chosen for spin-1 on small cells (V <= 16) and on request.
+    if (h->tune_kernel != 2 && !(h->g.C == 3 && h->g.V <= 16)) return 0;
     if (h->g.cell_bytes % 16 != 0 || h->g.qcell_bytes % 16 != 0) return 0;
     const uint32_t per = h->g.V + h->g.E;
     const size_t tables = (size_t)h->g.V * h->lat.F * (8 + h->real_bytes) + (size_t)(3 * h->g.E + 1) * 4 +

@@ -160,7 +160,7 @@ def test_hyperbolic_start_and_run(gpu, C, prec, kernel):
                                        ((0, 0, -0.5), 1e9, capi.RAMP_CONSTANT)])
     with Stepper(lat, p) as s:
         s.set_tuning(capi.TUNE_KERNEL, kernel)
-        assert s.get_tuning(capi.TUNE_KERNEL) == (kernel or (1 if C == 1 else 2))
+        assert s.get_tuning(capi.TUNE_KERNEL) == (kernel or (2 if C == 3 else 1))
         s.upload(capi.PSI_ODD, psi)
         s.set_ramp(ramp, 0.0)
         s.start()
