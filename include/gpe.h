@@ -196,7 +196,10 @@ gpe_status gpe_buffer(const gpe_handle* h, int32_t slot, gpe_pitched* out, size_
 /* Host <-> device copies in the reference file layout: (Z+2)(Y+2)(X+2) cells of
  * FP64 values, halo included (the ground_state.dat / "<t>.dat" format written at
  * Spin1GpeBCC.cu:1690-1699).  Halo cells are ignored on upload (kept zero).
- * count = number of doubles in host buffer.  These synchronise the stream. */
+ * count = number of doubles in host buffer.  These synchronise the stream.  A
+ * page-locked (pinned, device-mapped) host array is read or written by the
+ * conversion kernel directly over the host link; a pageable one goes through a
+ * device staging buffer (allocated on first use).  The results are the same. */
 gpe_status gpe_upload(gpe_handle* h, int32_t slot, const double* host, size_t count, void* stream);
 gpe_status gpe_download(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream);
 
