@@ -879,18 +879,30 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
         r[1] = P.p0[1] + P.bs * ((A)y * P.bw[1] + st.pos[3 * l + 1]);
         r[2] = P.p0[2] + P.bs * ((A)z * P.bw[2] + st.pos[3 * l + 2]);
         local_terms<A, C>(P, r, trap<A>(P, r), GPE_MODE_LEAPFROG, false, ps, Hl);
-        // interaction-only part: no trap, no external field, no loss / quadratic Zeeman
-        PhysR<A> Q = P;
-        Q.bq = Q.bqq = 0;
-        for (int k = 0; k < 3; ++k) Q.bb[k] = Q.bbq[k] = 0;
-        Q.flags &= ~(GPE_FLAG_THREE_BODY_LOSS | GPE_FLAG_QUADRATIC_ZEEMAN | GPE_FLAG_QUADRUPOLE_OFFSET);
-        local_terms<A, C>(Q, r, (A)0, GPE_MODE_LEAPFROG, false, ps, Hn);
+        // interaction-only part: no trap, no external field, no loss / quadratic
+        // Zeeman.  Scalars: psi^H (c0 n) psi = c0 n^2; spin-1: psi^H [c0 n +
+        // c2 <F>.F] psi = c0 n^2 + c2 |<F>|^2 with <F> = (Re m, Im m, n_1 - n_-1),
+        // m = sqrt2 (psi_1* psi_0 + psi_0* psi_-1); spin-2 through local_terms.
         A kin = 0, hl = 0, hn = 0;
+        if constexpr (C == 1) {
+            hn = P.c0 * rho * rho;
+        } else if constexpr (C == 3) {
+            const Cx<A> m = (A)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
+            const A fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
+            hn = P.c0 * rho * rho + P.c2 * (m.x * m.x + m.y * m.y + fz * fz);
+        } else {
+            PhysR<A> Q = P;
+            Q.bq = Q.bqq = 0;
+            for (int k = 0; k < 3; ++k) Q.bb[k] = Q.bbq[k] = 0;
+            Q.flags &= ~(GPE_FLAG_THREE_BODY_LOSS | GPE_FLAG_QUADRATIC_ZEEMAN | GPE_FLAG_QUADRUPOLE_OFFSET);
+            local_terms<A, C>(Q, r, (A)0, GPE_MODE_LEAPFROG, false, ps, Hn);
+#pragma unroll
+            for (int s = 0; s < C; ++s) hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
+        }
 #pragma unroll
         for (int s = 0; s < C; ++s) {
             kin += ps[s].x * L[s].x + ps[s].y * L[s].y;
             hl += ps[s].x * Hl[s].x + ps[s].y * Hl[s].y;
-            hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
         }
         A v[OBS_COUNT];
 #pragma unroll
