@@ -867,11 +867,24 @@ __global__ void __launch_bounds__(256) observe_kernel(StepArgs a) {
                 if (!isfinite(ps[s].x) || !isfinite(ps[s].y)) ++nbad;
             }
         }
-        for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
-            Cx<R> nv[C];
-            ld_node<R, C, true>(base + st.nb_off[f], nv);
+        if (a.tab.uniform_deg == 4) {
+            // 4 entries: table vectors, the 4 neighbour loads issued together
+            const NodeTab<A, 4> t = node_tab<A, 4>(st, l);
+            Cx<R> nv[4][C];
 #pragma unroll
-            for (int s = 0; s < C; ++s) L[s] += st.w[f] * (cx<A>((A)nv[s].x, (A)nv[s].y) - ps[s]);
+            for (int k = 0; k < 4; ++k) ld_node<R, C, true>(base + t.off[k], nv[k]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+#pragma unroll
+                for (int s = 0; s < C; ++s) L[s] += t.w[k] * (cx<A>((A)nv[k][s].x, (A)nv[k][s].y) - ps[s]);
+            }
+        } else {
+            for (int f = st.row_ptr[l]; f < st.row_ptr[l + 1]; ++f) {
+                Cx<R> nv[C];
+                ld_node<R, C, true>(base + st.nb_off[f], nv);
+#pragma unroll
+                for (int s = 0; s < C; ++s) L[s] += st.w[f] * (cx<A>((A)nv[s].x, (A)nv[s].y) - ps[s]);
+            }
         }
         const PhysR<A>& P = make_phys<A>(a);
         A r[3];
