@@ -384,8 +384,15 @@ int32_t gpe_current_slot(const gpe_handle* h);
  * quantities gpe_observe computes.  The reduction scratch is one fixed-size
  * device array inside the library (2049 x 12 doubles, about 197 KB per GPU that
  * loads the library, held until the process exits); lattices larger than
- * 160 nodes / 640 stencil entries per cell and grids of 2^32 sites or more are
- * rejected with GPE_ERR_INVALID_ARG.  The first call on each device looks up
+ * 160 nodes / 640 stencil entries per cell, row_ptr tables that do not start
+ * at 0 or that decrease, grids of 2^32 sites or more, and psi pointers, pitches
+ * or slice pitches that are not multiples of one complex value's size (8 bytes
+ * in FP32, 16 in FP64) are rejected with GPE_ERR_INVALID_ARG before the GPU is
+ * touched.  During condensate expansion pass the current block scale bs(t) as
+ * p->block_scale: positions and stencil weights then match the handle's step,
+ * and the integrals use dv = bs(t)^3 VOLUME, where gpe_observe keeps the
+ * initial bs0^3 VOLUME (multiply by (bs0/bs(t))^3 to compare).  The address
+ * lookup does not survive cudaDeviceReset.  The first call on each device looks up
  * the scratch array's device address with that device current; make that first
  * call before any stream capture.  Calls share the scratch: calls that overlap on
  * the GPU race, so order them on one stream.  Synchronises `stream`; errors are

@@ -16,6 +16,7 @@
 // nothing has to be cleared between calls.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "gpe_kernels.cuh"
@@ -149,9 +150,14 @@ namespace {
 
 // Device address of g_obs_scratch per device ordinal, looked up once per device
 // with that device current.  In host code the symbol's name only stands in for
-// the device array; a kernel must be given this address.
+// the device array; a kernel must be given this address.  The mutex makes the
+// first calls from several host threads safe.  The cached address belongs to the
+// device's current context: after cudaDeviceReset the module is loaded again and
+// the address may change, so a process that resets a device must not call this
+// entry point on that device afterwards.
 constexpr int kMaxDevices = 64;
 double* g_scratch_addr[kMaxDevices] = {nullptr};
+std::mutex g_scratch_mutex;
 
 // Errors are reported through gpe_last_error().
 gpe_status noalloc_fail(gpe_status st, const std::string& m) {
@@ -171,6 +177,11 @@ extern "C" gpe_status gpe_observe_noalloc(const gpe_lattice_desc* lat, const gpe
     const int V = lat->nodes;
     if (V <= 0 || V > kMaxNodes) return noalloc_fail(GPE_ERR_INVALID_ARG, "nodes beyond the static table size (160)");
     if (!lat->row_ptr || !lat->stencil || !lat->pos) return noalloc_fail(GPE_ERR_INVALID_ARG, "missing table");
+    // The kernel walks row_ptr[l] .. row_ptr[l+1] of the by-value tables, so every
+    // row must lie inside them: row_ptr starts at 0 and never decreases.
+    if (lat->row_ptr[0] != 0) return noalloc_fail(GPE_ERR_INVALID_ARG, "row_ptr[0] must be 0");
+    for (int l = 0; l < V; ++l)
+        if (lat->row_ptr[l + 1] < lat->row_ptr[l]) return noalloc_fail(GPE_ERR_INVALID_ARG, "row_ptr must not decrease");
     const int n = lat->row_ptr[V];
     if (n <= 0 || n > kMaxEntries) return noalloc_fail(GPE_ERR_INVALID_ARG, "stencil beyond the static table size (640)");
     const uint64_t sites = (uint64_t)p->dims[0] * p->dims[1] * p->dims[2] * (uint64_t)V;
@@ -179,19 +190,28 @@ extern "C" gpe_status gpe_observe_noalloc(const gpe_lattice_desc* lat, const gpe
     const size_t cell_bytes = (size_t)V * p->components * 2 * real_bytes;
     if (pitch < (p->dims[0] + 2) * cell_bytes || slice_pitch < pitch * (p->dims[1] + 2))
         return noalloc_fail(GPE_ERR_INVALID_ARG, "pitch or slice pitch smaller than the padded row or slice");
+    // Complex values are read as float2 / double2 vectors: psi, the pitch and the
+    // slice pitch must keep every value on a multiple of its own size.
+    const size_t align = 2 * real_bytes;
+    if (reinterpret_cast<uintptr_t>(psi) % align != 0 || pitch % align != 0 || slice_pitch % align != 0)
+        return noalloc_fail(GPE_ERR_INVALID_ARG, "psi, pitch and slice pitch must be multiples of one complex value's size");
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return noalloc_fail(GPE_ERR_NO_DEVICE, "no usable CUDA device");
-    if (!g_scratch_addr[dev]) {
+    double* scratch = nullptr;
+    {
         // Set-up on the first call on this device (this device is current here).
-        void* addr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&addr, g_obs_scratch);
-        if (e != cudaSuccess || !addr)
-            return noalloc_fail(GPE_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_scratch_addr[dev] = static_cast<double*>(addr);
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (!g_scratch_addr[dev]) {
+            void* addr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&addr, g_obs_scratch);
+            if (e != cudaSuccess || !addr)
+                return noalloc_fail(GPE_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_scratch_addr[dev] = static_cast<double*>(addr);
+        }
+        scratch = g_scratch_addr[dev];
     }
-    double* scratch = g_scratch_addr[dev];
 
     NoAllocTables tab;
     std::memset(&tab, 0, sizeof tab);

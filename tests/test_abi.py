@@ -116,3 +116,33 @@ def test_null_handles(lib):
     assert lib.gpe_start(None, None) == 1
     assert lib.gpe_destroy(None) == 0
     assert lib.gpe_sites(None) == 0
+
+
+def test_noalloc_rejects_bad_tables_and_alignment_on_host(lib):
+    """gpe_observe_noalloc checks its tables and the buffer's alignment before it
+    touches the GPU: a row table that does not start at 0 or that decreases would
+    index the by-value stencil outside its rows, and a pointer or pitch off the
+    complex value's size would make a misaligned vector load."""
+    lat = capi.Lattice("bcc")
+    p = capi.make_params(components=3, precision=capi.FP32, dims=(4, 4, 4), lattice=lat)
+    shape = capi.buffer_shape(lat, p)
+    pitch = shape[2] * lat.nodes * 3 * 8
+    slice_pitch = pitch * shape[1]
+    o = capi.Observables()
+
+    def call(desc, ptr, pt, sp, q=p):
+        return lib.gpe_observe_noalloc(C.byref(desc), C.byref(q), None, 0.0, C.c_void_p(ptr), pt, sp, C.byref(o), None)
+
+    for bad in ([1], [0, 4, 2]):
+        rp = lat.row_ptr.copy()
+        rp[:len(bad)] = bad
+        d = capi.LatticeDesc.from_buffer_copy(lat.desc)
+        d.row_ptr = rp.ctypes.data_as(C.POINTER(C.c_int32))
+        assert call(d, 1 << 20, pitch, slice_pitch) == 1
+        assert b"row_ptr" in lib.gpe_last_error()
+    for ptr, pt, sp in (((1 << 20) + 4, pitch, slice_pitch), (1 << 20, pitch + 4, slice_pitch + 4 * shape[1]),
+                        (1 << 20, pitch, slice_pitch + 4)):
+        assert call(lat.desc, ptr, pt, sp) == 1
+        assert b"multiples" in lib.gpe_last_error()
+    p64 = capi.make_params(components=3, precision=capi.FP64, dims=(4, 4, 4), lattice=lat)
+    assert call(lat.desc, (1 << 20) + 8, 2 * pitch, 2 * slice_pitch, p64) == 1

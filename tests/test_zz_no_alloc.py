@@ -61,6 +61,68 @@ def test_noalloc_matches_observe_twice(gpu, name, C, dims, prec):
             _compare(got, want)
 
 
+def test_noalloc_matches_observe_with_physics_switches(gpu):
+    """The switches the no-alloc kernel builds into its own parameters by hand:
+    quadratic Zeeman, quadrupole offset (non-zero bb_quad and bq_quad) and the
+    trap switched off after trap_off_time, on two calls in a row either side of
+    that time."""
+    lib = gpu
+    lat = capi.Lattice("bcc")
+    flags = capi.FLAG_QUADRATIC_ZEEMAN | capi.FLAG_QUADRUPOLE_OFFSET | capi.FLAG_TRAP_OFF_AFTER
+    p = capi.make_params(components=3, precision=capi.FP64, flags=flags, dims=(7, 6, 5), block_scale=0.3, dt=1e-4,
+                         trap_offset=100.0, trap_off_time=0.5, trap_lambda=(1.0, 1.1, 1.3), c0=120.0, c2=-7.0,
+                         quad_center=(0.1, -0.2, 0.3), lattice=lat)
+    ramp = capi.make_ramp(bq_segments=[(0.3, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0.1, -0.2, 0.5), 1e9, capi.RAMP_CONSTANT)], bq_quad_scale=0.7, bb_quad_scale=0.4)
+    shape = capi.buffer_shape(lat, p)
+    with Stepper(lat, p) as s:
+        s.set_ramp(ramp, 0.0)
+        pitched, _ = s.buffer(capi.PSI_EVEN)
+        for call, t in enumerate((0.25, 0.75)):
+            fields = capi.Fields()
+            assert lib.gpe_ramp_eval(C.byref(ramp), t, C.byref(fields)) == 0
+            assert fields.bq_quad != 0 and any(fields.bb_quad[i] != 0 for i in range(3))
+            s.upload(capi.PSI_EVEN, 0.2 * states.random_state(shape, seed=700 + call))
+            want = s.observe(capi.PSI_EVEN, t=t)
+            st, got = _noalloc(lib, lat, p, fields, t, pitched)
+            assert st == capi.GPE_OK, lib.gpe_last_error()
+            _compare(got, want)
+
+
+def test_noalloc_during_expansion(gpu):
+    """With condensate expansion the caller passes the current block scale
+    bs(t) as block_scale; the integrals then carry dv = bs(t)^3 VOLUME where the
+    handle keeps bs0^3 VOLUME."""
+    lib = gpu
+    lat = capi.Lattice("bcc")
+    bs0, t0, rate = 0.3, 0.1, 2.0
+    p = capi.make_params(components=3, precision=capi.FP64, dims=(7, 6, 5), block_scale=bs0, dt=1e-4, trap_offset=100.0,
+                         c0=120.0, c2=-7.0, lattice=lat)
+    fields = capi.make_fields(bq=0.3, bb=(0.1, -0.2, 0.5))
+    ramp = capi.make_ramp(bq_segments=[(fields.bq, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[(tuple(fields.bb), 1e9, capi.RAMP_CONSTANT)])
+    shape = capi.buffer_shape(lat, p)
+    with Stepper(lat, p) as s:
+        s.set_ramp(ramp, 0.0)
+        s.set_expansion(t0, rate)
+        pitched, _ = s.buffer(capi.PSI_EVEN)
+        for call, t in enumerate((0.2, 0.4)):
+            bs = bs0 * (1.0 + rate * (t - t0))
+            # the box origin p0 stays where the handle set it; only the block scale grows
+            q = capi.make_params(components=3, precision=capi.FP64, dims=(7, 6, 5), block_scale=bs, dt=1e-4,
+                                 p0=tuple(p.p0), trap_offset=100.0, c0=120.0, c2=-7.0, lattice=lat)
+            s.upload(capi.PSI_EVEN, 0.2 * states.random_state(shape, seed=800 + call))
+            want = s.observe(capi.PSI_EVEN, t=t)
+            st, got = _noalloc(lib, lat, q, fields, t, pitched)
+            assert st == capi.GPE_OK, lib.gpe_last_error()
+            k = (bs0 / bs) ** 3
+            for key in ("norm", "energy", "h_expect", "spin_norm"):
+                got[key] *= k
+            got["magnetization"] = [m * k for m in got["magnetization"]]
+            got["com"] = [c * k for c in got["com"]]
+            _compare(got, want)
+
+
 def test_noalloc_rejects_oversized_tables(gpu):
     lib = gpu
     lat = capi.Lattice("bcc")
