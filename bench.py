@@ -597,7 +597,8 @@ def run_gpu(args):
         s._nsteps += INNER
 
     kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_fixed_kernel<float,3,LEAPFROG,4>",
-                   capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>"}
+                   capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>",
+                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
     for key, val in ((capi.TUNE_TILE_CELLS, args.tile), (capi.TUNE_TILE_ROWS, args.rows), (capi.TUNE_ZCHUNK, args.zchunk),
@@ -776,7 +777,7 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 gather, 2 row tile, 3 z-march, 4 multi-row tile")
+    ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 gather, 2 row tile, 3 z-march, 4 multi-row tile, 5 slab ring")
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--rows", type=int, default=0)
     ap.add_argument("--zchunk", type=int, default=0)

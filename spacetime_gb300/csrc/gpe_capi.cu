@@ -38,6 +38,8 @@ template <typename R>
 cudaError_t launch_split(const StepArgs& a, int part, double qinit, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_parabolic_slab(const StepArgs& a, uint32_t Tx, uint32_t Ty, uint32_t S, cudaStream_t s);
 enum HyperKind {
     HK_FUSED_LEAPFROG = 0,
     HK_PSI_PARA_LEAPFROG,
@@ -704,6 +706,68 @@ static cudaError_t dispatch_march(const gpe_handle* h, const StepArgs& a, const 
     }
 }
 
+// Shape of the slab-ring kernel (Tx = 0: not used); S: psi_prev ring slots (0:
+// automatic).
+struct SlabShape {
+    uint32_t Tx = 0, Ty = 0, S = 0;
+};
+
+// Whether the slab kernel's rings fit for a Tx x Ty tile at two blocks per SM:
+// S (at least four) psi_prev slabs within 110 KB.
+static bool slab_slots(const gpe_handle* h, uint32_t Tx, uint32_t Ty, uint32_t S = 4) {
+    const uint64_t slab = (uint64_t)(Tx + 2) * (Ty + 2) * h->g.cell_bytes;
+    return S >= 4 && S <= 8 && S * slab <= 110ull * 1024;
+}
+
+// The slab-ring kernel applies to leapfrog steps on lattices whose nodes all have
+// 4 stencil entries, with 16-byte cells.  Tile: Tx x Ty cells with Tx * Ty * V <=
+// 384 threads and at least four slabs per block at two blocks per SM; by default
+// the shape with the least halo per cell, whole tiles preferred, then larger tiles.
+// GPE_TUNE_ZCHUNK, if set, is the number of psi_prev slabs.
+static SlabShape slab_shape(const gpe_handle* h) {
+    SlabShape r;
+    if (h->tune_kernel != 5) return r;
+    if (h->tab.uniform_deg != 4 || h->g.cell_bytes % 16 != 0) return r;
+    const uint32_t V = h->g.V, X = h->g.X, Y = h->g.Y;
+    const uint32_t S = h->tune_zchunk > 0 ? (uint32_t)h->tune_zchunk : 4u;
+    if (h->tune_tile > 0 && h->tune_rows > 0) {
+        const uint32_t Tx = (uint32_t)h->tune_tile, Ty = (uint32_t)h->tune_rows;
+        if (Tx * Ty * V <= 384 && slab_slots(h, Tx, Ty, S)) {
+            r.Tx = Tx;
+            r.Ty = Ty;
+            r.S = h->tune_zchunk > 0 ? S : 0;
+        }
+        return r;
+    }
+    double best = 1e30;
+    for (uint32_t Ty = 1; Ty <= Y && Ty <= 16; ++Ty)
+        for (uint32_t Tx = 1; Tx <= X && Tx * Ty * V <= 384; ++Tx) {
+            if (!slab_slots(h, Tx, Ty, S)) continue;
+            const double halo = (double)(Tx + 2) * (Ty + 2) / ((double)Tx * Ty);
+            const bool whole = X % Tx == 0 && Y % Ty == 0;
+            const double score = halo * (whole ? 1.0 : 1.25) - 1e-3 * Tx * Ty - 1e-4 * Tx;
+            if (score < best) {
+                best = score;
+                r.Tx = Tx;
+                r.Ty = Ty;
+                r.S = h->tune_zchunk > 0 ? S : 0;
+            }
+        }
+    return r;
+}
+
+template <int C>
+static cudaError_t dispatch_slab_c(const gpe_handle* h, const StepArgs& a, const SlabShape& m, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_parabolic_slab<double, C>(a, m.Tx, m.Ty, m.S, s)
+                              : launch_parabolic_slab<float, C>(a, m.Tx, m.Ty, m.S, s);
+}
+static cudaError_t dispatch_slab(const gpe_handle* h, const StepArgs& a, const SlabShape& m, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_slab_c<1>(h, a, m, s);
+        case 3: return dispatch_slab_c<3>(h, a, m, s);
+        default: return dispatch_slab_c<5>(h, a, m, s);
+    }
+}
 
 // Row buffers a block of RY x RZ output rows needs: the distinct (y, z) rows
 // (relative to the block origin) reached by the stencil's (dy, dz) offsets.
@@ -816,7 +880,7 @@ static cudaError_t dispatch_rows(const gpe_handle* h, const StepArgs& a, const R
 // automatic choice is the grid-stride gather kernel: on GB300 (FP32, 10^6-10^7
 // sites) it is as fast as the row tile or faster on every lattice and spin.
 static uint32_t tile_cells(const gpe_handle* h) {
-    if (h->tune_kernel == 0 || h->tune_kernel == 1 || h->tune_kernel == 3) return 0;
+    if (h->tune_kernel == 0 || h->tune_kernel == 1 || h->tune_kernel == 3 || h->tune_kernel == 5) return 0;
     if (h->g.cell_bytes % 16 != 0) return 0;
     const uint32_t V = h->g.V, X = h->g.X;
     uint32_t tmax = 256 / V;
@@ -900,8 +964,10 @@ gpe_status gpe::step_buffers(gpe_handle* h, char* next, const char* prev, const 
     const MarchShape ms = march_shape(h);
     const uint32_t T = tile_cells(h);
     const RowsShape rs = rows_shape(h);
+    const SlabShape ss = slab_shape(h);
     cudaError_t e;
-    if (mode == GPE_MODE_LEAPFROG && rs.T > 0) {
+    if (mode == GPE_MODE_LEAPFROG && ss.Tx > 0) e = dispatch_slab(h, a, ss, s);
+    else if (mode == GPE_MODE_LEAPFROG && rs.T > 0) {
         gpe_status bst = ensure_row_block(h, rs);
         if (bst) return bst;
         e = dispatch_rows(h, a, rs, s);
@@ -916,7 +982,8 @@ gpe_status gpe::step_buffers(gpe_handle* h, char* next, const char* prev, const 
 }
 
 bool gpe::leapfrog_from_supported(const gpe_handle* h) {
-    return h->p.scheme == GPE_SCHEME_PARABOLIC && rows_shape(h).T == 0 && march_shape(h).T == 0 && tile_cells(h) == 0;
+    return h->p.scheme == GPE_SCHEME_PARABOLIC && rows_shape(h).T == 0 && march_shape(h).T == 0 && tile_cells(h) == 0 &&
+           slab_shape(h).Tx == 0;
 }
 
 gpe_status gpe::leapfrog_from(gpe_handle* h, char* next, const char* cur, const char* old, const gpe_fields& B,
@@ -1133,7 +1200,7 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
 extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
     if (key == GPE_TUNE_KERNEL) {
-        if (value < 0 || value > 4) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
+        if (value < 0 || value > 5) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
         if (value >= 2 && h->g.cell_bytes % 16 != 0) return fail(GPE_ERR_UNSUPPORTED, "tiled kernels need 16-byte cells");
         const int old = h->tune_kernel;
         h->tune_kernel = value;
@@ -1144,6 +1211,10 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
         if (value == 4 && rows_cells(h) == 0) {
             h->tune_kernel = old;
             return fail(GPE_ERR_UNSUPPORTED, "the multi-row tile does not fit in shared memory");
+        }
+        if (value == 5 && slab_shape(h).Tx == 0) {
+            h->tune_kernel = old;
+            return fail(GPE_ERR_UNSUPPORTED, "the slab kernel needs 4 entries per node and a tile whose slabs fit");
         }
         return GPE_OK;
     }
@@ -1189,6 +1260,11 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
         // hyperbolic handles: the fused tile kernel or the gather kernel
         const uint32_t T = hyper_tile_cells(h);
         *value = key == GPE_TUNE_KERNEL ? (T > 0 ? 2 : 1) : (int32_t)T;
+        return GPE_OK;
+    }
+    const SlabShape ss = slab_shape(h);
+    if (ss.Tx > 0 && (key == GPE_TUNE_KERNEL || key == GPE_TUNE_TILE_CELLS || key == GPE_TUNE_TILE_ROWS)) {
+        *value = key == GPE_TUNE_KERNEL ? 5 : (int32_t)(key == GPE_TUNE_TILE_CELLS ? ss.Tx : ss.Ty);
         return GPE_OK;
     }
     if (key == GPE_TUNE_KERNEL) *value = tr > 0 ? 4 : ms.T > 0 ? 3 : (tile_cells(h) > 0 ? 2 : 1);

@@ -9,6 +9,8 @@ GPE_INSTANTIATE_TILE(float, 1)
 GPE_INSTANTIATE_TILE(double, 1)
 GPE_INSTANTIATE_MARCH(float, 1)
 GPE_INSTANTIATE_MARCH(double, 1)
+GPE_INSTANTIATE_SLAB(float, 1)
+GPE_INSTANTIATE_SLAB(double, 1)
 GPE_INSTANTIATE_ROWS(float, 1)
 GPE_INSTANTIATE_ROWS(double, 1)
 GPE_INSTANTIATE_INIT(float, 1)

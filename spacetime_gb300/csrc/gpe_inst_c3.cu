@@ -9,6 +9,8 @@ GPE_INSTANTIATE_TILE(float, 3)
 GPE_INSTANTIATE_TILE(double, 3)
 GPE_INSTANTIATE_MARCH(float, 3)
 GPE_INSTANTIATE_MARCH(double, 3)
+GPE_INSTANTIATE_SLAB(float, 3)
+GPE_INSTANTIATE_SLAB(double, 3)
 GPE_INSTANTIATE_ROWS(float, 3)
 GPE_INSTANTIATE_ROWS(double, 3)
 GPE_INSTANTIATE_INIT(float, 3)

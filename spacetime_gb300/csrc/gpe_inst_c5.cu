@@ -9,6 +9,8 @@ GPE_INSTANTIATE_TILE(float, 5)
 GPE_INSTANTIATE_TILE(double, 5)
 GPE_INSTANTIATE_MARCH(float, 5)
 GPE_INSTANTIATE_MARCH(double, 5)
+GPE_INSTANTIATE_SLAB(float, 5)
+GPE_INSTANTIATE_SLAB(double, 5)
 GPE_INSTANTIATE_ROWS(float, 5)
 GPE_INSTANTIATE_ROWS(double, 5)
 GPE_INSTANTIATE_INIT(float, 5)

@@ -2376,3 +2376,5 @@ cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
 #define GPE_INSTANTIATE_HYPER_TILE(R, C) template cudaError_t launch_hyper_tile<R, C>(const StepArgs&, uint32_t, cudaStream_t);
 
 }  // namespace gpe
+
+#include "gpe_slab.cuh"

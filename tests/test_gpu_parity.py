@@ -615,6 +615,86 @@ def test_march_kernel(gpu, name, C, dims, shape, prec):
     _close(go, odd, prec, "odd")
 
 
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C,dims,shape", [
+    ("bcc", 3, (16, 8, 5), (8, 4)),        # whole tiles
+    ("bcc", 3, (13, 7, 6), (8, 4)),        # ragged in x and y
+    ("bcc", 3, (7, 5, 4), (0, 0)),         # automatic shape
+    ("bcc", 1, (20, 9, 3), (16, 2)),
+    ("bcc", 5, (9, 6, 4), (4, 2)),
+    ("bcc", 3, (3, 2, 1), (0, 0)),         # one plane, a grid smaller than the default tile
+    ("a15", 3, (5, 3, 4), (2, 2)),
+    ("z", 1, (4, 5, 3), (2, 2)),
+    ("c15", 1, (3, 2, 3), (1, 1)),
+])
+def test_slab_kernel(gpu, name, C, dims, shape, prec):
+    """Slab-ring kernel (psi_prev planes in a ring of shared-memory slabs filled by
+    bulk copies, the column marching up z) against the oracle over three steps."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, prec, dims)
+    cell_bytes = lat.nodes * C * (16 if prec == capi.FP64 else 8)
+    # four psi_prev slabs must fit in 110 KB
+    while shape[0] and (shape[0] + 2) * (shape[1] + 2) * 4 * cell_bytes > 110 * 1024:
+        shape = (max(1, shape[0] // 2), shape[1] if shape[0] > 1 else max(1, shape[1] // 2))
+    even, odd = _rand(lat, p, 121), _rand(lat, p, 122)
+    f = capi.make_fields(**FIELDS)
+    with Stepper(lat, p) as s:
+        if shape[0]:
+            s.set_tuning(capi.TUNE_TILE_CELLS, shape[0])
+            s.set_tuning(capi.TUNE_TILE_ROWS, shape[1])
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_SLAB)
+        assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_SLAB
+        if shape[0]:
+            assert (s.get_tuning(capi.TUNE_TILE_CELLS), s.get_tuning(capi.TUNE_TILE_ROWS)) == shape
+        s.upload(capi.PSI_EVEN, even)
+        s.upload(capi.PSI_ODD, odd)
+        bufs = [capi.PSI_EVEN, capi.PSI_ODD]
+        for n in range(3):
+            s.step_explicit(bufs[(n + 1) % 2], bufs[n % 2], f, t=0.1 * n)
+        ge, go = s.download(capi.PSI_EVEN), s.download(capi.PSI_ODD)
+    b = [even, odd]
+    for n in range(3):
+        oracle.parabolic_step(lat, p, f, 0.1 * n, oracle.LEAPFROG, b[(n + 1) % 2], b[n % 2])
+    _close(ge, even, prec, "even")
+    _close(go, odd, prec, "odd")
+
+
+@pytest.mark.parametrize("C", [1, 3, 5])
+def test_slab_kernel_matches_gather_to_rounding(gpu, C):
+    """The slab kernel does the gather kernel's arithmetic in the same order (the
+    compiler may contract a different multiply-add): a ramped run of 20 leapfrog
+    steps agrees to a few FP32 ulps of the largest value."""
+    lat = capi.Lattice("bcc")
+    p = _params(lat, C, capi.FP32, (24, 17, 11))
+    ramp = capi.make_ramp(bq_segments=[(0.2, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0, 0, 0.5), 0.0, capi.RAMP_CONSTANT), ((0, 0, -0.5), 20 * p.dt, capi.RAMP_LINEAR),
+                                       ((0, 0, -0.5), 1e9, capi.RAMP_CONSTANT)])
+    psi = _rand(lat, p, 123)
+    out = []
+    for kernel in (capi.KERNEL_GATHER, capi.KERNEL_SLAB):
+        with Stepper(lat, p) as s:
+            s.set_tuning(capi.TUNE_KERNEL, kernel)
+            s.upload(capi.PSI_ODD, psi)
+            s.set_ramp(ramp, 0.0)
+            s.start()
+            s.step(20)
+            out.append((s.download(capi.PSI_EVEN), s.download(capi.PSI_ODD)))
+    for a, b in zip(out[0], out[1]):
+        scale = float(np.max(np.abs(a)))
+        err = float(np.max(np.abs(a - b)))
+        assert err <= 1e-6 * scale, "max|slab - gather| = %.3e, scale %.3e" % (err, scale)
+
+
+def test_slab_kernel_rejected_where_it_does_not_apply(gpu):
+    """FCC rows of 4 and 8 entries and the cube's 6: no slab kernel."""
+    for name in ("fcc", "cube"):
+        lat = capi.Lattice(name)
+        with Stepper(lat, _params(lat, 3, capi.FP32, (6, 4, 4))) as s:
+            with pytest.raises(capi.GpeError):
+                s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_SLAB)
+            assert s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER
+
+
 @pytest.mark.parametrize("name,C,want", [("bcc", 1, capi.KERNEL_GATHER), ("bcc", 5, capi.KERNEL_GATHER),
                                          ("fcc", 3, capi.KERNEL_GATHER), ("a15", 3, capi.KERNEL_GATHER),
                                          ("c15", 5, capi.KERNEL_GATHER), ("fcc", 1, capi.KERNEL_GATHER)])
