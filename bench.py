@@ -557,6 +557,21 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+def replica_throughput(local_ms, units_per_rank, world, device="cpu"):
+    """Replicas (one independent condensate per rank, no data-path collective):
+    the job's time is the slowest rank's, and the job processed world x the units
+    of one rank.  Returns (max over ranks of local_ms, units per second)."""
+    import torch
+
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    return ms, world * units_per_rank / (ms * 1e-3)
+
+
 def run_gpu(args):
     import ctypes as C
 
@@ -636,11 +651,7 @@ def run_gpu(args):
         launches = s.launches - launches0
         total_ms = ev_start.elapsed_time(ev_end)
         step_ms = sum(a.elapsed_time(b) for a, b in batch)
-    t_ms = torch.tensor([total_ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t_ms, op=dist.ReduceOp.MAX)
-    total_ms = float(t_ms.item())
-    value = world * sites * INNER * args.steps / (total_ms * 1e-3)
+    total_ms, value = replica_throughput(total_ms, sites * INNER * args.steps, world, "cuda")
     launch_ms = step_ms / (INNER * args.steps)
     algo_bytes = BYTES_PER_SITE_FP32 * sites
     achieved = algo_bytes / (launch_ms * 1e-3) / 1e9

@@ -7,8 +7,11 @@ set -e
 REF=${SPACETIME_REF:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-[ -f "$REF/GrossPitaevskii/GPBlocks.cpp" ] || { echo "reference tree not found at $REF" >&2; exit 3; }
+# without the reference tree there is nothing to build: say so and succeed
+[ -f "$REF/GrossPitaevskii/GPBlocks.cpp" ] || { echo "reference tree not found at $REF: oracle/_ref not built" >&2; exit 0; }
 mkdir -p "$OUT"
+# where the reference tree was found, for the tests that compare with its headers
+echo "$REF" > "$OUT/ref_root.txt"
 CXX=${CXX:-g++}
 FLAGS="-O2 -ffp-contract=off -w -include $HERE/ref_compat.h -I$REF"
 cd "$OUT"

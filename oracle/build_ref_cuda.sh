@@ -17,8 +17,11 @@ set -e
 REF=${SPACETIME_REF:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-[ -f "$REF/Spin1GpeBCC/Spin1GpeBCC.cu" ] || { echo "reference tree not found at $REF" >&2; exit 3; }
+# without the reference tree there is nothing to build: say so and succeed
+[ -f "$REF/Spin1GpeBCC/Spin1GpeBCC.cu" ] || { echo "reference tree not found at $REF: oracle/_ref not built" >&2; exit 0; }
 mkdir -p "$OUT"
+# where the reference tree was found, for the tests that compare with its headers
+echo "$REF" > "$OUT/ref_root.txt"
 NVCC=${NVCC:-nvcc}
 build() {  # $1 = program path without .cu, $2 = output name
     d=$(dirname "$1")

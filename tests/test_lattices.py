@@ -7,7 +7,20 @@ import pytest
 from spacetime_gb300 import capi
 from spacetime_gb300.lattices import import_mesh_tables as imp
 
-REF = os.environ.get("SPACETIME_REF", "/root/reference")
+def _reference_root():
+    """The reference tree: SPACETIME_REF, else where the oracle's build recipe
+    found it (oracle/_ref/ref_root.txt); empty if neither is known."""
+    env = os.environ.get("SPACETIME_REF", "")
+    if env:
+        return env
+    rec = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "ref_root.txt")
+    if os.path.exists(rec):
+        with open(rec) as f:
+            return f.read().strip()
+    return ""
+
+
+REF = _reference_root()
 
 
 @pytest.mark.parametrize("name", capi.LATTICE_NAMES)
@@ -54,7 +67,8 @@ def test_degrees():
     assert capi.Lattice("c15").nodes == 136 and capi.Lattice("c15").edges == 272
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "Spin1GpeBCC")), reason="reference tree not present")
+@pytest.mark.skipif(not REF or not os.path.isdir(os.path.join(REF, "Spin1GpeBCC")),
+                    reason="reference tree not known (set SPACETIME_REF, or build the oracle with it present)")
 def test_tables_match_reference_headers(tmp_path):
     written = imp.import_all(REF, str(tmp_path))
     import json
