@@ -611,6 +611,29 @@ def run_gpu(args):
         s.step(INNER)
         s._nsteps += INNER
 
+    def advance_observed(ev=None):
+        """One bench step: INNER leapfrog steps, the observables summed inside the
+        last one (FP32 node terms, FP64 sums); with --observe-fp64 a separate
+        observe pass with FP64 node terms after the steps.  ev: three events
+        recorded before the steps, after the INNER - 1 plain step launches, and
+        after the observed step (its finalize included)."""
+        if ev:
+            ev[0].record(stream)
+        if args.observe_fp64:
+            advance()
+            if ev:
+                ev[1].record(stream)
+            o = s.observe(cur_slot(), s._nsteps * DT)
+        else:
+            s.step(INNER - 1)
+            if ev:
+                ev[1].record(stream)
+            s._nsteps += INNER
+            o = s.step_observe(1)
+        if ev:
+            ev[2].record(stream)
+        return o
+
     kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_fixed_kernel<float,3,LEAPFROG,4>",
                    capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>",
                    capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>"}
@@ -631,56 +654,60 @@ def run_gpu(args):
         s.set_ramp(ramp, 0.0)
         s.start()
         for _ in range(args.warmup):
-            advance()
-            s.observe(cur_slot(), s._nsteps * DT)
+            advance_observed()
         barrier()
         launches0 = s.launches
         ev_start, ev_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        batch = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        batch = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in range(args.steps)]
         obs = []
         with ClockSampler(local) as clk:
             ev_start.record(stream)
             for k in range(args.steps):
-                batch[k][0].record(stream)
-                advance()
-                batch[k][1].record(stream)
-                obs.append(s.observe(cur_slot(), s._nsteps * DT))
+                obs.append(advance_observed(batch[k]))
             ev_end.record(stream)
             barrier()
         clocks = clk.summary()
         launches = s.launches - launches0
         total_ms = ev_start.elapsed_time(ev_end)
-        step_ms = sum(a.elapsed_time(b) for a, b in batch)
+        plain_ms = sum(a.elapsed_time(b) for a, b, _ in batch)
+        observed_ms = sum(b.elapsed_time(c) for _, b, c in batch) / args.steps
     total_ms, value = replica_throughput(total_ms, sites * INNER * args.steps, world, "cuda")
-    launch_ms = step_ms / (INNER * args.steps)
+    # the step kernel's mean duration over the plain launches (INNER - 1 per bench
+    # step; the observed step, with its finalize, is timed on its own)
+    plain_launches = (INNER - (0 if args.observe_fp64 else 1)) * args.steps
+    launch_ms = plain_ms / plain_launches
     algo_bytes = BYTES_PER_SITE_FP32 * sites
     achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = traffic_from_profile(kernel_name[chosen])
 
-    # ---- end to end through the C ABI with host buffers: H2D of the FP64 host state
-    # (reference file layout, pinned), start + 100 leapfrog steps + FP64 observables
-    # read back, every step.
+    # ---- end to end through the C ABI with host buffers, every step: the FP64 host
+    # state (reference file layout, pinned) in, start + 100 leapfrog steps with the
+    # observables summed in the last one, and the final FP64 state back out into a
+    # pinned host array (what a caller of the reference's time loop writes out at
+    # every save, Spin1GpeBCC.cu:1688-1692).
     host = torch.from_numpy(psi0.ravel()).pin_memory()
     host_np = host.numpy().reshape(psi0.shape)
+    out_host = torch.empty(psi0.size, dtype=torch.float64).pin_memory()
+    out_np = out_host.numpy().reshape(psi0.shape)
     e2e_steps = max(3, min(args.steps, 10))
+
+    def e2e_step():
+        s.upload(capi.PSI_ODD, host_np)
+        s.set_ramp(ramp, 0.0)
+        s.start()
+        s._nsteps = 0
+        o = advance_observed()
+        s.download(cur_slot(), out=out_np)
+        return o
+
     with torch.cuda.stream(stream):
         for _ in range(2):
-            s.upload(capi.PSI_ODD, host_np)
-            s.set_ramp(ramp, 0.0)
-            s.start()
-            s._nsteps = 0
-            advance()
-            s.observe(cur_slot(), s._nsteps * DT)
+            e2e_step()
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            s.upload(capi.PSI_ODD, host_np)
-            s.set_ramp(ramp, 0.0)
-            s.start()
-            s._nsteps = 0
-            advance()
-            s.observe(cur_slot(), s._nsteps * DT)
+            e2e_obs = e2e_step()
         barrier()
         e2e_s = time.perf_counter() - t0
     e2e_value = world * sites * INNER * e2e_steps / e2e_s
@@ -716,11 +743,14 @@ def run_gpu(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kernel_name[chosen], "tile_cells_rows_zchunk": tile, "algorithmic_bytes_per_launch": algo_bytes,
-                     "avg_launch_ms": launch_ms},
+                     "avg_launch_ms": launch_ms, "launches_timed": plain_launches},
+        "observed_step_ms": observed_ms,
         "e2e": {"value": e2e_value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
-                "d2h_bytes_per_step": 8 * 12, "steps": e2e_steps,
-                "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step(100) + gpe_observe"},
-        "observables": "FP64 node terms and sums" if args.observe_fp64 else "FP32 node terms, FP64 sums",
+                "d2h_bytes_per_step": int(psi0.nbytes) + 8 * 12, "steps": e2e_steps,
+                "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step_observe(100) + gpe_download (FP64 host, pinned)",
+                "norm_last": e2e_obs["norm"]},
+        "observables": "FP64 node terms and sums (separate pass)" if args.observe_fp64 else
+                       "summed inside the last step kernel of each bench step (FP32 node terms, FP64 sums)",
         "fp64_plain": {"value": fp64_value, "unit": "lattice-site-updates/s", "ms_per_launch": fp64_ms,
                        "speedup_fp32_fused": (sites / (launch_ms * 1e-3)) / fp64_value},
         "gpu_launches": launches,

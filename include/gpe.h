@@ -370,6 +370,18 @@ gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);
  * THREAD_BLOCK_X/Y/Z, Spin1GpeBCC.cu:39-41). */
 gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, size_t report_len, void* stream);
 
+/* n_steps leapfrog steps, as gpe_step, returning the observables of the state the
+ * last step reads (the state after n_steps - 1 steps, at the last step's time):
+ * the numbers gpe_observe(h, slot, t) gives for that state.  On the default
+ * (gather) step kernel they are summed inside that step's kernel from its own
+ * H psi, with no separate pass over the state: per-node terms in the storage
+ * precision (FP32 handles: as GPE_TUNE_OBSERVE_ARITH = 1), sums in FP64.  With
+ * another step kernel or scheme a separate observe pass runs before the last
+ * step.  Replaces the reference's integrate / localAvgSpinAndDensity reductions
+ * after a block of leapfrog launches (Spin1GpeBCC.cu:191-271, 992-1020, the save
+ * step of its time loop :1611-1658).  Synchronises `stream`. */
+gpe_status gpe_step_observe(gpe_handle* h, int32_t n_steps, gpe_observables* out, void* stream);
+
 /* Slot (GPE_PSI_EVEN or GPE_PSI_ODD) holding the newest state after the last
  * gpe_start / gpe_step / gpe_itp call. */
 int32_t gpe_current_slot(const gpe_handle* h);

@@ -40,6 +40,8 @@ template <typename R, int C>
 cudaError_t launch_leapfrog_march(const StepArgs& a, uint32_t T, uint32_t TY, uint32_t ZC, uint32_t threads, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_parabolic_slab(const StepArgs& a, uint32_t Tx, uint32_t Ty, uint32_t S, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_parabolic_observe(const StepArgs& a, double* out, cudaStream_t s);
 enum HyperKind {
     HK_FUSED_LEAPFROG = 0,
     HK_PSI_PARA_LEAPFROG,
@@ -1124,20 +1126,9 @@ extern "C" gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream) {
     return GPE_OK;
 }
 
-extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream) {
-    if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
-    if (!slot_ok(h, slot) || slot == GPE_Q_EVEN || slot == GPE_Q_ODD) return fail(GPE_ERR_INVALID_ARG, "psi slot");
-    cudaStream_t s = (cudaStream_t)stream;
-    StepArgs a = make_args(h, fields_at(h, t), t);
-    a.prev = h->interior[slot];
-    cudaError_t e = dispatch_observe(h, a, h->obs_out, s);
-    if (e != cudaSuccess) return cuda_fail(e, "observe launch");
-    h->launches += 2;
-    double r[OBS_COUNT];
-    CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    gpe_status dst = check_device_error(h, s);
-    if (dst) return dst;
+// The observables from the OBS_COUNT FP64 sums of an observe or observed-step
+// launch (dv = bs0^3 VOLUME).
+static gpe_status fill_observables(const gpe_handle* h, const double* r, gpe_observables* out) {
     const double dv = cell_dv(h);
     std::memset(out, 0, sizeof *out);
     out->norm = r[OBS_NORM] * dv;
@@ -1154,6 +1145,68 @@ extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_obs
     out->nonfinite = (int32_t)r[OBS_NONFINITE];
     if (out->nonfinite) return fail(GPE_ERR_NONFINITE, "state holds non-finite values");
     return GPE_OK;
+}
+
+template <int C>
+static cudaError_t dispatch_parabolic_observe_c(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_parabolic_observe<double, C>(a, out, s) : launch_parabolic_observe<float, C>(a, out, s);
+}
+
+extern "C" gpe_status gpe_step_observe(gpe_handle* h, int32_t n, gpe_observables* out, void* stream) {
+    if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (n < 1) return fail(GPE_ERR_INVALID_ARG, "step count must be at least 1");
+    cudaStream_t s = (cudaStream_t)stream;
+    gpe_status st = gpe_step(h, n - 1, stream);
+    if (st) return st;
+    const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
+    if (!leapfrog_from_supported(h)) {
+        // another step kernel (tile, slab, hyperbolic, split): a separate observe pass
+        gpe_observables o;
+        gpe_status ost = gpe_observe(h, h->cur, t, &o, stream);
+        if (ost && ost != GPE_ERR_NONFINITE) return ost;
+        st = gpe_step(h, 1, stream);
+        *out = o;
+        return st ? st : (ost ? fail(ost, "state holds non-finite values") : GPE_OK);
+    }
+    const gpe_fields B = fields_at(h, t);
+    const int prev = h->cur, next = h->cur == GPE_PSI_EVEN ? GPE_PSI_ODD : GPE_PSI_EVEN;
+    StepArgs a = make_args(h, B, t);
+    a.prev = h->interior[prev];
+    a.next = h->interior[next];
+    cudaError_t e;
+    switch (h->g.C) {
+        case 1: e = dispatch_parabolic_observe_c<1>(h, a, h->obs_out, s); break;
+        case 3: e = dispatch_parabolic_observe_c<3>(h, a, h->obs_out, s); break;
+        default: e = dispatch_parabolic_observe_c<5>(h, a, h->obs_out, s); break;
+    }
+    h->launches += 2;
+    h->epoch += 1;
+    if (e != cudaSuccess) return cuda_fail(e, "observed step launch");
+    h->cur = next;
+    h->nstep++;
+    double r[OBS_COUNT];
+    CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    gpe_status dst = check_device_error(h, s);
+    if (dst) return dst;
+    return fill_observables(h, r, out);
+}
+
+extern "C" gpe_status gpe_observe(gpe_handle* h, int32_t slot, double t, gpe_observables* out, void* stream) {
+    if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (!slot_ok(h, slot) || slot == GPE_Q_EVEN || slot == GPE_Q_ODD) return fail(GPE_ERR_INVALID_ARG, "psi slot");
+    cudaStream_t s = (cudaStream_t)stream;
+    StepArgs a = make_args(h, fields_at(h, t), t);
+    a.prev = h->interior[slot];
+    cudaError_t e = dispatch_observe(h, a, h->obs_out, s);
+    if (e != cudaSuccess) return cuda_fail(e, "observe launch");
+    h->launches += 2;
+    double r[OBS_COUNT];
+    CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    gpe_status dst = check_device_error(h, s);
+    if (dst) return dst;
+    return fill_observables(h, r, out);
 }
 
 extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* stream) {

@@ -401,18 +401,164 @@ __device__ __forceinline__ NodeTab<R, D> node_tab(const SmemTables<R>& st, uint3
     return node_tab<R, D>(st, l, (int)l * D);
 }
 
+// The step kernels' default: no observables.
+struct NoObs {
+    template <typename R, int C>
+    __device__ __forceinline__ void node(const PhysR<R>&, const R*, const Cx<R>*, const Cx<R>*) {}
+};
+
+// Observables of the state a step reads, summed by each thread over its nodes:
+// the per-node terms of observe_kernel (density, <psi|H psi>, interaction energy,
+// magnetisation, spin norm, centre of mass, max |psi_s|, non-finite count) in the
+// storage precision R, from the step's own H psi (Laplacian + local terms at the
+// step's time, already in registers), groups of kGroup nodes summed in R and each
+// group added in FP64 (FP64 storage: every node in FP64).  The thread's FP64 sums
+// live in shared memory (kObsSums x blockDim doubles, thread-major per sum), which
+// keeps the step kernel's register count, and so its occupancy, near the plain
+// step's.
+constexpr int kObsSums = OBS_MAXABS;  // the summed observables come first in ObsIndex
+static_assert(OBS_MAXABS + 2 == OBS_COUNT && OBS_NONFINITE == OBS_MAXABS + 1, "max and count last");
+template <typename R>
+struct ObsAcc {
+    static constexpr int kGroup = sizeof(R) == 4 ? 8 : 1;
+    double* sums;  // this thread's column of the block's kObsSums x blockDim array
+    R grp[kObsSums];
+    int in_group;
+    R tmax;
+    uint32_t nbad;
+    __device__ __forceinline__ explicit ObsAcc(double* block_sums) : sums(block_sums + threadIdx.x), in_group(0), tmax((R)0), nbad(0) {
+#pragma unroll
+        for (int k = 0; k < kObsSums; ++k) {
+            sums[k * blockDim.x] = 0.0;
+            grp[k] = (R)0;
+        }
+    }
+    template <typename RR, int C>
+    __device__ __forceinline__ void node(const PhysR<R>& P, const R r[3], const Cx<R>* ps, const Cx<R>* H) {
+        R v[kObsSums];
+#pragma unroll
+        for (int k = 0; k < kObsSums; ++k) v[k] = (R)0;
+        R rho = 0, hexp = 0;
+#pragma unroll
+        for (int s = 0; s < C; ++s) {
+            const R n2 = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+            rho += n2;
+            tmax = fmax(tmax, sqrt(n2));
+            if (!isfinite(ps[s].x) || !isfinite(ps[s].y)) ++nbad;
+            hexp += ps[s].x * H[s].x + ps[s].y * H[s].y;
+        }
+        v[OBS_NORM] = rho;
+        v[OBS_HEXP] = hexp;
+        v[OBS_COMX] = rho * r[0];
+        v[OBS_COMY] = rho * r[1];
+        v[OBS_COMZ] = rho * r[2];
+        // interaction energy as observe_kernel: c0 n^2 (scalar), c0 n^2 + c2 |<F>|^2
+        // (spin-1), psi^H (local terms without trap, fields, loss) psi (spin-2)
+        if constexpr (C == 1) {
+            v[OBS_EINT] = P.c0 * rho * rho;
+        } else if constexpr (C == 3) {
+            const Cx<R> m = (R)GPE_REF_SQRT_2 * (conj(ps[0]) * ps[1] + conj(ps[1]) * ps[2]);
+            const R fz = (ps[0].x * ps[0].x + ps[0].y * ps[0].y) - (ps[2].x * ps[2].x + ps[2].y * ps[2].y);
+            v[OBS_EINT] = P.c0 * rho * rho + P.c2 * (m.x * m.x + m.y * m.y + fz * fz);
+            v[OBS_MAGX] = m.x;
+            v[OBS_MAGY] = m.y;
+            v[OBS_MAGZ] = fz;
+            v[OBS_SPIN] = sqrt(m.x * m.x + m.y * m.y + fz * fz);
+        } else {
+            PhysR<R> Q = P;
+            Q.bq = Q.bqq = 0;
+            for (int k = 0; k < 3; ++k) Q.bb[k] = Q.bbq[k] = 0;
+            Q.flags &= ~(GPE_FLAG_THREE_BODY_LOSS | GPE_FLAG_QUADRATIC_ZEEMAN | GPE_FLAG_QUADRUPOLE_OFFSET);
+            Cx<R> Hn[5];
+#pragma unroll
+            for (int s = 0; s < 5; ++s) Hn[s] = cx<R>((R)0, (R)0);
+            local_terms<R, C>(Q, r, (R)0, GPE_MODE_LEAPFROG, false, ps, Hn);
+            R hn = 0;
+#pragma unroll
+            for (int s = 0; s < C; ++s) hn += ps[s].x * Hn[s].x + ps[s].y * Hn[s].y;
+            v[OBS_EINT] = hn;
+            const Cx<R> fp = (R)2 * (conj(ps[0]) * ps[1] + conj(ps[3]) * ps[4]) +
+                             (R)2.449489742783178098 * (conj(ps[1]) * ps[2] + conj(ps[2]) * ps[3]);
+            R n[5];
+            for (int s = 0; s < 5; ++s) n[s] = ps[s].x * ps[s].x + ps[s].y * ps[s].y;
+            const R fz = (R)2 * n[0] + n[1] - n[3] - (R)2 * n[4];
+            v[OBS_MAGX] = fp.x;
+            v[OBS_MAGY] = fp.y;
+            v[OBS_MAGZ] = fz;
+            v[OBS_SPIN] = sqrt(fp.x * fp.x + fp.y * fp.y + fz * fz);
+        }
+#pragma unroll
+        for (int k = 0; k < kObsSums; ++k) grp[k] += v[k];
+        if (++in_group == kGroup) flush();
+    }
+    __device__ __forceinline__ void flush() {
+#pragma unroll
+        for (int k = 0; k < kObsSums; ++k) {
+            sums[k * blockDim.x] += (double)grp[k];
+            grp[k] = (R)0;
+        }
+        in_group = 0;
+    }
+    // the block's sums into partials[blockIdx.x]: warp shuffles, then shared memory
+    // (red: 8 x OBS_COUNT doubles); every thread of the block must call it
+    __device__ __forceinline__ void block_reduce(double (*red)[OBS_COUNT], double* partials) {
+        flush();
+        double acc[OBS_COUNT];
+#pragma unroll
+        for (int k = 0; k < kObsSums; ++k) acc[k] = sums[k * blockDim.x];
+        acc[OBS_MAXABS] = (double)tmax;
+        acc[OBS_NONFINITE] = (double)nbad;
+#pragma unroll
+        for (int k = 0; k < OBS_COUNT; ++k) {
+            double v = acc[k];
+            for (int o = 16; o > 0; o >>= 1) {
+                const double u = __shfl_down_sync(0xffffffffu, v, o);
+                v = (k == OBS_MAXABS) ? fmax(v, u) : v + u;
+            }
+            acc[k] = v;
+        }
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < OBS_COUNT; ++k) red[warp][k] = acc[k];
+        }
+        __syncthreads();
+        if (threadIdx.x < OBS_COUNT) {
+            const int k = threadIdx.x;
+            double v = red[0][k];
+            for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = (k == OBS_MAXABS) ? fmax(v, red[w][k]) : v + red[w][k];
+            partials[(size_t)blockIdx.x * OBS_COUNT + k] = v;
+        }
+    }
+};
+
+// The accumulator of a step kernel: ObsAcc (its FP64 sums in the block's shared
+// array) or NoObs.
+template <bool OBS, typename R>
+struct ObsOf {
+    using type = NoObs;
+    __device__ static NoObs make(double*) { return NoObs(); }
+};
+template <typename R>
+struct ObsOf<true, R> {
+    using type = ObsAcc<R>;
+    __device__ static ObsAcc<R> make(double* sums) { return ObsAcc<R>(sums); }
+};
+
 // The local terms and the time update of one node, given its Laplacian sum in H
-// (Spin1GpeBCC.cu:867-916).  nv: the old next record (leapfrog).
-template <typename R, int C, int MODE>
+// (Spin1GpeBCC.cu:867-916).  nv: the old next record (leapfrog).  oa: where the
+// observables of prv go (ObsAcc), or nothing (NoObs).
+template <typename R, int C, int MODE, class OA = NoObs>
 __device__ __forceinline__ void node_finish(const PhysR<R>& P, const R pos[3], uint32_t x, uint32_t y, uint32_t z,
                                             const Cx<R>* prv, Cx<R>* H, Cx<R>* nv, char* nxt, char* hp,
-                                            const PhysR<R>* F = nullptr) {
+                                            const PhysR<R>* F = nullptr, OA* oa = nullptr) {
     R r[3];
     r[0] = P.p0[0] + P.bs * ((R)x * P.bw[0] + pos[0]);
     r[1] = P.p0[1] + P.bs * ((R)y * P.bw[1] + pos[1]);
     r[2] = P.p0[2] + P.bs * ((R)z * P.bw[2] + pos[2]);
     const R pot = trap<R>(P, r, F);
     local_terms<R, C>(P, r, pot, MODE, false, prv, H, F);
+    if constexpr (!std::is_same<OA, NoObs>::value) oa->template node<R, C>(P, r, prv, H);
     if constexpr (MODE == GPE_MODE_LEAPFROG || MODE == kModeLeapfrogFrom) {
         // next = old + 2 dt (-i H), the whole record written at once
 #pragma unroll
@@ -429,11 +575,12 @@ __device__ __forceinline__ void node_finish(const PhysR<R>& P, const R pos[3], u
 // (a multiple of 4 of them, f_more a multiple of 4) come from the shared tables, 4
 // loads at a time (FCC's octahedra: 8 entries beside the tetrahedra's 4).
 // prev/next/hpsi are the buffers' interior pointers; (x, y, z) the cell, l the node.
-template <typename R, int C, int MODE, int D, int G = D, bool MORE = false>
+template <typename R, int C, int MODE, int D, int G = D, bool MORE = false, class OA = NoObs>
 __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R, D>& t, const PhysR<R>& P,
                                                  const char* prev, char* next, char* hpsi, uint32_t x, uint32_t y,
                                                  uint32_t z, uint32_t l, const SmemTables<R>* st = nullptr,
-                                                 int f_more = 0, int f_end = 0, const PhysR<R>* F = nullptr) {
+                                                 int f_more = 0, int f_end = 0, const PhysR<R>* F = nullptr,
+                                                 OA* oa = nullptr) {
     const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
     const char* base = prev + cell_off;
     const uint32_t node_bytes = C * 2 * sizeof(R);
@@ -488,7 +635,7 @@ __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R,
         }
     }
     char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
-    node_finish<R, C, MODE>(P, t.pos, x, y, z, prv, H, nv, nxt, hp, F);
+    node_finish<R, C, MODE, OA>(P, t.pos, x, y, z, prv, H, nv, nxt, hp, F, oa);
 }
 
 // One node of a parabolic step: the DEC Laplacian gather, the local terms and the
@@ -497,16 +644,17 @@ __device__ __forceinline__ void parabolic_node_t(const Grid& g, const NodeTab<R,
 // entries (MORE: a multiple of 4, the first D taken as the node's table), the
 // neighbour loads issued G at a time.  F: where the step's fields come from (P if
 // null).
-template <typename R, int C, int MODE, int D = 0, int G = D, bool MORE = false>
+template <typename R, int C, int MODE, int D = 0, int G = D, bool MORE = false, class OA = NoObs>
 __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R>& st, const PhysR<R>& P, const char* prev,
                                                char* next, char* hpsi, uint32_t x, uint32_t y, uint32_t z, uint32_t l,
-                                               const PhysR<R>* F = nullptr) {
+                                               const PhysR<R>* F = nullptr, OA* oa = nullptr) {
     if constexpr (D > 0 && MORE) {
         const int f0 = st.row_ptr[l];
-        parabolic_node_t<R, C, MODE, D, G, true>(g, node_tab<R, D>(st, l, f0), P, prev, next, hpsi, x, y, z, l, &st,
-                                                 f0 + D, st.row_ptr[l + 1], F);
+        parabolic_node_t<R, C, MODE, D, G, true, OA>(g, node_tab<R, D>(st, l, f0), P, prev, next, hpsi, x, y, z, l, &st,
+                                                     f0 + D, st.row_ptr[l + 1], F, oa);
     } else if constexpr (D > 0) {
-        parabolic_node_t<R, C, MODE, D, G>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l, nullptr, 0, 0, F);
+        parabolic_node_t<R, C, MODE, D, G, false, OA>(g, node_tab<R, D>(st, l), P, prev, next, hpsi, x, y, z, l, nullptr, 0,
+                                                      0, F, oa);
     } else {
         const size_t cell_off = (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x * g.cell_bytes;
         const char* base = prev + cell_off;
@@ -548,18 +696,21 @@ __device__ __forceinline__ void parabolic_node(const Grid& g, const SmemTables<R
         }
         const R pos[3] = {st.pos[3 * l + 0], st.pos[3 * l + 1], st.pos[3 * l + 2]};
         char* hp = (MODE == GPE_MODE_ITP && hpsi) ? hpsi + cell_off + l * node_bytes : nullptr;
-        node_finish<R, C, MODE>(P, pos, x, y, z, prv, H, nv, nxt, hp, F);
+        node_finish<R, C, MODE, OA>(P, pos, x, y, z, prv, H, nv, nxt, hp, F, oa);
     }
 }
 
 // MODE: GPE_MODE_LEAPFROG / EULER / ITP.  Grid-stride over the nodes, one node
 // per thread per pass, on a fixed grid, so that each block stages the tables once.
-template <typename R, int C, int MODE, int D>
-__global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
+template <typename R, int C, int MODE, int D, bool OBS>
+__device__ __forceinline__ void parabolic_step_body(const StepArgs& a) {
     __shared__ SmemTables<R> st;
     load_tables<R>(st, a);
     __syncthreads();
     const PhysR<R>& P = make_phys<R>(a);
+    using OA = typename ObsOf<OBS, R>::type;
+    __shared__ double obs_sums[OBS ? kObsSums * 256 : 1];
+    OA oa = ObsOf<OBS, R>::make(obs_sums);
     for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
          gid += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)gid;
@@ -569,8 +720,21 @@ __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
         const uint32_t l = within - x * a.g.V;
         const uint32_t z = fdiv(row, a.divY);
         const uint32_t y = row - z * a.g.Y;
-        parabolic_node<R, C, MODE, D>(a.g, st, P, a.prev, a.next, a.hpsi, x, y, z, l);
+        parabolic_node<R, C, MODE, D, D, false, OA>(a.g, st, P, a.prev, a.next, a.hpsi, x, y, z, l, nullptr, &oa);
     }
+    if constexpr (OBS) {
+        __shared__ double red[8][OBS_COUNT];
+        oa.block_reduce(red, a.partials);
+    }
+}
+template <typename R, int C, int MODE, int D>
+__global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
+    parabolic_step_body<R, C, MODE, D, false>(a);
+}
+// The same with the observables of the state it reads (three blocks per SM).
+template <typename R, int C, int MODE, int D>
+__global__ void __launch_bounds__(256, 3) parabolic_step_obs_kernel(StepArgs a) {
+    parabolic_step_body<R, C, MODE, D, true>(a);
 }
 
 // The same update on a grid whose stride is a multiple of V: a thread keeps one
@@ -578,26 +742,43 @@ __global__ void __launch_bounds__(256) parabolic_step_kernel(StepArgs a) {
 // once into registers instead of from shared memory for every node.  Every node has
 // D entries, or (MORE) a multiple of 4 of them, the entries past the first D read
 // from the shared tables.  G: neighbour loads issued together.
-template <typename R, int C, int MODE, int D, int G, bool MORE>
-__global__ void __launch_bounds__(256) parabolic_fixed_kernel(StepArgs a) {
+template <typename R, int C, int MODE, int D, int G, bool MORE, bool OBS>
+__device__ __forceinline__ void parabolic_fixed_body(const StepArgs& a) {
     __shared__ SmemTables<R> st;
     load_tables<R>(st, a);
     __syncthreads();
     const PhysR<R>& P = make_phys<R>(a);
+    using OA = typename ObsOf<OBS, R>::type;
+    __shared__ double obs_sums[OBS ? kObsSums * 256 : 1];
+    OA oa = ObsOf<OBS, R>::make(obs_sums);
     uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= a.total) return;
+    if (!OBS && gid >= a.total) return;
     const uint32_t l = (uint32_t)gid - fdiv((uint32_t)gid, a.divV) * a.g.V;
     const int f0 = MORE ? st.row_ptr[l] : (int)l * D;
     const int f_end = MORE ? st.row_ptr[l + 1] : 0;
-    const NodeTab<R, D> t = node_tab<R, D>(st, l, f0);
+    const NodeTab<R, D> t = node_tab<R, D>(st, gid < a.total ? l : 0u, gid < a.total ? f0 : 0);
     for (; gid < a.total; gid += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t i = (uint32_t)gid;
         const uint32_t row = fdiv(i, a.divRow);
         const uint32_t x = fdiv(i - row * a.row_items, a.divV);
         const uint32_t z = fdiv(row, a.divY);
         const uint32_t y = row - z * a.g.Y;
-        parabolic_node_t<R, C, MODE, D, G, MORE>(a.g, t, P, a.prev, a.next, a.hpsi, x, y, z, l, &st, f0 + D, f_end);
+        parabolic_node_t<R, C, MODE, D, G, MORE, OA>(a.g, t, P, a.prev, a.next, a.hpsi, x, y, z, l, &st, f0 + D, f_end,
+                                                     nullptr, &oa);
     }
+    if constexpr (OBS) {
+        __shared__ double red[8][OBS_COUNT];
+        oa.block_reduce(red, a.partials);
+    }
+}
+template <typename R, int C, int MODE, int D, int G, bool MORE>
+__global__ void __launch_bounds__(256) parabolic_fixed_kernel(StepArgs a) {
+    parabolic_fixed_body<R, C, MODE, D, G, MORE, false>(a);
+}
+// The same with the observables of the state it reads (three blocks per SM).
+template <typename R, int C, int MODE, int D, int G, bool MORE>
+__global__ void __launch_bounds__(256, 3) parabolic_fixed_obs_kernel(StepArgs a) {
+    parabolic_fixed_body<R, C, MODE, D, G, MORE, true>(a);
 }
 
 // SM count of the current device (cached per device).
@@ -1047,16 +1228,18 @@ inline unsigned nblocks(uint64_t items, unsigned bs) { return (unsigned)((items 
 
 // One wave of resident blocks (the kernel's occupancy x SMs), fewer for small grids.
 // D > 0: the fixed-node kernel (see parabolic_fixed_kernel for D, G, MORE).
-template <typename R, int C, int MODE, int D, int G, bool MORE>
-cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s) {
+template <typename R, int C, int MODE, int D, int G, bool MORE, bool OBS = false>
+cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s, unsigned* grid = nullptr) {
     if constexpr (D > 0) {
         // the largest multiple of V / gcd(V, 256) blocks within one wave: the grid
         // stride is then a multiple of V
+        auto kf = OBS ? parabolic_fixed_obs_kernel<R, C, MODE, D, G, MORE> : parabolic_fixed_kernel<R, C, MODE, D, G, MORE>;
         static int occ_f = 0;
         if (occ_f == 0) {
-            cudaFuncSetAttribute(parabolic_fixed_kernel<R, C, MODE, D, G, MORE>,
-                                 cudaFuncAttributePreferredSharedMemoryCarveout, 25);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, parabolic_fixed_kernel<R, C, MODE, D, G, MORE>, 256, 0);
+            // a small shared-memory share leaves the rest of L1 to cache the gathers; the
+            // observed step also holds its FP64 sums there (20 KB per block)
+            cudaFuncSetAttribute(kf, cudaFuncAttributePreferredSharedMemoryCarveout, OBS ? 50 : 25);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, kf, 256, 0);
             if (occ_f < 1) occ_f = 1;
         }
         uint32_t gv = a.g.V, gb = 256;
@@ -1069,22 +1252,25 @@ cudaError_t launch_parabolic_m(const StepArgs& a, cudaStream_t s) {
         const uint64_t wave = std::min<uint64_t>((uint64_t)occ_f * (unsigned)device_sm_count(), (a.total + 255) / 256);
         const unsigned nb = (unsigned)(wave / m * m);
         if (nb > 0) {
-            parabolic_fixed_kernel<R, C, MODE, D, G, MORE><<<nb, 256, 0, s>>>(a);
+            kf<<<nb, 256, 0, s>>>(a);
+            if (grid) *grid = nb;
             return cudaGetLastError();
         }
     }
     // grids smaller than V / gcd(V, 256) blocks: the grid-stride kernel (the
     // 4-entry form where every node has 4 entries)
     constexpr int DS = (D == 4 && !MORE) ? 4 : 0;
+    auto ks = OBS ? parabolic_step_obs_kernel<R, C, MODE, DS> : parabolic_step_kernel<R, C, MODE, DS>;
     static int occ = 0;
     if (occ == 0) {
         // a small shared-memory share leaves the rest of L1 to cache the gathers
-        cudaFuncSetAttribute(parabolic_step_kernel<R, C, MODE, DS>, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, parabolic_step_kernel<R, C, MODE, DS>, 256, 0);
+        cudaFuncSetAttribute(ks, cudaFuncAttributePreferredSharedMemoryCarveout, OBS ? 50 : 25);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ks, 256, 0);
         if (occ < 1) occ = 1;
     }
     const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), (unsigned)occ * (unsigned)device_sm_count());
-    if (nb) parabolic_step_kernel<R, C, MODE, DS><<<nb, 256, 0, s>>>(a);
+    if (nb) ks<<<nb, 256, 0, s>>>(a);
+    if (grid) *grid = nb;
     return cudaGetLastError();
 }
 
@@ -1114,6 +1300,24 @@ cudaError_t launch_parabolic(const StepArgs& a, int mode, cudaStream_t s) {
         if (a.tab.uniform_deg == 6) return launch_parabolic_d<R, C, 6, 2>(a, mode, s);
     }
     return launch_parabolic_d<R, C, 0>(a, mode, s);
+}
+
+// A leapfrog step that also sums the observables of the state it reads (ObsAcc):
+// block partials into a.partials, then the fixed-order finalize into out.
+template <typename R, int C>
+cudaError_t launch_parabolic_observe(const StepArgs& a, double* out, cudaStream_t s) {
+    if (a.total == 0) return cudaErrorInvalidValue;
+    unsigned nb = 0;
+    cudaError_t e;
+    constexpr int G4 = C <= 3 ? 4 : 2;
+    if (a.tab.uniform_deg == 4) e = launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, 4, G4, false, true>(a, s, &nb);
+    else if (a.tab.quad_rows) e = launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, 4, G4, true, true>(a, s, &nb);
+    else if (a.tab.uniform_deg == 6)
+        e = launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, 6, (C == 1 ? 6 : (C == 3 ? 3 : 2)), false, true>(a, s, &nb);
+    else e = launch_parabolic_m<R, C, GPE_MODE_LEAPFROG, 0, 0, false, true>(a, s, &nb);
+    if (e != cudaSuccess) return e;
+    observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
+    return cudaGetLastError();
 }
 
 // kinds of hyperbolic launches
@@ -1325,6 +1529,7 @@ cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, c
 
 #define GPE_INSTANTIATE(R, C)                                                               \
     template cudaError_t launch_parabolic<R, C>(const StepArgs&, int, cudaStream_t);       \
+    template cudaError_t launch_parabolic_observe<R, C>(const StepArgs&, double*, cudaStream_t); \
     template cudaError_t launch_hyper<R, C>(const StepArgs&, int, cudaStream_t);           \
     template cudaError_t launch_observe<R, C>(const StepArgs&, double*, bool, cudaStream_t);     \
     template cudaError_t launch_scale<R, C>(const StepArgs&, const double*, double, cudaStream_t);

@@ -59,9 +59,15 @@ class Stepper:
         a = np.ascontiguousarray(arr, dtype=np.float64)
         capi.check(self.lib.gpe_upload(self._h, slot, a.ctypes.data_as(C.POINTER(C.c_double)), a.size, self.stream), "gpe_upload")
 
-    def download(self, slot: int) -> np.ndarray:
+    def download(self, slot: int, out: np.ndarray | None = None) -> np.ndarray:
+        """The slot's state as an FP64 host array in the reference file layout;
+        `out` (C-contiguous float64 of that shape, pinned for full link speed) is
+        filled in place when given."""
         edges = slot in (capi.Q_EVEN, capi.Q_ODD)
-        out = np.zeros(self.shape(edges))
+        if out is None:
+            out = np.zeros(self.shape(edges))
+        elif out.shape != tuple(self.shape(edges)) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("download: out must be a C-contiguous float64 array of shape %s" % (self.shape(edges),))
         capi.check(self.lib.gpe_download(self._h, slot, out.ctypes.data_as(C.POINTER(C.c_double)), out.size, self.stream), "gpe_download")
         return out
 
@@ -84,6 +90,13 @@ class Stepper:
 
     def step(self, n: int = 1):
         capi.check(self.lib.gpe_step(self._h, n, self.stream), "gpe_step")
+
+    def step_observe(self, n: int) -> dict:
+        """n leapfrog steps; the observables of the state the last step reads (after
+        n - 1 steps), summed inside that step's kernel (gpe_step_observe)."""
+        o = capi.Observables()
+        capi.check(self.lib.gpe_step_observe(self._h, n, C.byref(o), self.stream), "gpe_step_observe")
+        return o.as_dict()
 
     def step_explicit(self, next_slot, prev_slot, fields=None, t=0.0, mode=capi.MODE_LEAPFROG):
         f = C.byref(fields) if fields is not None else None

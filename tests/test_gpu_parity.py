@@ -826,3 +826,74 @@ def test_device_initial_state_matches_numpy(gpu, name, C, kind, prec):
         assert s.observe(capi.PSI_ODD)["norm"] == pytest.approx(1.0, rel=1e-12 if prec == capi.FP64 else 1e-6)
     tol = 1e-12 if prec == capi.FP64 else 1e-6
     assert np.max(np.abs(got - want)) <= tol * np.max(np.abs(want))
+
+
+def _obs_close(got, want, rel, what):
+    scale = max(abs(want["norm"]), abs(want["h_expect"]), 1e-30)
+    for k in ("norm", "energy", "h_expect", "spin_norm"):
+        assert got[k] == pytest.approx(want[k], rel=rel, abs=rel * scale), (what, k, got[k], want[k])
+    np.testing.assert_allclose(got["magnetization"], want["magnetization"], rtol=rel, atol=rel * scale, err_msg=what)
+    np.testing.assert_allclose(got["com"], want["com"], rtol=rel, atol=rel * scale * 10, err_msg=what)
+    assert got["max_abs"] == pytest.approx(want["max_abs"], rel=1e-6 if rel > 1e-9 else 1e-15), what
+    assert got["nonfinite"] == want["nonfinite"] == 0
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (12, 7, 5)), ("bcc", 1, (9, 8, 3)), ("bcc", 5, (6, 5, 4)),
+                                         ("fcc", 3, (6, 5, 4)), ("cube", 3, (20, 9, 7)), ("c15", 1, (3, 3, 2)),
+                                         ("a15", 5, (3, 2, 3)), ("bcc", 3, (1, 1, 1))])
+def test_step_observe_matches_step_and_observe(gpu, name, C, dims, prec):
+    """gpe_step_observe(n): the observables of the state the last step reads,
+    summed inside that step's kernel, equal gpe_observe of that state at the last
+    step's time (FP64 handles to 1e-11: the same FP64 terms added in another
+    order; FP32 handles against gpe_observe's FP32 node terms to 2e-6 of the
+    norm / energy scale: FP32 terms rounded in another order), and the states
+    equal plain stepping to rounding."""
+    lat = capi.Lattice(name)
+    flags = capi.FLAG_QUADRATIC_ZEEMAN | capi.FLAG_QUADRUPOLE_OFFSET if C == 3 else 0
+    p = _params(lat, C, prec, dims, flags=flags, quad_center=(0.1, -0.2, 0.05))
+    ramp = capi.make_ramp(bq_segments=[(0.3, 1e9, capi.RAMP_CONSTANT)],
+                          bb_segments=[((0.1, -0.2, 0.5), 0.0, capi.RAMP_CONSTANT), ((0.0, 0.1, -0.5), 8 * p.dt, capi.RAMP_LINEAR),
+                                       ((0.0, 0.1, -0.5), 1e9, capi.RAMP_CONSTANT)], bq_quad_scale=0.5, bb_quad_scale=0.25)
+    psi = _rand(lat, p, 131)
+    n = 5
+    with Stepper(lat, p) as a, Stepper(lat, p) as b:
+        for s in (a, b):
+            s.set_tuning(capi.TUNE_OBSERVE_ARITH, 1 if prec == capi.FP32 else 0)
+            s.upload(capi.PSI_ODD, psi)
+            s.set_ramp(ramp, 0.0)
+            s.start()
+        a.step(n - 1)
+        t_last = n * p.dt  # the start took step 0; the last of the n steps is step n
+        want = a.observe(a.current, t_last)
+        a.step(1)
+        n0 = b.launches
+        got = b.step_observe(n)
+        assert b.launches - n0 == n + 1  # n step launches + the finalize
+        assert a.current == b.current
+        sa, sb = a.download(a.current), b.download(b.current)
+    _obs_close(got, want, 1e-11 if prec == capi.FP64 else 2e-6, "%s C=%d" % (name, C))
+    scale = float(np.max(np.abs(sa)))
+    assert float(np.max(np.abs(sa - sb))) <= (1e-13 if prec == capi.FP64 else 1e-6) * scale
+
+
+def test_step_observe_with_another_kernel_and_scheme(gpu):
+    """Where the handle steps with a tile kernel or the hyperbolic scheme, the
+    observables come from a separate pass; the numbers are the same."""
+    for kind in ("tile", "hyper"):
+        lat = capi.Lattice("bcc")
+        kw = dict(scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01) if kind == "hyper" else {}
+        p = _params(lat, 3, capi.FP64, (8, 6, 5), **kw)
+        psi = _rand(lat, p, 132)
+        with Stepper(lat, p) as a, Stepper(lat, p) as b:
+            for s in (a, b):
+                if kind == "tile":
+                    s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_TILE)
+                s.upload(capi.PSI_ODD, psi)
+                s.start()
+            a.step(3)
+            want = a.observe(a.current, 4 * p.dt)
+            a.step(1)
+            got = b.step_observe(4)
+            assert np.array_equal(a.download(a.current), b.download(b.current))
+        _obs_close(got, want, 1e-13, kind)
