@@ -45,7 +45,8 @@ BYTES_PER_SITE_FP64 = 144
 #                 c0 = 2000, c2 = -20, c4 = 40, cyclic spinor + 1e-3 noise, sigma = 0.00225, dt = 2e-5
 LEGS = {
     "scalar-bcc32": dict(lattice="bcc", C=1, dims=(32, 32, 32), c0=2000.0, c2=0.0, c4=0.0, dt=1e-4, scheme=0,
-                         sigma=0.0, zeta=(1.0,), kappa=1, noise_abs=1e-3, noise_rel=0.0, bytes_fp32=24, seed=1),
+                         sigma=0.0, zeta=(1.0,), kappa=1, noise_abs=1e-3, noise_rel=0.0, bytes_fp32=24, seed=1,
+                         trap_offset=0.0),
     "spin2-c15-128": dict(lattice="c15", C=5, dims=(128, 128, 128), c0=2000.0, c2=-20.0, c4=40.0, dt=2e-5, scheme=1,
                           sigma=0.00225, zeta=(math.sqrt(1 / 3), 0, 0, math.sqrt(2 / 3), 0), kappa=0, noise_abs=0.0,
                           noise_rel=1e-3, bytes_fp32=360, seed=3),
@@ -80,9 +81,32 @@ def workload(precision):
     return lat, p, ramp, psi0
 
 
-def run_leg(args):
-    """An optional configuration: device-side initial state, start, `steps` x 100
-    steps timed with CUDA events, FP64 observables per bench step."""
+def leg_params(w, prec, dims=None):
+    """The leg's lattice and parameters (box [-8, 8]^3 along x) at `dims` (default
+    the leg's own)."""
+    from spacetime_gb300 import capi
+
+    lat = capi.Lattice(w["lattice"])
+    dims = tuple(dims or w["dims"])
+    bs = BOX / (dims[0] * lat.block_width[0])
+    p = capi.make_params(components=w["C"], scheme=w["scheme"], precision=prec, dims=dims, block_scale=bs, dt=w["dt"],
+                         trap_offset=w.get("trap_offset", 100.0), c0=w["c0"], c2=w["c2"], c4=w["c4"], sigma=w["sigma"],
+                         lattice=lat)
+    return lat, p
+
+
+def leg_init(w):
+    from spacetime_gb300 import capi
+
+    return capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"], noise_rel=w["noise_rel"],
+                          seed=w["seed"])
+
+
+def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
+    """A configuration on the device: seeded device-side initial state, start,
+    `steps` x `inner` steps timed with CUDA events on the launching stream (each
+    bench step's launches bracketed by events for the step kernel's mean
+    duration), FP64 observables after each bench step outside the kernel timing."""
     import ctypes as C
 
     import torch
@@ -90,23 +114,17 @@ def run_leg(args):
     from spacetime_gb300 import capi
     from spacetime_gb300.stepper import Stepper
 
-    w = LEGS[args.workload]
-    lat = capi.Lattice(w["lattice"])
-    bs = BOX / (w["dims"][0] * lat.block_width[0])
-    p = capi.make_params(components=w["C"], scheme=w["scheme"], precision=capi.FP32, dims=w["dims"], block_scale=bs,
-                         dt=w["dt"], trap_offset=100.0, c0=w["c0"], c2=w["c2"], c4=w["c4"], sigma=w["sigma"], lattice=lat)
+    lat, p = leg_params(w, capi.FP32, dims)
     stream = torch.cuda.Stream()
     s = Stepper(lat, p)
     s.stream = C.c_void_p(stream.cuda_stream)
-    if args.kernel:
-        s.set_tuning(capi.TUNE_KERNEL, args.kernel)
-    inner = args.inner or INNER
+    if kernel:
+        s.set_tuning(capi.TUNE_KERNEL, kernel)
     with torch.cuda.stream(stream):
-        s.init_state(s.current, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
-                                               noise_rel=w["noise_rel"], seed=w["seed"]))
+        s.init_state(s.current, leg_init(w))
         s.start()
         e0 = s.observe(s.current, 0.0)
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             s.step(inner)
         torch.cuda.synchronize()
         n0 = s.launches
@@ -115,7 +133,7 @@ def run_leg(args):
         with ClockSampler(0) as clk:
             a.record(stream)
             step_ms = 0.0
-            for _ in range(args.steps):
+            for _ in range(steps):
                 x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 x.record(stream)
                 s.step(inner)
@@ -129,46 +147,99 @@ def run_leg(args):
     sites = s.sites
     gather = s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER
     s.close()
-    drift = leg_drift(w, lat, args.drift_steps) if args.leg_drift else None
-    launch_ms = step_ms / (inner * args.steps)
+    launch_ms = step_ms / (inner * steps)
     algo = w["bytes_fp32"] * sites
     peak, kind = measured_peak()
     name = KERNEL_OF_SCHEME[w["scheme"]] % w["C"]
     if w["scheme"] == 1 and gather:
         name = "hyper_step_kernel<float,%d> (gather form)" % w["C"]
-    res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
-           "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f32", "data": "synthetic", "config": dict(w, workload=args.workload, sites=sites, inner_steps_per_step=inner),
-           "roofline": {"bound": "hbm", "achieved": algo / (launch_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": algo / (launch_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": name,
-                        "algorithmic_bytes_per_launch": algo, "avg_launch_ms": launch_ms, "traffic": None},
-           "gpu_launches": launches, "clocks": clk.summary(),
-           "energy_rel_drift": abs(obs[-1]["energy"] - e0["energy"]) / abs(e0["energy"]) if obs else None,
-           "norm_last": obs[-1]["norm"] if obs else None}
-    if drift is not None:
-        res["drift"] = drift
-    print(json.dumps(res))
-    return 0
+    if w["scheme"] == 0 and gather:
+        name = "parabolic_fixed_kernel<float,%d,LEAPFROG,4>" % w["C"]
+    return {"metric": "lattice-site-updates/s", "value": sites * inner * steps / (total_ms * 1e-3),
+            "unit": "lattice-site-updates/s", "steps": steps, "inner_steps_per_step": inner, "sites": sites,
+            "ms_per_step": total_ms / steps, "dims": list(p.dims),
+            "roofline": {"bound": "hbm", "achieved": algo / (launch_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / (launch_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": name,
+                         "algorithmic_bytes_per_launch": algo, "avg_launch_ms": launch_ms, "traffic": None},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "energy_rel_drift": abs(obs[-1]["energy"] - e0["energy"]) / abs(e0["energy"]) if obs else None,
+            "norm_last": obs[-1]["norm"] if obs else None}
 
 
-def leg_drift(w, lat, nsteps, every=100):
-    """FP32 against FP64 on the leg's workload from the same seeded device state:
-    observables (FP64 arithmetic) every `every` steps."""
+def leg_e2e(w, steps, inner, dims=None):
+    """End to end through the C ABI with host buffers, every step: the FP64 host
+    state (reference file layout, pinned) in, start (q from psi for the hyperbolic
+    scheme), `inner` steps with the observables summed in the last one (or after it,
+    on kernels without the fused form), the final FP64 state out into pinned host
+    memory."""
+    import ctypes as C
+
     import torch
 
     from spacetime_gb300 import capi
     from spacetime_gb300.stepper import Stepper
 
-    bs = BOX / (w["dims"][0] * lat.block_width[0])
-    runs = {}
+    lat, p = leg_params(w, capi.FP32, dims)
+    stream = torch.cuda.Stream()
+    s = Stepper(lat, p)
+    s.stream = C.c_void_p(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        s.init_state(capi.PSI_ODD, leg_init(w))
+        psi0 = s.download(capi.PSI_ODD)
+        host = torch.from_numpy(psi0.ravel()).pin_memory().numpy().reshape(psi0.shape)
+        out = torch.empty(psi0.size, dtype=torch.float64).pin_memory().numpy().reshape(psi0.shape)
+
+        def one():
+            s.upload(capi.PSI_ODD, host)
+            s.start()
+            o = s.step_observe(inner)
+            s.download(s.current, out=out)
+            return o
+
+        one()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o = one()
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+    sites = s.sites
+    s.close()
+    return {"value": sites * inner * steps / el, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
+            "d2h_bytes_per_step": int(psi0.nbytes) + 96, "steps": steps, "inner_steps_per_step": inner,
+            "dims": list(p.dims), "norm_last": o["norm"],
+            "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step_observe(%d) + gpe_download (FP64 host, pinned)" % inner}
+
+
+def run_leg(args):
+    """--workload <leg>: one configuration's timing, printed as one JSON line."""
+    w = LEGS[args.workload]
+    inner = args.inner or INNER
+    res = time_leg(w, args.steps, inner, args.warmup, args.kernel)
+    res.update({"n_gpus": 1, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": dict(w, workload=args.workload, sites=res["sites"], inner_steps_per_step=inner)})
+    if args.leg_drift:
+        res["drift"] = leg_drift(w, None, args.drift_steps)
+    print(json.dumps(res))
+    return 0
+
+
+def leg_drift(w, lat, nsteps, every=100, dims=None):
+    """FP32 against FP64 on the leg's workload from the same seeded device state:
+    observables (FP64 arithmetic) every `every` steps, and at the end the max-abs
+    difference of the two states."""
+    import torch
+
+    from spacetime_gb300 import capi
+    from spacetime_gb300.stepper import Stepper
+
+    runs, last = {}, {}
+    t0 = time.perf_counter()
     for prec in (capi.FP32, capi.FP64):
-        p = capi.make_params(components=w["C"], scheme=w["scheme"], precision=prec, dims=w["dims"], block_scale=bs,
-                             dt=w["dt"], trap_offset=100.0, c0=w["c0"], c2=w["c2"], c4=w["c4"], sigma=w["sigma"],
-                             lattice=lat)
+        lat, p = leg_params(w, prec, dims)
         s = Stepper(lat, p)
-        s.init_state(s.current, capi.make_init(zeta=w["zeta"], kappa=w["kappa"], noise_abs=w["noise_abs"],
-                                               noise_rel=w["noise_rel"], seed=w["seed"]))
+        s.init_state(s.current, leg_init(w))
         s.start()
         e = [s.observe(s.current, 0.0)]
         done = 0
@@ -179,13 +250,16 @@ def leg_drift(w, lat, nsteps, every=100):
             e.append(s.observe(s.current, done * w["dt"]))
         torch.cuda.synchronize()
         runs[prec] = e
+        last[prec] = s.download(s.current)
         s.close()
     e32, e64 = runs[capi.FP32], runs[capi.FP64]
-    return {"steps": nsteps, "every": every,
+    return {"steps": nsteps, "every": every, "dims": list(dims or w["dims"]), "against": "libgpe FP64 (plain) stepper",
             "energy_rel_diff_max": max(abs(a["energy"] - b["energy"]) / abs(b["energy"]) for a, b in zip(e32, e64)),
             "norm_rel_diff_max": max(abs(a["norm"] - b["norm"]) / abs(b["norm"]) for a, b in zip(e32, e64)),
             "energy_rel_drift_fp32": abs(e32[-1]["energy"] - e32[0]["energy"]) / abs(e32[0]["energy"]),
-            "energy_rel_drift_fp64": abs(e64[-1]["energy"] - e64[0]["energy"]) / abs(e64[0]["energy"])}
+            "energy_rel_drift_fp64": abs(e64[-1]["energy"] - e64[0]["energy"]) / abs(e64[0]["energy"]),
+            "psi_max_abs_err": float(np.max(np.abs(last[capi.FP32] - last[capi.FP64]))),
+            "psi_max_abs": float(np.max(np.abs(last[capi.FP64]))), "seconds": time.perf_counter() - t0}
 
 
 # Adjoint ramp control: spin-1, BCC 64^3 cells, 2000 steps, Bz(t) and Bq(t) with 16
@@ -196,8 +270,15 @@ ADJ = dict(dims=(64, 64, 64), steps=2000, stride=45, knots=16, fd_knots=8, h=1e-
 
 
 def run_adjoint(args):
-    """--workload adjoint-bcc64: gradient of the ramp-control loss through the adjoint
-    kernel (FP32 and FP64), timed, and checked against central differences."""
+    """--workload adjoint-bcc64: one JSON line."""
+    print(json.dumps(adjoint_result(args.steps, args.adjoint_steps, args.fd_knots)))
+    return 0
+
+
+def adjoint_result(reps, n_steps, fd_knots):
+    """Gradient of the ramp-control loss through the adjoint kernel (FP32 and
+    FP64), timed from host knots to host gradient, and checked against central
+    differences of the FP64 run."""
     import torch
 
     from spacetime_gb300 import capi, states
@@ -218,9 +299,9 @@ def run_adjoint(args):
     out = {}
     for prec in (capi.FP32, capi.FP64):
         s = Stepper(lat, params(prec))
-        rc = RampControl(s, args.adjoint_steps, ADJ["knots"], lambda: s.init_state(capi.PSI_ODD, init), target,
+        rc = RampControl(s, n_steps, ADJ["knots"], lambda: s.init_state(capi.PSI_ODD, init), target,
                          stride=ADJ["stride"])
-        reps = max(1, args.steps) if prec == capi.FP32 else 1
+        reps = max(1, reps) if prec == capi.FP32 else 1
         fwd, bwd, grads, loss = [], [], None, None
         n0 = s.launches
         for it in range(reps + (1 if prec == capi.FP32 else 0)):
@@ -242,7 +323,7 @@ def run_adjoint(args):
              "launches_per_gradient": launches}
         if prec == capi.FP64:
             rng = np.random.default_rng(ADJ["seed"])
-            picks = rng.choice(2 * ADJ["knots"], args.fd_knots, replace=False)
+            picks = rng.choice(2 * ADJ["knots"], fd_knots, replace=False)
             fd = []
             for i in picks:
                 kp, km = k.copy().ravel(), k.copy().ravel()
@@ -268,16 +349,16 @@ def run_adjoint(args):
     sites = lat.nodes * dims[0] * dims[1] * dims[2]
     f32 = out[capi.FP32]
     grad_s = f32["forward_s"] + f32["backward_s"]
-    res = {"metric": "adjoint gradient evaluations/s (forward + reverse run, %d steps)" % args.adjoint_steps,
+    res = {"metric": "adjoint gradient evaluations/s (forward + reverse run, %d steps)" % n_steps,
            "value": 1.0 / grad_s,
-           "unit": "gradients/s", "n_gpus": 1, "steps": max(1, args.steps), "warmup": 1,
+           "unit": "gradients/s", "n_gpus": 1, "steps": max(1, reps), "warmup": 1,
            "ms_per_step": 1e3 * grad_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic",
            "config": {"workload": "adjoint ramp control, spin-1 BCC 64^3 cells (%d sites), %d steps, %d+%d knots, "
-                                  "%d-step checkpoints" % (sites, args.adjoint_steps, ADJ["knots"], ADJ["knots"], ADJ["stride"]),
+                                  "%d-step checkpoints" % (sites, n_steps, ADJ["knots"], ADJ["knots"], ADJ["stride"]),
                       "dt": DT, "c0": C0, "c2": C2, "loss": "1 - |<monopole|psi(T)>|^2"},
            "forward_ms": 1e3 * f32["forward_s"], "backward_ms": 1e3 * f32["backward_s"],
-           "reverse_site_updates_per_s": sites * args.adjoint_steps / f32["backward_s"],
+           "reverse_site_updates_per_s": sites * n_steps / f32["backward_s"],
            "gpu_launches": f32["launches_per_gradient"],
            "loss_fp32": f32["loss"], "loss_fp64": out[capi.FP64]["loss"],
            "fp64_adjoint_vs_fd_max_rel": float(rel_fd64.max()), "fp32_adjoint_vs_fd_max_rel": float(rel_fd32.max()),
@@ -285,8 +366,15 @@ def run_adjoint(args):
            "fd_h": ADJ["h"], "fd_knots": [int(i) for i in picks], "fd": [float(x) for x in fd],
            "adjoint_fp64_at_fd_knots": [float(x) for x in g64[picks]],
            "fp64_forward_ms": 1e3 * out[capi.FP64]["forward_s"], "fp64_backward_ms": 1e3 * out[capi.FP64]["backward_s"]}
-    print(json.dumps(res))
-    return 0
+    # the timed call already runs through the public API from host arrays: the knots
+    # in (the per-step fields and the FP64 target state uploaded by
+    # gpe_adjoint_forward), the gradient out
+    fields_bytes = n_steps * 8 * 8
+    res["e2e"] = {"value": res["value"], "unit": "gradients/s", "h2d_bytes_per_step": int(fields_bytes + target.nbytes),
+                  "d2h_bytes_per_step": int(5 * 8 + n_steps * 4 * 8),
+                  "path": "torch knots -> gpe_adjoint_forward (fields + target from host) -> gpe_adjoint_backward "
+                          "(gradient to host) -> torch"}
+    return res
 
 
 # Batched ensemble: 256 condensates, block-cell edge n ~ U{24..80}, lattice ~ U{BCC,
@@ -294,7 +382,8 @@ def run_adjoint(args):
 # linear between two values in [-1, 1] over 2000 steps, Bq constant in [0, 0.5]),
 # box [-8, 8]^3, dt = 5e-5, FP32 with FP64 observables; all advanced by the
 # persistent batch kernel, n steps recorded in one CUDA graph.
-ENS = dict(members=256, edge=(24, 80), lattices=("bcc", "fcc", "a15", "c15"), seed=5, dt=5e-5, ramp_steps=2000)
+ENS = dict(members=256, edge=(24, 80), lattices=("bcc", "fcc", "a15", "c15"), seed=5, dt=5e-5, ramp_steps=2000,
+           steps=2000)
 
 
 def ensemble_members(count=None):
@@ -319,8 +408,15 @@ def ensemble_members(count=None):
 
 
 def run_ensemble(args):
-    """--workload ensemble-256: every member advanced by the persistent batch kernel,
-    `inner` steps per graph replay, timed with CUDA events."""
+    """--workload ensemble-256: one JSON line."""
+    print(json.dumps(ensemble_result(args.members, args.inner or 100, args.steps, args.warmup)))
+    return 0
+
+
+def ensemble_result(n_members, inner, replays, warmup):
+    """Every member advanced by the persistent batch kernel: `inner` steps in one
+    persistent launch per CUDA-graph replay, `replays` replays timed with CUDA
+    events (warm-up: `warmup` uncaptured 10-step batch calls)."""
     import ctypes as C
 
     import torch
@@ -329,10 +425,9 @@ def run_ensemble(args):
     from spacetime_gb300.batch import Batch
     from spacetime_gb300.stepper import Stepper
 
-    inner = args.inner or 100
     stream = torch.cuda.Stream()
     sp = C.c_void_p(stream.cuda_stream)
-    members, algo, state_bytes, specs = [], 0, 0, ensemble_members(args.members)
+    members, algo, state_bytes, specs = [], 0, 0, ensemble_members(n_members)
     t_setup = time.perf_counter()
     for i, (name, comps, n, omega, ramp) in enumerate(specs):
         lat = capi.Lattice(name)
@@ -356,13 +451,13 @@ def run_ensemble(args):
     sites = b.sites
     tune = b.autotune(steps=2)
     e_first = [members[k].observe(members[k].current) for k in (0, len(members) // 2, len(members) - 1)]
+    for _ in range(max(1, warmup)):
+        b.step(10)
     b.capture(inner, sp)
-    for _ in range(max(1, args.warmup)):
-        b.replay()
     n0 = b.launches
     ev = []
     with ClockSampler(0) as clk:
-        for _ in range(args.steps):
+        for _ in range(replays):
             x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             x.record(stream)
             b.replay()
@@ -374,17 +469,17 @@ def run_ensemble(args):
     launches = b.launches - n0
     e_last = [members[k].observe(members[k].current) for k in (0, len(members) // 2, len(members) - 1)]
     peak, kind = measured_peak()
-    step_ms = total_ms / (args.steps * inner)
+    step_ms = total_ms / (replays * inner)
     counts = {}
     for name, comps, n, _, _ in specs:
         key = "%s/%s" % (name, "spin1" if comps == 3 else "scalar")
         counts[key] = counts.get(key, 0) + 1
-    res = {"metric": "lattice-site-updates/s", "value": sites * inner * args.steps / (total_ms * 1e-3),
-           "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup),
-           "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    res = {"metric": "lattice-site-updates/s", "value": sites * inner * replays / (total_ms * 1e-3),
+           "unit": "lattice-site-updates/s", "n_gpus": 1, "steps": replays, "warmup": max(1, warmup),
+           "ms_per_step": total_ms / replays, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32", "data": "synthetic",
            "config": {"workload": "ensemble of %d condensates (edge 24..80, BCC/FCC/A15/C15, scalar + spin-1), "
-                                  "%d leapfrog steps per CUDA-graph replay" % (len(members), inner),
+                                  "%d leapfrog steps in one persistent launch per CUDA-graph replay" % (len(members), inner),
                       "sites": sites, "members": counts, "dt": ENS["dt"],
                       "l2": "inputs larger than L2 (%.1f GB per state buffer set), no flush" % (state_bytes / 1e9)},
            "roofline": {"bound": "hbm", "achieved": algo / (step_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -393,11 +488,20 @@ def run_ensemble(args):
            "gpu_launches": launches, "graph_replays": args.steps, "clocks": clk.summary(), "setup_s": setup_s,
            "autotune": tune,
            "norm_rel_change": [abs(b2["norm"] - a2["norm"]) / a2["norm"] for a2, b2 in zip(e_first, e_last)]}
+    # end to end: each replay's graph copies the members' step state (ramp, time,
+    # slot) from pinned host memory; after it every member's observables come back
+    t0 = time.perf_counter()
+    obs_all = [m.observe(m.current) for m in members]
+    res["e2e"] = {"value": sites * inner * replays / (total_ms * 1e-3 + (time.perf_counter() - t0) * replays),
+                  "unit": "lattice-site-updates/s", "h2d_bytes_per_step": len(members) * (C.sizeof(capi.Ramp) + 48),
+                  "d2h_bytes_per_step": 96 * len(members),
+                  "path": "gpe_batch_replay (graph: member state from pinned host memory + one persistent launch) + "
+                          "gpe_observe of every member",
+                  "norm_min_max": [min(o["norm"] for o in obs_all), max(o["norm"] for o in obs_all)]}
     b.close()
     for s in members:
         s.close()
-    print(json.dumps(res))
-    return 0
+    return res
 
 
 def config_dict():
@@ -485,6 +589,329 @@ def cpu_baseline(seconds=10.0):
             break
     return {"value": sites * n / el, "unit": "lattice-site-updates/s", "cores": threads, "kind": "port",
             "sample": "%d leapfrog steps of the full 96^3 spin-1 BCC grid (FP64 oracle, OpenMP %d threads), %.1f s" % (n, threads, el)}
+
+
+def _gpblocks_inputs(cells=32, g=2000.0, dt=1e-4):
+    """Config 1 in the reference CPU stepper's own layout (GrossPitaevskii/
+    GPBlocks.cpp:460-523): flat value arrays with the one-cell leading pad, the
+    BCC index table, dt folded into lapfac, lapfac0, g and the potential
+    V = |x|^2 / 2 (no offset) as integrateInTime does; the TF vortex + 1e-3 noise
+    of the GPU leg as the even and odd states."""
+    from spacetime_gb300 import capi, states
+
+    w = LEGS["scalar-bcc32"]
+    lat, p = leg_params(w, capi.FP64, (cells,) * 3)
+    X = Y = Z = cells
+    V = lat.nodes
+    deg = int(lat.row_ptr[1] - lat.row_ptr[0])
+    bsize, bxsize = V, (X + 1) * V
+    bxysize = (Y + 1) * bxsize
+    ii0 = bxysize + bxsize + bsize
+    vsize = ii0 + (Z + 1) * bxysize
+    st = lat.data["stencil"]
+    lapind = np.array([e[2] * bxysize + e[1] * bxsize + e[0] * bsize + e[3] for e in st], dtype=np.int64)
+    h = float(st[0][4])
+    bs = p.block_scale
+    dt_ref = 2 * dt  # one GPBlocks update advances by dt_ref / 2 (its odd buffer is shifted by -dt_ref / 2)
+    lapfac = -0.5 * h / (bs * bs)
+    lapfac0 = deg * (-lapfac)
+    psi = states.vortex_state(lat, p, seed=w["seed"], noise=1e-3)  # (Z+2, Y+2, X+2, V, 1, 2)
+    flat = np.zeros((vsize, 2))
+    pot = np.zeros(vsize)
+    r = states.node_positions(lat, p)  # (Z, Y, X, V, 3)
+    for k in range(Z):
+        for j in range(Y):
+            base = ii0 + k * bxysize + j * bxsize
+            flat[base:base + X * V] = psi[k + 1, j + 1, 1:X + 1, :, 0, :].reshape(-1, 2)
+            pot[base:base + X * V] = 0.5 * np.sum(r[k, j] ** 2, axis=-1).ravel()
+    return dict(X=X, Y=Y, Z=Z, V=V, deg=deg, lapind=lapind, lapfac=lapfac * dt_ref, lapfac0=lapfac0 * dt_ref,
+                g=g * dt_ref, pot=pot * dt_ref, even=flat.ravel().copy(), odd=flat.ravel().copy())
+
+
+def _gpblocks_worker(cells, steps, start_at):
+    """One process of the whole-socket sample: set up its own copy of config 1,
+    wait for the common start time, run `steps` GPBlocks steps (2 updates of every
+    value each) and print (site-updates, start, end) as JSON."""
+    from oracle import oracle
+
+    d = _gpblocks_inputs(cells)
+    while time.time() < start_at:
+        time.sleep(0.01)
+    t0 = time.time()
+    oracle.gpblocks_run(d["X"], d["Y"], d["Z"], d["V"], d["deg"], d["lapind"], d["lapfac"], d["lapfac0"], d["g"], d["pot"],
+                        d["even"], d["odd"], steps)
+    t1 = time.time()
+    print(json.dumps([d["X"] * d["Y"] * d["Z"] * d["V"] * 2 * steps, t0, t1]))
+
+
+def cpu_gpblocks(seconds=5.0, cells=32):
+    """Config 1 on the reference's CPU stepper (GPBlocks.cpp:560-606), in its
+    bit-exact restatement orc_gpblocks_run (the reference's printed norms
+    reproduced exactly, tests/test_oracle_golden.py): one core, then one copy per
+    host core at once (separate processes) for the socket's aggregate."""
+    from oracle import oracle
+
+    d = _gpblocks_inputs(cells)
+    sites = d["X"] * d["Y"] * d["Z"] * d["V"]
+    oracle.gpblocks_run(d["X"], d["Y"], d["Z"], d["V"], d["deg"], d["lapind"], d["lapfac"], d["lapfac0"], d["g"], d["pot"],
+                        d["even"], d["odd"], 2)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        oracle.gpblocks_run(d["X"], d["Y"], d["Z"], d["V"], d["deg"], d["lapind"], d["lapfac"], d["lapfac0"], d["g"],
+                            d["pot"], d["even"], d["odd"], 5)
+        n += 5
+    el = time.perf_counter() - t0
+    one = sites * 2 * n / el
+    res = {"value": one, "unit": "lattice-site-updates/s", "cores": 1, "kind": "port",
+           "sample": "%d GPBlocks steps (2 updates of every value each) of config 1 (%d^3 BCC cells), one thread, "
+                     "%.1f s; orc_gpblocks_run restates integrateInTime's loop and reproduces the reference's printed "
+                     "norms bit for bit" % (n, cells, el)}
+    cores = os.cpu_count() or 1
+    per = max(2, int(seconds * one / (2 * sites)))
+    start_at = time.time() + 8.0
+    code = "import bench; bench._gpblocks_worker(%d, %d, %r)" % (cells, per, start_at)
+    procs = [subprocess.Popen([sys.executable, "-c", code], cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                              text=True) for _ in range(cores)]
+    rows = []
+    try:
+        for pr in procs:
+            out, _ = pr.communicate(timeout=8.0 + 20 * seconds + 60)
+            if pr.returncode == 0 and out.strip():
+                rows.append(json.loads(out.strip().splitlines()[-1]))
+    except subprocess.TimeoutExpired:
+        for pr in procs:
+            pr.kill()
+    if len(rows) == cores:
+        wall = max(r[2] for r in rows) - min(r[1] for r in rows)
+        res["all_cores"] = {"value": sum(r[0] for r in rows) / wall, "cores": cores,
+                            "sample": "%d processes x %d steps at once, %.1f s from the first start to the last end "
+                                      "(set-up excluded)" % (cores, per, wall)}
+    else:
+        res["all_cores"] = {"unavailable": "%d of %d worker processes reported" % (len(rows), cores)}
+    return res
+
+
+def cpu_oracle_leg(w, dims, seconds=5.0):
+    """A leg's step on the FP64 oracle (all host threads), a bounded sample of the
+    same workload at `dims`."""
+    from oracle import oracle
+    from spacetime_gb300 import capi, states
+
+    lat, p = leg_params(w, capi.FP64, dims)
+    threads = os.cpu_count() or 1
+    sites = lat.nodes * int(np.prod(dims))
+    if w["C"] == 1:
+        psi = states.vortex_state(lat, p, seed=w["seed"], noise=1e-3, kappa=w["kappa"])
+    else:
+        psi = states.spinor_state(lat, p, w["zeta"], seed=w["seed"], noise=1e-3)
+    f = capi.make_fields()
+    n = 0
+    if w["scheme"] == 0:
+        bufs = [psi.copy(), psi.copy()]
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, bufs[(n + 1) % 2], bufs[n % 2], None, threads)
+            n += 1
+        what = "FP64 oracle leapfrog (orc_parabolic_step)"
+    else:
+        qshape = capi.buffer_shape(lat, p, True)
+        ps, qs = [psi.copy(), psi.copy()], [np.zeros(qshape), np.zeros(qshape)]
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            oracle.hyper_run(lat, p, ps[n % 2], ps[(n + 1) % 2], qs[n % 2], qs[(n + 1) % 2], 1, fields=f, threads=threads)
+            n += 1
+        what = "FP64 oracle hyperbolic psi + q step (orc_q_psi_step + orc_q_step)"
+    el = time.perf_counter() - t0
+    return {"value": sites * n / el, "unit": "lattice-site-updates/s", "cores": threads, "kind": "port",
+            "sample": "%d steps of %s on %s %s, %d threads, %.1f s" % (n, what, w["lattice"], "x".join(map(str, dims)),
+                                                                     threads, el)}
+
+
+def cpu_adjoint(seconds=5.0):
+    """Config 4 on the host: the CPU has no adjoint, so its gradient is central
+    differences, two forward runs per knot.  The FP64 oracle's leapfrog step on the
+    64^3 spin-1 workload is timed (all host threads) and the gradient rate derived
+    as 1 / (2 x 32 knots x 2000 steps x the step time)."""
+    from oracle import oracle
+    from spacetime_gb300 import capi, states
+
+    lat = capi.Lattice("bcc")
+    dims = ADJ["dims"]
+    bs = BOX / (dims[0] * lat.block_width[0])
+    p = capi.make_params(components=3, precision=capi.FP64, dims=dims, block_scale=bs, dt=DT, trap_offset=100.0, c0=C0,
+                         c2=C2, lattice=lat)
+    psi = states.spinor_state(lat, p, states.POLAR, seed=2, noise=1e-3)
+    bufs = [psi.copy(), psi.copy()]
+    threads = os.cpu_count() or 1
+    f = capi.make_fields(bq=0.2, bb=(0, 0, 0.5))
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, bufs[(n + 1) % 2], bufs[n % 2], None, threads)
+        n += 1
+    t_step = (time.perf_counter() - t0) / n
+    runs = 2 * 2 * ADJ["knots"]
+    return {"value": 1.0 / (runs * ADJ["steps"] * t_step), "unit": "gradients/s", "cores": threads, "kind": "port",
+            "sample": "%d FP64 oracle leapfrog steps of the 64^3 spin-1 grid, %d threads, %.3f s per step; a gradient "
+                      "by central differences takes %d forward runs of %d steps" % (n, threads, t_step, runs, ADJ["steps"])}
+
+
+def cpu_ensemble(seconds=5.0, count=4):
+    """Config 5 on the host: the FP64 oracle's leapfrog on the first `count`
+    members of the ensemble, each for an equal share of `seconds` (all host
+    threads); site-updates per second over the sample."""
+    from oracle import oracle
+    from spacetime_gb300 import capi, states
+
+    threads = os.cpu_count() or 1
+    done, el = 0, 0.0
+    names = []
+    for i, (name, comps, n, omega, ramp) in enumerate(ensemble_members(count)):
+        lat = capi.Lattice(name)
+        bs = BOX / (n * lat.block_width[0])
+        p = capi.make_params(components=comps, precision=capi.FP64, dims=(n, n, n), block_scale=bs, dt=ENS["dt"],
+                             trap_offset=100.0, trap_lambda=omega, c0=C0, c2=C2 if comps == 3 else 0.0, lattice=lat)
+        psi = states.spinor_state(lat, p, states.POLAR if comps == 3 else (1.0,), seed=1000 + i, noise=1e-3)
+        bufs = [psi.copy(), psi.copy()]
+        f = oracle.ramp_eval(ramp, 0.0)
+        k, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < seconds / count:
+            oracle.parabolic_step(lat, p, f, 0.0, oracle.LEAPFROG, bufs[(k + 1) % 2], bufs[k % 2], None, threads)
+            k += 1
+        el += time.perf_counter() - t0
+        done += lat.nodes * n ** 3 * k
+        names.append("%s/%s/%d^3" % (name, "spin1" if comps == 3 else "scalar", n))
+    return {"value": done / el, "unit": "lattice-site-updates/s", "cores": threads, "kind": "port",
+            "sample": "FP64 oracle leapfrog on members %s, %.1f s, %d threads" % (", ".join(names), el, threads)}
+
+
+LEG_NAMES = ("scalar-bcc32", "spin2-c15", "adjoint-bcc64", "ensemble-256")
+
+
+def run_legs(args):
+    """The benchmark plan's other configurations, each with its own value,
+    roofline, end-to-end number, CPU baseline and precision record:
+      scalar-bcc32   config 1: scalar BCC 32^3, g = 2000, no trap offset, 1000 steps
+                     per bench step; the reference CPU stepper (GPBlocks) as baseline
+      spin2-c15      config 3: relativistic spin-2 C15 128^3; FP32 against FP64 over
+                     10^4 steps at a smaller grid
+      adjoint-bcc64  config 4: ramp-control gradients by the adjoint kernel
+      ensemble-256   config 5: 256 uneven condensates, 2000 steps in one persistent
+                     launch"""
+    import torch
+
+    sel = LEG_NAMES if args.legs == "all" else tuple(x for x in args.legs.split(",") if x)
+    out = {}
+    for name in sel:
+        t0 = time.perf_counter()
+        try:
+            if name == "scalar-bcc32":
+                w = LEGS["scalar-bcc32"]
+                r = time_leg(w, steps=10, inner=100, warmup=3)
+                r["config"] = {"workload": "scalar GPE, BCC 32^3 block cells, box [-8,8]^3, trap (1,1,1) without offset, "
+                                           "g = 2000, TF vortex + 1e-3 noise, dt = 1e-4; 100 steps per bench step",
+                               "l2": "L2-resident (3.8 MB per FP32 buffer): the fraction is of the HBM peak"}
+                r["e2e"] = leg_e2e(w, steps=5, inner=1000)
+                r["cpu_baseline"] = cpu_gpblocks(args.cpu_seconds / 2)
+                r["drift"] = scalar_reference_drift()
+            elif name == "spin2-c15":
+                w = LEGS["spin2-c15-128"]
+                r = time_leg(w, steps=2, inner=10, warmup=1)
+                cells = args.c15_drift_cells
+                r["config"] = {"workload": "relativistic spin-2 GPE (hyperbolic psi + q), C15 128^3 block cells "
+                                           "(285,212,672 sites), c0 = 2000, c2 = -20, c4 = 40, cyclic + 1e-3 noise, "
+                                           "sigma = 0.00225, dt = 2e-5; 10 steps per bench step",
+                               "l2": "inputs larger than L2 (68.5 GB of FP32 psi + q), no flush"}
+                r["e2e"] = leg_e2e(w, steps=3, inner=100, dims=(48, 48, 48))
+                r["drift"] = leg_drift(w, None, args.c15_drift_steps, dims=(cells,) * 3)
+                r["drift"]["note"] = ("no reference program runs spin-2 on C15; the FP64 run is libgpe's FP64 hyperbolic "
+                                      "stepper, pinned to the reference's RelativisticSpin2Gpe kernels on BCC by golden vectors")
+                r["cpu_baseline"] = cpu_oracle_leg(w, (24, 24, 24), args.cpu_seconds / 2)
+            elif name == "adjoint-bcc64":
+                r = adjoint_result(2, ADJ["steps"], ADJ["fd_knots"])
+                r["cpu_baseline"] = cpu_adjoint(args.cpu_seconds / 2)
+            elif name == "ensemble-256":
+                r = ensemble_result(ENS["members"], ENS["steps"], 1, 1)
+                r["cpu_baseline"] = cpu_ensemble(args.cpu_seconds / 2)
+            else:
+                r = {"error": "unknown leg"}
+        except Exception as e:  # a failing leg is reported, the others still run
+            r = {"error": "%s: %s" % (type(e).__name__, str(e)[:300])}
+        r["wall_s"] = time.perf_counter() - t0
+        out[name] = r
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
+
+
+def scalar_reference_drift():
+    """Config 1 in FP32 against an FP64 run of the reference's own scalar BCC
+    kernel (GPUGrossPitaevskii_BCC.cu:327-347, compiled unmodified for sm_103a),
+    1000 steps, observables every 100 (the checker of oracle/ref_cuda_drift.py)."""
+    from oracle import ref_cuda, ref_cuda_drift
+
+    if not ref_cuda.available("scalar_bcc"):
+        return {"unavailable": "reference cubins not built (oracle/build_ref_cuda.sh needs the reference tree)"}
+    d = ref_cuda_drift.run_scalar(32, 1000, 100, trap_offset=0.0)
+    d["against"] = "the reference's FP64 scalar BCC update kernel"
+    return d
+
+
+def fp64_reference_timing(stream, launches=50):
+    """The reference's own FP64 spin-1 leapfrog kernel (Spin1GpeBCC.cu:793-917,
+    compiled unmodified for sm_103a by oracle/build_ref_cuda.sh, launched with its
+    own launch shape Spin1GpeBCC.cu:1375-1380) on the headline grid, timed with CUDA
+    events: the FP64 plain GPU stepper of the benchmark plan."""
+    import ctypes as C
+
+    import torch
+
+    from oracle import ref_cuda as R
+    from spacetime_gb300 import capi, states
+    from spacetime_gb300.stepper import Stepper
+
+    if not R.available("spin1_bcc"):
+        return {"unavailable": "reference cubins not built (oracle/build_ref_cuda.sh needs the reference tree)"}
+    lat = capi.Lattice("bcc")
+    bs = BOX / (DIMS[0] * lat.block_width[0])
+    p64 = capi.make_params(components=3, precision=capi.FP64, dims=DIMS, block_scale=bs, dt=DT,
+                           trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=C0, c2=C2, lattice=lat)
+    ref = Stepper(lat, p64)
+    drv = R.Driver()
+    try:
+        psi0 = states.spinor_state(lat, p64, states.POLAR, seed=2, noise=1e-3)
+        ref.upload(capi.PSI_ODD, psi0)
+        ref.upload(capi.PSI_EVEN, psi0)
+        ent, w = R.stencil_int4(lat)
+        d_ent, d_w = drv.upload(ent), drv.upload(w)
+        grid, block = R.spinor_grid(p64, lat.nodes)
+        leap = drv.function("spin1_bcc", "leapfrog")
+        slots = [R.pitched(ref, capi.PSI_EVEN), R.pitched(ref, capi.PSI_ODD)]
+        f = capi.make_fields(bq=0.2, bb=(0.0, 0.0, 0.5))
+
+        def step(k):
+            drv.launch(leap, grid, block, [slots[(k + 1) % 2], slots[k % 2], C.c_void_p(d_ent), C.c_void_p(d_w),
+                                           R.mag_fields(f), R.uint3(p64), C.c_double(bs), R.double3(p64.p0),
+                                           C.c_double(C0), C.c_double(C2), C.c_double(0.0), C.c_bool(False),
+                                           C.c_bool(False), C.c_bool(False), C.c_double(DT), C.c_double((k + 1) * DT)])
+
+        for k in range(5):
+            step(k)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()  # the driver API launches go to the legacy default stream
+        for k in range(launches):
+            step(k)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / launches
+    finally:
+        drv.close()
+        ref.close()
+    sites = lat.nodes * DIMS[0] * DIMS[1] * DIMS[2]
+    return {"value": sites / (ms * 1e-3), "unit": "lattice-site-updates/s", "ms_per_launch": ms,
+            "kernel": "Spin1GpeBCC.cu leapfrog, FP64, compiled unmodified for sm_103a",
+            "launch": {"grid": list(grid), "block": list(block)}, "launches_timed": launches,
+            "trap": "the program's compiled-in lambda (1, 1, %.6f) + %g" % (R.LAMBDA_Z, R.TRAP_OFFSET)}
 
 
 def run_reference(args):
@@ -731,9 +1158,19 @@ def run_gpu(args):
     s64.close()
     fp64_value = sites / (fp64_ms * 1e-3)
 
+    # ---- the reference's own FP64 spin-1 leapfrog kernel on the same grid
+    fp64_ref = fp64_reference_timing(stream) if rank == 0 and args.fp64_reference else None
+    if fp64_ref and "value" in fp64_ref:
+        fp64_ref["speedup_fp32_fused"] = (sites / (launch_ms * 1e-3)) / fp64_ref["value"]
+
+    # ---- precision: FP32 fused against an FP64 run of the reference's own kernels
+    # (libgpe's FP64 stepper where the reference's cubins are not built)
     drift = None
     if args.drift_steps > 0 and rank == 0:
-        drift = measure_drift(args.drift_steps, stream)
+        drift = reference_drift(args.drift_steps)
+        if drift is None:
+            drift = measure_drift(args.drift_steps, stream)
+            drift["against"] = "libgpe FP64 (plain) stepper"
 
     result = {
         "metric": "lattice-site-updates/s", "value": value, "unit": "lattice-site-updates/s", "n_gpus": world,
@@ -758,16 +1195,35 @@ def run_gpu(args):
         "clocks": clocks,
         "observables_last": obs[-1] if obs else None,
     }
+    if fp64_ref is not None:
+        result["fp64_reference"] = fp64_ref
     if drift is not None:
         result["drift"] = drift
     if rank == 0 and args.cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     s.close()
+    if rank == 0 and args.legs != "none":
+        result["legs"] = run_legs(args)
     if rank == 0:
         print(json.dumps(result))
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def reference_drift(nsteps):
+    """The headline workload in FP32 against an FP64 run of the reference's own
+    forwardEuler + leapfrog (Spin1GpeBCC.cu:667-917, compiled unmodified), from the
+    same state, with the trap the program compiles in: energy and norm every 100
+    steps, the max-abs wavefunction error at the end (the checker of
+    oracle/ref_cuda_drift.py).  None where the reference's cubins are not built."""
+    from oracle import ref_cuda, ref_cuda_drift
+
+    if not ref_cuda.available("spin1_bcc"):
+        return None
+    d = ref_cuda_drift.run(DIMS[0], nsteps, 100, DT, BOX)
+    d["against"] = "the reference's FP64 spin-1 forwardEuler + leapfrog kernels"
+    return d
 
 
 def measure_drift(nsteps, stream):
@@ -833,9 +1289,19 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=ADJ["steps"], help="adjoint-bcc64: steps of the recorded run")
     ap.add_argument("--fd-knots", type=int, default=ADJ["fd_knots"], help="adjoint-bcc64: knots checked by central differences")
     ap.add_argument("--members", type=int, default=ENS["members"], help="ensemble-256: members of the ensemble (a prefix)")
+    ap.add_argument("--legs", default="all",
+                    help="default run: the other configurations to add to the line (all, none, or a comma list of %s)"
+                    % ",".join(LEG_NAMES))
+    ap.add_argument("--c15-drift-cells", type=int, default=32, help="spin2-c15 leg: grid edge of the 10^4-step FP32/FP64 run")
+    ap.add_argument("--c15-drift-steps", type=int, default=10000, help="spin2-c15 leg: steps of the FP32/FP64 run")
+    ap.add_argument("--no-fp64-reference", dest="fp64_reference", action="store_false",
+                    help="skip timing the reference's FP64 kernel")
+    ap.add_argument("--quick", action="store_true", help="headline only: no legs, drift, CPU baseline or FP64 timings")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
+    if args.quick:
+        args.legs, args.drift_steps, args.cpu_baseline, args.fp64_reference = "none", 0, False, False
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "adjoint-bcc64":

@@ -112,7 +112,7 @@ def run(cells=96, steps=10000, every=100, dt=5e-5, box=16.0):
         f32.close()
 
 
-def run_scalar(cells=32, steps=1000, every=100, dt=1e-4, box=16.0, g=2000.0):
+def run_scalar(cells=32, steps=1000, every=100, dt=1e-4, box=16.0, g=2000.0, trap_offset=R.TRAP_OFFSET):
     """The scalar workload (BCC 32^3, box [-8, 8]^3, trap omega = (1, 1, 1), g = 2000,
     Thomas-Fermi vortex + 1e-3 noise) on the reference's scalar BCC `update`
     (GPUGrossPitaevskii_BCC.cu:327-347): next += dt_ref (-i H prev) with
@@ -124,7 +124,7 @@ def run_scalar(cells=32, steps=1000, every=100, dt=1e-4, box=16.0, g=2000.0):
 
     lat = capi.Lattice("bcc")
     bs = box / (cells * lat.block_width[0])
-    common = dict(components=1, dims=(cells, cells, cells), block_scale=bs, dt=dt, trap_offset=R.TRAP_OFFSET, c0=g,
+    common = dict(components=1, dims=(cells, cells, cells), block_scale=bs, dt=dt, trap_offset=trap_offset, c0=g,
                   lattice=lat)
     p64 = capi.make_params(precision=capi.FP64, **common)
     p32 = capi.make_params(precision=capi.FP32, **common)
@@ -169,8 +169,8 @@ def run_scalar(cells=32, steps=1000, every=100, dt=1e-4, box=16.0, g=2000.0):
         a = ref.download(capi.PSI_EVEN if cur == 0 else capi.PSI_ODD)
         b = f32.download(f32.current)
         e = np.array(rows)
-        return {"workload": "scalar BCC %d^3 cells, g %g, TF vortex + 1e-3 noise, dt %g (dt_ref %g), trap (1, 1, 1) + 100"
-                            % (cells, g, dt, 2 * dt),
+        return {"workload": "scalar BCC %d^3 cells, g %g, TF vortex + 1e-3 noise, dt %g (dt_ref %g), trap (1, 1, 1) + %g"
+                            % (cells, g, dt, 2 * dt, trap_offset),
                 "steps": steps, "every": every,
                 "reference": "GPUGrossPitaevskii_BCC.cu update, FP64, compiled unmodified for sm_103a",
                 "psi_max_abs_err": float(np.max(np.abs(a - b))), "psi_max_abs": float(np.max(np.abs(a))),
