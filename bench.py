@@ -485,7 +485,7 @@ def ensemble_result(n_members, inner, replays, warmup):
            "roofline": {"bound": "hbm", "achieved": algo / (step_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": algo / (step_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": "batch_kernel<float,3>",
                         "algorithmic_bytes_per_step": algo, "avg_step_ms": step_ms, "traffic": None},
-           "gpu_launches": launches, "graph_replays": args.steps, "clocks": clk.summary(), "setup_s": setup_s,
+           "gpu_launches": launches, "graph_replays": replays, "clocks": clk.summary(), "setup_s": setup_s,
            "autotune": tune,
            "norm_rel_change": [abs(b2["norm"] - a2["norm"]) / a2["norm"] for a2, b2 in zip(e_first, e_last)]}
     # end to end: each replay's graph copies the members' step state (ramp, time,
@@ -1296,12 +1296,15 @@ def main():
     ap.add_argument("--c15-drift-steps", type=int, default=10000, help="spin2-c15 leg: steps of the FP32/FP64 run")
     ap.add_argument("--no-fp64-reference", dest="fp64_reference", action="store_false",
                     help="skip timing the reference's FP64 kernel")
-    ap.add_argument("--quick", action="store_true", help="headline only: no legs, drift, CPU baseline or FP64 timings")
+    ap.add_argument("--quick", action="store_true",
+                    help="headline only: no drift, CPU baseline or FP64 timings, and no legs unless --legs names some")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.quick:
-        args.legs, args.drift_steps, args.cpu_baseline, args.fp64_reference = "none", 0, False, False
+        args.drift_steps, args.cpu_baseline, args.fp64_reference = 0, False, False
+        if args.legs == "all":
+            args.legs = "none"
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "adjoint-bcc64":
