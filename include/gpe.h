@@ -334,9 +334,14 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  *                      cells, T | X and TY | Y),
  *                  4 = row-block kernel (a block of RY x RZ output rows; bulk copies
  *                      of every row the block's stencil touches; all gathers from
- *                      shared memory; needs 16-byte cells, RY | Y, RZ | Z).  The
- *                      automatic choice is 1 (grid-stride, whole-record loads); 2-4 on
- *                      request, and gpe_autotune may pick any of them.
+ *                      shared memory; needs 16-byte cells, RY | Y, RZ | Z),
+ *                  5 = slab-ring kernel (one block per column of TILE_CELLS x
+ *                      TILE_ROWS cells marching up z, the previous planes in a ring
+ *                      of shared-memory slabs filled by bulk copies; lattices with
+ *                      4 entries per node and 16-byte cells; ZCHUNK, if set, is the
+ *                      number of slabs).  The automatic choice is 1 (grid-stride,
+ *                      whole-record loads); 2-5 on request, and gpe_autotune may
+ *                      pick any of 1-4.
  * GPE_TUNE_TILE_CELLS: cells per tile row (0 = automatic).
  * GPE_TUNE_TILE_ROWS: rows per tile along y (z-march TY, row-block RY; 0 = automatic).
  * GPE_TUNE_ZCHUNK: z-march planes per block, or row-block RZ (0 = automatic).
