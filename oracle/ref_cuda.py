@@ -13,6 +13,7 @@ tests/golden/make_ref_cuda_golden.py, never by the library.
 
 Kernels (names as the compiler exports them):
   spin1_bcc      leapfrog / forwardEuler       Spin1GpeBCC/Spin1GpeBCC.cu:667-917
+                 maxHamilton, localAvgSpinAndDensity, uvTheta (node fields, :144-189, 235-326)
   spin2_bcc      leapfrog / forwardEuler       Spin2GpeBCC/Spin2GpeBCC.cu:698-990
   rel_spin2_bcc  update_psi / update_q          RelativisticSpin2Gpe/RelativisticSpin2Gpe.cu:971-1132
   rel_spin1_bcc  update_psi / update_q_hyper    RelativisticSpin1Gpe/common_kernels.h:176-255, hyper_kernels.h:80-116
@@ -45,6 +46,9 @@ REL_SCALAR_SIGMA = 0.001                                  # RelativisticGpeBCC.c
 NAMES = {
     ("spin1_bcc", "leapfrog"): "_Z8leapfrog10PitchedPtrS_PK4int4PKd9MagFields5uint3d7double3dddbbbdd",
     ("spin1_bcc", "euler"): "_Z12forwardEuler10PitchedPtrS_P4int4Pd9MagFields5uint3d7double3dddbbbdd",
+    ("spin1_bcc", "maxHamilton"): "_Z11maxHamiltonPd10PitchedPtr9MagFields5uint3d7double3dddd",
+    ("spin1_bcc", "localAvgSpinAndDensity"): "_Z22localAvgSpinAndDensityPdP7double3S_10PitchedPtr5uint3",
+    ("spin1_bcc", "uvTheta"): "_Z7uvThetaP7double3S0_Pd10PitchedPtr5uint3",
     ("spin2_bcc", "leapfrog"): "_Z8leapfrog10PitchedPtrS_PK4int4PKd9MagFields5uint3d7double3ddddd",
     ("spin2_bcc", "euler"): "_Z12forwardEuler10PitchedPtrS_P4int4Pd9MagFields5uint3d7double3ddddd",
     ("rel_spin2_bcc", "update_psi"): "_Z10update_psi10PitchedPtrS_S_PK4int2PKd9MagFields5uint3d7double3ddddbd",

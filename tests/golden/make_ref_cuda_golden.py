@@ -298,6 +298,40 @@ def scalar_case(drv, name, program, lattice, dims, dt, g, seed):
                 times=np.zeros(NSTEPS), in_even=interior(even0), in_odd=interior(odd0), **out)
 
 
+def fields_case(drv, name, dims, c0, c2, seed, t=0.25):
+    """The spin-1 program's per-node output kernels on one seeded state:
+    localAvgSpinAndDensity (Spin1GpeBCC.cu:235-271), uvTheta (:273-326) and
+    maxHamilton (:144-189, with the program's compiled-in trap at time t and one
+    field row), each writing FP64 arrays in the order V (z X Y + y X + x) + l."""
+    lat = capi.Lattice("bcc")
+    p = capi.make_params(components=3, precision=capi.FP64, dims=dims, block_scale=0.3, dt=2e-4,
+                         trap_lambda=(1.0, 1.0, R.LAMBDA_Z), trap_offset=R.TRAP_OFFSET, c0=c0, c2=c2, lattice=lat)
+    s = Stepper(lat, p)
+    shape = capi.buffer_shape(lat, p)
+    psi = 0.2 * states.random_state(shape, seed=seed)
+    s.upload(capi.PSI_EVEN, psi)
+    n = lat.nodes * dims[0] * dims[1] * dims[2]
+    zeros = np.zeros(n)
+    d_norm, d_spin, d_dens = drv.upload(zeros), drv.upload(np.zeros(3 * n)), drv.upload(zeros)
+    d_u, d_v, d_th, d_h = drv.upload(np.zeros(3 * n)), drv.upload(np.zeros(3 * n)), drv.upload(zeros), drv.upload(zeros)
+    grid, block = R.spinor_grid(p, lat.nodes)
+    buf = R.pitched(s, capi.PSI_EVEN)
+    F = fields_table(1, seed + 7)
+    vp = R.C.c_void_p
+    drv.launch(drv.function("spin1_bcc", "localAvgSpinAndDensity"), grid, block,
+               [vp(d_norm), vp(d_spin), vp(d_dens), buf, R.uint3(p)])
+    drv.launch(drv.function("spin1_bcc", "uvTheta"), grid, block, [vp(d_u), vp(d_v), vp(d_th), buf, R.uint3(p)])
+    drv.launch(drv.function("spin1_bcc", "maxHamilton"), grid, block,
+               [vp(d_h), buf, R.mag_fields(as_fields(F[0])), R.uint3(p), R.C.c_double(p.block_scale), R.double3(p.p0),
+                R.C.c_double(c0), R.C.c_double(c2), R.C.c_double(0.0), R.C.c_double(t)])
+    get = lambda d, k: drv.download(d, 8 * k * n).view(np.float64).reshape(n, k)  # noqa: E731
+    out = {"out_spin_norm": get(d_norm, 1)[:, 0], "out_avg_spin": get(d_spin, 3), "out_density": get(d_dens, 1)[:, 0],
+           "out_u": get(d_u, 3), "out_v": get(d_v, 3), "out_theta": get(d_th, 1)[:, 0], "out_max_hamilton": get(d_h, 1)[:, 0]}
+    s.close()
+    return dict(kind="fields", lattice="bcc", params=params_dict(p), fields=F, times=np.array([t]), in_even=interior(psi),
+                **out)
+
+
 CASES = [
     ("spin1_bcc", lambda d: spinor_case(d, "spin1_bcc", "spin1_bcc", "bcc", 3, (5, 3, 2), 0, 2e-4, 120.0, -7.0, 0.0, 0.0, 11)),
     ("spin1_bcc_toggles", lambda d: spinor_case(d, "spin1_bcc_toggles", "spin1_bcc", "bcc", 3, (4, 3, 3),
@@ -321,6 +355,7 @@ CASES = [
     ("scalar_c15", lambda d: scalar_case(d, "scalar_c15", "scalar_c15", "c15", (2, 2, 2), 2e-4, 150.0, 61)),
     ("scalar_a15", lambda d: scalar_case(d, "scalar_a15", "scalar_a15", "a15", (3, 2, 2), 2e-4, 150.0, 71)),
     ("scalar_fcc", lambda d: scalar_case(d, "scalar_fcc", "scalar_fcc", "fcc", (3, 3, 2), 2e-4, 150.0, 81)),
+    ("fields_spin1_bcc", lambda d: fields_case(d, "fields_spin1_bcc", (4, 3, 2), 120.0, -7.0, 97)),
 ]
 
 
@@ -331,7 +366,7 @@ def main(outdir):
     drv = R.Driver()
     try:
         for name, fn in CASES:
-            program = name.replace("_toggles", "").replace("_expansion", "").replace("itp_", "")
+            program = name.replace("_toggles", "").replace("_expansion", "").replace("itp_", "").replace("fields_", "")
             if os.path.exists(os.path.join(outdir, "ref_cuda_%s.npz" % name)) and "--all" not in sys.argv:
                 continue  # keep the vectors already made
             if not R.available(program):

@@ -199,3 +199,49 @@ def test_batch_constant_slots_exhausted(gpu):
         _close(fillers)
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+def test_batch_matches_oracle(gpu, prec):
+    """A mixed batch (BCC spin-1, FCC scalar with the trap switched off mid-run,
+    C15 scalar, A15 spin-1), every member against the FP64 CPU oracle's own time
+    loop: forwardEuler at t0, then leapfrog steps with the member's ramp evaluated
+    at t0 + (k+1) dt (Spin1GpeBCC.cu:1428-1603).  FP64 <= 1e-12 and FP32 <= 2e-5 of
+    max|psi|, the parity tolerances of the single-condensate kernels."""
+    from oracle import oracle
+
+    specs = [("bcc", 3, (7, 5, 4)), ("fcc", 1, (6, 5, 4)), ("c15", 1, (3, 2, 3)), ("a15", 3, (3, 4, 3))]
+    n = 9
+    members, init = [], []
+    for i, sp in enumerate(specs):
+        s = _member(sp, prec, i)
+        init.append(s.download(capi.PSI_ODD))
+        members.append(s)
+    try:
+        with Batch(members) as b:
+            b.set_tuning(capi.BATCH_ITEM_NODES, 150)
+            b.step(n)
+        for i, (sp, s) in enumerate(zip(specs, members)):
+            name, comps, dims = sp
+            lat = capi.Lattice(name)
+            flags = capi.FLAG_TRAP_OFF_AFTER if i == 1 else 0
+            p = capi.make_params(components=comps, precision=capi.FP64, dims=dims, block_scale=0.3, dt=2e-4,
+                                 trap_offset=100.0, trap_lambda=(0.8 + 0.05 * i, 1.0, 1.2 - 0.04 * i), c0=120.0 + 10 * i,
+                                 c2=-7.0, c4=3.0, flags=flags, trap_off_time=1.5e-3, lattice=lat)
+            ramp = capi.make_ramp(bq_segments=[(0.1 * i, 0.0, capi.RAMP_CONSTANT), (0.3, 12 * 2e-4, capi.RAMP_LINEAR)],
+                                  bb_segments=[((0.0, 0.0, 0.5), 0.0, capi.RAMP_CONSTANT),
+                                               ((0.1 * i, -0.1, -0.5), 10 * 2e-4, capi.RAMP_LINEAR),
+                                               ((0.2, 0.0, 0.3), 6 * 2e-4, capi.RAMP_SQRT)],
+                                  bq_quad_scale=0.5, bb_quad_scale=0.25)
+            t0 = 1e-4 * i
+            odd = init[i].copy()
+            even = np.zeros_like(odd)
+            oracle.parabolic_step(lat, p, oracle.ramp_eval(ramp, ramp.time_scale * t0), t0, oracle.EULER, even, odd)
+            want = oracle.leapfrog_run(lat, p, even, odd, n, ramp=ramp, t0=t0)
+            got = s.download(s.current)
+            scale = float(np.max(np.abs(want)))
+            err = float(np.max(np.abs(got - want)))
+            tol = 1e-12 if prec == capi.FP64 else 2e-5
+            assert err <= tol * scale, (name, comps, err, scale)
+    finally:
+        _close(members)

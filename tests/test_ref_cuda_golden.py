@@ -10,7 +10,9 @@ GPUGrossPitaevskii_C15.cu:90-155, 469-482), the hyperbolic imaginary-time pair
 itp_q + itp_psi and get_Hpsi of the spin-2 and
 spin-1 ground-state loops (RelativisticSpin2Gpe.cu:558-807;
 RelativisticSpin1Gpe/hyper_kernels.h:4-40, common_kernels.h:17-94), and the
-scalar BCC / C15 / A15 / FCC updates -- made by
+scalar BCC / C15 / A15 / FCC updates, and the spin-1 program's per-node output
+kernels localAvgSpinAndDensity, uvTheta and maxHamilton (Spin1GpeBCC.cu:144-326)
+-- made by
 tests/golden/make_ref_cuda_golden.py on a GB300 from seeded inputs.
 
 CPU: the FP64 oracle replays each run: max |oracle - reference| <= 1e-12 * max|reference|
@@ -80,8 +82,27 @@ def _check(got, want, tol, what):
     assert err <= tol * scale, "%s: max|diff| = %.3e, scale %.3e" % (what, err, scale)
 
 
+def _fields_check(get, d, tol, uv=True):
+    """The node-field kernels' outputs (localAvgSpinAndDensity, uvTheta,
+    maxHamilton) against `get(kind, fields, t)` -> (Z, Y, X, V, K).  uv: also the
+    u, v, theta frame (its orientation is ill-conditioned where |m| ~ |n|, so it
+    is compared on FP64 states only)."""
+    f = _fields(d["fields"][0])
+    t = float(d["times"][0])
+    spin = get(capi.FIELD_SPIN, f, t).reshape(-1, 5)
+    _check(spin[:, 0], d["out_spin_norm"], tol, "spin norm")
+    _check(spin[:, 1:4], d["out_avg_spin"], tol, "local average spin")
+    _check(spin[:, 4], d["out_density"], tol, "density")
+    if uv:
+        uvt = get(capi.FIELD_UV_THETA, f, t).reshape(-1, 7)
+        _check(uvt[:, 0:3], d["out_u"], tol, "u")
+        _check(uvt[:, 3:6], d["out_v"], tol, "v")
+        _check(uvt[:, 6], d["out_theta"], tol, "theta")
+    _check(get(capi.FIELD_MAX_HAMILTON, f, t).reshape(-1), d["out_max_hamilton"], tol, "max Hamilton")
+
+
 def test_golden_files_present():
-    assert len(FILES) >= 14, "reference-kernel golden vectors missing"
+    assert len(FILES) >= 15, "reference-kernel golden vectors missing"
 
 
 @pytest.mark.parametrize("path", FILES, ids=IDS)
@@ -89,6 +110,10 @@ def test_oracle_vs_reference_cuda(path):
     d = _load(path)
     lat, p = _params(d, capi.FP64)
     n = d["fields"].shape[0]
+    if d["kind"] == "fields":
+        psi = _embed(d["in_even"])
+        _fields_check(lambda kind, f, t: oracle.node_fields(lat, p, f, t, kind, psi), d, 1e-12)
+        return
     if d["kind"] == "spinor":
         even, odd = _embed(d["in_even"]), _embed(d["in_odd"])
         bufs = [odd, even]
@@ -144,6 +169,17 @@ def test_kernels_vs_reference_cuda(gpu, path, prec):
     tol = 1e-12 if prec == capi.FP64 else 2e-5
     n = d["fields"].shape[0]
     with Stepper(lat, p) as s:
+        if d["kind"] == "fields":
+            # FP64 fields from the stored values: FP32 storage rounds the state itself
+            s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
+
+            def get(kind, f, t):
+                s.set_ramp(capi.make_ramp(bq_segments=[(f.bq, 1e9, capi.RAMP_CONSTANT)],
+                                          bb_segments=[(tuple(f.bb), 1e9, capi.RAMP_CONSTANT)]), 0.0)
+                return s.node_fields(capi.PSI_EVEN, kind, t)
+
+            _fields_check(get, d, 1e-12 if prec == capi.FP64 else 2e-5, uv=prec == capi.FP64)
+            return
         if d["kind"] == "split":
             s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
             s.upload(capi.Q_EVEN, _embed(d["in_qeven"]))
