@@ -18,6 +18,8 @@ template <typename R, int C>
 cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s);
+template <typename R, int C>
+cudaError_t launch_norm(const StepArgs& a, double* out, cudaStream_t s);
 cudaError_t launch_dot(const StepArgs& a, int precision, int C, double* out, cudaStream_t s);
 struct InitArgs {
     double zeta[5][2];
@@ -633,6 +635,18 @@ static cudaError_t dispatch_observe(const gpe_handle* h, const StepArgs& a, doub
     }
 }
 template <int C>
+static cudaError_t dispatch_norm_c(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_norm<double, C>(a, out, s) : launch_norm<float, C>(a, out, s);
+}
+// sum |psi|^2 of a.prev into out[OBS_NORM] (the other entries zero)
+static cudaError_t dispatch_norm(const gpe_handle* h, const StepArgs& a, double* out, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return dispatch_norm_c<1>(h, a, out, s);
+        case 3: return dispatch_norm_c<3>(h, a, out, s);
+        default: return dispatch_norm_c<5>(h, a, out, s);
+    }
+}
+template <int C>
 static cudaError_t dispatch_scale_c(const gpe_handle* h, const StepArgs& a, const double* n, double dv, cudaStream_t s) {
     return h->real_bytes == 8 ? launch_scale<double, C>(a, n, dv, s) : launch_scale<float, C>(a, n, dv, s);
 }
@@ -1227,7 +1241,7 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
         StepArgs a = make_args(h, zero, 0.0);
         a.prev = h->interior[next];
         a.next = h->interior[next];
-        cudaError_t e = dispatch_observe(h, a, h->obs_out, s);
+        cudaError_t e = dispatch_norm(h, a, h->obs_out, s);
         if (e != cudaSuccess) return cuda_fail(e, "itp norm");
         e = dispatch_scale(h, a, h->obs_out, dv, s);
         if (e != cudaSuccess) return cuda_fail(e, "itp scale");
@@ -1481,7 +1495,7 @@ extern "C" gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init
     h->epoch += 1;
     if (init->normalize) {
         a.prev = h->interior[slot];
-        e = dispatch_observe(h, a, h->obs_out, s);
+        e = dispatch_norm(h, a, h->obs_out, s);
         if (e == cudaSuccess) e = dispatch_scale(h, a, h->obs_out, cell_dv(h), s);
         if (e != cudaSuccess) return cuda_fail(e, "init normalisation");
         h->launches += 3;

@@ -1197,8 +1197,59 @@ static __global__ void __launch_bounds__(256) observe_finalize_kernel(const doub
     }
 }
 
+// The squared norm sum_nodes |psi|^2 of a psi buffer alone (density + integrate,
+// Spin1GpeBCC.cu:191-211, 328-348, for normalize_h :955-975): grid-stride, whole-
+// record loads, the per-node terms in the storage precision (FP32 storage: groups
+// of 8 nodes summed in FP32, each group added in FP64), FP64 block sums written to
+// the OBS_NORM column of the partials (the other columns zero) for
+// observe_finalize_kernel.
+template <typename R, int C>
+__global__ void __launch_bounds__(256) norm_kernel(StepArgs a) {
+    __shared__ double red[8];
+    constexpr int kGroup = sizeof(R) == 4 ? 8 : 1;
+    double acc = 0.0;
+    R grp = (R)0;
+    int in_group = 0;
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
+         gid += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)gid;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * a.g.V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        Cx<R> v[C];
+        ld_node<R, C, true>(a.prev + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes +
+                                l * node_bytes, v);
+        R n2 = 0;
+#pragma unroll
+        for (int s = 0; s < C; ++s) n2 += v[s].x * v[s].x + v[s].y * v[s].y;
+        grp += n2;
+        if (++in_group == kGroup) {
+            acc += (double)grp;
+            grp = (R)0;
+            in_group = 0;
+        }
+    }
+    acc += (double)grp;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x < OBS_COUNT) {
+        double v = 0.0;
+        if (threadIdx.x == OBS_NORM)
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w];
+        a.partials[(size_t)blockIdx.x * OBS_COUNT + threadIdx.x] = v;
+    }
+}
+
 // Scale every interior value of a psi buffer by 1/sqrt(norm) where norm is read
-// from device memory (normalize, Spin1GpeBCC.cu:412-434).
+// from device memory (normalize, Spin1GpeBCC.cu:412-434: FP64 storage divides by
+// the square root as the reference does; FP32 storage multiplies by its
+// reciprocal, computed in FP64 and rounded once).
 template <typename R, int C>
 __global__ void __launch_bounds__(256) scale_kernel(StepArgs a, const double* norm_sum, double dv) {
     const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1213,12 +1264,21 @@ __global__ void __launch_bounds__(256) scale_kernel(StepArgs a, const double* no
     const size_t cell_off = (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes;
     char* p = a.next + cell_off + l * (C * 2 * sizeof(R));
     const double sq = sqrt(norm_sum[OBS_NORM] * dv);
+    if constexpr (sizeof(R) == 8) {
 #pragma unroll
-    for (int s = 0; s < C; ++s) {
-        Cx<R> v = ldc_rw<R>(p + s * 2 * sizeof(R));
-        v.x = (R)((double)v.x / sq);
-        v.y = (R)((double)v.y / sq);
-        stc<R>(p + s * 2 * sizeof(R), v);
+        for (int s = 0; s < C; ++s) {
+            Cx<R> v = ldc_rw<R>(p + s * 2 * sizeof(R));
+            v.x = v.x / sq;
+            v.y = v.y / sq;
+            stc<R>(p + s * 2 * sizeof(R), v);
+        }
+    } else {
+        const R inv = (R)(1.0 / sq);
+        Cx<R> v[C];
+        ld_node<R, C, false>(p, v);
+#pragma unroll
+        for (int s = 0; s < C; ++s) v[s] = inv * v[s];
+        st_node<R, C>(p, v);
     }
 }
 
@@ -1522,6 +1582,19 @@ cudaError_t launch_observe(const StepArgs& a, double* out, bool node_fp32, cudaS
 }
 
 template <typename R, int C>
+cudaError_t launch_norm(const StepArgs& a, double* out, cudaStream_t s) {
+    static int occ = 0;
+    if (occ == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, norm_kernel<R, C>, 256, 0);
+        occ = std::max(occ, 1);
+    }
+    const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), (unsigned)occ * (unsigned)device_sm_count());
+    norm_kernel<R, C><<<nb, 256, 0, s>>>(a);
+    observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
+    return cudaGetLastError();
+}
+
+template <typename R, int C>
 cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, cudaStream_t s) {
     scale_kernel<R, C><<<nblocks(a.total, 256), 256, 0, s>>>(a, norm_sum, dv);
     return cudaGetLastError();
@@ -1532,7 +1605,8 @@ cudaError_t launch_scale(const StepArgs& a, const double* norm_sum, double dv, c
     template cudaError_t launch_parabolic_observe<R, C>(const StepArgs&, double*, cudaStream_t); \
     template cudaError_t launch_hyper<R, C>(const StepArgs&, int, cudaStream_t);           \
     template cudaError_t launch_observe<R, C>(const StepArgs&, double*, bool, cudaStream_t);     \
-    template cudaError_t launch_scale<R, C>(const StepArgs&, const double*, double, cudaStream_t);
+    template cudaError_t launch_scale<R, C>(const StepArgs&, const double*, double, cudaStream_t); \
+    template cudaError_t launch_norm<R, C>(const StepArgs&, double*, cudaStream_t);
 
 }  // namespace gpe
 
