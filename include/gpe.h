@@ -224,6 +224,17 @@ typedef struct {
 } gpe_init;
 gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init* init, void* stream);
 
+/* Re-spins a state in place, keeping its density: at every node
+ * psi'_m = sqrt(rho |zeta_m|^2) zeta_m / |zeta_m| with rho = sum_m |psi_m|^2, for
+ * zeta given as C (re, im) pairs (the density becomes rho sum_m |zeta_m|^2).
+ * Replaces the reference's phase-preparation kernels applied to a loaded ground
+ * state: polarState (zeta = (0, 1, 0)), ferromagneticState ((1, 0, 0)) and
+ * mixedState ((sqrt(mix), sqrt(1 - mix), 0)), Spin1GpeBCC.cu:463-551, 1395-1407;
+ * unState ((0, 0, 1, 0, 0)), horizontalBnState ((1, 0, 0, 0, e^{i phase}) /
+ * sqrt 2), verticalBnState ((0, 1, 0, e^{i phase}, 0) / sqrt 2) and cyclicState
+ * ((sqrt(1/3), 0, 0, sqrt(2/3) e^{i phase}, 0)), Spin2GpeBCC.cu:417-558. */
+gpe_status gpe_respin(gpe_handle* h, int32_t slot, const double* zeta, void* stream);
+
 /* Install the field ramp used by gpe_step / gpe_start (device-side getSignal). */
 gpe_status gpe_set_ramp(gpe_handle* h, const gpe_ramp* ramp, double t0);
 

@@ -200,3 +200,21 @@ def gpblocks_norm(ii0, vsize, psi0, even, volume):
     out = np.zeros(2)
     lib().orc_gpblocks_norm(ii0, vsize, _dp(psi0), _dp(even), volume, _dp(out))
     return out
+
+
+def respin(psi, zeta):
+    """The phase-preparation kernels of the reference, in place on a host state
+    (file layout, halo untouched since it is zero): at every node each component
+    becomes sqrt(rho * w_m) times the phase of zeta_m, rho the node's density and
+    w_m = |zeta_m|^2 -- polarState / ferromagneticState / mixedState
+    (Spin1GpeBCC.cu:463-551), unState / horizontalBnState / verticalBnState /
+    cyclicState (Spin2GpeBCC.cu:417-558)."""
+    zeta = np.asarray(zeta, dtype=np.complex128)
+    rho = np.sum(psi[..., 0] ** 2 + psi[..., 1] ** 2, axis=-1)
+    for m, z in enumerate(zeta):
+        w = z.real * z.real + z.imag * z.imag
+        a = np.sqrt(w)
+        amp = np.sqrt(rho * w)
+        psi[..., m, 0] = amp * (z.real / a if a > 0 else 0.0)
+        psi[..., m, 1] = amp * (z.imag / a if a > 0 else 0.0)
+    return psi

@@ -14,6 +14,8 @@ tests/golden/make_ref_cuda_golden.py, never by the library.
 Kernels (names as the compiler exports them):
   spin1_bcc      leapfrog / forwardEuler       Spin1GpeBCC/Spin1GpeBCC.cu:667-917
                  maxHamilton, localAvgSpinAndDensity, uvTheta (node fields, :144-189, 235-326)
+                 polarState, ferromagneticState, mixedState (:463-551)
+  spin2_bcc      unState, horizontalBnState, verticalBnState, cyclicState (Spin2GpeBCC.cu:417-558)
   spin2_bcc      leapfrog / forwardEuler       Spin2GpeBCC/Spin2GpeBCC.cu:698-990
   rel_spin2_bcc  update_psi / update_q          RelativisticSpin2Gpe/RelativisticSpin2Gpe.cu:971-1132
   rel_spin1_bcc  update_psi / update_q_hyper    RelativisticSpin1Gpe/common_kernels.h:176-255, hyper_kernels.h:80-116
@@ -47,6 +49,13 @@ NAMES = {
     ("spin1_bcc", "leapfrog"): "_Z8leapfrog10PitchedPtrS_PK4int4PKd9MagFields5uint3d7double3dddbbbdd",
     ("spin1_bcc", "euler"): "_Z12forwardEuler10PitchedPtrS_P4int4Pd9MagFields5uint3d7double3dddbbbdd",
     ("spin1_bcc", "maxHamilton"): "_Z11maxHamiltonPd10PitchedPtr9MagFields5uint3d7double3dddd",
+    ("spin1_bcc", "polarState"): "_Z10polarState10PitchedPtr5uint3",
+    ("spin1_bcc", "ferromagneticState"): "_Z18ferromagneticState10PitchedPtr5uint3",
+    ("spin1_bcc", "mixedState"): "_Z10mixedState10PitchedPtr5uint3d",
+    ("spin2_bcc", "unState"): "_Z7unState10PitchedPtr5uint3",
+    ("spin2_bcc", "horizontalBnState"): "_Z17horizontalBnState10PitchedPtr5uint3d",
+    ("spin2_bcc", "verticalBnState"): "_Z15verticalBnState10PitchedPtr5uint3d",
+    ("spin2_bcc", "cyclicState"): "_Z11cyclicState10PitchedPtr5uint3d",
     ("spin1_bcc", "localAvgSpinAndDensity"): "_Z22localAvgSpinAndDensityPdP7double3S_10PitchedPtr5uint3",
     ("spin1_bcc", "uvTheta"): "_Z7uvThetaP7double3S0_Pd10PitchedPtr5uint3",
     ("spin2_bcc", "leapfrog"): "_Z8leapfrog10PitchedPtrS_PK4int4PKd9MagFields5uint3d7double3ddddd",

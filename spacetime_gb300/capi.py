@@ -315,6 +315,7 @@ def load_library(path: str = LIB_PATH):
         "gpe_itp": (C.c_int, [vp, C.c_int32, P(C.c_double), vp]),
         "gpe_observe": (C.c_int, [vp, C.c_int32, C.c_double, P(Observables), vp]),
         "gpe_step_observe": (C.c_int, [vp, C.c_int32, P(Observables), vp]),
+        "gpe_respin": (C.c_int, [vp, C.c_int32, P(C.c_double), vp]),
         "gpe_set_expansion": (C.c_int, [vp, C.c_double, C.c_double]),
         "gpe_node_field_count": (C.c_int, [vp, C.c_int32, P(C.c_size_t), P(C.c_size_t)]),
         "gpe_node_fields": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_double, P(C.c_double), C.c_size_t, vp]),

@@ -29,6 +29,12 @@ struct InitArgs {
 };
 template <typename R, int C>
 cudaError_t launch_init(const StepArgs& a, const InitArgs& in, cudaStream_t s);
+struct RespinArgs {
+    double w[5];
+    double u[5][2];
+};
+template <typename R, int C>
+cudaError_t launch_respin(const StepArgs& a, const RespinArgs& r, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_leapfrog_tile(const StepArgs& a, uint32_t T, int carveout, cudaStream_t s);
 template <typename R, int C>
@@ -1460,6 +1466,41 @@ extern "C" gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, s
 template <int C>
 static cudaError_t dispatch_init_c(const gpe_handle* h, const StepArgs& a, const InitArgs& in, cudaStream_t s) {
     return h->real_bytes == 8 ? launch_init<double, C>(a, in, s) : launch_init<float, C>(a, in, s);
+}
+
+template <int C>
+static cudaError_t dispatch_respin_c(const gpe_handle* h, const StepArgs& a, const RespinArgs& r, cudaStream_t s) {
+    return h->real_bytes == 8 ? launch_respin<double, C>(a, r, s) : launch_respin<float, C>(a, r, s);
+}
+
+extern "C" gpe_status gpe_respin(gpe_handle* h, int32_t slot, const double* zeta, void* stream) {
+    if (!h || !zeta) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    if (slot != GPE_PSI_EVEN && slot != GPE_PSI_ODD) return fail(GPE_ERR_INVALID_ARG, "psi slot");
+    RespinArgs r;
+    std::memset(&r, 0, sizeof r);
+    for (int m = 0; m < h->g.C; ++m) {
+        const double re = zeta[2 * m], im = zeta[2 * m + 1];
+        if (!std::isfinite(re) || !std::isfinite(im)) return fail(GPE_ERR_INVALID_ARG, "zeta must be finite");
+        r.w[m] = re * re + im * im;
+        const double a = std::sqrt(r.w[m]);
+        r.u[m][0] = a > 0 ? re / a : 0.0;
+        r.u[m][1] = a > 0 ? im / a : 0.0;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    gpe_fields zero;
+    std::memset(&zero, 0, sizeof zero);
+    StepArgs a = make_args(h, zero, 0.0);
+    a.next = h->interior[slot];
+    cudaError_t e;
+    switch (h->g.C) {
+        case 1: e = dispatch_respin_c<1>(h, a, r, s); break;
+        case 3: e = dispatch_respin_c<3>(h, a, r, s); break;
+        default: e = dispatch_respin_c<5>(h, a, r, s); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "respin kernel");
+    h->launches += 1;
+    h->epoch += 1;
+    return GPE_OK;
 }
 
 extern "C" gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init* init, void* stream) {

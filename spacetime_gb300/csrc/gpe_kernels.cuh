@@ -2443,7 +2443,54 @@ cudaError_t launch_init(const StepArgs& a, const InitArgs& in, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-#define GPE_INSTANTIATE_INIT(R, C) template cudaError_t launch_init<R, C>(const StepArgs&, const InitArgs&, cudaStream_t);
+// The spinor of a state replaced at every node, its density kept: psi'_m =
+// sqrt(rho w_m) u_m with rho = sum_m |psi_m|^2, w_m = |zeta_m|^2 and u_m =
+// zeta_m / |zeta_m| (polarState / ferromagneticState / mixedState,
+// Spin1GpeBCC.cu:463-551; unState / horizontalBnState / verticalBnState /
+// cyclicState, Spin2GpeBCC.cu:417-558: each writes sqrt(rho x weight) times a
+// phase into its fixed components).  a.next: the slot's interior pointer.
+struct RespinArgs {
+    double w[5];
+    double u[5][2];
+};
+
+template <typename R, int C>
+__global__ void __launch_bounds__(256) respin_kernel(StepArgs a, RespinArgs r) {
+    const uint32_t node_bytes = C * 2 * sizeof(R);
+    for (uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < a.total;
+         gid += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = (uint32_t)gid;
+        const uint32_t row = fdiv(i, a.divRow);
+        const uint32_t within = i - row * a.row_items;
+        const uint32_t x = fdiv(within, a.divV);
+        const uint32_t l = within - x * a.g.V;
+        const uint32_t z = fdiv(row, a.divY);
+        const uint32_t y = row - z * a.g.Y;
+        char* p = a.next + (size_t)z * a.g.slice + (size_t)y * a.g.pitch + (size_t)x * a.g.cell_bytes + l * node_bytes;
+        Cx<R> v[C];
+        ld_node<R, C, false>(p, v);
+        R rho = 0;
+#pragma unroll
+        for (int m = 0; m < C; ++m) rho += v[m].x * v[m].x + v[m].y * v[m].y;
+#pragma unroll
+        for (int m = 0; m < C; ++m) {
+            const R amp = sqrt(rho * (R)r.w[m]);
+            v[m] = cx<R>(amp * (R)r.u[m][0], amp * (R)r.u[m][1]);
+        }
+        st_node<R, C>(p, v);
+    }
+}
+
+template <typename R, int C>
+cudaError_t launch_respin(const StepArgs& a, const RespinArgs& r, cudaStream_t s) {
+    const unsigned nb = std::min<unsigned>(nblocks(a.total, 256), 8u * (unsigned)device_sm_count());
+    if (nb) respin_kernel<R, C><<<nb, 256, 0, s>>>(a, r);
+    return cudaGetLastError();
+}
+
+#define GPE_INSTANTIATE_INIT(R, C)                                                                \
+    template cudaError_t launch_init<R, C>(const StepArgs&, const InitArgs&, cudaStream_t);      \
+    template cudaError_t launch_respin<R, C>(const StepArgs&, const RespinArgs&, cudaStream_t);
 
 }  // namespace gpe
 

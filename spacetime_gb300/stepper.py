@@ -75,6 +75,15 @@ class Stepper:
         """Seeded Thomas-Fermi state written on the device (gpe_init_state)."""
         capi.check(self.lib.gpe_init_state(self._h, slot, C.byref(init), self.stream), "gpe_init_state")
 
+    def respin(self, slot: int, zeta):
+        """Replace the spinor at every node, keeping the density (gpe_respin):
+        psi_m <- sqrt(rho |zeta_m|^2) zeta_m / |zeta_m|."""
+        z = np.zeros(2 * self.params.components)
+        for m, c in enumerate(zeta):
+            c = complex(c)
+            z[2 * m], z[2 * m + 1] = c.real, c.imag
+        capi.check(self.lib.gpe_respin(self._h, slot, z.ctypes.data_as(C.POINTER(C.c_double)), self.stream), "gpe_respin")
+
     def buffer(self, slot: int):
         p = capi.Pitched()
         cb = C.c_size_t()

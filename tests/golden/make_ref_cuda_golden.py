@@ -332,6 +332,31 @@ def fields_case(drv, name, dims, c0, c2, seed, t=0.25):
                 **out)
 
 
+def respin_case(drv, name, program, C, kernels, seed):
+    """The programs' phase-preparation kernels, each applied to a fresh copy of one
+    seeded state (Spin1GpeBCC.cu:463-551, Spin2GpeBCC.cu:417-558).  kernels:
+    (kernel, phase argument or None, the spinor zeta it writes)."""
+    lat = capi.Lattice("bcc")
+    p = capi.make_params(components=C, precision=capi.FP64, dims=(4, 3, 2), block_scale=0.3, lattice=lat)
+    s = Stepper(lat, p)
+    psi = 0.2 * states.random_state(capi.buffer_shape(lat, p), seed=seed)
+    grid, block = R.spinor_grid(p, lat.nodes)
+    outs, zetas = [], []
+    for kern, phase, zeta in kernels:
+        s.upload(capi.PSI_EVEN, psi)
+        args = [R.pitched(s, capi.PSI_EVEN), R.uint3(p)]
+        if phase is not None:
+            args.append(R.C.c_double(phase))
+        drv.launch(drv.function(program, kern), grid, block, args)
+        outs.append(interior(s.download(capi.PSI_EVEN)))
+        zetas.append(np.array(zeta, dtype=np.complex128))
+    s.close()
+    return dict(kind="respin", lattice="bcc", params=params_dict(p), fields=np.zeros((1, 8)), times=np.zeros(1),
+                in_even=interior(psi), out_states=np.stack(outs), zetas=np.stack(zetas),
+                kernels=np.array([k for k, _, _ in kernels]))
+
+
+S2, S13, S23 = 0.5 ** 0.5, (1.0 / 3.0) ** 0.5, (2.0 / 3.0) ** 0.5
 CASES = [
     ("spin1_bcc", lambda d: spinor_case(d, "spin1_bcc", "spin1_bcc", "bcc", 3, (5, 3, 2), 0, 2e-4, 120.0, -7.0, 0.0, 0.0, 11)),
     ("spin1_bcc_toggles", lambda d: spinor_case(d, "spin1_bcc_toggles", "spin1_bcc", "bcc", 3, (4, 3, 3),
@@ -356,6 +381,14 @@ CASES = [
     ("scalar_a15", lambda d: scalar_case(d, "scalar_a15", "scalar_a15", "a15", (3, 2, 2), 2e-4, 150.0, 71)),
     ("scalar_fcc", lambda d: scalar_case(d, "scalar_fcc", "scalar_fcc", "fcc", (3, 3, 2), 2e-4, 150.0, 81)),
     ("fields_spin1_bcc", lambda d: fields_case(d, "fields_spin1_bcc", (4, 3, 2), 120.0, -7.0, 97)),
+    ("respin_spin1_bcc", lambda d: respin_case(d, "respin_spin1_bcc", "spin1_bcc", 3, [
+        ("polarState", None, (0, 1, 0)), ("ferromagneticState", None, (1, 0, 0)),
+        ("mixedState", 0.3, (0.3 ** 0.5, 0.7 ** 0.5, 0))], 99)),
+    ("respin_spin2_bcc", lambda d: respin_case(d, "respin_spin2_bcc", "spin2_bcc", 5, [
+        ("unState", None, (0, 0, 1, 0, 0)),
+        ("horizontalBnState", 0.7, (S2, 0, 0, 0, S2 * np.exp(0.7j))),
+        ("verticalBnState", 1.1, (0, S2, 0, S2 * np.exp(1.1j), 0)),
+        ("cyclicState", 0.4, (S13, 0, 0, S23 * np.exp(0.4j), 0))], 101)),
 ]
 
 
@@ -366,7 +399,8 @@ def main(outdir):
     drv = R.Driver()
     try:
         for name, fn in CASES:
-            program = name.replace("_toggles", "").replace("_expansion", "").replace("itp_", "").replace("fields_", "")
+            program = (name.replace("_toggles", "").replace("_expansion", "").replace("itp_", "").replace("fields_", "")
+                       .replace("respin_", ""))
             if os.path.exists(os.path.join(outdir, "ref_cuda_%s.npz" % name)) and "--all" not in sys.argv:
                 continue  # keep the vectors already made
             if not R.available(program):

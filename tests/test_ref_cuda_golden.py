@@ -12,7 +12,8 @@ spin-1 ground-state loops (RelativisticSpin2Gpe.cu:558-807;
 RelativisticSpin1Gpe/hyper_kernels.h:4-40, common_kernels.h:17-94), and the
 scalar BCC / C15 / A15 / FCC updates, and the spin-1 program's per-node output
 kernels localAvgSpinAndDensity, uvTheta and maxHamilton (Spin1GpeBCC.cu:144-326)
--- made by
+and the phase-preparation kernels of the spin-1 and spin-2 programs
+(Spin1GpeBCC.cu:463-551, Spin2GpeBCC.cu:417-558) -- made by
 tests/golden/make_ref_cuda_golden.py on a GB300 from seeded inputs.
 
 CPU: the FP64 oracle replays each run: max |oracle - reference| <= 1e-12 * max|reference|
@@ -102,7 +103,7 @@ def _fields_check(get, d, tol, uv=True):
 
 
 def test_golden_files_present():
-    assert len(FILES) >= 15, "reference-kernel golden vectors missing"
+    assert len(FILES) >= 17, "reference-kernel golden vectors missing"
 
 
 @pytest.mark.parametrize("path", FILES, ids=IDS)
@@ -113,6 +114,10 @@ def test_oracle_vs_reference_cuda(path):
     if d["kind"] == "fields":
         psi = _embed(d["in_even"])
         _fields_check(lambda kind, f, t: oracle.node_fields(lat, p, f, t, kind, psi), d, 1e-12)
+        return
+    if d["kind"] == "respin":
+        for zeta, want in zip(d["zetas"], d["out_states"]):
+            _check(oracle.respin(_embed(d["in_even"]), zeta), want, 1e-14, str(zeta))
         return
     if d["kind"] == "spinor":
         even, odd = _embed(d["in_even"]), _embed(d["in_odd"])
@@ -179,6 +184,12 @@ def test_kernels_vs_reference_cuda(gpu, path, prec):
                 return s.node_fields(capi.PSI_EVEN, kind, t)
 
             _fields_check(get, d, 1e-12 if prec == capi.FP64 else 2e-5, uv=prec == capi.FP64)
+            return
+        if d["kind"] == "respin":
+            for zeta, want in zip(d["zetas"], d["out_states"]):
+                s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
+                s.respin(capi.PSI_EVEN, zeta)
+                _check(s.download(capi.PSI_EVEN), want, 1e-14 if prec == capi.FP64 else 1e-6, str(zeta))
             return
         if d["kind"] == "split":
             s.upload(capi.PSI_EVEN, _embed(d["in_even"]))
