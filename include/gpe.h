@@ -235,6 +235,37 @@ gpe_status gpe_init_state(gpe_handle* h, int32_t slot, const gpe_init* init, voi
  * ((sqrt(1/3), 0, 0, sqrt(2/3) e^{i phase}, 0)), Spin2GpeBCC.cu:417-558. */
 gpe_status gpe_respin(gpe_handle* h, int32_t slot, const double* zeta, void* stream);
 
+/* Axisymmetric vortex state Psi = f(r, z) e^{i kappa phi} of a scalar condensate
+ * in the trap V = (r^2 + trap_ratio^2 z^2) / 2, host code: the reference's
+ * VortexState (GrossPitaevskii/VortexState.cpp:11-237), which builds the initial
+ * state of its CPU stepper (GPBlocks.cpp:477-486, main).  The grid is setRange's:
+ * r in [rmin, rmax) in rsize = round((rmax - rmin) / rstep) steps, z in [0, zmax)
+ * in zsize = round(zmax / zstep) steps, mirrored at z = 0.
+ * gpe_vortex_profile relaxes f from the reference's initial guess
+ * (iterateSolution: Gauss-Seidel sweeps with the Rayleigh quotient for mu and a
+ * renormalisation after each, until a sweep changes f by less than eps in the
+ * weighted squared sense, at most max_iters sweeps) into f[i * zsize + j]; with
+ * f = NULL it only reports rsize and zsize.  mu and the sweeps taken are
+ * returned if the pointers are given.
+ * gpe_vortex_sample evaluates Psi at every interior node of a grid (getPsi:
+ * bilinear interpolation of f, times ((x + iy)/r)^kappa) into a host array in
+ * the reference file layout (as gpe_upload takes it), into component 0 (the
+ * scalar, or the first spinor component for gpe_respin to re-spin); the halo
+ * and the other components are zero. */
+typedef struct {
+    uint32_t kappa;
+    double g;
+    double rmin, rmax, rstep;
+    double zmax, zstep;
+    double trap_ratio;
+    uint32_t max_iters;
+    double eps;
+} gpe_vortex_params;
+gpe_status gpe_vortex_profile(const gpe_vortex_params* vp, double* f, size_t count, uint32_t* rsize, uint32_t* zsize,
+                              double* mu, uint32_t* iterations);
+gpe_status gpe_vortex_sample(const gpe_vortex_params* vp, const double* f, const gpe_lattice_desc* lat,
+                             const gpe_params* p, double* host, size_t count);
+
 /* Install the field ramp used by gpe_step / gpe_start (device-side getSignal). */
 gpe_status gpe_set_ramp(gpe_handle* h, const gpe_ramp* ramp, double t0);
 

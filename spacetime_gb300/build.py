@@ -18,7 +18,7 @@ LIB = os.path.join(PKG, "libgpe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["gpe_capi.cu", "gpe_inst_c1.cu", "gpe_inst_c3.cu", "gpe_inst_c5.cu", "gpe_noalloc.cu", "gpe_adjoint.cu", "gpe_batch.cu",
-           "gpe_fields.cu"]
+           "gpe_fields.cu", "gpe_vortex.cu"]
 
 
 def nvcc() -> str:

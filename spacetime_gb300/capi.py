@@ -68,6 +68,21 @@ class LatticeDesc(C.Structure):
     ]
 
 
+class VortexParams(C.Structure):
+    _fields_ = [
+        ("kappa", C.c_uint32),
+        ("g", C.c_double),
+        ("rmin", C.c_double),
+        ("rmax", C.c_double),
+        ("rstep", C.c_double),
+        ("zmax", C.c_double),
+        ("zstep", C.c_double),
+        ("trap_ratio", C.c_double),
+        ("max_iters", C.c_uint32),
+        ("eps", C.c_double),
+    ]
+
+
 class Params(C.Structure):
     _fields_ = [
         ("components", C.c_int32),
@@ -316,6 +331,10 @@ def load_library(path: str = LIB_PATH):
         "gpe_observe": (C.c_int, [vp, C.c_int32, C.c_double, P(Observables), vp]),
         "gpe_step_observe": (C.c_int, [vp, C.c_int32, P(Observables), vp]),
         "gpe_respin": (C.c_int, [vp, C.c_int32, P(C.c_double), vp]),
+        "gpe_vortex_profile": (C.c_int, [P(VortexParams), P(C.c_double), C.c_size_t, P(C.c_uint32), P(C.c_uint32),
+                                         P(C.c_double), P(C.c_uint32)]),
+        "gpe_vortex_sample": (C.c_int, [P(VortexParams), P(C.c_double), P(LatticeDesc), P(Params), P(C.c_double),
+                                        C.c_size_t]),
         "gpe_set_expansion": (C.c_int, [vp, C.c_double, C.c_double]),
         "gpe_node_field_count": (C.c_int, [vp, C.c_int32, P(C.c_size_t), P(C.c_size_t)]),
         "gpe_node_fields": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_double, P(C.c_double), C.c_size_t, vp]),
@@ -374,3 +393,26 @@ def exported_symbols_from_header(header: str | None = None) -> list:
         text = f.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(gpe_[a-z0-9_]+)\s*\(", text)))
+
+
+def vortex_state(lat: "Lattice", params: "Params", kappa=1, g=None, rmin=0.0, rmax=None, zmax=None, rstep=0.1,
+                 zstep=0.1, trap_ratio=1.0, max_iters=100000, eps=1e-28):
+    """The relaxed vortex state Psi = f(r, z) e^{i kappa phi} (gpe_vortex_profile,
+    the reference's VortexState) sampled at every node of the grid of `params`
+    (gpe_vortex_sample): (host array in the file layout, mu, sweeps taken).
+    g defaults to params.c0; rmax and zmax to the box's half-extent + 1, as the
+    reference's CPU stepper sets them up."""
+    lib = load_library()
+    half = max(abs(params.p0[i]) for i in range(3))
+    vp = VortexParams(kappa, params.c0 if g is None else g, rmin, half + 1.0 if rmax is None else rmax, rstep,
+                      half + 1.0 if zmax is None else zmax, zstep, trap_ratio, max_iters, eps)
+    rs, zs = C.c_uint32(), C.c_uint32()
+    check(lib.gpe_vortex_profile(C.byref(vp), None, 0, C.byref(rs), C.byref(zs), None, None), "gpe_vortex_profile")
+    f = np.zeros(rs.value * zs.value)
+    mu, it = C.c_double(), C.c_uint32()
+    check(lib.gpe_vortex_profile(C.byref(vp), f.ctypes.data_as(C.POINTER(C.c_double)), f.size, None, None, C.byref(mu),
+                                 C.byref(it)), "gpe_vortex_profile")
+    out = np.zeros(buffer_shape(lat, params))
+    check(lib.gpe_vortex_sample(C.byref(vp), f.ctypes.data_as(C.POINTER(C.c_double)), C.byref(lat.desc), C.byref(params),
+                                out.ctypes.data_as(C.POINTER(C.c_double)), out.size), "gpe_vortex_sample")
+    return out, mu.value, it.value
