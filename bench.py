@@ -130,24 +130,25 @@ def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
         n0 = s.launches
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         obs = []
+        # the step launches' device time from the library's events on this stream
+        # (layout changes of interleaved calls timed apart)
+        s.set_tuning(capi.TUNE_TIMING, 1)
+        s.step_timing(reset=True)
         with ClockSampler(0) as clk:
             a.record(stream)
-            step_ms = 0.0
             for _ in range(steps):
-                x, y = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                x.record(stream)
                 s.step(inner)
-                y.record(stream)
                 obs.append(s.observe(s.current))
-                step_ms += x.elapsed_time(y)
             b.record(stream)
             torch.cuda.synchronize()
+        timing = s.step_timing(reset=True)
         total_ms = a.elapsed_time(b)
         launches = s.launches - n0
     sites = s.sites
     gather = s.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_GATHER
+    interleaved = timing["interleaved_calls"] > 0
     s.close()
-    launch_ms = step_ms / (inner * steps)
+    launch_ms = timing["step_ms"] / timing["step_launches"]
     algo = w["bytes_fp32"] * sites
     peak, kind = measured_peak()
     name = KERNEL_OF_SCHEME[w["scheme"]] % w["C"]
@@ -155,6 +156,8 @@ def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
         name = "hyper_step_kernel<float,%d> (gather form)" % w["C"]
     if w["scheme"] == 0 and gather:
         name = "parabolic_fixed_kernel<float,%d,LEAPFROG,4>" % w["C"]
+    if interleaved:
+        name = "il_step_kernel<%d>" % w["C"]
     return {"metric": "lattice-site-updates/s", "value": sites * inner * steps / (total_ms * 1e-3),
             "unit": "lattice-site-updates/s", "steps": steps, "inner_steps_per_step": inner, "sites": sites,
             "ms_per_step": total_ms / steps, "dims": list(p.dims),
@@ -1038,32 +1041,20 @@ def run_gpu(args):
         s.step(INNER)
         s._nsteps += INNER
 
-    def advance_observed(ev=None):
-        """One bench step: INNER leapfrog steps, the observables summed inside the
-        last one (FP32 node terms, FP64 sums); with --observe-fp64 a separate
-        observe pass with FP64 node terms after the steps.  ev: three events
-        recorded before the steps, after the INNER - 1 plain step launches, and
-        after the observed step (its finalize included)."""
-        if ev:
-            ev[0].record(stream)
+    def advance_observed():
+        """One bench step: INNER leapfrog steps in one gpe_step_observe call, the
+        observables summed inside the last one (FP32 node terms, FP64 sums); with
+        --observe-fp64 gpe_step(INNER) and a separate observe pass with FP64 node
+        terms after it."""
         if args.observe_fp64:
             advance()
-            if ev:
-                ev[1].record(stream)
-            o = s.observe(cur_slot(), s._nsteps * DT)
-        else:
-            s.step(INNER - 1)
-            if ev:
-                ev[1].record(stream)
-            s._nsteps += INNER
-            o = s.step_observe(1)
-        if ev:
-            ev[2].record(stream)
-        return o
+            return s.observe(cur_slot(), s._nsteps * DT)
+        s._nsteps += INNER
+        return s.step_observe(INNER)
 
     kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_fixed_kernel<float,3,LEAPFROG,4>",
                    capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>",
-                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>"}
+                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>", capi.KERNEL_INTERLEAVED: "il_step_kernel<3>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
     for key, val in ((capi.TUNE_TILE_CELLS, args.tile), (capi.TUNE_TILE_ROWS, args.rows), (capi.TUNE_ZCHUNK, args.zchunk),
@@ -1085,24 +1076,31 @@ def run_gpu(args):
         barrier()
         launches0 = s.launches
         ev_start, ev_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        batch = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3)) for _ in range(args.steps)]
         obs = []
+        # the library's CUDA events on this stream time each call's plain step
+        # launches, its observed step and its layout changes (gpe_get_step_timing)
+        s.set_tuning(capi.TUNE_TIMING, 1)
+        s.step_timing(reset=True)
         with ClockSampler(local) as clk:
             ev_start.record(stream)
             for k in range(args.steps):
-                obs.append(advance_observed(batch[k]))
+                obs.append(advance_observed())
             ev_end.record(stream)
             barrier()
+        timing = s.step_timing(reset=True)
+        s.set_tuning(capi.TUNE_TIMING, 0)
         clocks = clk.summary()
         launches = s.launches - launches0
         total_ms = ev_start.elapsed_time(ev_end)
-        plain_ms = sum(a.elapsed_time(b) for a, b, _ in batch)
-        observed_ms = sum(b.elapsed_time(c) for _, b, c in batch) / args.steps
     total_ms, value = replica_throughput(total_ms, sites * INNER * args.steps, world, "cuda")
     # the step kernel's mean duration over the plain launches (INNER - 1 per bench
-    # step; the observed step, with its finalize, is timed on its own)
-    plain_launches = (INNER - (0 if args.observe_fp64 else 1)) * args.steps
-    launch_ms = plain_ms / plain_launches
+    # step; the observed step, with its finalize, and the layout changes are timed
+    # on their own)
+    plain_launches = int(timing["step_launches"])
+    launch_ms = timing["step_ms"] / plain_launches
+    observed_ms = timing["observed_ms"] / timing["observed_launches"] if timing["observed_launches"] else None
+    if timing["interleaved_calls"]:
+        chosen = capi.KERNEL_INTERLEAVED
     algo_bytes = BYTES_PER_SITE_FP32 * sites
     achieved = algo_bytes / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
@@ -1161,7 +1159,7 @@ def run_gpu(args):
     # ---- the reference's own FP64 spin-1 leapfrog kernel on the same grid
     fp64_ref = fp64_reference_timing(stream) if rank == 0 and args.fp64_reference else None
     if fp64_ref and "value" in fp64_ref:
-        fp64_ref["speedup_fp32_fused"] = (sites / (launch_ms * 1e-3)) / fp64_ref["value"]
+        fp64_ref["speedup_fp32_fused"] = (value / world) / fp64_ref["value"]
 
     # ---- precision: FP32 fused against an FP64 run of the reference's own kernels
     # (libgpe's FP64 stepper where the reference's cubins are not built)
@@ -1182,6 +1180,8 @@ def run_gpu(args):
                      "kernel": kernel_name[chosen], "tile_cells_rows_zchunk": tile, "algorithmic_bytes_per_launch": algo_bytes,
                      "avg_launch_ms": launch_ms, "launches_timed": plain_launches},
         "observed_step_ms": observed_ms,
+        "layout_change_ms_per_call": timing["convert_ms"] / timing["calls"] if timing["interleaved_calls"] else None,
+        "step_timing": timing,
         "e2e": {"value": e2e_value, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
                 "d2h_bytes_per_step": int(psi0.nbytes) + 8 * 12, "steps": e2e_steps,
                 "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step_observe(100) + gpe_download (FP64 host, pinned)",
@@ -1189,7 +1189,7 @@ def run_gpu(args):
         "observables": "FP64 node terms and sums (separate pass)" if args.observe_fp64 else
                        "summed inside the last step kernel of each bench step (FP32 node terms, FP64 sums)",
         "fp64_plain": {"value": fp64_value, "unit": "lattice-site-updates/s", "ms_per_launch": fp64_ms,
-                       "speedup_fp32_fused": (sites / (launch_ms * 1e-3)) / fp64_value},
+                       "speedup_fp32_fused": (value / world) / fp64_value},
         "gpu_launches": launches,
         "autotune": tuning_report,
         "clocks": clocks,

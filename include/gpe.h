@@ -381,9 +381,19 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  *                      TILE_ROWS cells marching up z, the previous planes in a ring
  *                      of shared-memory slabs filled by bulk copies; lattices with
  *                      4 entries per node and 16-byte cells; ZCHUNK, if set, is the
- *                      number of slabs).  The automatic choice is 1 (grid-stride,
- *                      whole-record loads); 2-5 on request, and gpe_autotune may
- *                      pick any of 1-4.
+ *                      number of slabs),
+ *                  6 = interleaved kernel for every gpe_step / gpe_step_observe
+ *                      call (FP32, parabolic scheme, lattices with 4 entries per
+ *                      node: BCC, A15, C15, Z).  The call changes the two psi
+ *                      slots into a cell-interleaved layout (node l, component s of
+ *                      32 cells along x contiguous), steps there and changes them
+ *                      back; the states are those of the gather kernel.
+ *                  The automatic choice (0) is the interleaved kernel for calls of
+ *                  16 or more steps on the handles it applies to (the two layout
+ *                  changes cost about two steps), else 1 (grid-stride gather,
+ *                  whole-record loads) -- which gpe_get_tuning reports; 2-5 on
+ *                  request, and gpe_autotune may pick any of 1-4 (it times single
+ *                  steps; its gather candidate is recorded as 0).
  * GPE_TUNE_TILE_CELLS: cells per tile row (0 = automatic).
  * GPE_TUNE_TILE_ROWS: rows per tile along y (z-march TY, row-block RY; 0 = automatic).
  * GPE_TUNE_ZCHUNK: z-march planes per block, or row-block RZ (0 = automatic).
@@ -395,7 +405,11 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  *                   either way; mode 0 is bound by GB300's narrow FP64 pipe.
  * GPE_TUNE_CARVEOUT: shared-memory share (percent) of the unified L1 / shared
  *                   memory for the row-tile kernel; the rest caches its off-row
- *                   gathers (0 = driver default). */
+ *                   gathers (0 = driver default).
+ * GPE_TUNE_TIMING: 1 = time every gpe_step / gpe_step_observe call with CUDA
+ *                   events on its stream (each such call then synchronises the
+ *                   stream at its end) and add the times to gpe_get_step_timing;
+ *                   0 = off (default). */
 enum {
     GPE_TUNE_KERNEL = 0,
     GPE_TUNE_TILE_CELLS = 1,
@@ -403,10 +417,29 @@ enum {
     GPE_TUNE_ZCHUNK = 3,
     GPE_TUNE_THREADS = 4,
     GPE_TUNE_OBSERVE_ARITH = 5,
-    GPE_TUNE_CARVEOUT = 6
+    GPE_TUNE_CARVEOUT = 6,
+    GPE_TUNE_TIMING = 7
 };
 gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value);
 gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);
+
+/* Device time of the gpe_step / gpe_step_observe calls made while GPE_TUNE_TIMING
+ * was 1, from CUDA events on the calls' streams: the plain step launches, the
+ * observed steps (their finalize included) and the layout changes of interleaved
+ * calls.  `reset` non-zero zeroes the sums after reading.  No counterpart in the
+ * reference (its programs time whole loops with host clocks). */
+typedef struct {
+    uint64_t calls;              /* calls timed */
+    uint64_t step_launches;      /* plain step launches */
+    double step_ms;              /* their device time */
+    uint64_t observed_launches;  /* observed steps */
+    double observed_ms;          /* their device time, finalize included */
+    uint64_t convert_launches;   /* layout changes (interleaved calls: 4 per call) */
+    double convert_ms;           /* their device time */
+    int32_t interleaved_calls;   /* calls that ran the interleaved kernel */
+    int32_t reserved;
+} gpe_step_timing;
+gpe_status gpe_get_step_timing(gpe_handle* h, gpe_step_timing* out, int32_t reset);
 
 /* Autotuner: times every eligible step kernel and tile shape (cells per tile, rows
  * per block, threads per block) on this handle's own buffers with CUDA events,

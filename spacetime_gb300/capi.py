@@ -35,9 +35,10 @@ RAMP_CONSTANT, RAMP_LINEAR, RAMP_SQRT = 0, 1, 2
 RAMP_MAX_SEGMENTS = 32
 PSI_EVEN, PSI_ODD, Q_EVEN, Q_ODD, HPSI = 0, 1, 2, 3, 4
 MODE_LEAPFROG, MODE_EULER, MODE_ITP = 0, 1, 2
-TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS, TUNE_OBSERVE_ARITH, TUNE_CARVEOUT = 0, 1, 2, 3, 4, 5, 6
+TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS, TUNE_OBSERVE_ARITH, TUNE_CARVEOUT, TUNE_TIMING = (
+    0, 1, 2, 3, 4, 5, 6, 7)
 FIELD_DENSITY, FIELD_SPIN, FIELD_UV_THETA, FIELD_MAX_HAMILTON, FIELD_PROJ_X, FIELD_PROJ_Y = 0, 1, 2, 3, 4, 5
-KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS, KERNEL_SLAB = 0, 1, 2, 3, 4, 5
+KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS, KERNEL_SLAB, KERNEL_INTERLEAVED = 0, 1, 2, 3, 4, 5, 6
 BATCH_ITEM_NODES, BATCH_STEPS_PER_LAUNCH, BATCH_BLOCKS_PER_SM, BATCH_BARRIER_TIMEOUT_MS, BATCH_TEST_EXTRA_ARRIVALS = 0, 1, 2, 3, 4
 
 
@@ -173,6 +174,24 @@ class Observables(C.Structure):
             "max_abs": self.max_abs,
             "nonfinite": self.nonfinite,
         }
+
+
+class StepTiming(C.Structure):
+    """gpe_step_timing: device time of the timed gpe_step / gpe_step_observe calls."""
+    _fields_ = [
+        ("calls", C.c_uint64),
+        ("step_launches", C.c_uint64),
+        ("step_ms", C.c_double),
+        ("observed_launches", C.c_uint64),
+        ("observed_ms", C.c_double),
+        ("convert_launches", C.c_uint64),
+        ("convert_ms", C.c_double),
+        ("interleaved_calls", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 # ------------------------------------------------------------------ lattices
@@ -346,6 +365,7 @@ def load_library(path: str = LIB_PATH):
         "gpe_autotune": (C.c_int, [vp, C.c_int32, C.c_char_p, C.c_size_t, vp]),
         "gpe_observe_noalloc": (C.c_int, [P(LatticeDesc), P(Params), P(Fields), C.c_double, vp, C.c_size_t, C.c_size_t, P(Observables), vp]),
         "gpe_get_tuning": (C.c_int, [vp, C.c_int32, P(C.c_int32)]),
+        "gpe_get_step_timing": (C.c_int, [vp, P(StepTiming), C.c_int32]),
         "gpe_adjoint_forward": (C.c_int, [vp, C.c_int32, P(Fields), C.c_int32, P(C.c_double), C.c_size_t, P(C.c_double), vp]),
         "gpe_adjoint_backward": (C.c_int, [vp, P(C.c_double), P(C.c_double), vp]),
         "gpe_batch_create": (C.c_int, [P(vp), C.c_int32, P(vp)]),

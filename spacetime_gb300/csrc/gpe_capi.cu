@@ -1,4 +1,5 @@
 // gpe_capi.cu -- host implementation of the libgpe C ABI (include/gpe.h).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -50,6 +51,11 @@ template <typename R, int C>
 cudaError_t launch_parabolic_slab(const StepArgs& a, uint32_t Tx, uint32_t Ty, uint32_t S, cudaStream_t s);
 template <typename R, int C>
 cudaError_t launch_parabolic_observe(const StepArgs& a, double* out, cudaStream_t s);
+template <int C>
+cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, size_t max_blocks, bool obs, double* out, cudaStream_t s);
+template <int C>
+unsigned il_blocks(const ILGrid& G, bool obs, size_t max_blocks);
+cudaError_t launch_il_convert(char* aos, const Grid& g, char* il, const ILGrid& G, bool to_il, cudaStream_t s);
 enum HyperKind {
     HK_FUSED_LEAPFROG = 0,
     HK_PSI_PARA_LEAPFROG,
@@ -198,6 +204,10 @@ static void release(gpe_handle* h) {
     if (h->field_buf) cudaFree(h->field_buf);
     if (h->err) cudaFree(h->err);
     if (h->blk) cudaFree(h->blk);
+    for (char* b : h->il)
+        if (b) cudaFree(b);
+    if (h->tev_ok)
+        for (cudaEvent_t ev : h->tev) cudaEventDestroy(ev);
     adjoint_release(h);
 }
 
@@ -368,7 +378,9 @@ extern "C" gpe_status gpe_create(const gpe_lattice* lat, const gpe_params* p, gp
         delete h;
         return st;
     }
-    h->partial_blocks = (sites + 255) / 256;
+    // block partial sums: one row per 256 sites, and at least a wave of the
+    // interleaved observed step's blocks on small grids
+    h->partial_blocks = std::max<size_t>((sites + 255) / 256, 2048);
     if (cudaMalloc(&h->partials, h->partial_blocks * OBS_COUNT * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&h->obs_out, OBS_COUNT * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&h->err, sizeof(int)) != cudaSuccess || cudaMemset(h->err, 0, sizeof(int)) != cudaSuccess) {
@@ -1117,10 +1129,8 @@ extern "C" gpe_status gpe_start(gpe_handle* h, void* stream) {
     return GPE_OK;
 }
 
-extern "C" gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream) {
-    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
-    if (n < 0) return fail(GPE_ERR_INVALID_ARG, "negative step count");
-    cudaStream_t s = (cudaStream_t)stream;
+// n steps in the handle's layout.
+static gpe_status plain_steps(gpe_handle* h, int32_t n, cudaStream_t s) {
     if (h->p.scheme == GPE_SCHEME_SPLIT) {
         // update_psi(I) + update_q(q_I), then update_psi(R) + update_q(q_R)
         // (RelativisticGpeC15/GPUGrossPitaevskii_C15.cu:477-482), one launch each
@@ -1143,6 +1153,170 @@ extern "C" gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream) {
         h->cur = next;
         h->nstep++;
     }
+    return GPE_OK;
+}
+
+// ------------------------------------------------------- call timing (GPE_TUNE_TIMING)
+
+// Events on the call's stream: 0 call start, 1 steps start (after the layout change
+// in), 2 observed step start, 3 observed step end, 4 call end (after the layout
+// change out).  finish() waits for event 4 and adds the intervals to h->timing.
+struct StepTimer {
+    gpe_handle* h;
+    cudaStream_t s;
+    bool on;
+    StepTimer(gpe_handle* hh, cudaStream_t ss) : h(hh), s(ss), on(hh->tune_timing != 0) {
+        if (on && !h->tev_ok) {
+            for (cudaEvent_t& ev : h->tev)
+                if (cudaEventCreate(&ev) != cudaSuccess) on = false;
+            h->tev_ok = on;
+            if (!on) cudaGetLastError();
+        }
+    }
+    void mark(int i) {
+        if (on) cudaEventRecord(h->tev[i], s);
+    }
+    void finish(uint64_t plain, uint64_t observed, uint64_t converts, bool interleaved) {
+        if (!on || cudaEventSynchronize(h->tev[4]) != cudaSuccess) return;
+        float ms[4] = {0, 0, 0, 0};
+        for (int i = 0; i < 4; ++i) cudaEventElapsedTime(&ms[i], h->tev[i], h->tev[i + 1]);
+        gpe_step_timing& T = h->timing;
+        T.calls += 1;
+        T.step_launches += plain;
+        T.step_ms += ms[1];
+        T.observed_launches += observed;
+        T.observed_ms += ms[2];
+        T.convert_launches += converts;
+        T.convert_ms += ms[0] + ms[3];
+        T.interleaved_calls += interleaved ? 1 : 0;
+    }
+};
+
+// ---------------------------------------------------------- interleaved steps
+
+// Calls shorter than this stay in the handle's layout: the two layout changes in
+// and the two out cost about as much as two steps.
+constexpr int32_t kIlMinSteps = 16;
+
+static unsigned il_grid_blocks(const gpe_handle* h, bool obs) {
+    const ILGrid G = make_il_grid(h->g);
+    switch (h->g.C) {
+        case 1: return il_blocks<1>(G, obs, h->partial_blocks);
+        case 3: return il_blocks<3>(G, obs, h->partial_blocks);
+        default: return il_blocks<5>(G, obs, h->partial_blocks);
+    }
+}
+
+// The interleaved kernel applies: FP32, parabolic, every node 4 entries, a grid
+// with at least V / gcd(V, 8) blocks of work.
+static bool il_applies(const gpe_handle* h) {
+    if (h->p.scheme != GPE_SCHEME_PARABOLIC || h->real_bytes != 4 || h->tab.uniform_deg != 4) return false;
+    return il_grid_blocks(h, false) > 0 && il_grid_blocks(h, true) > 0;
+}
+
+static bool use_interleaved(const gpe_handle* h, int32_t n) {
+    if (n < 1 || (h->tune_kernel != 0 && h->tune_kernel != 6)) return false;
+    if (h->tune_kernel == 0 && n < kIlMinSteps) return false;
+    return il_applies(h);
+}
+
+static gpe_status ensure_il(gpe_handle* h, cudaStream_t s) {
+    const ILGrid G = make_il_grid(h->g);
+    for (int k = 0; k < 2; ++k) {
+        if (h->il[k]) continue;
+        void* p = nullptr;
+        if (cudaMalloc(&p, G.bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GPE_ERR_OOM, "cudaMalloc (interleaved state)");
+        }
+        h->il[k] = static_cast<char*>(p);
+        // the halo rows and the padding cells stay zero
+        CUDA_TRY(cudaMemsetAsync(p, 0, G.bytes, s));
+    }
+    h->ilg = G;
+    return GPE_OK;
+}
+
+static cudaError_t dispatch_il_step(const gpe_handle* h, const StepArgs& a, bool obs, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return launch_il_step<1>(a, h->ilg, h->partial_blocks, obs, h->obs_out, s);
+        case 3: return launch_il_step<3>(a, h->ilg, h->partial_blocks, obs, h->obs_out, s);
+        default: return launch_il_step<5>(a, h->ilg, h->partial_blocks, obs, h->obs_out, s);
+    }
+}
+
+static gpe_status fill_observables(const gpe_handle* h, const double* r, gpe_observables* out);
+
+// n leapfrog steps through the interleaved layout: both psi slots changed in,
+// the steps (the observables of the state the last one reads summed inside it when
+// out is given), both slots changed back.
+static gpe_status il_steps(gpe_handle* h, int32_t n, gpe_observables* out, cudaStream_t s) {
+    gpe_status st = ensure_il(h, s);
+    if (st) return st;
+    StepTimer tm(h, s);
+    tm.mark(0);
+    for (int k = GPE_PSI_EVEN; k <= GPE_PSI_ODD; ++k) {
+        cudaError_t e = launch_il_convert(h->interior[k], h->g, h->il[k], h->ilg, true, s);
+        if (e != cudaSuccess) return cuda_fail(e, "layout change (in)");
+    }
+    h->launches += 2;
+    tm.mark(1);
+    const int32_t plain = out ? n - 1 : n;
+    for (int32_t k = 0; k < n; ++k) {
+        const bool obs = k == plain;
+        if (obs) tm.mark(2);
+        const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
+        const gpe_fields B = fields_at(h, t);
+        const int prev = h->cur, next = h->cur == GPE_PSI_EVEN ? GPE_PSI_ODD : GPE_PSI_EVEN;
+        StepArgs a = make_args(h, B, t);
+        a.prev = h->il[prev];
+        a.next = h->il[next];
+        cudaError_t e = dispatch_il_step(h, a, obs, s);
+        if (e != cudaSuccess) return cuda_fail(e, "interleaved step launch");
+        h->launches += obs ? 2 : 1;
+        h->epoch += 1;
+        h->cur = next;
+        h->nstep++;
+    }
+    if (!out) tm.mark(2);
+    tm.mark(3);
+    for (int k = GPE_PSI_EVEN; k <= GPE_PSI_ODD; ++k) {
+        cudaError_t e = launch_il_convert(h->interior[k], h->g, h->il[k], h->ilg, false, s);
+        if (e != cudaSuccess) return cuda_fail(e, "layout change (out)");
+    }
+    h->launches += 2;
+    tm.mark(4);
+    tm.finish(plain, out ? 1 : 0, 4, true);
+    if (!out) return GPE_OK;
+    double r[OBS_COUNT];
+    CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    gpe_status dst = check_device_error(h, s);
+    if (dst) return dst;
+    return fill_observables(h, r, out);
+}
+
+extern "C" gpe_status gpe_get_step_timing(gpe_handle* h, gpe_step_timing* out, int32_t reset) {
+    if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
+    *out = h->timing;
+    if (reset) std::memset(&h->timing, 0, sizeof h->timing);
+    return GPE_OK;
+}
+
+extern "C" gpe_status gpe_step(gpe_handle* h, int32_t n, void* stream) {
+    if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
+    if (n < 0) return fail(GPE_ERR_INVALID_ARG, "negative step count");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (use_interleaved(h, n)) return il_steps(h, n, nullptr, s);
+    StepTimer tm(h, s);
+    tm.mark(0);
+    tm.mark(1);
+    gpe_status st = plain_steps(h, n, s);
+    if (st) return st;
+    tm.mark(2);
+    tm.mark(3);
+    tm.mark(4);
+    tm.finish(n, 0, 0, false);
     return GPE_OK;
 }
 
@@ -1176,15 +1350,23 @@ extern "C" gpe_status gpe_step_observe(gpe_handle* h, int32_t n, gpe_observables
     if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
     if (n < 1) return fail(GPE_ERR_INVALID_ARG, "step count must be at least 1");
     cudaStream_t s = (cudaStream_t)stream;
-    gpe_status st = gpe_step(h, n - 1, stream);
+    if (use_interleaved(h, n)) return il_steps(h, n, out, s);
+    StepTimer tm(h, s);
+    tm.mark(0);
+    tm.mark(1);
+    gpe_status st = plain_steps(h, n - 1, s);
     if (st) return st;
+    tm.mark(2);
     const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
     if (!leapfrog_from_supported(h)) {
         // another step kernel (tile, slab, hyperbolic, split): a separate observe pass
         gpe_observables o;
         gpe_status ost = gpe_observe(h, h->cur, t, &o, stream);
         if (ost && ost != GPE_ERR_NONFINITE) return ost;
-        st = gpe_step(h, 1, stream);
+        st = plain_steps(h, 1, s);
+        tm.mark(3);
+        tm.mark(4);
+        tm.finish(n - 1, 1, 0, false);
         *out = o;
         return st ? st : (ost ? fail(ost, "state holds non-finite values") : GPE_OK);
     }
@@ -1204,6 +1386,9 @@ extern "C" gpe_status gpe_step_observe(gpe_handle* h, int32_t n, gpe_observables
     if (e != cudaSuccess) return cuda_fail(e, "observed step launch");
     h->cur = next;
     h->nstep++;
+    tm.mark(3);
+    tm.mark(4);
+    tm.finish(n - 1, 1, 0, false);
     double r[OBS_COUNT];
     CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
@@ -1273,7 +1458,14 @@ extern "C" gpe_status gpe_itp(gpe_handle* h, int32_t n, double* mu_out, void* st
 extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) {
     if (!h) return fail(GPE_ERR_INVALID_ARG, "null handle");
     if (key == GPE_TUNE_KERNEL) {
-        if (value < 0 || value > 5) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
+        if (value < 0 || value > 6) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
+        if (value == 6) {
+            if (!il_applies(h))
+                return fail(GPE_ERR_UNSUPPORTED, "the interleaved kernel needs FP32, the parabolic scheme, 4 entries per node "
+                                                 "and a grid of at least V / gcd(V, 8) blocks of work");
+            h->tune_kernel = 6;
+            return GPE_OK;
+        }
         if (value >= 2 && h->g.cell_bytes % 16 != 0) return fail(GPE_ERR_UNSUPPORTED, "tiled kernels need 16-byte cells");
         const int old = h->tune_kernel;
         h->tune_kernel = value;
@@ -1289,6 +1481,11 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
             h->tune_kernel = old;
             return fail(GPE_ERR_UNSUPPORTED, "the slab kernel needs 4 entries per node and a tile whose slabs fit");
         }
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_TIMING) {
+        if (value != 0 && value != 1) return fail(GPE_ERR_INVALID_ARG, "timing: 0 (off) or 1 (on)");
+        h->tune_timing = value;
         return GPE_OK;
     }
     if (key == GPE_TUNE_CARVEOUT) {
@@ -1340,6 +1537,14 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
         *value = key == GPE_TUNE_KERNEL ? 5 : (int32_t)(key == GPE_TUNE_TILE_CELLS ? ss.Tx : ss.Ty);
         return GPE_OK;
     }
+    if (key == GPE_TUNE_TIMING) {
+        *value = h->tune_timing;
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_KERNEL && h->tune_kernel == 6) {
+        *value = 6;
+        return GPE_OK;
+    }
     if (key == GPE_TUNE_KERNEL) *value = tr > 0 ? 4 : ms.T > 0 ? 3 : (tile_cells(h) > 0 ? 2 : 1);
     else if (key == GPE_TUNE_TILE_CELLS) *value = (int32_t)(tr > 0 ? tr : ms.T > 0 ? ms.T : tile_cells(h));
     else if (key == GPE_TUNE_TILE_ROWS) *value = (int32_t)(tr > 0 ? rows_shape(h).RY : ms.TY);
@@ -1373,7 +1578,9 @@ extern "C" gpe_status gpe_autotune(gpe_handle* h, int32_t steps, char* report, s
         int kernel, tile, rows, zchunk, threads;
     };
     std::vector<Cand> cands;
-    cands.push_back({1, 0, 0, 0, 0});
+    // the gather kernel as the automatic choice (0), which also keeps the
+    // interleaved kernel for long calls
+    cands.push_back({0, 0, 0, 0, 0});
     if (h->g.cell_bytes % 16 == 0) {
         cands.push_back({2, 0, 0, 0, 0});
         const uint32_t ryz[4][2] = {{1, 1}, {2, 1}, {1, 2}, {2, 2}};

@@ -83,6 +83,15 @@ struct gpe_handle {
     int32_t* blk = nullptr;   // device row-block table of the current shape
     uint32_t blk_ry = 0, blk_rz = 0, blk_nbuf = 0;
     gpe::AdjointStore adj;
+    // interleaved copies of the psi slots (index = slot) for multi-step calls,
+    // allocated on first use
+    char* il[2] = {nullptr, nullptr};
+    gpe::ILGrid ilg{};
+    // device timing of gpe_step / gpe_step_observe calls (GPE_TUNE_TIMING)
+    int tune_timing = 0;
+    bool tev_ok = false;
+    cudaEvent_t tev[5] = {};
+    gpe_step_timing timing{};
 };
 
 namespace gpe {

@@ -36,4 +36,6 @@ cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint3
     if (precision == GPE_FP64) return launch_pack<double>(packed, dev_base, X, Y, Z, vals, pitch, slice, to_device, s);
     return launch_pack<float>(packed, dev_base, X, Y, Z, vals, pitch, slice, to_device, s);
 }
+GPE_INSTANTIATE_IL(1)
+GPE_DEFINE_IL_CONVERT
 }  // namespace gpe

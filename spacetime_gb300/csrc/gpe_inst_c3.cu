@@ -17,4 +17,5 @@ GPE_INSTANTIATE_INIT(float, 3)
 GPE_INSTANTIATE_INIT(double, 3)
 GPE_INSTANTIATE_HYPER_TILE(float, 3)
 GPE_INSTANTIATE_HYPER_TILE(double, 3)
+GPE_INSTANTIATE_IL(3)
 }  // namespace gpe

@@ -17,4 +17,5 @@ GPE_INSTANTIATE_INIT(float, 5)
 GPE_INSTANTIATE_INIT(double, 5)
 GPE_INSTANTIATE_HYPER_TILE(float, 5)
 GPE_INSTANTIATE_HYPER_TILE(double, 5)
+GPE_INSTANTIATE_IL(5)
 }  // namespace gpe

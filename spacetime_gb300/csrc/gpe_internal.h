@@ -81,6 +81,34 @@ struct Grid {
     uint32_t cell_bytes, qcell_bytes;
 };
 
+// Geometry of an FP32 state in the cell-interleaved layout.  Rows (y, z) run from
+// -1 to Y and -1 to Z (the halo rows and planes are zero); a row holds GX groups of
+// 32 consecutive cells along x; a group holds [node l][component s][cell of the
+// group][re, im], so that node l's component s of 32 neighbouring cells is one
+// contiguous 256-byte run.  Cells x >= X of the last group, and the cells x = -1
+// and x = X, read as zero.
+constexpr uint32_t kIlCells = 32;
+struct ILGrid {
+    uint32_t X, Y, Z, V, C, GX;
+    size_t gb;     // bytes per group: V * C * 32 * 8
+    size_t row;    // bytes per row: GX * gb
+    size_t bytes;  // the buffer: (Y + 2) (Z + 2) rows
+};
+
+inline ILGrid make_il_grid(const Grid& g) {
+    ILGrid G;
+    G.X = g.X;
+    G.Y = g.Y;
+    G.Z = g.Z;
+    G.V = g.V;
+    G.C = g.C;
+    G.GX = (g.X + kIlCells - 1) / kIlCells;
+    G.gb = (size_t)g.V * g.C * kIlCells * 8;
+    G.row = G.GX * G.gb;
+    G.bytes = (size_t)(g.Y + 2) * (g.Z + 2) * G.row;
+    return G;
+}
+
 // Physics constants of a step (double; converted per kernel).
 struct Phys {
     double p0[3];

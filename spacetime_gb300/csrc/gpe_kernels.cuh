@@ -2704,3 +2704,4 @@ cudaError_t launch_hyper_tile(const StepArgs& a, uint32_t T, cudaStream_t s) {
 }  // namespace gpe
 
 #include "gpe_slab.cuh"
+#include "gpe_il.cuh"

@@ -196,6 +196,13 @@ class Stepper:
         capi.check(self.lib.gpe_get_tuning(self._h, key, C.byref(v)), "gpe_get_tuning")
         return v.value
 
+    def step_timing(self, reset: bool = True) -> dict:
+        """Device time of the gpe_step / gpe_step_observe calls made while
+        TUNE_TIMING was 1 (gpe_get_step_timing); the sums restart when `reset`."""
+        t = capi.StepTiming()
+        capi.check(self.lib.gpe_get_step_timing(self._h, C.byref(t), 1 if reset else 0), "gpe_get_step_timing")
+        return t.as_dict()
+
     def autotune(self, steps: int = 10) -> list:
         """Pick the fastest step kernel / tile shape for this handle (gpe_autotune)."""
         import json
