@@ -389,9 +389,12 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  *                      32 cells along x contiguous), steps there and changes them
  *                      back; the states are those of the gather kernel.
  *                  The automatic choice (0) is the interleaved kernel for calls of
- *                  16 or more steps on the handles it applies to (the two layout
- *                  changes cost about two steps), else 1 (grid-stride gather,
- *                  whole-record loads) -- which gpe_get_tuning reports; 2-5 on
+ *                  16 or more steps on the spinor handles it applies to (faster
+ *                  there by 12-50 %; not for scalars, whose 8-byte records
+ *                  already load as coalesced runs; the layout changes cost a few
+ *                  steps per call), else 1
+ *                  (grid-stride gather, whole-record loads) -- which
+ *                  gpe_get_tuning reports; 2-5 on
  *                  request, and gpe_autotune may pick any of 1-4 (it times single
  *                  steps; its gather candidate is recorded as 0).
  * GPE_TUNE_TILE_CELLS: cells per tile row (0 = automatic).

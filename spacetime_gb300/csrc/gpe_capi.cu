@@ -1214,9 +1214,17 @@ static bool il_applies(const gpe_handle* h) {
     return il_grid_blocks(h, false) > 0 && il_grid_blocks(h, true) > 0;
 }
 
+// Where the automatic choice takes the interleaved kernel, by measurement (FP32
+// leapfrog, one launch, fraction of the measured copy peak, gather / interleaved;
+// BCC 96^3, A15 64^3, C15 48^3, Z 56^3): spin-1 BCC 0.68 / 0.85, A15 0.63 / 0.85,
+// C15 0.62 / 0.70, Z 0.66 / 0.77; spin-2 BCC 0.66 / 0.89, A15 0.59 / 0.88, C15
+// 0.60 / 0.72, Z 0.64 / 0.79.  Not for scalars (BCC 0.68 / 0.51, C15 0.64 / 0.40:
+// an 8-byte record already loads as one coalesced run in the handle's layout).
+static bool il_auto(const gpe_handle* h) { return h->g.C >= 3; }
+
 static bool use_interleaved(const gpe_handle* h, int32_t n) {
     if (n < 1 || (h->tune_kernel != 0 && h->tune_kernel != 6)) return false;
-    if (h->tune_kernel == 0 && n < kIlMinSteps) return false;
+    if (h->tune_kernel == 0 && (n < kIlMinSteps || !il_auto(h))) return false;
     return il_applies(h);
 }
 

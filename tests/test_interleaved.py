@@ -134,6 +134,7 @@ def test_interleaved_step_observe(gpu, name, C, dims):
             s.upload(capi.PSI_ODD, psi)
             s.set_ramp(_ramp(p.dt), 0.0)
             s.start()
+        b.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)
         b.set_tuning(capi.TUNE_TIMING, 1)
         a.step(n - 1)
         want = a.observe(a.current, n * p.dt)
@@ -152,6 +153,24 @@ def test_interleaved_step_observe(gpu, name, C, dims):
     np.testing.assert_allclose(got["com"], want["com"], rtol=2e-6, atol=2e-5 * scale)
     assert got["max_abs"] == pytest.approx(want["max_abs"], rel=1e-6)
     assert got["nonfinite"] == 0
+
+
+@pytest.mark.parametrize("name,C,want", [("bcc", 3, 1), ("a15", 3, 1), ("bcc", 5, 1), ("z", 5, 1), ("bcc", 1, 0),
+                                         ("z", 3, 1), ("c15", 3, 1), ("c15", 5, 1), ("c15", 1, 0), ("a15", 1, 0)])
+def test_automatic_choice_by_lattice(gpu, name, C, want):
+    """The automatic choice takes the interleaved kernel for long calls on spinor
+    handles (where it measured faster) and keeps the gather kernel for scalars."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, (33, 2, 2) if lat.nodes > 40 else (40, 3, 2))
+    with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_TIMING, 1)
+        s.upload(capi.PSI_ODD, _state(lat, p, 9))
+        s.start()
+        s.step(16)
+        assert s.step_timing()["interleaved_calls"] == want
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)   # applies everywhere on 4-entry lattices
+        s.step(1)
+        assert s.step_timing()["interleaved_calls"] == 1
 
 
 def test_interleaved_rejected_where_it_does_not_apply(gpu):
