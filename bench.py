@@ -157,7 +157,7 @@ def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
     if w["scheme"] == 0 and gather:
         name = "parabolic_fixed_kernel<float,%d,LEAPFROG,4>" % w["C"]
     if interleaved:
-        name = "il_step_kernel<%d>" % w["C"]
+        name = "il_step_kernel<%d,%d>" % (w["C"], 8 if w["lattice"] == "fcc" else 4)
     return {"metric": "lattice-site-updates/s", "value": sites * inner * steps / (total_ms * 1e-3),
             "unit": "lattice-site-updates/s", "steps": steps, "inner_steps_per_step": inner, "sites": sites,
             "ms_per_step": total_ms / steps, "dims": list(p.dims),
@@ -412,14 +412,16 @@ def ensemble_members(count=None):
 
 def run_ensemble(args):
     """--workload ensemble-256: one JSON line."""
-    print(json.dumps(ensemble_result(args.members, args.inner or 100, args.steps, args.warmup)))
+    print(json.dumps(ensemble_result(args.members, args.inner or 100, args.steps, args.warmup, args.batch_layout)))
     return 0
 
 
-def ensemble_result(n_members, inner, replays, warmup):
+def ensemble_result(n_members, inner, replays, warmup, layout=1):
     """Every member advanced by the persistent batch kernel: `inner` steps in one
     persistent launch per CUDA-graph replay, `replays` replays timed with CUDA
-    events (warm-up: `warmup` uncaptured 10-step batch calls)."""
+    events (warm-up: `warmup` uncaptured 10-step batch calls).  layout 1: the
+    spin-1 members in the interleaved layout (changed in and back inside every
+    replay), 0: every member in its handle's layout."""
     import ctypes as C
 
     import torch
@@ -451,6 +453,7 @@ def ensemble_result(n_members, inner, replays, warmup):
     setup_s = time.perf_counter() - t_setup
     b = Batch(members)
     b.stream = sp
+    b.set_tuning(capi.BATCH_LAYOUT, layout)
     sites = b.sites
     tune = b.autotune(steps=2)
     e_first = [members[k].observe(members[k].current) for k in (0, len(members) // 2, len(members) - 1)]
@@ -486,7 +489,7 @@ def ensemble_result(n_members, inner, replays, warmup):
                       "sites": sites, "members": counts, "dt": ENS["dt"],
                       "l2": "inputs larger than L2 (%.1f GB per state buffer set), no flush" % (state_bytes / 1e9)},
            "roofline": {"bound": "hbm", "achieved": algo / (step_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": algo / (step_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": "batch_kernel<float,3>",
+                        "frac": algo / (step_ms * 1e-3) / 1e9 / peak, "peak_kind": kind, "kernel": "batch_kernel<float,3,true,%s>" % ("true" if layout else "false"),
                         "algorithmic_bytes_per_step": algo, "avg_step_ms": step_ms, "traffic": None},
            "gpu_launches": launches, "graph_replays": replays, "clocks": clk.summary(), "setup_s": setup_s,
            "autotune": tune,
@@ -498,8 +501,8 @@ def ensemble_result(n_members, inner, replays, warmup):
     res["e2e"] = {"value": sites * inner * replays / (total_ms * 1e-3 + (time.perf_counter() - t0) * replays),
                   "unit": "lattice-site-updates/s", "h2d_bytes_per_step": len(members) * (C.sizeof(capi.Ramp) + 48),
                   "d2h_bytes_per_step": 96 * len(members),
-                  "path": "gpe_batch_replay (graph: member state from pinned host memory + one persistent launch) + "
-                          "gpe_observe of every member",
+                  "path": "gpe_batch_replay (graph: member state from pinned host memory, the interleaved members' "
+                          "layout changes in, one persistent launch, layout changes out) + gpe_observe of every member",
                   "norm_min_max": [min(o["norm"] for o in obs_all), max(o["norm"] for o in obs_all)]}
     b.close()
     for s in members:
@@ -1054,7 +1057,7 @@ def run_gpu(args):
 
     kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_fixed_kernel<float,3,LEAPFROG,4>",
                    capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>",
-                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>", capi.KERNEL_INTERLEAVED: "il_step_kernel<3>"}
+                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>", capi.KERNEL_INTERLEAVED: "il_step_kernel<3,4>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
     for key, val in ((capi.TUNE_TILE_CELLS, args.tile), (capi.TUNE_TILE_ROWS, args.rows), (capi.TUNE_ZCHUNK, args.zchunk),
@@ -1289,6 +1292,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=ADJ["steps"], help="adjoint-bcc64: steps of the recorded run")
     ap.add_argument("--fd-knots", type=int, default=ADJ["fd_knots"], help="adjoint-bcc64: knots checked by central differences")
     ap.add_argument("--members", type=int, default=ENS["members"], help="ensemble-256: members of the ensemble (a prefix)")
+    ap.add_argument("--batch-layout", type=int, default=1, choices=[0, 1],
+                    help="ensemble-256: 1 spinor members in the interleaved layout, 0 every member in its handle's")
     ap.add_argument("--legs", default="all",
                     help="default run: the other configurations to add to the line (all, none, or a comma list of %s)"
                     % ",".join(LEG_NAMES))

@@ -560,13 +560,19 @@ typedef struct gpe_batch gpe_batch;
  * (default 10000).  GPE_BATCH_TEST_EXTRA_ARRIVALS is a test hook for the failure
  * path: the barrier then waits for that many arrivals that never come, every wait
  * runs out, the kernel returns and the call reports GPE_ERR_TIMEOUT (set it back
- * to 0 to step again). */
+ * to 0 to step again).  GPE_BATCH_LAYOUT 1 (default): FP32 spin-1 members on
+ * lattices with rows of 4 (or of 4 and 8) stencil entries are stepped in the
+ * cell-interleaved layout of gpe_step's interleaved kernel -- each call changes
+ * their two psi slots in and back (4 layout-change launches per member, in the
+ * captured graph too) and the states are those of the gather form bit for bit;
+ * 0: every member in its handle's layout.  Changing it drops a captured run. */
 enum {
     GPE_BATCH_ITEM_NODES = 0,
     GPE_BATCH_STEPS_PER_LAUNCH = 1,
     GPE_BATCH_BLOCKS_PER_SM = 2,
     GPE_BATCH_BARRIER_TIMEOUT_MS = 3,
-    GPE_BATCH_TEST_EXTRA_ARRIVALS = 4
+    GPE_BATCH_TEST_EXTRA_ARRIVALS = 4,
+    GPE_BATCH_LAYOUT = 5
 };
 gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count, gpe_batch** out);
 gpe_status gpe_batch_destroy(gpe_batch* b);

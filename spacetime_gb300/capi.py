@@ -40,6 +40,7 @@ TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS, TUNE_OB
 FIELD_DENSITY, FIELD_SPIN, FIELD_UV_THETA, FIELD_MAX_HAMILTON, FIELD_PROJ_X, FIELD_PROJ_Y = 0, 1, 2, 3, 4, 5
 KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS, KERNEL_SLAB, KERNEL_INTERLEAVED = 0, 1, 2, 3, 4, 5, 6
 BATCH_ITEM_NODES, BATCH_STEPS_PER_LAUNCH, BATCH_BLOCKS_PER_SM, BATCH_BARRIER_TIMEOUT_MS, BATCH_TEST_EXTRA_ARRIVALS = 0, 1, 2, 3, 4
+BATCH_LAYOUT = 5
 
 
 class StencilEntry(C.Structure):

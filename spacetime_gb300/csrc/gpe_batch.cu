@@ -47,6 +47,11 @@ struct BatchMember {
     uint32_t row_items; // X * V
     int32_t C;
     int32_t cslot;      // slot of the member's MemberConst, or -1
+    int32_t il_deg;     // 0: the handle's layout; 4 or 8: psi[] are the member's
+                        // cell-interleaved copies, rows of at most il_deg entries
+    ILGrid ilg;
+    FastDiv divGX;
+    const int32_t* il_off;  // interleaved entry offsets (il_offsets), or null
 };
 
 // The values an FP32 member's node loop reads for every node, kept in constant
@@ -183,13 +188,73 @@ __device__ __forceinline__ void batch_rows(const MK& M, const SmemTables<R>& st,
     }
 }
 
+// Rows row0 .. row0 + rows - 1 of a member in the interleaved layout (FP32).
+// Warp task t = u V + l within the item: node l of the item's u-th group
+// (il_lane_group, counted row after row): the 8 warps of a block take
+// consecutive nodes of the same groups, as the single-condensate interleaved
+// kernel's warps do, so the neighbour records they gather are read while they are
+// still in L2.  A node's stencil comes from the shared tables for every task:
+// st.nb_off holds the member's interleaved entry offsets (il_offsets: rows, node
+// and dx, with dx + 1 in the two low bits), to which each lane adds its own cell
+// and, where x + dx leaves the group, the step to the neighbouring group.  The
+// per-lane update is il_task, bit for bit the single-condensate kernel's.
+template <int C, int D, int CELLS>
+__device__ __forceinline__ void batch_il_rows(const BatchMember& M, const SmemTables<float>& st, const PhysR<float>& P,
+                                              const PhysR<float>* F, const char* prev, char* next, uint32_t row0,
+                                              uint32_t rows) {
+    const ILGrid& G = M.ilg;
+    const uint32_t sub = threadIdx.x & (CELLS - 1);
+    constexpr uint32_t kWarps = kBatchThreads / 32;
+    constexpr uint32_t kWG = 32 / CELLS;
+    const uint32_t nq = rows * G.GX;
+    const uint32_t tasks = (nq + kWG - 1) / kWG * G.V;
+    const int32_t wrap = (int32_t)G.gb - CELLS * 8;
+    NoObs no;
+    for (uint32_t t = threadIdx.x >> 5; t < tasks; t += kWarps) {
+        const uint32_t u = fdiv(t, M.divV);
+        const uint32_t l = t - u * G.V;
+        uint32_t gx, y, z;
+        if (!il_lane_group<CELLS>(G, u, nq, row0, M.divGX, M.divY, gx, y, z)) continue;
+        const int f0 = st.row_ptr[l];
+        const int nd = D == 4 ? 4 : st.row_ptr[l + 1] - f0;
+        int32_t off[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            off[k] = 1;
+            if (k < nd) {
+                const int32_t b = st.nb_off[f0 + k];
+                const int xl = (int)sub + (b & 3) - 1;
+                const int32_t gs = xl < 0 ? -1 : (xl >= CELLS ? 1 : 0);
+                off[k] = ((b & ~3) + (int32_t)sub * 8 + gs * wrap) | (b & 3);
+            }
+        }
+        il_task<C, D, CELLS, NoObs>(G, P, F, prev, next, off, st.w + f0, nd, st.pos + 3 * l, sub, l, gx, y, z, &no);
+    }
+}
+
 // One work item: the member's kernel form by its spin and row lengths.  Members
 // whose nodes all have 4 neighbours issue the 4 loads together; rows of 4 and 8
-// (FCC) take their entries in vectors of 4.
-template <typename R, int CMASK, typename MK>
+// (FCC) take their entries in vectors of 4.  Interleaved members (FP32 spin-1):
+// batch_il_rows.
+template <typename R, int CMASK, bool IL, typename MK>
 __device__ __forceinline__ void batch_item(const BatchMember& M, const MK& K, const SmemTables<R>& st,
                                            const PhysR<R>& P, const PhysR<R>* F, const char* prev, char* next,
                                            uint32_t row0, uint32_t rows) {
+    if constexpr (IL && sizeof(R) == 4) {
+        if (M.il_deg) {
+            const bool c32 = M.ilg.cells == 32;
+            if ((CMASK & 2) && M.C == 3) {
+                if (M.il_deg == 4) {
+                    if (c32) batch_il_rows<3, 4, 32>(M, st, P, F, prev, next, row0, rows);
+                    else batch_il_rows<3, 4, 16>(M, st, P, F, prev, next, row0, rows);
+                } else {
+                    if (c32) batch_il_rows<3, 8, 32>(M, st, P, F, prev, next, row0, rows);
+                    else batch_il_rows<3, 8, 16>(M, st, P, F, prev, next, row0, rows);
+                }
+            }
+            return;
+        }
+    }
     const bool d4 = M.tab.uniform_deg == 4, quad = M.tab.quad_rows != 0;
     if ((CMASK & 1) && M.C == 1) {
         if (d4) batch_rows<R, 1, 4>(K, st, P, F, prev, next, row0, rows);
@@ -207,8 +272,9 @@ __device__ __forceinline__ void batch_item(const BatchMember& M, const MK& K, co
 // CMASK: which component counts the batch holds (bit 0: 1, bit 1: 3, bit 2: 5), so
 // that a batch of scalar and spin-1 members does not carry spin-2 registers; such
 // FP32 batches fit 64 registers, 4 blocks per SM.  CONSTP (FP32): every member has
-// a MemberConst slot.
-template <typename R, int CMASK, bool CONSTP>
+// a MemberConst slot.  IL (FP32): some members are stepped in the interleaved
+// layout.
+template <typename R, int CMASK, bool CONSTP, bool IL>
 __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4) ? 3 : 4) batch_kernel(BatchArgs A) {
     static_assert(!CONSTP || sizeof(R) == 4, "constant-memory members are FP32");
     __shared__ SmemTables<R> st;
@@ -240,8 +306,9 @@ __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4
                 __syncthreads();
                 const int V = M.g.V, nent = M.tab.entries;
                 for (int i = threadIdx.x; i <= V; i += kBatchThreads) st.row_ptr[i] = M.tab.row_ptr[i];
+                const int32_t* offs = IL && M.il_deg ? M.il_off : M.tab.nb_off;
                 for (int i = threadIdx.x; i < nent; i += kBatchThreads) {
-                    st.nb_off[i] = M.tab.nb_off[i];
+                    st.nb_off[i] = offs[i];
                     if constexpr (sizeof(R) == 4) st.w[i] = M.tab.w32[i];
                     else st.w[i] = M.tab.w64[i];
                 }
@@ -262,9 +329,9 @@ __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4
             char* next = M.psi[prev_slot ^ 1];
             if constexpr (CONSTP) {
                 const MemberConst& K = c_members[M.cslot];
-                batch_item<R, CMASK>(M, K, st, K.p, &P, prev, next, w.row0, w.rows);
+                batch_item<R, CMASK, IL>(M, K, st, K.p, &P, prev, next, w.row0, w.rows);
             } else {
-                batch_item<R, CMASK>(M, M, st, P, nullptr, prev, next, w.row0, w.rows);
+                batch_item<R, CMASK, IL>(M, M, st, P, nullptr, prev, next, w.row0, w.rows);
             }
         }
         if (s + 1 < A.nsteps) {
@@ -275,12 +342,12 @@ __global__ void __launch_bounds__(kBatchThreads, sizeof(R) == 8 ? 1 : (CMASK & 4
     }
 }
 
-template <typename R, int CMASK, bool CONSTP>
+template <typename R, int CMASK, bool CONSTP, bool IL = false>
 static void* batch_kernel_ptr() {
-    return reinterpret_cast<void*>(&batch_kernel<R, CMASK, CONSTP>);
+    return reinterpret_cast<void*>(&batch_kernel<R, CMASK, CONSTP, IL>);
 }
 
-static void* batch_kernel_for(int precision, int cmask, bool constp) {
+static void* batch_kernel_for(int precision, int cmask, bool constp, bool il) {
     typedef void* (*Fn)();
     static const Fn f32[8] = {nullptr, batch_kernel_ptr<float, 1, false>, batch_kernel_ptr<float, 2, false>,
                               batch_kernel_ptr<float, 3, false>, batch_kernel_ptr<float, 4, false>,
@@ -290,13 +357,23 @@ static void* batch_kernel_for(int precision, int cmask, bool constp) {
                                batch_kernel_ptr<float, 3, true>, batch_kernel_ptr<float, 4, true>,
                                batch_kernel_ptr<float, 5, true>, batch_kernel_ptr<float, 6, true>,
                                batch_kernel_ptr<float, 7, true>};
+    // interleaved members are spinors: masks with bit 1 or 2
+    static const Fn f32i[8] = {nullptr, nullptr, batch_kernel_ptr<float, 2, false, true>,
+                               batch_kernel_ptr<float, 3, false, true>, batch_kernel_ptr<float, 4, false, true>,
+                               batch_kernel_ptr<float, 5, false, true>, batch_kernel_ptr<float, 6, false, true>,
+                               batch_kernel_ptr<float, 7, false, true>};
+    static const Fn f32ci[8] = {nullptr, nullptr, batch_kernel_ptr<float, 2, true, true>,
+                                batch_kernel_ptr<float, 3, true, true>, batch_kernel_ptr<float, 4, true, true>,
+                                batch_kernel_ptr<float, 5, true, true>, batch_kernel_ptr<float, 6, true, true>,
+                                batch_kernel_ptr<float, 7, true, true>};
     static const Fn f64[8] = {nullptr, batch_kernel_ptr<double, 1, false>, batch_kernel_ptr<double, 2, false>,
                               batch_kernel_ptr<double, 3, false>, batch_kernel_ptr<double, 4, false>,
                               batch_kernel_ptr<double, 5, false>, batch_kernel_ptr<double, 6, false>,
                               batch_kernel_ptr<double, 7, false>};
     if (cmask < 1 || cmask > 7) return nullptr;
     if (precision == GPE_FP64) return f64[cmask]();
-    return (constp ? f32c : f32)[cmask]();
+    const Fn* t = il ? (constp ? f32ci : f32i) : (constp ? f32c : f32);
+    return t[cmask] ? t[cmask]() : nullptr;
 }
 
 // Constant-memory slots of FP32 members, per device.
@@ -352,6 +429,10 @@ struct gpe_batch {
     unsigned* d_bar = nullptr;
     int* d_err = nullptr;
     std::vector<int> cslots;         // FP32: one constant-memory slot per member, or none
+    int32_t layout = 1;              // GPE_BATCH_LAYOUT
+    std::vector<int> il_deg;         // per member: 0, or the interleaved rows (4 or 8)
+    std::vector<void*> il_off;       // per member: device interleaved entry offsets, or null
+    bool any_il = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int32_t graph_steps = 0;
@@ -378,6 +459,88 @@ void member_constants(const gpe_handle* h, BatchMember& M) {
     M.row_items = a.row_items;
     M.C = h->g.C;
     M.cslot = -1;
+    M.il_deg = 0;
+    M.ilg = make_il_grid(h->g);
+    M.divGX = make_fastdiv(M.ilg.GX);
+    M.il_off = nullptr;
+}
+
+// A member's stencil entries as byte offsets in the interleaved layout, relative to
+// a group's base, for the group's first cell: the rows (dz, dy), the node and dx,
+// with dx + 1 (|dx| <= 1) in the two low bits.  Empty if one does not fit 32 bits.
+std::vector<int32_t> il_offsets(const gpe_handle* h) {
+    const ILGrid G = make_il_grid(h->g);
+    const int64_t node_run = (int64_t)G.C * G.cells * 8;
+    std::vector<int32_t> out;
+    for (const gpe_stencil_entry& e : h->lat.stencil) {
+        const int64_t b = ((int64_t)e.dz * (G.Y + 2) + e.dy) * (int64_t)G.row + (int64_t)e.node * node_run + (int64_t)e.dx * 8;
+        if (b > INT32_MAX - 3 || b < INT32_MIN) return {};
+        out.push_back((int32_t)b | (e.dx + 1));
+    }
+    return out;
+}
+
+// The layout member m is stepped in: the interleaved one for FP32 spin-1 members on
+// lattices with rows of 4 (or of 4 and 8) entries when GPE_BATCH_LAYOUT is 1 (the
+// default), the handle's own otherwise.  (Spin-2 members keep the handle's layout:
+// their interleaved path does not fit the batch kernel's registers.)
+int member_il_deg(const gpe_batch* b, const gpe_handle* h) {
+    if (!b->layout || b->precision != GPE_FP32 || h->g.C != 3) return 0;
+    return il_stencil_deg(h);
+}
+
+// Every member's BatchMember (constants, layout, constant-memory slot) into d_members.
+gpe_status upload_members(gpe_batch* b) {
+    const size_t n = b->members.size();
+    std::vector<BatchMember> hm(n);
+    b->il_deg.assign(n, 0);
+    b->il_off.resize(n, nullptr);
+    b->any_il = false;
+    for (size_t i = 0; i < n; ++i) {
+        gpe_handle* h = b->members[i];
+        member_constants(h, hm[i]);
+        if (!b->cslots.empty()) hm[i].cslot = b->cslots[i];
+        const int deg = member_il_deg(b, h);
+        const std::vector<int32_t> offs = deg ? il_offsets(h) : std::vector<int32_t>();
+        if (deg && !offs.empty()) {
+            if (gpe_status st = il_ensure(h, 0)) return st;
+            if (!b->il_off[i]) {
+                if (cudaMalloc(&b->il_off[i], offs.size() * sizeof(int32_t)) != cudaSuccess)
+                    return fail(GPE_ERR_OOM, "cudaMalloc (batch interleaved offsets)");
+                cudaError_t e = cudaMemcpy(b->il_off[i], offs.data(), offs.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+                if (e != cudaSuccess) return cuda_fail(e, "batch interleaved offsets");
+            }
+            hm[i].il_off = static_cast<const int32_t*>(b->il_off[i]);
+            hm[i].il_deg = deg;
+            hm[i].psi[GPE_PSI_EVEN] = h->il[GPE_PSI_EVEN];
+            hm[i].psi[GPE_PSI_ODD] = h->il[GPE_PSI_ODD];
+            b->il_deg[i] = deg;
+            b->any_il = true;
+        }
+    }
+    cudaError_t e = cudaMemcpy(b->d_members, hm.data(), n * sizeof(BatchMember), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "batch members upload");
+    return GPE_OK;
+}
+
+// The interleaved members' two psi slots changed into (to_il) or out of their
+// interleaved copies.
+gpe_status convert_members(gpe_batch* b, bool to_il, cudaStream_t s) {
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        if (!b->il_deg[i]) continue;
+        gpe_handle* h = b->members[i];
+        for (int k = GPE_PSI_EVEN; k <= GPE_PSI_ODD; ++k) {
+            cudaError_t e = launch_il_convert(h->interior[k], h->g, h->il[k], h->ilg, to_il, s);
+            if (e != cudaSuccess) return cuda_fail(e, to_il ? "batch layout change (in)" : "batch layout change (out)");
+        }
+    }
+    return GPE_OK;
+}
+
+uint64_t convert_launch_count(const gpe_batch* b) {
+    uint64_t n = 0;
+    for (int d : b->il_deg) n += d ? 4 : 0;
+    return n;
 }
 
 // A lattice is told apart by its node and stencil-entry counts per cell.
@@ -464,7 +627,7 @@ gpe_status fill_state(gpe_batch* b) {
 }
 
 gpe_status grid_size(gpe_batch* b) {
-    void* fn = batch_kernel_for(b->precision, b->cmask, !b->cslots.empty());
+    void* fn = batch_kernel_for(b->precision, b->cmask, !b->cslots.empty(), b->any_il);
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kBatchThreads, 0);
     if (e != cudaSuccess) return batch_fail_cuda(e, "occupancy of the batch kernel");
@@ -475,14 +638,17 @@ gpe_status grid_size(gpe_batch* b) {
     return GPE_OK;
 }
 
-// Enqueues n steps of every member: the state upload, then ceil(n / K) persistent
-// launches.  Capturable into a CUDA graph (the state copy reads the pinned host
+// Enqueues n steps of every member: the state upload, the interleaved members'
+// layout change in (convert), ceil(n / K) persistent launches, and the layout
+// change back.  Capturable into a CUDA graph (the state copy reads the pinned host
 // array when the graph runs).
 gpe_status enqueue_steps(gpe_batch* b, int32_t n, cudaStream_t s, const BatchMember* members, uint32_t nmembers,
-                         const BatchState* h_state, int grid) {
+                         const BatchState* h_state, int grid, bool convert) {
     cudaError_t e = cudaMemcpyAsync(b->d_state, h_state, nmembers * sizeof(BatchState), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return batch_fail_cuda(e, "batch state upload");
-    void* fn = batch_kernel_for(b->precision, b->cmask, !b->cslots.empty());
+    if (convert)
+        if (gpe_status st = convert_members(b, true, s)) return st;
+    void* fn = batch_kernel_for(b->precision, b->cmask, !b->cslots.empty(), b->any_il);
     const int32_t K = std::min(b->steps_per_launch > 0 ? b->steps_per_launch : n, kMaxStepsPerLaunch);
     for (int32_t done = 0; done < n; done += K) {
         const int32_t steps = std::min(K, n - done);
@@ -517,6 +683,10 @@ gpe_status enqueue_steps(gpe_batch* b, int32_t n, cudaStream_t s, const BatchMem
         cfg.numAttrs = 1;
         if ((e = cudaLaunchKernelExC(&cfg, fn, args)) != cudaSuccess) return batch_fail_cuda(e, "batch kernel launch");
         b->launches += 1;
+    }
+    if (convert) {
+        if (gpe_status st = convert_members(b, false, s)) return st;
+        b->launches += convert_launch_count(b);
     }
     return GPE_OK;
 }
@@ -554,6 +724,9 @@ void release_batch(gpe_batch* b) {
     if (b->d_err) cudaFree(b->d_err);
     give_slots(b->device, b->cslots);
     b->cslots.clear();
+    for (void* p : b->il_off)
+        if (p) cudaFree(p);
+    b->il_off.clear();
 }
 
 }  // namespace
@@ -630,8 +803,7 @@ extern "C" gpe_status gpe_batch_create(gpe_handle* const* members, int32_t count
         return fail(GPE_ERR_OOM, "batch allocation");
     }
     cudaMemset(b->d_err, 0, sizeof(int));
-    cudaError_t e = cudaMemcpy(b->d_members, hm.data(), count * sizeof(BatchMember), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) st = cuda_fail(e, "batch members upload");
+    st = upload_members(b);
     if (!st) st = grid_size(b);
     if (!st) st = rebuild_items(b);
     if (st) {
@@ -660,7 +832,7 @@ extern "C" gpe_status gpe_batch_step(gpe_batch* b, int32_t n, void* stream) {
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "batch step");
     if (gpe_status st = fill_state(b)) return st;
-    gpe_status st = enqueue_steps(b, n, s, b->d_members, (uint32_t)b->members.size(), b->h_state, b->grid);
+    gpe_status st = enqueue_steps(b, n, s, b->d_members, (uint32_t)b->members.size(), b->h_state, b->grid, true);
     if (st) return st;
     advance_members(b, n);
     return check_batch_error(b, s);
@@ -679,7 +851,7 @@ extern "C" gpe_status gpe_batch_capture(gpe_batch* b, int32_t n, void* stream) {
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
     const uint64_t launches = b->launches;
-    gpe_status st = enqueue_steps(b, n, s, b->d_members, (uint32_t)b->members.size(), b->h_state, b->grid);
+    gpe_status st = enqueue_steps(b, n, s, b->d_members, (uint32_t)b->members.size(), b->h_state, b->grid, true);
     b->launches = launches;
     cudaGraph_t g = nullptr;
     e = cudaStreamEndCapture(s, &g);
@@ -707,8 +879,8 @@ extern "C" gpe_status gpe_batch_replay(gpe_batch* b, void* stream) {
     if (gpe_status st = fill_state(b)) return st;
     e = cudaGraphLaunch(b->exec, s);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
-    const int32_t K = b->steps_per_launch > 0 ? b->steps_per_launch : b->graph_steps;
-    b->launches += (uint64_t)((b->graph_steps + K - 1) / K);
+    const int32_t K = std::min(b->steps_per_launch > 0 ? b->steps_per_launch : b->graph_steps, kMaxStepsPerLaunch);
+    b->launches += (uint64_t)((b->graph_steps + K - 1) / K) + convert_launch_count(b);
     advance_members(b, b->graph_steps);
     return check_batch_error(b, s);
 }
@@ -741,6 +913,21 @@ extern "C" gpe_status gpe_batch_set_tuning(gpe_batch* b, int32_t key, int32_t va
         b->tune_blocks_per_sm = value;
         return grid_size(b);
     }
+    if (key == GPE_BATCH_LAYOUT) {
+        if (value < 0 || value > 1) return fail(GPE_ERR_INVALID_ARG, "batch layout (0 or 1)");
+        if (value == b->layout) return GPE_OK;
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) return cuda_fail(e, "batch layout");
+        // a captured run holds the old layout's kernel and layout changes
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        if (b->graph) cudaGraphDestroy(b->graph);
+        b->exec = nullptr;
+        b->graph = nullptr;
+        b->graph_steps = 0;
+        b->layout = value;
+        if (gpe_status st = upload_members(b)) return st;
+        return grid_size(b);
+    }
     return fail(GPE_ERR_INVALID_ARG, "unknown batch tuning key");
 }
 
@@ -751,6 +938,7 @@ extern "C" gpe_status gpe_batch_get_tuning(const gpe_batch* b, int32_t key, int3
     else if (key == GPE_BATCH_BLOCKS_PER_SM) *value = b->grid / (b->sms ? b->sms : 1);
     else if (key == GPE_BATCH_BARRIER_TIMEOUT_MS) *value = b->barrier_timeout_ms;
     else if (key == GPE_BATCH_TEST_EXTRA_ARRIVALS) *value = b->extra_arrivals;
+    else if (key == GPE_BATCH_LAYOUT) *value = b->layout;
     else return fail(GPE_ERR_INVALID_ARG, "unknown batch tuning key");
     return GPE_OK;
 }
@@ -789,8 +977,24 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
             member_constants(h, hm[i]);
             if (!b->cslots.empty()) hm[i].cslot = b->cslots[which[i]];
             hs[i] = b->h_state[which[i]];
+            const int deg = b->il_deg[which[i]];
             for (int slot = 0; slot < 2 && ok; ++slot) {
                 void* p = nullptr;
+                if (deg) {
+                    // interleaved members: a zeroed scratch copy in that layout
+                    if (cudaMalloc(&p, h->ilg.bytes) != cudaSuccess) {
+                        ok = false;
+                        break;
+                    }
+                    scratch.push_back(p);
+                    cudaMemsetAsync(p, 0, h->ilg.bytes, s);
+                    if (launch_il_convert(h->interior[slot], h->g, static_cast<char*>(p), h->ilg, true, s) != cudaSuccess) {
+                        ok = false;
+                        break;
+                    }
+                    hm[i].psi[slot] = static_cast<char*>(p);
+                    continue;
+                }
                 if (cudaMalloc(&p, h->alloc_bytes[slot]) != cudaSuccess) {
                     ok = false;
                     break;
@@ -799,6 +1003,8 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
                 cudaMemcpyAsync(p, h->alloc[slot], h->alloc_bytes[slot], cudaMemcpyDeviceToDevice, s);
                 hm[i].psi[slot] = static_cast<char*>(p) + (h->interior[slot] - static_cast<char*>(h->alloc[slot]));
             }
+            hm[i].il_deg = deg;
+            hm[i].il_off = deg ? static_cast<const int32_t*>(b->il_off[which[i]]) : nullptr;
         }
         BatchMember* dm = nullptr;
         BatchState* ps = nullptr;
@@ -834,12 +1040,12 @@ extern "C" gpe_status gpe_batch_autotune(gpe_batch* b, int32_t steps, char* repo
             // as many blocks as give each the work a block has in the whole batch
             const double share = (double)b->item_cost.back() / (double)full_cost;
             const int tgrid = std::max(1, std::min(b->grid, (int)std::lround(share * b->grid)));
-            if (enqueue_steps(b, 1, s, dm, (uint32_t)which.size(), ps, tgrid) != GPE_OK) {
+            if (enqueue_steps(b, 1, s, dm, (uint32_t)which.size(), ps, tgrid, false) != GPE_OK) {
                 ok = false;
                 break;
             }
             cudaEventRecord(e0, s);
-            gpe_status st = enqueue_steps(b, steps, s, dm, (uint32_t)which.size(), ps, tgrid);
+            gpe_status st = enqueue_steps(b, steps, s, dm, (uint32_t)which.size(), ps, tgrid, false);
             cudaEventRecord(e1, s);
             if (st != GPE_OK || cudaEventSynchronize(e1) != cudaSuccess) {
                 ok = false;

@@ -52,9 +52,10 @@ cudaError_t launch_parabolic_slab(const StepArgs& a, uint32_t Tx, uint32_t Ty, u
 template <typename R, int C>
 cudaError_t launch_parabolic_observe(const StepArgs& a, double* out, cudaStream_t s);
 template <int C>
-cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, size_t max_blocks, bool obs, double* out, cudaStream_t s);
+cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, int deg, size_t max_blocks, bool obs, double* out,
+                           cudaStream_t s);
 template <int C>
-unsigned il_blocks(const ILGrid& G, bool obs, size_t max_blocks);
+unsigned il_blocks(const ILGrid& G, int deg, bool obs, size_t max_blocks);
 cudaError_t launch_il_convert(char* aos, const Grid& g, char* il, const ILGrid& G, bool to_il, cudaStream_t s);
 enum HyperKind {
     HK_FUSED_LEAPFROG = 0,
@@ -245,6 +246,8 @@ static gpe_status build_tables(gpe_handle* h) {
         quad = len > 0 && len % 4 == 0;
     }
     h->tab.quad_rows = quad ? 1 : 0;
+    h->tab.max_deg = 0;
+    for (int l = 0; l < L.V; ++l) h->tab.max_deg = std::max(h->tab.max_deg, L.row_ptr[l + 1] - L.row_ptr[l]);
     // rows (dy, dz) touched by the stencil, the own row first
     h->nrows = 1;
     h->rdy[0] = h->rdz[0] = 0;
@@ -1198,19 +1201,35 @@ struct StepTimer {
 // and the two out cost about as much as two steps.
 constexpr int32_t kIlMinSteps = 16;
 
+// Rows the interleaved kernel takes: 4 entries in every row (BCC, A15, C15, Z), or
+// rows of 4 and 8 (FCC), every neighbour in an adjacent cell (|dx|, |dy|, |dz| <= 1);
+// 0 otherwise.
+namespace gpe {
+int il_stencil_deg(const gpe_handle* h) {
+    for (const gpe_stencil_entry& e : h->lat.stencil)
+        if (e.dx < -1 || e.dx > 1 || e.dy < -1 || e.dy > 1 || e.dz < -1 || e.dz > 1) return 0;
+    if (h->tab.uniform_deg == 4) return 4;
+    if (h->tab.quad_rows && h->tab.max_deg == 8) return 8;
+    return 0;
+}
+}  // namespace gpe
+
+static int il_deg(const gpe_handle* h) { return il_stencil_deg(h); }
+
 static unsigned il_grid_blocks(const gpe_handle* h, bool obs) {
     const ILGrid G = make_il_grid(h->g);
+    const int deg = il_deg(h);
     switch (h->g.C) {
-        case 1: return il_blocks<1>(G, obs, h->partial_blocks);
-        case 3: return il_blocks<3>(G, obs, h->partial_blocks);
-        default: return il_blocks<5>(G, obs, h->partial_blocks);
+        case 1: return il_blocks<1>(G, deg, obs, h->partial_blocks);
+        case 3: return il_blocks<3>(G, deg, obs, h->partial_blocks);
+        default: return il_blocks<5>(G, deg, obs, h->partial_blocks);
     }
 }
 
-// The interleaved kernel applies: FP32, parabolic, every node 4 entries, a grid
-// with at least V / gcd(V, 8) blocks of work.
+// The interleaved kernel applies: FP32, parabolic, rows of 4 (or of 4 and 8)
+// entries with neighbours in adjacent cells.
 static bool il_applies(const gpe_handle* h) {
-    if (h->p.scheme != GPE_SCHEME_PARABOLIC || h->real_bytes != 4 || h->tab.uniform_deg != 4) return false;
+    if (h->p.scheme != GPE_SCHEME_PARABOLIC || h->real_bytes != 4 || il_deg(h) == 0) return false;
     return il_grid_blocks(h, false) > 0 && il_grid_blocks(h, true) > 0;
 }
 
@@ -1228,7 +1247,8 @@ static bool use_interleaved(const gpe_handle* h, int32_t n) {
     return il_applies(h);
 }
 
-static gpe_status ensure_il(gpe_handle* h, cudaStream_t s) {
+namespace gpe {
+gpe_status il_ensure(gpe_handle* h, cudaStream_t s) {
     const ILGrid G = make_il_grid(h->g);
     for (int k = 0; k < 2; ++k) {
         if (h->il[k]) continue;
@@ -1244,12 +1264,15 @@ static gpe_status ensure_il(gpe_handle* h, cudaStream_t s) {
     h->ilg = G;
     return GPE_OK;
 }
+}  // namespace gpe
+
+static gpe_status ensure_il(gpe_handle* h, cudaStream_t s) { return il_ensure(h, s); }
 
 static cudaError_t dispatch_il_step(const gpe_handle* h, const StepArgs& a, bool obs, cudaStream_t s) {
     switch (h->g.C) {
-        case 1: return launch_il_step<1>(a, h->ilg, h->partial_blocks, obs, h->obs_out, s);
-        case 3: return launch_il_step<3>(a, h->ilg, h->partial_blocks, obs, h->obs_out, s);
-        default: return launch_il_step<5>(a, h->ilg, h->partial_blocks, obs, h->obs_out, s);
+        case 1: return launch_il_step<1>(a, h->ilg, il_deg(h), h->partial_blocks, obs, h->obs_out, s);
+        case 3: return launch_il_step<3>(a, h->ilg, il_deg(h), h->partial_blocks, obs, h->obs_out, s);
+        default: return launch_il_step<5>(a, h->ilg, il_deg(h), h->partial_blocks, obs, h->obs_out, s);
     }
 }
 
@@ -1469,8 +1492,8 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
         if (value < 0 || value > 6) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
         if (value == 6) {
             if (!il_applies(h))
-                return fail(GPE_ERR_UNSUPPORTED, "the interleaved kernel needs FP32, the parabolic scheme, 4 entries per node "
-                                                 "and a grid of at least V / gcd(V, 8) blocks of work");
+                return fail(GPE_ERR_UNSUPPORTED, "the interleaved kernel needs FP32, the parabolic scheme, rows of 4 (or 4 and 8) entries "
+                                                 "with neighbours in adjacent cells");
             h->tune_kernel = 6;
             return GPE_OK;
         }

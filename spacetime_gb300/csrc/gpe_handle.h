@@ -115,4 +115,9 @@ gpe_status check_device_error(gpe_handle* h, cudaStream_t s);
 cudaError_t launch_pack_any(int precision, double* packed, char* dev_base, uint32_t X, uint32_t Y, uint32_t Z,
                             uint32_t vals, size_t pitch, size_t slice, bool to_device, cudaStream_t s);
 void adjoint_release(gpe_handle* h);
+// The interleaved layout (gpe_il.cuh): the longest row the interleaved step takes
+// on this handle's lattice (4, or 8 for rows of 4 and 8), 0 if it does not apply;
+// and the handle's two interleaved psi copies, allocated (zeroed) on first use.
+int il_stencil_deg(const gpe_handle* h);
+gpe_status il_ensure(gpe_handle* h, cudaStream_t s);
 }  // namespace gpe

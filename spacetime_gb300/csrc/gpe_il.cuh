@@ -9,7 +9,7 @@
 // is the same in every cell, so node l's k-th neighbour in those cells is node l'
 // of 32 consecutive cells shifted by (dx, dy, dz): with the layout of ILGrid
 // (gpe_internal.h) every load and store of the step -- own record, old next
-// record, the four neighbours, the update -- is one contiguous 256-byte run per
+// record, the neighbours, the update -- is one contiguous 256-byte run per
 // component, a single line pair per request.
 //
 // The handle's slots stay in the handle's layout; a multi-step call converts the
@@ -24,9 +24,9 @@ __host__ __device__ inline size_t il_row(const ILGrid& G, uint32_t y, uint32_t z
     return ((size_t)(z + 1) * (G.Y + 2) + (y + 1)) * G.row;
 }
 
-// Handle layout <-> interleaved layout of the interior cells, one tile of 32
-// cells x JT complex values (j = l C + s) per pass, staged in shared memory
-// (32 x (JT + 1) float2, the padding against bank conflicts) so that both sides
+// Handle layout <-> interleaved layout of the interior cells, one tile of a
+// group's cells x JT complex values (j = l C + s) per pass, staged in shared
+// memory (cells x (JT + 1) float2, the padding against bank conflicts) so that both sides
 // are read and written in contiguous 16-byte runs.  aos: the slot's interior
 // pointer.  J = V C and JT are even (every lattice with 4 entries per node has an
 // even node count), so a cell's values and the tiles start on 16-byte boundaries.
@@ -34,13 +34,14 @@ __host__ __device__ inline size_t il_row(const ILGrid& G, uint32_t y, uint32_t z
 // before it stores any of them.  The interleaved halo rows and padding cells are
 // not touched.
 constexpr uint32_t kIlConvThreads = 256;
-constexpr uint32_t kIlConvLoads = 8;  // 32 cells x 128 values / 2 per load / 256 threads
+constexpr uint32_t kIlConvLoads = 32 * 128 / 2 / kIlConvThreads;  // at most 32 cells x 128 values / 2 per load / threads
 template <bool TO_IL>
 __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos, Grid g, char* il, ILGrid G, uint32_t JT,
                                                                     uint32_t jtiles, uint32_t tiles, FastDiv djt,
                                                                     FastDiv dgx, FastDiv dy) {
-    extern __shared__ float2 il_tile[];  // 32 x (JT + 1)
+    extern __shared__ float2 il_tile[];  // cells x (JT + 1)
     const uint32_t J = G.V * G.C;
+    const uint32_t cells = G.cells, hc = cells / 2;
     const uint32_t ld = JT + 1;
     for (uint32_t w = blockIdx.x; w < tiles; w += gridDim.x) {
         const uint32_t r1 = fdiv(w, djt);
@@ -51,10 +52,10 @@ __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos
         const uint32_t y = r2 - z * G.Y;
         const uint32_t j0 = jt * JT;
         const uint32_t nj = min(JT, J - j0);   // even
-        const uint32_t nc = min(kIlCells, G.X - gx * kIlCells);
+        const uint32_t nc = min(cells, G.X - gx * cells);
         const uint32_t half = nj / 2;          // 16-byte runs per cell of the tile
-        char* arow = aos + (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)gx * kIlCells * g.cell_bytes + (size_t)j0 * 8;
-        char* irow = il + il_row(G, y, z) + (size_t)gx * G.gb + (size_t)j0 * kIlCells * 8;
+        char* arow = aos + (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)gx * cells * g.cell_bytes + (size_t)j0 * 8;
+        char* irow = il + il_row(G, y, z) + (size_t)gx * G.gb + (size_t)j0 * cells * 8;
         float4 buf[kIlConvLoads];
         if (TO_IL) {
             // cell-major 16-byte runs of the handle's layout
@@ -81,10 +82,10 @@ __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos
 #pragma unroll
             for (uint32_t k = 0; k < kIlConvLoads; ++k) {
                 const uint32_t i = threadIdx.x + k * kIlConvThreads;
-                const uint32_t jj = i / (kIlCells / 2), c = 2 * (i % (kIlCells / 2));
+                const uint32_t jj = i / hc, c = 2 * (i % hc);
                 if (jj < nj && c < nc) {
                     const float2 a = il_tile[c * ld + jj];
-                    char* dst = irow + ((size_t)jj * kIlCells + c) * 8;
+                    char* dst = irow + ((size_t)jj * cells + c) * 8;
                     if (c + 1 < nc) {
                         const float2 b = il_tile[(c + 1) * ld + jj];
                         *reinterpret_cast<float4*>(dst) = make_float4(a.x, a.y, b.x, b.y);
@@ -97,13 +98,13 @@ __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos
 #pragma unroll
             for (uint32_t k = 0; k < kIlConvLoads; ++k) {
                 const uint32_t i = threadIdx.x + k * kIlConvThreads;
-                const uint32_t jj = i / (kIlCells / 2), c = 2 * (i % (kIlCells / 2));
-                if (jj < nj && c < nc) buf[k] = __ldg(reinterpret_cast<const float4*>(irow + ((size_t)jj * kIlCells + c) * 8));
+                const uint32_t jj = i / hc, c = 2 * (i % hc);
+                if (jj < nj && c < nc) buf[k] = __ldg(reinterpret_cast<const float4*>(irow + ((size_t)jj * cells + c) * 8));
             }
 #pragma unroll
             for (uint32_t k = 0; k < kIlConvLoads; ++k) {
                 const uint32_t i = threadIdx.x + k * kIlConvThreads;
-                const uint32_t jj = i / (kIlCells / 2), c = 2 * (i % (kIlCells / 2));
+                const uint32_t jj = i / hc, c = 2 * (i % hc);
                 if (jj < nj && c < nc) {
                     il_tile[c * ld + jj] = make_float2(buf[k].x, buf[k].y);
                     if (c + 1 < nc) il_tile[(c + 1) * ld + jj] = make_float2(buf[k].z, buf[k].w);
@@ -125,14 +126,126 @@ __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos
     }
 }
 
-// One FP32 leapfrog step in the interleaved layout, lattices whose nodes all have
-// 4 stencil entries (BCC, A15, C15, Z): next <- next + 2 dt (-i H prev).  Warp
-// task t = ((z Y + y) GX + gx) V + l: node l of the cells gx*32 + lane of row
-// (y, z).  The grid's warp count is a multiple of V, so a warp keeps its node, and
-// with it its 4 entries and position, in registers.  OBS: the observables of prev
-// are summed on the way (ObsAcc, as the gather kernels' observed step).
-template <int C, bool OBS>
+// Node l's stencil in the interleaved layout, for cell `sub` of a group (the
+// lane's cell in its group): neighbour k is node e.w of the cells shifted by (dx,
+// dy, dz), a fixed offset from the group base: the rows (dz, dy), the node, and
+// sub + dx within the group or (first / last cell) the last / first cell of the
+// group before / after it.  The offset is a multiple of 8, so its two low bits carry dx
+// + 1 (|dx| <= 1, checked on the host) for the halo test of cells x + dx outside
+// [0, X).  ent / wt: the node's table entries and weights; nd (4, or 4 or 8 for
+// D = 8) of them.
+template <int D, int CELLS>
+__device__ __forceinline__ void il_node_stencil(const ILGrid& G, const int4* ent, const float* wt, int nd, uint32_t sub,
+                                                int32_t* off, float* w) {
+    const uint32_t node_run = G.C * CELLS * 8;   // bytes between nodes of a group
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        off[k] = 1;
+        w[k] = 0.f;
+        if (k < nd) {
+            const int4 e = ent[k];
+            const int xl = (int)sub + e.x;                        // -1 .. CELLS
+            const int64_t gshift = xl < 0 ? -1 : (xl >= CELLS ? 1 : 0);
+            const int64_t cell = xl - gshift * (int64_t)CELLS;
+            off[k] = (int32_t)(((int64_t)e.z * (G.Y + 2) + e.y) * (int64_t)G.row + (int64_t)e.w * node_run +
+                               gshift * (int64_t)G.gb + cell * 8) |
+                     (e.x + 1);
+            w[k] = wt[k];
+        }
+    }
+}
+
+// The group a lane works on in warp task u: the q-th group of the rows row0 ..
+// (q = u 32 / CELLS + the lane's group within its warp, counted row after row),
+// as (gx, y, z); false past the last group (nq groups).
+template <int CELLS>
+__device__ __forceinline__ bool il_lane_group(const ILGrid& G, uint32_t u, uint32_t nq, uint32_t row0, FastDiv dGX,
+                                              FastDiv dY, uint32_t& gx, uint32_t& y, uint32_t& z) {
+    const uint32_t q = (32 / CELLS) * u + (threadIdx.x & 31) / CELLS;
+    if (q >= nq) return false;
+    const uint32_t r = fdiv(q, dGX);
+    gx = q - r * G.GX;
+    const uint32_t row = row0 + r;
+    z = fdiv(row, dY);
+    y = row - z * G.Y;
+    return true;
+}
+
+// One lane's node of an interleaved leapfrog step: node l of cell gx CELLS + sub
+// of row (y, z), next <- next + 2 dt (-i H prev), with the arithmetic and its order of
+// parabolic_node_t + node_finish.  F: where the step's fields come from (P if
+// null); oa: where the observables of prev go.
+template <int C, int D, int CELLS, class OA>
+__device__ __forceinline__ void il_task(const ILGrid& G, const PhysR<float>& P, const PhysR<float>* F, const char* prev,
+                                        char* next, const int32_t* off, const float* w, int nd, const float* pos,
+                                        uint32_t sub, uint32_t l, uint32_t gx, uint32_t y, uint32_t z, OA* oa) {
+    constexpr uint32_t kComp = CELLS * 8;   // bytes between a record's components
+    const uint32_t x = gx * CELLS + sub;
+    if (x >= G.X) return;
+    const size_t gbase = il_row(G, y, z) + (size_t)gx * G.gb;
+    const size_t own = gbase + (size_t)l * (G.C * kComp) + (size_t)sub * 8;
+    Cx<float> prv[C], nv[C], H[C];
+#pragma unroll
+    for (int s = 0; s < C; ++s) {
+        prv[s] = ldc<float>(prev + own + s * kComp);
+        nv[s] = ldc_rw<float>(next + own + s * kComp);
+    }
+#pragma unroll
+    for (int s = 0; s < C; ++s) H[s] = cx<float>(0.f, 0.f);
+    // DEC Laplacian, sum_f w_f (psi_nb - psi) in entry order (Spin1GpeBCC.cu:835-865),
+    // the loads of a group of 4 entries issued together; cells x + dx outside
+    // [0, X) are the zero halo
+#pragma unroll
+    for (int k0 = 0; k0 < D; k0 += 4) {
+        if (k0 >= nd) break;
+        Cx<float> v[4][C];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int32_t o = off[k0 + k];
+            const bool in = (unsigned)((int)x + (o & 3) - 1) < G.X;
+            const char* p = prev + gbase + (in ? (o & ~3) : 0);
+#pragma unroll
+            for (int s = 0; s < C; ++s) v[k][s] = in ? ldc<float>(p + s * kComp) : cx<float>(0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+#pragma unroll
+            for (int s = 0; s < C; ++s) H[s] += w[k0 + k] * (v[k][s] - prv[s]);
+        }
+    }
+    // local terms and the leapfrog update, as node_finish
+    float rr[3];
+    rr[0] = P.p0[0] + P.bs * ((float)x * P.bw[0] + pos[0]);
+    rr[1] = P.p0[1] + P.bs * ((float)y * P.bw[1] + pos[1]);
+    rr[2] = P.p0[2] + P.bs * ((float)z * P.bw[2] + pos[2]);
+    const float pot = trap<float>(P, rr, F);
+    local_terms<float, C>(P, rr, pot, GPE_MODE_LEAPFROG, false, prv, H, F);
+    if constexpr (!std::is_same<OA, NoObs>::value) oa->template node<float, C>(P, rr, prv, H);
+#pragma unroll
+    for (int s = 0; s < C; ++s) {
+        nv[s] += (2.f * P.dt) * cx<float>(H[s].y, -H[s].x);
+        stc<float>(next + own + s * kComp, nv[s]);
+    }
+}
+
+// Warp tasks per node of an interleaved step (the grid's groups counted row after
+// row, 32 / cells per warp task).
+__host__ __device__ inline uint32_t il_warp_tasks(const ILGrid& G) {
+    const uint32_t wg = 32 / G.cells;
+    return (G.Y * G.Z * G.GX + wg - 1) / wg;
+}
+
+// One FP32 leapfrog step in the interleaved layout: next <- next + 2 dt (-i H prev).
+// D = 4: every node has 4 stencil entries (BCC, A15, C15, Z); D = 8: rows of 4 or 8
+// entries (FCC's tetrahedra and octahedra).  Warp task t = u V + l: node l of the
+// u-th group (il_lane_group).  The grid's warp count is a multiple
+// of V, so a warp keeps its node, and with it its entries and position, in
+// registers; the row length is the same in every lane of a warp, so the second
+// group of 4 entries is a uniform branch.  OBS: the observables of prev are summed
+// on the way (ObsAcc, as the gather kernels' observed step).
+template <int C, int D, int CELLS, bool OBS>
 __device__ __forceinline__ void il_step_body(const StepArgs& a, const ILGrid& G, uint32_t tasks, FastDiv dGX) {
+    static_assert(D == 4 || D == 8, "rows of 4, or of 4 and 8 entries");
     __shared__ SmemTables<float> st;
     load_tables<float>(st, a);
     __syncthreads();
@@ -140,79 +253,22 @@ __device__ __forceinline__ void il_step_body(const StepArgs& a, const ILGrid& G,
     using OA = typename ObsOf<OBS, float>::type;
     __shared__ double obs_sums[OBS ? kObsSums * 256 : 1];
     OA oa = ObsOf<OBS, float>::make(obs_sums);
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t sub = threadIdx.x & (CELLS - 1);
     const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t l = warp - fdiv(warp, a.divV) * G.V;
-    constexpr uint32_t kComp = kIlCells * 8;   // bytes between a record's components
-    const uint32_t node_run = G.C * kComp;     // bytes between nodes of a group
-    // neighbour k of node l: node e.w of the cells shifted by (dx, dy, dz); for
-    // this lane the shift is a fixed offset from its own group's base: the rows
-    // (dz, dy), the node, and lane + dx within the group or (lane 0 / 31) the last
-    // / first cell of the group before / after it
-    int dx[4];
-    int32_t off[4];
-    float w[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int4 e = a.tab.ent4[l * 4 + k];
-        dx[k] = e.x;
-        const int xl = (int)lane + e.x;                       // -1 .. 32
-        const int64_t gshift = xl < 0 ? -1 : (xl >= (int)kIlCells ? 1 : 0);
-        const int64_t cell = xl - gshift * (int64_t)kIlCells;
-        off[k] = (int32_t)(((int64_t)e.z * (G.Y + 2) + e.y) * (int64_t)G.row + (int64_t)e.w * node_run +
-                           gshift * (int64_t)G.gb + cell * 8);
-        w[k] = st.w[l * 4 + k];
-    }
+    const uint32_t nq = G.Y * G.Z * G.GX;
+    const int f0 = st.row_ptr[l];
+    const int nd = D == 4 ? 4 : st.row_ptr[l + 1] - f0;   // 4 or 8, the same in the whole warp
+    int32_t off[D];
+    float w[D];
+    il_node_stencil<D, CELLS>(G, a.tab.ent4 + f0, st.w + f0, nd, sub, off, w);
     const float pos[3] = {st.pos[3 * l], st.pos[3 * l + 1], st.pos[3 * l + 2]};
-    const char* prev = a.prev;
-    char* next = a.next;
     for (uint32_t t = warp; t < tasks; t += nwarps) {
-        const uint32_t r = fdiv(t, a.divV);
-        const uint32_t row = fdiv(r, dGX);
-        const uint32_t gx = r - row * G.GX;
-        const uint32_t z = fdiv(row, a.divY);
-        const uint32_t y = row - z * G.Y;
-        const uint32_t x = gx * kIlCells + lane;
-        if (x >= G.X) continue;
-        const size_t gbase = il_row(G, y, z) + (size_t)gx * G.gb;
-        const size_t own = gbase + (size_t)l * node_run + (size_t)lane * 8;
-        Cx<float> prv[C], nv[C], H[C];
-#pragma unroll
-        for (int s = 0; s < C; ++s) {
-            prv[s] = ldc<float>(prev + own + s * kComp);
-            nv[s] = ldc_rw<float>(next + own + s * kComp);
-        }
-#pragma unroll
-        for (int s = 0; s < C; ++s) H[s] = cx<float>(0.f, 0.f);
-        // DEC Laplacian, sum_f w_f (psi_nb - psi) in entry order (Spin1GpeBCC.cu:835-865);
-        // cells x + dx outside [0, X) are the zero halo
-        Cx<float> v[4][C];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const bool in = (unsigned)((int)x + dx[k]) < G.X;
-            const char* p = prev + gbase + (in ? off[k] : 0);
-#pragma unroll
-            for (int s = 0; s < C; ++s) v[k][s] = in ? ldc<float>(p + s * kComp) : cx<float>(0.f, 0.f);
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-#pragma unroll
-            for (int s = 0; s < C; ++s) H[s] += w[k] * (v[k][s] - prv[s]);
-        }
-        // local terms and the leapfrog update, as node_finish
-        float rr[3];
-        rr[0] = P.p0[0] + P.bs * ((float)x * P.bw[0] + pos[0]);
-        rr[1] = P.p0[1] + P.bs * ((float)y * P.bw[1] + pos[1]);
-        rr[2] = P.p0[2] + P.bs * ((float)z * P.bw[2] + pos[2]);
-        const float pot = trap<float>(P, rr, nullptr);
-        local_terms<float, C>(P, rr, pot, GPE_MODE_LEAPFROG, false, prv, H, nullptr);
-        if constexpr (OBS) oa.template node<float, C>(P, rr, prv, H);
-#pragma unroll
-        for (int s = 0; s < C; ++s) {
-            nv[s] += (2.f * P.dt) * cx<float>(H[s].y, -H[s].x);
-            stc<float>(next + own + s * kComp, nv[s]);
-        }
+        const uint32_t u = fdiv(t, a.divV);
+        uint32_t gx, y, z;
+        if (il_lane_group<CELLS>(G, u, nq, 0, dGX, a.divY, gx, y, z))
+            il_task<C, D, CELLS, OA>(G, P, nullptr, a.prev, a.next, off, w, nd, pos, sub, l, gx, y, z, &oa);
     }
     if constexpr (OBS) {
         __shared__ double red[8][OBS_COUNT];
@@ -226,37 +282,47 @@ __device__ __forceinline__ void il_step_body(const StepArgs& a, const ILGrid& G,
 // shared memory per thread).
 constexpr unsigned kIlPlainThreads = 128;
 constexpr unsigned kIlObsThreads = 256;
-template <int C>
+#ifndef IL_B81
+#define IL_B81 8
+#endif
+#ifndef IL_B83
+#define IL_B83 5
+#endif
+#ifndef IL_B85
+#define IL_B85 4
+#endif
+template <int C, int D>
 struct IlBounds {
-    // spin-1 BCC 96^3: 7 blocks (72 registers) 0.131 ms per step, 8 (64) 0.147,
-    // 9 (56) 0.145; spin-2 BCC 96^3: 4 blocks (105) 0.222 ms, 5 (96) 0.211, 6 (80) 0.218
-    static constexpr int kMin = C == 5 ? 5 : (C == 3 ? 7 : 8);
-    static constexpr int kMinObs = C == 5 ? 2 : 3;
+    // D = 4: spin-1 BCC 96^3: 7 blocks (72 registers) 0.131 ms per step, 8 (64)
+    // 0.147, 9 (56) 0.145; spin-2 BCC 96^3: 4 blocks (105) 0.222 ms, 5 (96) 0.211,
+    // 6 (80) 0.218.  D = 8 keeps 12 more registers for the second group of entries.
+    static constexpr int kMin = D == 8 ? (C == 5 ? IL_B85 : (C == 3 ? IL_B83 : IL_B81)) : (C == 5 ? 5 : (C == 3 ? 7 : 8));
+    static constexpr int kMinObs = (C == 5 || (C == 3 && D == 8)) ? 2 : 3;
 };
 
-template <int C>
-__global__ void __launch_bounds__(kIlPlainThreads, IlBounds<C>::kMin) il_step_kernel(StepArgs a, ILGrid G, uint32_t tasks,
+template <int C, int D, int CELLS>
+__global__ void __launch_bounds__(kIlPlainThreads, IlBounds<C, D>::kMin) il_step_kernel(StepArgs a, ILGrid G, uint32_t tasks,
                                                                                     FastDiv dGX) {
-    il_step_body<C, false>(a, G, tasks, dGX);
+    il_step_body<C, D, CELLS, false>(a, G, tasks, dGX);
 }
-template <int C>
-__global__ void __launch_bounds__(kIlObsThreads, IlBounds<C>::kMinObs) il_step_obs_kernel(StepArgs a, ILGrid G,
+template <int C, int D, int CELLS>
+__global__ void __launch_bounds__(kIlObsThreads, IlBounds<C, D>::kMinObs) il_step_obs_kernel(StepArgs a, ILGrid G,
                                                                                         uint32_t tasks, FastDiv dGX) {
-    il_step_body<C, true>(a, G, tasks, dGX);
+    il_step_body<C, D, CELLS, true>(a, G, tasks, dGX);
 }
 
-// Blocks of one interleaved step: one wave at the kernel's occupancy, a multiple
-// of V / gcd(V, warps per block) (the grid's warp count a multiple of V), at most
-// one warp per task and at most `max_blocks` (the handle's partial-sum rows); 0 if
-// no such grid.
-template <int C>
-unsigned il_blocks(const ILGrid& G, bool obs, size_t max_blocks) {
+// Blocks of one interleaved step (rows of D entries at most): one wave at the
+// kernel's occupancy or one warp per task if that is fewer, as a multiple of m =
+// V / gcd(V, warps per block) (the grid's warp count a multiple of V), and at most
+// `max_blocks` (the handle's partial-sum rows); 0 if no such grid.
+template <int C, int D, int CELLS>
+unsigned il_blocks_d(const ILGrid& G, bool obs, size_t max_blocks) {
     static int occ[2] = {0, 0};
     const unsigned threads = obs ? kIlObsThreads : kIlPlainThreads;
     const unsigned wpb = threads / 32;
     int& o = occ[obs ? 1 : 0];
     if (o == 0) {
-        auto k = obs ? il_step_obs_kernel<C> : il_step_kernel<C>;
+        auto k = obs ? il_step_obs_kernel<C, D, CELLS> : il_step_kernel<C, D, CELLS>;
         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, obs ? 50 : 25);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, (int)threads, 0);
         if (o < 1) o = 1;
@@ -268,32 +334,56 @@ unsigned il_blocks(const ILGrid& G, bool obs, size_t max_blocks) {
         gb = r;
     }
     const uint64_t m = G.V / gv;
-    const uint64_t tasks = (uint64_t)G.Y * G.Z * G.GX * G.V;
+    const uint64_t tasks = (uint64_t)il_warp_tasks(G) * G.V;
     uint64_t nb = std::min<uint64_t>((uint64_t)o * (unsigned)device_sm_count(), (tasks + wpb - 1) / wpb);
-    nb = std::min<uint64_t>(nb, max_blocks);
-    return (unsigned)(nb / m * m);
+    // rounded down (a block past the wave would start only when another ends);
+    // grids of fewer tasks than m blocks' warps take m blocks, some warps idle
+    nb = nb >= m ? nb / m * m : m;
+    if (nb > max_blocks) nb = max_blocks / m * m;
+    return (unsigned)nb;
 }
 
-// One interleaved leapfrog step (a.prev / a.next: interleaved buffers); obs: sum
-// the observables of a.prev into a.partials and finalize them into out.
 template <int C>
-cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, size_t max_blocks, bool obs, double* out, cudaStream_t s) {
-    const unsigned nb = il_blocks<C>(G, obs, max_blocks);
+unsigned il_blocks(const ILGrid& G, int deg, bool obs, size_t max_blocks) {
+    if (G.cells == 32)
+        return deg == 4 ? il_blocks_d<C, 4, 32>(G, obs, max_blocks) : il_blocks_d<C, 8, 32>(G, obs, max_blocks);
+    return deg == 4 ? il_blocks_d<C, 4, 16>(G, obs, max_blocks) : il_blocks_d<C, 8, 16>(G, obs, max_blocks);
+}
+
+// One interleaved leapfrog step (a.prev / a.next: interleaved buffers) on rows of
+// at most deg (4 or 8) entries; obs: sum the observables of a.prev into a.partials
+// and finalize them into out.
+template <int C, int D, int CELLS>
+cudaError_t launch_il_step_d(const StepArgs& a, const ILGrid& G, size_t max_blocks, bool obs, double* out, cudaStream_t s) {
+    const unsigned nb = il_blocks_d<C, D, CELLS>(G, obs, max_blocks);
     if (nb == 0) return cudaErrorInvalidConfiguration;
-    const uint32_t tasks = G.Y * G.Z * G.GX * G.V;
+    const uint32_t tasks = il_warp_tasks(G) * G.V;
     const FastDiv dGX = make_fastdiv(G.GX);
     if (obs) {
-        il_step_obs_kernel<C><<<nb, kIlObsThreads, 0, s>>>(a, G, tasks, dGX);
+        il_step_obs_kernel<C, D, CELLS><<<nb, kIlObsThreads, 0, s>>>(a, G, tasks, dGX);
         observe_finalize_kernel<<<1, 256, 0, s>>>(a.partials, nb, out);
     } else {
-        il_step_kernel<C><<<nb, kIlPlainThreads, 0, s>>>(a, G, tasks, dGX);
+        il_step_kernel<C, D, CELLS><<<nb, kIlPlainThreads, 0, s>>>(a, G, tasks, dGX);
     }
     return cudaGetLastError();
 }
 
-#define GPE_INSTANTIATE_IL(C)                                                                                      \
-    template cudaError_t launch_il_step<C>(const StepArgs&, const ILGrid&, size_t, bool, double*, cudaStream_t); \
-    template unsigned il_blocks<C>(const ILGrid&, bool, size_t);
+template <int C>
+cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, int deg, size_t max_blocks, bool obs, double* out,
+                           cudaStream_t s) {
+    if (G.cells == 32) {
+        if (deg == 4) return launch_il_step_d<C, 4, 32>(a, G, max_blocks, obs, out, s);
+        if (deg == 8) return launch_il_step_d<C, 8, 32>(a, G, max_blocks, obs, out, s);
+    } else if (G.cells == 16) {
+        if (deg == 4) return launch_il_step_d<C, 4, 16>(a, G, max_blocks, obs, out, s);
+        if (deg == 8) return launch_il_step_d<C, 8, 16>(a, G, max_blocks, obs, out, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+#define GPE_INSTANTIATE_IL(C)                                                                                           \
+    template cudaError_t launch_il_step<C>(const StepArgs&, const ILGrid&, int, size_t, bool, double*, cudaStream_t); \
+    template unsigned il_blocks<C>(const ILGrid&, int, bool, size_t);
 
 // Both directions of the layout change for one state buffer (interior pointer aos).
 // Defined once (GPE_DEFINE_IL_CONVERT in one translation unit).
@@ -308,7 +398,7 @@ cudaError_t launch_il_convert(char* aos, const Grid& g, char* il, const ILGrid& 
         const uint64_t tiles = (uint64_t)G.Y * G.Z * G.GX * jtiles;                                                  \
         if (tiles == 0) return cudaSuccess;                                                                          \
         if (tiles > 0xffffffffu) return cudaErrorInvalidValue;                                                       \
-        const size_t smem = (size_t)kIlCells * (JT + 1) * sizeof(float2);                                            \
+        const size_t smem = (size_t)G.cells * (JT + 1) * sizeof(float2);                                             \
         const unsigned nb = (unsigned)std::min<uint64_t>(tiles, (uint64_t)device_sm_count() * 8);                    \
         const FastDiv djt = make_fastdiv(jtiles), dgx = make_fastdiv(G.GX), dy = make_fastdiv(G.Y);                  \
         if (to_il)                                                                                                   \

@@ -83,17 +83,27 @@ struct Grid {
 
 // Geometry of an FP32 state in the cell-interleaved layout.  Rows (y, z) run from
 // -1 to Y and -1 to Z (the halo rows and planes are zero); a row holds GX groups of
-// 32 consecutive cells along x; a group holds [node l][component s][cell of the
-// group][re, im], so that node l's component s of 32 neighbouring cells is one
-// contiguous 256-byte run.  Cells x >= X of the last group, and the cells x = -1
-// and x = X, read as zero.
-constexpr uint32_t kIlCells = 32;
+// `cells` (32 or 16) consecutive cells along x; a group holds [node l][component
+// s][cell of the group][re, im], so that node l's component s of a group's cells
+// is one contiguous run of 8 cells bytes.  Cells x >= X of the last group, and the
+// cells x = -1 and x = X, read as zero.  A warp takes node l of 32 / cells groups,
+// the grid's groups counted row after row.  The group width is chosen per grid:
+// 32 where that leaves no more lanes idle than 16 would (X a multiple of 32, or
+// X mod 32 > 16), 16 otherwise.  Measured (FP32 leapfrog, fraction of the copy
+// peak, 32 / 16): spin-1 BCC 96^3 0.860 / 0.833, A15 64^3 0.857 / 0.832, Z 56^3
+// 0.774 / 0.750, C15 48^3 0.700 / 0.829; the 256-member ensemble 0.555 / 0.568.
 struct ILGrid {
     uint32_t X, Y, Z, V, C, GX;
-    size_t gb;     // bytes per group: V * C * 32 * 8
-    size_t row;    // bytes per row: GX * gb
-    size_t bytes;  // the buffer: (Y + 2) (Z + 2) rows
+    uint32_t cells; // cells per group: 32 or 16
+    size_t gb;      // bytes per group: V * C * cells * 8
+    size_t row;     // bytes per row: GX * gb
+    size_t bytes;   // the buffer: (Y + 2) (Z + 2) rows
 };
+
+inline uint32_t il_group_cells(uint32_t X) {
+    const uint32_t g32 = (X + 31) / 32, g16 = (X + 15) / 16;
+    return 32 * g32 <= 16 * g16 ? 32 : 16;
+}
 
 inline ILGrid make_il_grid(const Grid& g) {
     ILGrid G;
@@ -102,8 +112,9 @@ inline ILGrid make_il_grid(const Grid& g) {
     G.Z = g.Z;
     G.V = g.V;
     G.C = g.C;
-    G.GX = (g.X + kIlCells - 1) / kIlCells;
-    G.gb = (size_t)g.V * g.C * kIlCells * 8;
+    G.cells = il_group_cells(g.X);
+    G.GX = (g.X + G.cells - 1) / G.cells;
+    G.gb = (size_t)g.V * g.C * G.cells * 8;
     G.row = G.GX * G.gb;
     G.bytes = (size_t)(g.Y + 2) * (g.Z + 2) * G.row;
     return G;
@@ -159,6 +170,7 @@ struct DevTables {
     int faces;
     int uniform_deg;      // > 0 when every node has the same number of entries
     int quad_rows;        // 1 when rows differ in length and every row is a positive multiple of 4 long
+    int max_deg;          // the longest row
 };
 
 struct StepArgs {

@@ -74,7 +74,11 @@ def test_batch_step_matches_members(gpu, prec, per_launch):
             b.set_tuning(capi.BATCH_STEPS_PER_LAUNCH, per_launch)
             b.step(11)
             n0 = b.launches
-            assert n0 == (1 if per_launch == 0 else 4)
+            # FP32 spin-1 members are stepped in the interleaved layout: 4 layout
+            # changes each per call
+            n_il = sum(1 for sp in SPECS if sp[1] == 3) if prec == capi.FP32 else 0
+            assert b.get_tuning(capi.BATCH_LAYOUT) == 1
+            assert n0 == (1 if per_launch == 0 else 4) + 4 * n_il
         for r in ref:
             r.step(11)
         _compare(mem, ref, prec)
@@ -102,6 +106,36 @@ def test_batch_graph_replay(gpu):
         _compare(mem, ref, prec)
     finally:
         _close(mem + ref)
+
+
+def test_batch_layouts_agree(gpu):
+    """FP32 spin-1 members stepped in the interleaved layout (GPE_BATCH_LAYOUT 1,
+    FCC's rows of 4 and 8 and groups of 16 and 32 cells included) leave every
+    member's two psi slots bit for bit as the handle layout (0) does, directly and
+    through a captured graph."""
+    specs = [("bcc", 3, (40, 3, 2)), ("fcc", 3, (35, 2, 3)), ("fcc", 3, (64, 2, 2)), ("a15", 3, (3, 2, 2)),
+             ("c15", 3, (2, 2, 3)), ("bcc", 1, (5, 6, 7)), ("fcc", 5, (6, 3, 2)), ("bcc", 3, (50, 2, 2))]
+    outs = []
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    for layout in (0, 1):
+        mem = [_member(spec, capi.FP32, i) for i, spec in enumerate(specs)]
+        try:
+            with Batch(mem) as b:
+                b.stream = sp
+                b.set_tuning(capi.BATCH_LAYOUT, layout)
+                assert b.get_tuning(capi.BATCH_LAYOUT) == layout
+                b.set_tuning(capi.BATCH_ITEM_NODES, 300)
+                b.step(6)
+                b.capture(5, sp)
+                b.replay()
+            outs.append([(m.current, m.download(capi.PSI_EVEN), m.download(capi.PSI_ODD)) for m in mem])
+        finally:
+            _close(mem)
+    for (ca, ea, oa), (cb, eb, ob) in zip(*outs):
+        assert ca == cb
+        np.testing.assert_array_equal(ea, eb)
+        np.testing.assert_array_equal(oa, ob)
 
 
 def test_batch_autotune_keeps_state(gpu):
@@ -204,13 +238,14 @@ def test_batch_constant_slots_exhausted(gpu):
 @pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
 def test_batch_matches_oracle(gpu, prec):
     """A mixed batch (BCC spin-1, FCC scalar with the trap switched off mid-run,
-    C15 scalar, A15 spin-1), every member against the FP64 CPU oracle's own time
+    C15 scalar, A15 spin-1, FCC spin-1), every member against the FP64 CPU oracle's own time
     loop: forwardEuler at t0, then leapfrog steps with the member's ramp evaluated
     at t0 + (k+1) dt (Spin1GpeBCC.cu:1428-1603).  FP64 <= 1e-12 and FP32 <= 2e-5 of
     max|psi|, the parity tolerances of the single-condensate kernels."""
     from oracle import oracle
 
-    specs = [("bcc", 3, (7, 5, 4)), ("fcc", 1, (6, 5, 4)), ("c15", 1, (3, 2, 3)), ("a15", 3, (3, 4, 3))]
+    specs = [("bcc", 3, (7, 5, 4)), ("fcc", 1, (6, 5, 4)), ("c15", 1, (3, 2, 3)), ("a15", 3, (3, 4, 3)),
+             ("fcc", 3, (5, 3, 2))]
     n = 9
     members, init = [], []
     for i, sp in enumerate(specs):

@@ -37,7 +37,8 @@ def _state(lat, p, seed, amp=0.2):
 # (lattice, C, dims): X a multiple of 32, ragged (padding cells), and below 32
 CASES = [("bcc", 3, (64, 3, 2)), ("bcc", 3, (40, 5, 3)), ("bcc", 1, (37, 4, 3)), ("bcc", 5, (33, 3, 2)),
          ("bcc", 3, (9, 4, 5)), ("a15", 3, (35, 2, 2)), ("a15", 1, (6, 3, 2)), ("c15", 1, (33, 2, 2)),
-         ("c15", 5, (5, 2, 2)), ("z", 3, (34, 2, 2))]
+         ("c15", 5, (5, 2, 2)), ("z", 3, (34, 2, 2)), ("fcc", 3, (40, 3, 2)), ("fcc", 1, (33, 2, 3)),
+         ("fcc", 5, (7, 3, 2)), ("fcc", 3, (64, 2, 2))]
 
 
 @pytest.mark.parametrize("name,C,dims", CASES)
@@ -66,7 +67,8 @@ def test_interleaved_equals_gather(gpu, name, C, dims):
             np.testing.assert_array_equal(a.download(slot), b.download(slot), err_msg="slot %d" % slot)
 
 
-@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (40, 3, 2)), ("a15", 1, (34, 2, 2)), ("bcc", 5, (9, 3, 2))])
+@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (40, 3, 2)), ("a15", 1, (34, 2, 2)), ("bcc", 5, (9, 3, 2)),
+                                         ("fcc", 3, (35, 2, 2))])
 def test_interleaved_against_oracle(gpu, name, C, dims):
     """Three steps from two random states against the FP64 oracle's leapfrog
     (FP32 tolerance 2e-5 of the state's scale), through gpe_step with the
@@ -115,7 +117,8 @@ def test_automatic_choice_by_call_length(gpu):
         np.testing.assert_array_equal(a.download(a.current), b.download(b.current))
 
 
-@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (40, 5, 3)), ("c15", 1, (33, 2, 2)), ("bcc", 5, (34, 3, 2))])
+@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (40, 5, 3)), ("c15", 1, (33, 2, 2)), ("bcc", 5, (34, 3, 2)),
+                                         ("fcc", 3, (34, 3, 2))])
 def test_interleaved_step_observe(gpu, name, C, dims):
     """gpe_step_observe(20) in the interleaved layout: the states of the gather
     kernel's plain steps to rounding (the observed step is another kernel, whose
@@ -156,10 +159,13 @@ def test_interleaved_step_observe(gpu, name, C, dims):
 
 
 @pytest.mark.parametrize("name,C,want", [("bcc", 3, 1), ("a15", 3, 1), ("bcc", 5, 1), ("z", 5, 1), ("bcc", 1, 0),
-                                         ("z", 3, 1), ("c15", 3, 1), ("c15", 5, 1), ("c15", 1, 0), ("a15", 1, 0)])
+                                         ("z", 3, 1), ("c15", 3, 1), ("c15", 5, 1), ("c15", 1, 0), ("a15", 1, 0),
+                                         ("fcc", 3, 1), ("fcc", 5, 1), ("fcc", 1, 0)])
 def test_automatic_choice_by_lattice(gpu, name, C, want):
     """The automatic choice takes the interleaved kernel for long calls on spinor
-    handles (where it measured faster) and keeps the gather kernel for scalars."""
+    handles (where it measured faster) and keeps the gather kernel for scalars;
+    forced, it applies to scalars too, on every lattice with rows of 4 (or of 4 and
+    8) entries."""
     lat = capi.Lattice(name)
     p = _params(lat, C, (33, 2, 2) if lat.nodes > 40 else (40, 3, 2))
     with Stepper(lat, p) as s:
@@ -168,16 +174,15 @@ def test_automatic_choice_by_lattice(gpu, name, C, want):
         s.start()
         s.step(16)
         assert s.step_timing()["interleaved_calls"] == want
-        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)   # applies everywhere on 4-entry lattices
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)
         s.step(1)
         assert s.step_timing()["interleaved_calls"] == 1
 
 
 def test_interleaved_rejected_where_it_does_not_apply(gpu):
-    """FP64, FCC's rows of 4 and 8, the cube's 6 and the hyperbolic scheme: no
+    """FP64, the cube's rows of 6 entries and the hyperbolic scheme: no
     interleaved kernel; the automatic choice stays the gather kernel there."""
-    cases = [("bcc", dict(precision=capi.FP64)), ("fcc", {}), ("cube", {}),
-             ("bcc", dict(scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01))]
+    cases = [("bcc", dict(precision=capi.FP64)), ("cube", {}), ("bcc", dict(scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01))]
     for name, kw in cases:
         lat = capi.Lattice(name)
         with Stepper(lat, _params(lat, 3, (40, 3, 2), **kw)) as s:
