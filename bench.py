@@ -157,7 +157,7 @@ def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
     if w["scheme"] == 0 and gather:
         name = "parabolic_fixed_kernel<float,%d,LEAPFROG,4>" % w["C"]
     if interleaved:
-        name = "il_step_kernel<%d,%d>" % (w["C"], 8 if w["lattice"] == "fcc" else 4)
+        name = "il_step_kernel<%d,%d,%d>" % (w["C"], 8 if w["lattice"] == "fcc" else 4, il_group_cells(p.dims[0]))
     return {"metric": "lattice-site-updates/s", "value": sites * inner * steps / (total_ms * 1e-3),
             "unit": "lattice-site-updates/s", "steps": steps, "inner_steps_per_step": inner, "sites": sites,
             "ms_per_step": total_ms / steps, "dims": list(p.dims),
@@ -167,6 +167,12 @@ def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
             "gpu_launches": launches, "clocks": clk.summary(),
             "energy_rel_drift": abs(obs[-1]["energy"] - e0["energy"]) / abs(e0["energy"]) if obs else None,
             "norm_last": obs[-1]["norm"] if obs else None}
+
+
+def il_group_cells(x):
+    """Cells per group of the interleaved layout for an x edge (the library's rule:
+    32 unless 16 leaves fewer lanes idle)."""
+    return 32 if 32 * ((x + 31) // 32) <= 16 * ((x + 15) // 16) else 16
 
 
 def leg_e2e(w, steps, inner, dims=None):
@@ -1057,7 +1063,7 @@ def run_gpu(args):
 
     kernel_name = {capi.KERNEL_TILE: "leapfrog_tile_kernel<float,3>", capi.KERNEL_GATHER: "parabolic_fixed_kernel<float,3,LEAPFROG,4>",
                    capi.KERNEL_MARCH: "leapfrog_march_kernel<float,3>", capi.KERNEL_ROWS: "leapfrog_rows_kernel<float,3>",
-                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>", capi.KERNEL_INTERLEAVED: "il_step_kernel<3,4>"}
+                   capi.KERNEL_SLAB: "parabolic_slab_kernel<float,3,4>", capi.KERNEL_INTERLEAVED: "il_step_kernel<3,4,32>"}
     if args.kernel:
         s.set_tuning(capi.TUNE_KERNEL, args.kernel)
     for key, val in ((capi.TUNE_TILE_CELLS, args.tile), (capi.TUNE_TILE_ROWS, args.rows), (capi.TUNE_ZCHUNK, args.zchunk),
