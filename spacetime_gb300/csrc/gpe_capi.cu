@@ -57,6 +57,8 @@ cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, int deg, size_t m
 template <int C>
 unsigned il_blocks(const ILGrid& G, int deg, bool obs, size_t max_blocks);
 cudaError_t launch_il_convert(char* aos, const Grid& g, char* il, const ILGrid& G, bool to_il, cudaStream_t s);
+template <int C>
+cudaError_t launch_il_hyper(const StepArgs& a, const ILGrid& G, const ILGrid& Gq, const int32_t* tab, cudaStream_t s);
 enum HyperKind {
     HK_FUSED_LEAPFROG = 0,
     HK_PSI_PARA_LEAPFROG,
@@ -207,6 +209,9 @@ static void release(gpe_handle* h) {
     if (h->blk) cudaFree(h->blk);
     for (char* b : h->il)
         if (b) cudaFree(b);
+    for (char* b : h->ilq)
+        if (b) cudaFree(b);
+    if (h->il_htab) cudaFree(h->il_htab);
     if (h->tev_ok)
         for (cudaEvent_t ev : h->tev) cudaEventDestroy(ev);
     adjoint_release(h);
@@ -1241,8 +1246,45 @@ static bool il_applies(const gpe_handle* h) {
 // an 8-byte record already loads as one coalesced run in the handle's layout).
 static bool il_auto(const gpe_handle* h) { return h->g.C >= 3; }
 
+// The q slots' geometry as a Grid whose "nodes" are the E edges of a cell.
+static Grid q_grid(const gpe_handle* h) {
+    Grid q = h->g;
+    q.V = h->g.E;
+    q.slice = h->g.qslice;
+    q.pitch = h->g.qpitch;
+    q.cell_bytes = h->g.qcell_bytes;
+    return q;
+}
+
+// The interleaved hyperbolic step applies: FP32, the hyperbolic scheme, 4 edges
+// per node, an even number of complex values per psi and q cell, and every edge
+// and incidence within adjacent cells.
+static bool il_hyper_applies(const gpe_handle* h) {
+    const Grid& g = h->g;
+    if (h->p.scheme != GPE_SCHEME_HYPERBOLIC || h->real_bytes != 4 || h->lat.F != 4 || g.E == 0) return false;
+    if ((g.V * g.C) % 2 || (g.E * g.C) % 2) return false;
+    if (g.cell_bytes != g.V * g.C * 8 || g.qcell_bytes != g.E * g.C * 8) return false;
+    auto adj = [](int dx, int dy, int dz) { return dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1; };
+    for (const gpe_edge& e : h->lat.edges)
+        if (!adj(e.dx, e.dy, e.dz)) return false;
+    for (const gpe_incidence& r : h->lat.incidence)
+        if (!adj(r.dx, r.dy, r.dz)) return false;
+    return true;
+}
+
+// Where the automatic choice takes the interleaved hyperbolic step, by measurement
+// (FP32, one fused launch, fraction of the measured copy peak, gather / row tile /
+// interleaved): spin-1 BCC 96^3 0.56 / 0.73 / 0.91, C15 40^3 0.57 / 0.52 / 0.75;
+// not for spin-2 (BCC 96^3 0.77 / 0.68 / 0.69, C15 128^3 0.68 / 0.68 / 0.54) nor
+// scalars (BCC 128^3 0.64 / 0.45 / 0.62).
+static bool il_hyper_auto(const gpe_handle* h) { return h->g.C == 3; }
+
 static bool use_interleaved(const gpe_handle* h, int32_t n) {
     if (n < 1 || (h->tune_kernel != 0 && h->tune_kernel != 6)) return false;
+    if (h->p.scheme == GPE_SCHEME_HYPERBOLIC) {
+        if (h->tune_kernel == 0 && (n < kIlMinSteps || !il_hyper_auto(h))) return false;
+        return il_hyper_applies(h);
+    }
     if (h->tune_kernel == 0 && (n < kIlMinSteps || !il_auto(h))) return false;
     return il_applies(h);
 }
@@ -1268,6 +1310,78 @@ gpe_status il_ensure(gpe_handle* h, cudaStream_t s) {
 
 static gpe_status ensure_il(gpe_handle* h, cudaStream_t s) { return il_ensure(h, s); }
 
+// Hyperbolic handles: the interleaved q copies (zeroed) and the offset tables of
+// il_hyper_kernel, on first use: V*4 incidences (edge `edge` of the cell at (dx, dy,
+// dz)) relative to a q group's base, E to-nodes (node `to` of the cell at (dx, dy,
+// dz)) relative to a psi group's base -- each for the group's first cell, with dx +
+// 1 in the two low bits -- and E from-nodes.
+static gpe_status ensure_il_hyper(gpe_handle* h, cudaStream_t s) {
+    gpe_status st = ensure_il(h, s);
+    if (st) return st;
+    const ILGrid G = h->ilg;
+    const ILGrid Gq = make_il_grid(q_grid(h));
+    for (int k = 0; k < 2; ++k) {
+        if (h->ilq[k]) continue;
+        void* p = nullptr;
+        if (cudaMalloc(&p, Gq.bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(GPE_ERR_OOM, "cudaMalloc (interleaved q)");
+        }
+        h->ilq[k] = static_cast<char*>(p);
+        CUDA_TRY(cudaMemsetAsync(p, 0, Gq.bytes, s));
+    }
+    h->ilgq = Gq;
+    if (h->il_htab) return GPE_OK;
+    const int64_t run = (int64_t)h->g.C * G.cells * 8;   // bytes between nodes (edges) of a group
+    std::vector<int32_t> tab;
+    auto put = [&](int64_t b, int dx) {
+        if (b > INT32_MAX - 3 || b < INT32_MIN) return false;
+        tab.push_back((int32_t)b | (dx + 1));
+        return true;
+    };
+    for (const gpe_incidence& r : h->lat.incidence)
+        if (!put(((int64_t)r.dz * (Gq.Y + 2) + r.dy) * (int64_t)Gq.row + (int64_t)r.edge * run + (int64_t)r.dx * 8, r.dx))
+            return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit interleaved offsets");
+    for (const gpe_edge& e : h->lat.edges)
+        if (!put(((int64_t)e.dz * (G.Y + 2) + e.dy) * (int64_t)G.row + (int64_t)e.to * run + (int64_t)e.dx * 8, e.dx))
+            return fail(GPE_ERR_INVALID_ARG, "grid too large for 32-bit interleaved offsets");
+    for (const gpe_edge& e : h->lat.edges) tab.push_back((int32_t)(e.from * run));
+    void* p = nullptr;
+    if (cudaMalloc(&p, tab.size() * sizeof(int32_t)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GPE_ERR_OOM, "cudaMalloc (interleaved hyperbolic tables)");
+    }
+    h->il_htab = static_cast<int32_t*>(p);
+    CUDA_TRY(cudaMemcpy(p, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    return GPE_OK;
+}
+
+static cudaError_t dispatch_il_hyper(const gpe_handle* h, const StepArgs& a, cudaStream_t s) {
+    switch (h->g.C) {
+        case 1: return launch_il_hyper<1>(a, h->ilg, h->ilgq, h->il_htab, s);
+        case 3: return launch_il_hyper<3>(a, h->ilg, h->ilgq, h->il_htab, s);
+        default: return launch_il_hyper<5>(a, h->ilg, h->ilgq, h->il_htab, s);
+    }
+}
+
+// The layout change of the interleaved slots of a call: psi, and q on hyperbolic
+// handles (4 or 8 launches).
+static gpe_status il_convert_all(gpe_handle* h, bool to_il, cudaStream_t s) {
+    for (int k = GPE_PSI_EVEN; k <= GPE_PSI_ODD; ++k) {
+        cudaError_t e = launch_il_convert(h->interior[k], h->g, h->il[k], h->ilg, to_il, s);
+        if (e != cudaSuccess) return cuda_fail(e, to_il ? "layout change (in)" : "layout change (out)");
+    }
+    h->launches += 2;
+    if (h->p.scheme != GPE_SCHEME_HYPERBOLIC) return GPE_OK;
+    const Grid gq = q_grid(h);
+    for (int k = 0; k < 2; ++k) {
+        cudaError_t e = launch_il_convert(h->interior[GPE_Q_EVEN + k], gq, h->ilq[k], h->ilgq, to_il, s);
+        if (e != cudaSuccess) return cuda_fail(e, to_il ? "layout change (in)" : "layout change (out)");
+    }
+    h->launches += 2;
+    return GPE_OK;
+}
+
 static cudaError_t dispatch_il_step(const gpe_handle* h, const StepArgs& a, bool obs, cudaStream_t s) {
     switch (h->g.C) {
         case 1: return launch_il_step<1>(a, h->ilg, il_deg(h), h->partial_blocks, obs, h->obs_out, s);
@@ -1282,15 +1396,13 @@ static gpe_status fill_observables(const gpe_handle* h, const double* r, gpe_obs
 // the steps (the observables of the state the last one reads summed inside it when
 // out is given), both slots changed back.
 static gpe_status il_steps(gpe_handle* h, int32_t n, gpe_observables* out, cudaStream_t s) {
-    gpe_status st = ensure_il(h, s);
+    const bool hyper = h->p.scheme == GPE_SCHEME_HYPERBOLIC;
+    if (hyper && out) return fail(GPE_ERR_UNSUPPORTED, "hyperbolic interleaved steps sum no observables");
+    gpe_status st = hyper ? ensure_il_hyper(h, s) : ensure_il(h, s);
     if (st) return st;
     StepTimer tm(h, s);
     tm.mark(0);
-    for (int k = GPE_PSI_EVEN; k <= GPE_PSI_ODD; ++k) {
-        cudaError_t e = launch_il_convert(h->interior[k], h->g, h->il[k], h->ilg, true, s);
-        if (e != cudaSuccess) return cuda_fail(e, "layout change (in)");
-    }
-    h->launches += 2;
+    if ((st = il_convert_all(h, true, s))) return st;
     tm.mark(1);
     const int32_t plain = out ? n - 1 : n;
     for (int32_t k = 0; k < n; ++k) {
@@ -1302,7 +1414,15 @@ static gpe_status il_steps(gpe_handle* h, int32_t n, gpe_observables* out, cudaS
         StepArgs a = make_args(h, B, t);
         a.prev = h->il[prev];
         a.next = h->il[next];
-        cudaError_t e = dispatch_il_step(h, a, obs, s);
+        cudaError_t e;
+        if (hyper) {
+            // q slots follow the psi slots (GPE_Q_EVEN with GPE_PSI_EVEN)
+            a.q = h->ilq[prev == GPE_PSI_EVEN ? 0 : 1];
+            a.qnext = h->ilq[next == GPE_PSI_EVEN ? 0 : 1];
+            e = dispatch_il_hyper(h, a, s);
+        } else {
+            e = dispatch_il_step(h, a, obs, s);
+        }
         if (e != cudaSuccess) return cuda_fail(e, "interleaved step launch");
         h->launches += obs ? 2 : 1;
         h->epoch += 1;
@@ -1311,13 +1431,9 @@ static gpe_status il_steps(gpe_handle* h, int32_t n, gpe_observables* out, cudaS
     }
     if (!out) tm.mark(2);
     tm.mark(3);
-    for (int k = GPE_PSI_EVEN; k <= GPE_PSI_ODD; ++k) {
-        cudaError_t e = launch_il_convert(h->interior[k], h->g, h->il[k], h->ilg, false, s);
-        if (e != cudaSuccess) return cuda_fail(e, "layout change (out)");
-    }
-    h->launches += 2;
+    if ((st = il_convert_all(h, false, s))) return st;
     tm.mark(4);
-    tm.finish(plain, out ? 1 : 0, 4, true);
+    tm.finish(plain, out ? 1 : 0, hyper ? 8 : 4, true);
     if (!out) return GPE_OK;
     double r[OBS_COUNT];
     CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
@@ -1381,11 +1497,21 @@ extern "C" gpe_status gpe_step_observe(gpe_handle* h, int32_t n, gpe_observables
     if (!h || !out) return fail(GPE_ERR_INVALID_ARG, "null argument");
     if (n < 1) return fail(GPE_ERR_INVALID_ARG, "step count must be at least 1");
     cudaStream_t s = (cudaStream_t)stream;
-    if (use_interleaved(h, n)) return il_steps(h, n, out, s);
+    int32_t pre = n - 1;  // steps before the observed one
+    if (use_interleaved(h, n)) {
+        if (h->p.scheme != GPE_SCHEME_HYPERBOLIC) return il_steps(h, n, out, s);
+        // hyperbolic: the first n - 1 steps in the interleaved layout, the observed
+        // step below
+        if (use_interleaved(h, pre)) {
+            gpe_status ist = il_steps(h, pre, nullptr, s);
+            if (ist) return ist;
+            pre = 0;
+        }
+    }
     StepTimer tm(h, s);
     tm.mark(0);
     tm.mark(1);
-    gpe_status st = plain_steps(h, n - 1, s);
+    gpe_status st = plain_steps(h, pre, s);
     if (st) return st;
     tm.mark(2);
     const double t = h->t0 + (double)(h->nstep + 1) * h->p.dt;
@@ -1397,7 +1523,7 @@ extern "C" gpe_status gpe_step_observe(gpe_handle* h, int32_t n, gpe_observables
         st = plain_steps(h, 1, s);
         tm.mark(3);
         tm.mark(4);
-        tm.finish(n - 1, 1, 0, false);
+        tm.finish(pre, 1, 0, false);
         *out = o;
         return st ? st : (ost ? fail(ost, "state holds non-finite values") : GPE_OK);
     }
@@ -1419,7 +1545,7 @@ extern "C" gpe_status gpe_step_observe(gpe_handle* h, int32_t n, gpe_observables
     h->nstep++;
     tm.mark(3);
     tm.mark(4);
-    tm.finish(n - 1, 1, 0, false);
+    tm.finish(pre, 1, 0, false);
     double r[OBS_COUNT];
     CUDA_TRY(cudaMemcpyAsync(r, h->obs_out, sizeof r, cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
@@ -1491,9 +1617,10 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
     if (key == GPE_TUNE_KERNEL) {
         if (value < 0 || value > 6) return fail(GPE_ERR_INVALID_ARG, "kernel choice");
         if (value == 6) {
-            if (!il_applies(h))
-                return fail(GPE_ERR_UNSUPPORTED, "the interleaved kernel needs FP32, the parabolic scheme, rows of 4 (or 4 and 8) entries "
-                                                 "with neighbours in adjacent cells");
+            if (!il_applies(h) && !il_hyper_applies(h))
+                return fail(GPE_ERR_UNSUPPORTED, "the interleaved kernel needs FP32, the parabolic scheme with rows of 4 (or 4 and 8) "
+                                                 "entries or the hyperbolic scheme with 4 edges per node, and neighbours in "
+                                                 "adjacent cells");
             h->tune_kernel = 6;
             return GPE_OK;
         }
@@ -1558,9 +1685,11 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
     const MarchShape ms = march_shape(h);
     const uint32_t tr = rows_cells(h);
     if (h->p.scheme == GPE_SCHEME_HYPERBOLIC && (key == GPE_TUNE_KERNEL || key == GPE_TUNE_TILE_CELLS)) {
-        // hyperbolic handles: the fused tile kernel or the gather kernel
+        // hyperbolic handles: the interleaved kernel on request, else the fused tile
+        // kernel or the gather kernel (calls of 16 or more steps on spinor handles
+        // take the interleaved kernel by themselves)
         const uint32_t T = hyper_tile_cells(h);
-        *value = key == GPE_TUNE_KERNEL ? (T > 0 ? 2 : 1) : (int32_t)T;
+        *value = key == GPE_TUNE_KERNEL ? (h->tune_kernel == 6 ? 6 : (T > 0 ? 2 : 1)) : (int32_t)T;
         return GPE_OK;
     }
     const SlabShape ss = slab_shape(h);

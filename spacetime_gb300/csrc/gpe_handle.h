@@ -87,6 +87,11 @@ struct gpe_handle {
     // allocated on first use
     char* il[2] = {nullptr, nullptr};
     gpe::ILGrid ilg{};
+    // hyperbolic handles: interleaved copies of the q slots (index = slot - GPE_Q_EVEN)
+    // and the interleaved offset tables of the fused step (il_hyper_tables)
+    char* ilq[2] = {nullptr, nullptr};
+    gpe::ILGrid ilgq{};
+    int32_t* il_htab = nullptr;
     // device timing of gpe_step / gpe_step_observe calls (GPE_TUNE_TIMING)
     int tune_timing = 0;
     bool tev_ok = false;

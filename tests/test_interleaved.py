@@ -180,9 +180,11 @@ def test_automatic_choice_by_lattice(gpu, name, C, want):
 
 
 def test_interleaved_rejected_where_it_does_not_apply(gpu):
-    """FP64, the cube's rows of 6 entries and the hyperbolic scheme: no
-    interleaved kernel; the automatic choice stays the gather kernel there."""
-    cases = [("bcc", dict(precision=capi.FP64)), ("cube", {}), ("bcc", dict(scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01))]
+    """FP64, the cube's rows of 6 entries (parabolic) and 6 edges per node
+    (hyperbolic), the split scheme: no interleaved kernel; the automatic choice
+    stays the gather kernel there."""
+    cases = [("bcc", dict(precision=capi.FP64)), ("cube", {}), ("cube", dict(scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01)),
+             ("bcc", dict(scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01, precision=capi.FP64))]
     for name, kw in cases:
         lat = capi.Lattice(name)
         with Stepper(lat, _params(lat, 3, (40, 3, 2), **kw)) as s:
@@ -208,3 +210,99 @@ def test_explicit_kernels_keep_their_layout(gpu):
             s.set_tuning(capi.TUNE_KERNEL, k)
             s.step(20)
             assert s.step_timing()["interleaved_calls"] == 0
+
+
+# hyperbolic (psi + q): x edges giving groups of 16 (40, 33, 37, 48, 9) and of 32 cells (64, 20)
+HYPER_CASES = [("bcc", 3, (40, 3, 2)), ("bcc", 3, (64, 2, 2)), ("bcc", 5, (33, 2, 2)), ("bcc", 1, (37, 3, 2)),
+               ("c15", 5, (5, 2, 2)), ("c15", 5, (20, 1, 2)), ("c15", 3, (48, 2, 1)), ("bcc227", 3, (9, 3, 2))]
+
+
+def _hyper_pair(name, C, dims, seed):
+    lat = capi.Lattice(name)
+    p = _params(lat, C, dims, scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01)
+    return lat, p, _state(lat, p, seed)
+
+
+@pytest.mark.parametrize("name,C,dims", HYPER_CASES)
+def test_interleaved_hyperbolic_equals_gather(gpu, name, C, dims):
+    """20 fused hyperbolic steps (update_psi + update_q, RelativisticSpin2Gpe.cu:1873-1874)
+    with a ramp: the interleaved kernel leaves psi and q, both slots of each, bit
+    for bit as the gather kernel does; one call, 8 layout changes."""
+    lat, p, psi = _hyper_pair(name, C, dims, 17)
+    with Stepper(lat, p) as a, Stepper(lat, p) as b:
+        a.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_GATHER)
+        b.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)
+        assert b.get_tuning(capi.TUNE_KERNEL) == capi.KERNEL_INTERLEAVED
+        for s in (a, b):
+            s.upload(capi.PSI_ODD, psi)
+            s.set_ramp(_ramp(p.dt), 0.0)
+            s.start()
+        b.set_tuning(capi.TUNE_TIMING, 1)
+        for s in (a, b):
+            s.step(20)
+        t = b.step_timing()
+        assert t["interleaved_calls"] == 1 and t["step_launches"] == 20 and t["convert_launches"] == 8
+        assert a.current == b.current
+        for slot in (capi.PSI_EVEN, capi.PSI_ODD, capi.Q_EVEN, capi.Q_ODD):
+            np.testing.assert_array_equal(a.download(slot), b.download(slot), err_msg="slot %d" % slot)
+
+
+@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (35, 2, 2)), ("c15", 5, (3, 2, 1))])
+def test_interleaved_hyperbolic_against_oracle(gpu, name, C, dims):
+    """gpe_start then 5 interleaved hyperbolic steps against the FP64 oracle's
+    start and time loop (FP32 tolerance 2e-5 of the state's scale, psi and q)."""
+    from oracle import oracle as orc
+    lat, p, psi = _hyper_pair(name, C, dims, 23)
+    with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)
+        s.upload(capi.PSI_ODD, psi)
+        s.set_ramp(None, 0.0)
+        s.start()
+        s.step(5)
+        got_p, got_q = s.download(s.current), s.download(capi.Q_EVEN if s.current == capi.PSI_EVEN else capi.Q_ODD)
+    p64 = _params(lat, C, dims, scheme=capi.SCHEME_HYPERBOLIC, sigma=0.01, precision=capi.FP64)
+    po, pe = psi.copy(), np.zeros_like(psi)
+    qo = np.zeros(capi.buffer_shape(lat, p64, True))
+    qe = np.zeros_like(qo)
+    f0 = capi.make_fields()
+    orc.q_step(lat, p64, orc.Q_PARA, qo, qo, po)
+    orc.q_psi_step(lat, p64, f0, 0.0, orc.EULER, False, pe, po, qo)
+    orc.q_step(lat, p64, orc.Q_PARA, qe, qe, pe)
+    rp, rq = orc.hyper_run(lat, p64, pe, po, qe, qo, 5)
+    for got, want in ((got_p, rp), (got_q, rq)):
+        scale = float(np.max(np.abs(want)))
+        assert float(np.max(np.abs(got - want))) <= 2e-5 * scale
+
+
+def test_interleaved_hyperbolic_step_observe(gpu):
+    """gpe_step_observe(20) on a hyperbolic spinor handle: 19 interleaved steps, the
+    observables of the state the last step reads, then that step -- the states and
+    observables of the gather kernel's call (the same kernels' arithmetic)."""
+    lat, p, psi = _hyper_pair("bcc", 3, (40, 3, 2), 29)
+    with Stepper(lat, p) as a, Stepper(lat, p) as b:
+        a.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_GATHER)
+        for s in (a, b):
+            s.upload(capi.PSI_ODD, psi)
+            s.set_ramp(_ramp(p.dt), 0.0)
+            s.start()
+        b.set_tuning(capi.TUNE_TIMING, 1)
+        oa, ob = a.step_observe(20), b.step_observe(20)
+        assert b.step_timing()["interleaved_calls"] == 1
+        for slot in (capi.PSI_EVEN, capi.PSI_ODD, capi.Q_EVEN, capi.Q_ODD):
+            np.testing.assert_array_equal(a.download(slot), b.download(slot))
+        for k in ("norm", "energy", "h_expect"):
+            assert oa[k] == ob[k], k
+
+
+@pytest.mark.parametrize("C,want", [(3, 1), (5, 0), (1, 0)])
+def test_interleaved_hyperbolic_automatic_choice(gpu, C, want):
+    """Calls of 16 or more steps on hyperbolic spin-1 handles take the interleaved
+    kernel by themselves (where it measured faster); spin-2 and scalars keep the
+    gather kernel."""
+    lat, p, psi = _hyper_pair("bcc", C, (40, 3, 2), 31)
+    with Stepper(lat, p) as s:
+        s.set_tuning(capi.TUNE_TIMING, 1)
+        s.upload(capi.PSI_ODD, psi)
+        s.start()
+        s.step(16)
+        assert s.step_timing()["interleaved_calls"] == want
