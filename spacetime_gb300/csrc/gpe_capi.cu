@@ -1257,11 +1257,12 @@ static Grid q_grid(const gpe_handle* h) {
 }
 
 // The interleaved hyperbolic step applies: FP32, the hyperbolic scheme, 4 edges
-// per node, an even number of complex values per psi and q cell, and every edge
-// and incidence within adjacent cells.
+// per node and 2 edges per node of a cell (BCC, BCC-227, C15), an even number of
+// complex values per psi and q cell, and every edge and incidence within adjacent
+// cells.
 static bool il_hyper_applies(const gpe_handle* h) {
     const Grid& g = h->g;
-    if (h->p.scheme != GPE_SCHEME_HYPERBOLIC || h->real_bytes != 4 || h->lat.F != 4 || g.E == 0) return false;
+    if (h->p.scheme != GPE_SCHEME_HYPERBOLIC || h->real_bytes != 4 || h->lat.F != 4 || g.E != 2 * g.V) return false;
     if ((g.V * g.C) % 2 || (g.E * g.C) % 2) return false;
     if (g.cell_bytes != g.V * g.C * 8 || g.qcell_bytes != g.E * g.C * 8) return false;
     auto adj = [](int dx, int dy, int dz) { return dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1; };
@@ -1272,12 +1273,12 @@ static bool il_hyper_applies(const gpe_handle* h) {
     return true;
 }
 
-// Where the automatic choice takes the interleaved hyperbolic step, by measurement
-// (FP32, one fused launch, fraction of the measured copy peak, gather / row tile /
-// interleaved): spin-1 BCC 96^3 0.56 / 0.73 / 0.91, C15 40^3 0.57 / 0.52 / 0.75;
-// not for spin-2 (BCC 96^3 0.77 / 0.68 / 0.69, C15 128^3 0.68 / 0.68 / 0.54) nor
-// scalars (BCC 128^3 0.64 / 0.45 / 0.62).
-static bool il_hyper_auto(const gpe_handle* h) { return h->g.C == 3; }
+// Where the automatic choice takes the interleaved hyperbolic step: everywhere it
+// applies, by measurement (FP32, one fused launch, fraction of the measured copy
+// peak, gather / row tile / interleaved): scalar BCC 128^3 0.64 / 0.46 / 0.71,
+// spin-1 BCC 96^3 0.56 / 0.74 / 0.97, C15 40^3 0.57 / 0.51 / 0.80, spin-2 BCC 96^3
+// 0.77 / 0.69 / 0.99, C15 48^3 0.75 / 0.67 / 0.93, C15 128^3 0.69 / 0.69 / 0.86.
+static bool il_hyper_auto(const gpe_handle*) { return true; }
 
 static bool use_interleaved(const gpe_handle* h, int32_t n) {
     if (n < 1 || (h->tune_kernel != 0 && h->tune_kernel != 6)) return false;

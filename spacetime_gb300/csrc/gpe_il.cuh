@@ -390,68 +390,62 @@ cudaError_t launch_il_step(const StepArgs& a, const ILGrid& G, int deg, size_t m
 
 // The fused hyperbolic leapfrog step (update_psi + update_q of
 // RelativisticSpin2Gpe.cu:1873-1874, both reading the previous (psi, q)) in the
-// interleaved layout: psi in G (V nodes per cell), q in Gq (the E edges of a cell
-// in place of the nodes).  A warp keeps one item j of the V + E items of a cell for
-// the whole launch (the grid's warp count is a multiple of V + E): j < V updates
-// node j from its F = 4 incident edges (d1 q, RelativisticSpin2Gpe.cu:1051-1066),
-// j >= V edge j - V from its two nodes (d0 psi, :986-1019).  Warp task t = u (V +
-// E) + j: item j of the u-th group, so the warps that read a group's psi and q
-// lines run together.  tab: the handle's interleaved offset tables (il_hyper_tables:
-// V*4 incidences relative to the q group base, E to-nodes relative to the psi group
+// interleaved layout: psi in G (V nodes per cell), q in Gq (the E = 2V edges of a
+// cell in place of the nodes).  A warp keeps node j and edges 2j, 2j + 1 for the
+// whole launch (the grid's warp count is a multiple of V): warp task t = u V + j
+// updates node j of the u-th group from its 4 incident edges (d1 q,
+// RelativisticSpin2Gpe.cu:1051-1066), then its two edges from their nodes (d0 psi,
+// :986-1019).  Every warp does the same work, so the warps that read a group's psi
+// and q lines stay together (a warp per node or edge let the edge warps run ahead
+// of the node warps, and spin-2 then read 48 % more from DRAM than the algorithmic
+// bytes).  tab: the handle's interleaved offset tables (il_hyper_tables: V*4
+// incidences relative to the q group base, E to-nodes relative to the psi group
 // base, both with dx + 1 in the two low bits, and E from-nodes).  The arithmetic
 // and its order are hyper_step_kernel's (fused leapfrog), so the states are its
 // states bit for bit.
 template <int C, int CELLS>
 __device__ __forceinline__ void il_hyper_body(const StepArgs& a, const ILGrid& G, const ILGrid& Gq, const int32_t* tab,
-                                              uint32_t tasks, FastDiv dGX, FastDiv dItems) {
+                                              uint32_t tasks, FastDiv dGX) {
     const uint32_t V = G.V, E = Gq.V;
     const uint32_t sub = threadIdx.x & (CELLS - 1);
     const uint32_t warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-    const uint32_t j = warp - fdiv(warp, dItems) * (V + E);
+    const uint32_t j = warp - fdiv(warp, a.divV) * V;
     const PhysR<float>& P = make_phys<float>(a);
     constexpr uint32_t kComp = CELLS * 8;
     const uint32_t nq = G.Y * G.Z * G.GX;
-    const bool node = j < V;
-    // the item's offsets for this lane (cell sub + dx, stepping into the next /
-    // previous group where it leaves this one) and, for a node, its weights and
-    // position
-    int32_t off[4];
-    float w[4] = {0.f, 0.f, 0.f, 0.f};
-    float pos[3] = {0.f, 0.f, 0.f};
-    int32_t from = 0;
-    {
-        const int32_t wrap = node ? (int32_t)Gq.gb - (int32_t)kComp : (int32_t)G.gb - (int32_t)kComp;
+    // this lane's offsets (cell sub + dx, stepping into the next / previous group
+    // where it leaves this one): the node's 4 incidences in q, its edges' to-nodes
+    // in psi; the edges' from-nodes; the node's weights and position
+    auto lane_off = [&](int32_t b, int32_t wrap) {
+        const int xl = (int)sub + (b & 3) - 1;
+        const int32_t gs = xl < 0 ? -1 : (xl >= CELLS ? 1 : 0);
+        return ((b & ~3) + (int32_t)sub * 8 + gs * wrap) | (b & 3);
+    };
+    int32_t off[4], eto[2], efrom[2];
+    float w[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            off[k] = 1;
-            if (node || k == 0) {
-                const int32_t b = node ? tab[4 * j + k] : tab[4 * V + (j - V)];
-                const int xl = (int)sub + (b & 3) - 1;
-                const int32_t gs = xl < 0 ? -1 : (xl >= CELLS ? 1 : 0);
-                off[k] = ((b & ~3) + (int32_t)sub * 8 + gs * wrap) | (b & 3);
-            }
-        }
-        if (node) {
-#pragma unroll
-            for (int k = 0; k < 4; ++k) w[k] = a.tab.inc_w32[4 * j + k];
-            pos[0] = a.tab.pos32[3 * j];
-            pos[1] = a.tab.pos32[3 * j + 1];
-            pos[2] = a.tab.pos32[3 * j + 2];
-        } else {
-            from = tab[4 * V + E + (j - V)] + (int32_t)sub * 8;
-        }
+    for (int k = 0; k < 4; ++k) {
+        off[k] = lane_off(tab[4 * j + k], (int32_t)Gq.gb - (int32_t)kComp);
+        w[k] = a.tab.inc_w32[4 * j + k];
     }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        eto[r] = lane_off(tab[4 * V + 2 * j + r], (int32_t)G.gb - (int32_t)kComp);
+        efrom[r] = tab[4 * V + E + 2 * j + r] + (int32_t)sub * 8;
+    }
+    const float pos[3] = {a.tab.pos32[3 * j], a.tab.pos32[3 * j + 1], a.tab.pos32[3 * j + 2]};
     const float dts = P.dts;
     for (uint32_t t = warp; t < tasks; t += nwarps) {
-        const uint32_t u = fdiv(t, dItems);
+        const uint32_t u = fdiv(t, a.divV);
         uint32_t gx, y, z;
         if (!il_lane_group<CELLS>(G, u, nq, 0, dGX, a.divY, gx, y, z)) continue;
         const uint32_t x = gx * CELLS + sub;
         if (x >= G.X) continue;
         const size_t gbase = il_row(G, y, z) + (size_t)gx * G.gb;
         const size_t qbase = il_row(Gq, y, z) + (size_t)gx * Gq.gb;
-        if (node) {
+        {
+            // node j
             const size_t own = gbase + (size_t)j * (C * kComp) + (size_t)sub * 8;
             Cx<float> prv[C], H[C], nv[C];
 #pragma unroll
@@ -493,20 +487,22 @@ __device__ __forceinline__ void il_hyper_body(const StepArgs& a, const ILGrid& G
                 nv[s] += (2.f * P.dt) * cx<float>(H[s].y, -H[s].x);
                 stc<float>(a.next + own + s * kComp, nv[s]);
             }
-        } else {
-            const size_t own = qbase + (size_t)(j - V) * (C * kComp) + (size_t)sub * 8;
+        }
+#pragma unroll 1
+        for (int e = 0; e < 2; ++e) {
+            // edge 2j + e: q_update, hyperbolic leapfrog: next_q += i 2 (dt/sigma)(prev_q + d0 psi)
+            const size_t own = qbase + (size_t)(2 * j + e) * (C * kComp) + (size_t)sub * 8;
             Cx<float> to[C], fr[C], pq[C], v[C];
-            const int32_t o = off[0];
+            const int32_t o = eto[e];
             const bool in = (unsigned)((int)x + (o & 3) - 1) < G.X;
             const char* pt = a.prev + gbase + (in ? (o & ~3) : 0);
 #pragma unroll
             for (int s = 0; s < C; ++s) {
                 to[s] = in ? ldc<float>(pt + s * kComp) : cx<float>(0.f, 0.f);
-                fr[s] = ldc<float>(a.prev + gbase + from + s * kComp);
+                fr[s] = ldc<float>(a.prev + gbase + efrom[e] + s * kComp);
                 pq[s] = ldc<float>(a.q + own + s * kComp);
                 v[s] = ldc_rw<float>(a.qnext + own + s * kComp);
             }
-            // q_update, hyperbolic leapfrog: next_q += i 2 (dt/sigma)(prev_q + d0 psi)
 #pragma unroll
             for (int s = 0; s < C; ++s) {
                 const Cx<float> d0psi = to[s] - fr[s];
@@ -527,8 +523,8 @@ struct IlHyperBounds {
 
 template <int C, int CELLS>
 __global__ void __launch_bounds__(kIlPlainThreads, IlHyperBounds<C>::kMin)
-    il_hyper_kernel(StepArgs a, ILGrid G, ILGrid Gq, const int32_t* tab, uint32_t tasks, FastDiv dGX, FastDiv dItems) {
-    il_hyper_body<C, CELLS>(a, G, Gq, tab, tasks, dGX, dItems);
+    il_hyper_kernel(StepArgs a, ILGrid G, ILGrid Gq, const int32_t* tab, uint32_t tasks, FastDiv dGX) {
+    il_hyper_body<C, CELLS>(a, G, Gq, tab, tasks, dGX);
 }
 
 template <int C, int CELLS>
@@ -540,7 +536,7 @@ unsigned il_hyper_blocks_c(const ILGrid& G, const ILGrid& Gq) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, il_hyper_kernel<C, CELLS>, (int)kIlPlainThreads, 0);
         if (occ < 1) occ = 1;
     }
-    const uint32_t items = G.V + Gq.V;
+    const uint32_t items = G.V;
     uint32_t gv = items, gb = wpb;
     while (gb) {
         const uint32_t r = gv % gb;
@@ -558,17 +554,16 @@ unsigned il_hyper_blocks_c(const ILGrid& G, const ILGrid& Gq) {
 // a.q / a.qnext: interleaved buffers).
 template <int C>
 cudaError_t launch_il_hyper(const StepArgs& a, const ILGrid& G, const ILGrid& Gq, const int32_t* tab, cudaStream_t s) {
-    const uint32_t items = G.V + Gq.V;
-    const uint64_t tasks64 = (uint64_t)il_warp_tasks(G) * items;
-    if (tasks64 > 0xffffffffu || G.cells != Gq.cells || G.GX != Gq.GX) return cudaErrorInvalidValue;
+    const uint64_t tasks64 = (uint64_t)il_warp_tasks(G) * G.V;
+    if (tasks64 > 0xffffffffu || G.cells != Gq.cells || G.GX != Gq.GX || Gq.V != 2 * G.V) return cudaErrorInvalidValue;
     const uint32_t tasks = (uint32_t)tasks64;
-    const FastDiv dGX = make_fastdiv(G.GX), dItems = make_fastdiv(items);
+    const FastDiv dGX = make_fastdiv(G.GX);
     if (G.cells == 32) {
         const unsigned nb = il_hyper_blocks_c<C, 32>(G, Gq);
-        il_hyper_kernel<C, 32><<<nb, kIlPlainThreads, 0, s>>>(a, G, Gq, tab, tasks, dGX, dItems);
+        il_hyper_kernel<C, 32><<<nb, kIlPlainThreads, 0, s>>>(a, G, Gq, tab, tasks, dGX);
     } else {
         const unsigned nb = il_hyper_blocks_c<C, 16>(G, Gq);
-        il_hyper_kernel<C, 16><<<nb, kIlPlainThreads, 0, s>>>(a, G, Gq, tab, tasks, dGX, dItems);
+        il_hyper_kernel<C, 16><<<nb, kIlPlainThreads, 0, s>>>(a, G, Gq, tab, tasks, dGX);
     }
     return cudaGetLastError();
 }

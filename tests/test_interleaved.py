@@ -294,11 +294,10 @@ def test_interleaved_hyperbolic_step_observe(gpu):
             assert oa[k] == ob[k], k
 
 
-@pytest.mark.parametrize("C,want", [(3, 1), (5, 0), (1, 0)])
+@pytest.mark.parametrize("C,want", [(3, 1), (5, 1), (1, 1)])
 def test_interleaved_hyperbolic_automatic_choice(gpu, C, want):
-    """Calls of 16 or more steps on hyperbolic spin-1 handles take the interleaved
-    kernel by themselves (where it measured faster); spin-2 and scalars keep the
-    gather kernel."""
+    """Calls of 16 or more steps on hyperbolic handles take the interleaved kernel
+    by themselves (it measured faster for every spin)."""
     lat, p, psi = _hyper_pair("bcc", C, (40, 3, 2), 31)
     with Stepper(lat, p) as s:
         s.set_tuning(capi.TUNE_TIMING, 1)
