@@ -24,38 +24,45 @@ __host__ __device__ inline size_t il_row(const ILGrid& G, uint32_t y, uint32_t z
     return ((size_t)(z + 1) * (G.Y + 2) + (y + 1)) * G.row;
 }
 
-// Handle layout <-> interleaved layout of the interior cells, one tile of a
-// group's cells x JT complex values (j = l C + s) per pass, staged in shared
-// memory (cells x (JT + 1) float2, the padding against bank conflicts) so that both sides
-// are read and written in contiguous 16-byte runs.  aos: the slot's interior
-// pointer.  J = V C and JT are even (every lattice with 4 entries per node has an
-// even node count), so a cell's values and the tiles start on 16-byte boundaries.
-// Each thread issues all its loads of a tile (at most kIlConvLoads 16-byte loads)
-// before it stores any of them.  The interleaved halo rows and padding cells are
-// not touched.
+// Handle layout <-> interleaved layout of the interior cells, one tile of KG
+// consecutive groups' cells (TC = KG cells of a row, contiguous in the handle's
+// layout) x JT complex values (j = l C + s) per pass, staged in shared memory (TC x
+// (JT + 1) float2, the padding against bank conflicts) so that both sides are read
+// and written in contiguous 16-byte runs.  KG is as many groups as keep a thread's
+// share of a tile within kIlConvLoads 16-byte loads (for J = 36, spin-1 BCC, three
+// groups of 32 cells: one group per pass left 2 loads per thread and ran at half
+// the copy rate).  aos: the slot's interior pointer.  J = V C and JT are even (every
+// lattice with 4 entries per node has an even node count), so a cell's values and
+// the tiles start on 16-byte boundaries.  Each thread issues all its loads of a
+// tile before it stores any of them.  The interleaved halo rows and padding cells
+// are not touched.
 constexpr uint32_t kIlConvThreads = 256;
-constexpr uint32_t kIlConvLoads = 32 * 128 / 2 / kIlConvThreads;  // at most 32 cells x 128 values / 2 per load / threads
+constexpr uint32_t kIlConvLoads = 8;  // 16-byte loads per thread and tile: TC x JT <= 4096 values
 template <bool TO_IL>
 __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos, Grid g, char* il, ILGrid G, uint32_t JT,
-                                                                    uint32_t jtiles, uint32_t tiles, FastDiv djt,
-                                                                    FastDiv dgx, FastDiv dy) {
-    extern __shared__ float2 il_tile[];  // cells x (JT + 1)
+                                                                    uint32_t KG, uint32_t GXT, uint32_t jtiles,
+                                                                    uint32_t tiles, FastDiv djt, FastDiv dgx,
+                                                                    FastDiv dy) {
+    extern __shared__ float2 il_tile[];  // TC x (JT + 1)
     const uint32_t J = G.V * G.C;
-    const uint32_t cells = G.cells, hc = cells / 2;
+    const uint32_t cells = G.cells;
+    const uint32_t TC = KG * cells, htc = TC / 2;
     const uint32_t ld = JT + 1;
     for (uint32_t w = blockIdx.x; w < tiles; w += gridDim.x) {
         const uint32_t r1 = fdiv(w, djt);
         const uint32_t jt = w - r1 * jtiles;
         const uint32_t r2 = fdiv(r1, dgx);
-        const uint32_t gx = r1 - r2 * G.GX;
+        const uint32_t gxt = r1 - r2 * GXT;
         const uint32_t z = fdiv(r2, dy);
         const uint32_t y = r2 - z * G.Y;
         const uint32_t j0 = jt * JT;
         const uint32_t nj = min(JT, J - j0);   // even
-        const uint32_t nc = min(cells, G.X - gx * cells);
+        const uint32_t x0 = gxt * TC;
+        const uint32_t nc = min(TC, G.X - x0);
         const uint32_t half = nj / 2;          // 16-byte runs per cell of the tile
-        char* arow = aos + (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)gx * cells * g.cell_bytes + (size_t)j0 * 8;
-        char* irow = il + il_row(G, y, z) + (size_t)gx * G.gb + (size_t)j0 * cells * 8;
+        char* arow = aos + (size_t)z * g.slice + (size_t)y * g.pitch + (size_t)x0 * g.cell_bytes + (size_t)j0 * 8;
+        // cell c of the tile: group gxt KG + c / cells, cell c % cells of it
+        char* irow = il + il_row(G, y, z) + (size_t)gxt * KG * G.gb + (size_t)j0 * cells * 8;
         float4 buf[kIlConvLoads];
         if (TO_IL) {
             // cell-major 16-byte runs of the handle's layout
@@ -82,10 +89,11 @@ __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos
 #pragma unroll
             for (uint32_t k = 0; k < kIlConvLoads; ++k) {
                 const uint32_t i = threadIdx.x + k * kIlConvThreads;
-                const uint32_t jj = i / hc, c = 2 * (i % hc);
+                const uint32_t jj = i / htc, c = 2 * (i % htc);
                 if (jj < nj && c < nc) {
+                    const uint32_t gl = c / cells, cl = c - gl * cells;
                     const float2 a = il_tile[c * ld + jj];
-                    char* dst = irow + ((size_t)jj * cells + c) * 8;
+                    char* dst = irow + (size_t)gl * G.gb + ((size_t)jj * cells + cl) * 8;
                     if (c + 1 < nc) {
                         const float2 b = il_tile[(c + 1) * ld + jj];
                         *reinterpret_cast<float4*>(dst) = make_float4(a.x, a.y, b.x, b.y);
@@ -98,13 +106,16 @@ __global__ void __launch_bounds__(kIlConvThreads, 4) il_convert_kernel(char* aos
 #pragma unroll
             for (uint32_t k = 0; k < kIlConvLoads; ++k) {
                 const uint32_t i = threadIdx.x + k * kIlConvThreads;
-                const uint32_t jj = i / hc, c = 2 * (i % hc);
-                if (jj < nj && c < nc) buf[k] = __ldg(reinterpret_cast<const float4*>(irow + ((size_t)jj * cells + c) * 8));
+                const uint32_t jj = i / htc, c = 2 * (i % htc);
+                if (jj < nj && c < nc) {
+                    const uint32_t gl = c / cells, cl = c - gl * cells;
+                    buf[k] = __ldg(reinterpret_cast<const float4*>(irow + (size_t)gl * G.gb + ((size_t)jj * cells + cl) * 8));
+                }
             }
 #pragma unroll
             for (uint32_t k = 0; k < kIlConvLoads; ++k) {
                 const uint32_t i = threadIdx.x + k * kIlConvThreads;
-                const uint32_t jj = i / hc, c = 2 * (i % hc);
+                const uint32_t jj = i / htc, c = 2 * (i % htc);
                 if (jj < nj && c < nc) {
                     il_tile[c * ld + jj] = make_float2(buf[k].x, buf[k].y);
                     if (c + 1 < nc) il_tile[(c + 1) * ld + jj] = make_float2(buf[k].z, buf[k].w);
@@ -578,16 +589,22 @@ cudaError_t launch_il_convert(char* aos, const Grid& g, char* il, const ILGrid& 
         if (J % 2 || g.cell_bytes != J * 8) return cudaErrorInvalidValue;                                            \
         const uint32_t JT = J < 128 ? J : 128;                                                                       \
         const uint32_t jtiles = (J + JT - 1) / JT;                                                                   \
-        const uint64_t tiles = (uint64_t)G.Y * G.Z * G.GX * jtiles;                                                  \
+        /* groups per tile: TC JT <= 2 kIlConvLoads kIlConvThreads values, TC <= 1024 cells */                       \
+        uint32_t KG = std::min<uint32_t>(2 * kIlConvLoads * kIlConvThreads / (G.cells * JT), 1024 / G.cells);      \
+        KG = std::max<uint32_t>(1, std::min<uint32_t>(KG, G.GX));                                                   \
+        const uint32_t GXT = (G.GX + KG - 1) / KG;                                                                   \
+        const uint64_t tiles = (uint64_t)G.Y * G.Z * GXT * jtiles;                                                   \
         if (tiles == 0) return cudaSuccess;                                                                          \
         if (tiles > 0xffffffffu) return cudaErrorInvalidValue;                                                       \
-        const size_t smem = (size_t)G.cells * (JT + 1) * sizeof(float2);                                             \
+        const size_t smem = (size_t)KG * G.cells * (JT + 1) * sizeof(float2);                                        \
         const unsigned nb = (unsigned)std::min<uint64_t>(tiles, (uint64_t)device_sm_count() * 8);                    \
-        const FastDiv djt = make_fastdiv(jtiles), dgx = make_fastdiv(G.GX), dy = make_fastdiv(G.Y);                  \
+        const FastDiv djt = make_fastdiv(jtiles), dgx = make_fastdiv(GXT), dy = make_fastdiv(G.Y);                   \
         if (to_il)                                                                                                   \
-            il_convert_kernel<true><<<nb, kIlConvThreads, smem, s>>>(aos, g, il, G, JT, jtiles, (uint32_t)tiles, djt, dgx, dy); \
+            il_convert_kernel<true><<<nb, kIlConvThreads, smem, s>>>(aos, g, il, G, JT, KG, GXT, jtiles, (uint32_t)tiles, \
+                                                                     djt, dgx, dy);                                  \
         else                                                                                                         \
-            il_convert_kernel<false><<<nb, kIlConvThreads, smem, s>>>(aos, g, il, G, JT, jtiles, (uint32_t)tiles, djt, dgx, dy); \
+            il_convert_kernel<false><<<nb, kIlConvThreads, smem, s>>>(aos, g, il, G, JT, KG, GXT, jtiles,            \
+                                                                      (uint32_t)tiles, djt, dgx, dy);                \
         return cudaGetLastError();                                                                                   \
     }
 
