@@ -199,7 +199,11 @@ gpe_status gpe_buffer(const gpe_handle* h, int32_t slot, gpe_pitched* out, size_
  * count = number of doubles in host buffer.  These synchronise the stream.  A
  * page-locked (pinned, device-mapped) host array is read or written by the
  * conversion kernel directly over the host link; a pageable one goes through a
- * device staging buffer (allocated on first use).  The results are the same. */
+ * device staging buffer (allocated on first use).  With GPE_TUNE_TRANSFER 1 a
+ * pinned array goes through the staging buffer too: a DMA copy by a copy engine
+ * and a conversion at device-memory speed, so that the copy overlaps kernels that
+ * other streams run (the direct form's conversion kernel holds SMs for the whole
+ * transfer).  The results are the same. */
 gpe_status gpe_upload(gpe_handle* h, int32_t slot, const double* host, size_t count, void* stream);
 gpe_status gpe_download(gpe_handle* h, int32_t slot, double* host, size_t count, void* stream);
 
@@ -412,7 +416,12 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  * GPE_TUNE_TIMING: 1 = time every gpe_step / gpe_step_observe call with CUDA
  *                   events on its stream (each such call then synchronises the
  *                   stream at its end) and add the times to gpe_get_step_timing;
- *                   0 = off (default). */
+ *                   0 = off (default).
+ * GPE_TUNE_TRANSFER: path of gpe_upload / gpe_download for pinned host arrays:
+ *                   0 = the conversion kernel reads or writes the host array over
+ *                   the host link (default; the fastest for a lone stream), 1 = a
+ *                   DMA copy through the device staging buffer (overlaps other
+ *                   streams' kernels). */
 enum {
     GPE_TUNE_KERNEL = 0,
     GPE_TUNE_TILE_CELLS = 1,
@@ -421,7 +430,8 @@ enum {
     GPE_TUNE_THREADS = 4,
     GPE_TUNE_OBSERVE_ARITH = 5,
     GPE_TUNE_CARVEOUT = 6,
-    GPE_TUNE_TIMING = 7
+    GPE_TUNE_TIMING = 7,
+    GPE_TUNE_TRANSFER = 8
 };
 gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value);
 gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* value);

@@ -37,6 +37,7 @@ PSI_EVEN, PSI_ODD, Q_EVEN, Q_ODD, HPSI = 0, 1, 2, 3, 4
 MODE_LEAPFROG, MODE_EULER, MODE_ITP = 0, 1, 2
 TUNE_KERNEL, TUNE_TILE_CELLS, TUNE_TILE_ROWS, TUNE_ZCHUNK, TUNE_THREADS, TUNE_OBSERVE_ARITH, TUNE_CARVEOUT, TUNE_TIMING = (
     0, 1, 2, 3, 4, 5, 6, 7)
+TUNE_TRANSFER = 8
 FIELD_DENSITY, FIELD_SPIN, FIELD_UV_THETA, FIELD_MAX_HAMILTON, FIELD_PROJ_X, FIELD_PROJ_Y = 0, 1, 2, 3, 4, 5
 KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILE, KERNEL_MARCH, KERNEL_ROWS, KERNEL_SLAB, KERNEL_INTERLEAVED = 0, 1, 2, 3, 4, 5, 6
 BATCH_ITEM_NODES, BATCH_STEPS_PER_LAUNCH, BATCH_BLOCKS_PER_SM, BATCH_BARRIER_TIMEOUT_MS, BATCH_TEST_EXTRA_ARRIVALS = 0, 1, 2, 3, 4

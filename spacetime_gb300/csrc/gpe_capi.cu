@@ -487,9 +487,12 @@ static gpe_status transfer(gpe_handle* h, int32_t slot, double* host, size_t cou
     cudaStream_t s = (cudaStream_t)stream;
     // pinned (page-locked, device-mapped) host arrays are read or written by the
     // pack kernel itself over the host link, without the staging copy
+    // (GPE_TUNE_TRANSFER 1: a DMA copy through the staging buffer instead, which
+    // leaves the SMs to other streams' kernels while the copy runs)
     double* mapped = nullptr;
     cudaPointerAttributes attr;
-    if (cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer)
+    if (h->tune_transfer == 0 && cudaPointerGetAttributes(&attr, host) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+        attr.devicePointer)
         mapped = static_cast<double*>(attr.devicePointer);
     else
         cudaGetLastError();  // an unregistered pointer is not an error here
@@ -1647,6 +1650,11 @@ extern "C" gpe_status gpe_set_tuning(gpe_handle* h, int32_t key, int32_t value) 
         h->tune_timing = value;
         return GPE_OK;
     }
+    if (key == GPE_TUNE_TRANSFER) {
+        if (value != 0 && value != 1) return fail(GPE_ERR_INVALID_ARG, "transfer: 0 (direct) or 1 (DMA through staging)");
+        h->tune_transfer = value;
+        return GPE_OK;
+    }
     if (key == GPE_TUNE_CARVEOUT) {
         if (value < 0 || value > 100) return fail(GPE_ERR_INVALID_ARG, "carveout: 0 (driver default) or 1..100 percent");
         h->tune_carveout = value;
@@ -1700,6 +1708,10 @@ extern "C" gpe_status gpe_get_tuning(const gpe_handle* h, int32_t key, int32_t* 
     }
     if (key == GPE_TUNE_TIMING) {
         *value = h->tune_timing;
+        return GPE_OK;
+    }
+    if (key == GPE_TUNE_TRANSFER) {
+        *value = h->tune_transfer;
         return GPE_OK;
     }
     if (key == GPE_TUNE_KERNEL && h->tune_kernel == 6) {

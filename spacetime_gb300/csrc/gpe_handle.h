@@ -78,6 +78,7 @@ struct gpe_handle {
     int tune_threads = 0;  // GPE_TUNE_THREADS
     int tune_observe = 0;  // GPE_TUNE_OBSERVE_ARITH
     int tune_carveout = 0; // GPE_TUNE_CARVEOUT
+    int tune_transfer = 0; // GPE_TUNE_TRANSFER
     uint32_t nrows = 0;    // multi-row tile kernel: (dy, dz) rows the stencil uses, own row first
     int32_t rdy[9] = {0}, rdz[9] = {0};
     int32_t* blk = nullptr;   // device row-block table of the current shape

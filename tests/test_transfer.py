@@ -35,3 +35,29 @@ def test_pinned_and_pageable_transfers_agree(gpu, name, comps, prec):
     if prec == capi.FP64:
         interior = (slice(1, -1),) * 3
         assert np.array_equal(b[interior], src[interior])
+
+
+@pytest.mark.parametrize("prec", [capi.FP64, capi.FP32])
+def test_transfer_by_dma_agrees(gpu, prec):
+    """GPE_TUNE_TRANSFER 1: pinned host arrays go through the staging buffer by DMA
+    copies; the device state and the downloaded array equal the direct form's, bit
+    for bit, and the setting reads back."""
+    lat = capi.Lattice("bcc")
+    p = capi.make_params(components=3, precision=prec, dims=(6, 4, 3), block_scale=0.3, dt=1e-4, lattice=lat)
+    src = 0.3 * states.random_state(capi.buffer_shape(lat, p), seed=83)
+    pinned = torch.from_numpy(src.copy()).pin_memory()
+    got = []
+    for mode in (0, 1):
+        with Stepper(lat, p) as s:
+            s.set_tuning(capi.TUNE_TRANSFER, mode)
+            assert s.get_tuning(capi.TUNE_TRANSFER) == mode
+            s.upload(capi.PSI_ODD, pinned.numpy())
+            s.start()
+            s.step(3)
+            out = torch.zeros(src.shape, dtype=torch.float64).pin_memory()
+            s.download(s.current, out=out.numpy())
+            got.append(out.numpy().copy())
+    assert np.array_equal(got[0], got[1])
+    with Stepper(lat, p) as s:
+        with pytest.raises(capi.GpeError):
+            s.set_tuning(capi.TUNE_TRANSFER, 2)
