@@ -178,13 +178,17 @@ def il_group_cells(x):
     return 32 if 32 * ((x + 31) // 32) <= 16 * ((x + 15) // 16) else 16
 
 
-def leg_e2e(w, steps, inner, dims=None):
+def leg_e2e(w, steps, inner, dims=None, flight=1):
     """End to end through the C ABI with host buffers, every step: the FP64 host
     state (reference file layout, pinned) in, start (q from psi for the hyperbolic
     scheme), `inner` steps with the observables summed in the last one (or after it,
     on kernels without the fused form), the final FP64 state out into pinned host
-    memory."""
+    memory.  flight > 1: that many condensates in flight, one handle, stream, pinned
+    host arrays and host thread each, the copies by DMA through the staging buffer
+    (GPE_TUNE_TRANSFER 1) so that one condensate's copies run while another's kernels
+    do; the value counts the steps of all, over the wall time of all."""
     import ctypes as C
+    import threading
 
     import torch
 
@@ -192,35 +196,61 @@ def leg_e2e(w, steps, inner, dims=None):
     from spacetime_gb300.stepper import Stepper
 
     lat, p = leg_params(w, capi.FP32, dims)
-    stream = torch.cuda.Stream()
-    s = Stepper(lat, p)
-    s.stream = C.c_void_p(stream.cuda_stream)
-    with torch.cuda.stream(stream):
-        s.init_state(capi.PSI_ODD, leg_init(w))
-        psi0 = s.download(capi.PSI_ODD)
+    runs = []
+    for _ in range(flight):
+        stream = torch.cuda.Stream()
+        s = Stepper(lat, p)
+        s.stream = C.c_void_p(stream.cuda_stream)
+        if flight > 1:
+            s.set_tuning(capi.TUNE_TRANSFER, 1)
+        with torch.cuda.stream(stream):
+            s.init_state(capi.PSI_ODD, leg_init(w))
+            psi0 = s.download(capi.PSI_ODD)
         host = torch.from_numpy(psi0.ravel()).pin_memory().numpy().reshape(psi0.shape)
         out = torch.empty(psi0.size, dtype=torch.float64).pin_memory().numpy().reshape(psi0.shape)
+        runs.append({"s": s, "stream": stream, "in": host, "out": out, "obs": None, "err": None})
 
-        def one():
-            s.upload(capi.PSI_ODD, host)
-            s.start()
-            o = s.step_observe(inner)
-            s.download(s.current, out=out)
-            return o
+    def work(r, n):
+        try:
+            s = r["s"]
+            for _ in range(n):
+                s.upload(capi.PSI_ODD, r["in"])
+                s.start()
+                r["obs"] = s.step_observe(inner)
+                s.download(s.current, out=r["out"])
+        except Exception as e:  # reported in the line
+            r["err"] = "%s: %s" % (type(e).__name__, e)
 
-        one()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            o = one()
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-    sites = s.sites
-    s.close()
-    return {"value": sites * inner * steps / el, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": int(psi0.nbytes),
-            "d2h_bytes_per_step": int(psi0.nbytes) + 96, "steps": steps, "inner_steps_per_step": inner,
-            "dims": list(p.dims), "norm_last": o["norm"],
-            "path": "gpe_upload (FP64 host, pinned) + gpe_start + gpe_step_observe(%d) + gpe_download (FP64 host, pinned)" % inner}
+    def all_runs(n):
+        if flight == 1:
+            work(runs[0], n)
+            return
+        ths = [threading.Thread(target=work, args=(r, n)) for r in runs]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+
+    all_runs(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    all_runs(steps)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    sites = runs[0]["s"].sites
+    nbytes = int(runs[0]["in"].nbytes)
+    for r in runs:
+        r["s"].close()
+    res = {"value": flight * sites * inner * steps / el, "unit": "lattice-site-updates/s", "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes + 96, "steps": flight * steps, "inner_steps_per_step": inner,
+           "dims": list(p.dims), "condensates_in_flight": flight,
+           "norm_last": runs[0]["obs"]["norm"] if runs[0]["obs"] else None,
+           "path": "%d condensate(s) in flight, every step: gpe_upload (FP64 host, pinned) + gpe_start + "
+                   "gpe_step_observe(%d) + gpe_download (FP64 host, pinned)" % (flight, inner)}
+    errs = [r["err"] for r in runs if r["err"]]
+    if errs:
+        res["error"] = errs[0]
+    return res
 
 
 def run_leg(args):
@@ -837,7 +867,8 @@ def run_legs(args):
                                            "sigma = 0.00225, dt = 2e-5; 100 steps per bench step (one call: the "
                                            "layout changes in and out of the interleaved kernel's call included)",
                                "l2": "inputs larger than L2 (68.5 GB of FP32 psi + q), no flush"}
-                r["e2e"] = leg_e2e(w, steps=3, inner=100, dims=(48, 48, 48))
+                r["e2e"] = leg_e2e(w, steps=3, inner=100, dims=(48, 48, 48), flight=3)
+                r["e2e_serial"] = leg_e2e(w, steps=3, inner=100, dims=(48, 48, 48))
                 r["drift"] = leg_drift(w, None, args.c15_drift_steps, dims=(cells,) * 3)
                 r["drift"]["note"] = ("no reference program runs spin-2 on C15; the FP64 run is libgpe's FP64 hyperbolic "
                                       "stepper, pinned to the reference's RelativisticSpin2Gpe kernels on BCC by golden vectors")
