@@ -188,6 +188,57 @@ __device__ __forceinline__ void batch_rows(const MK& M, const SmemTables<R>& st,
     }
 }
 
+// Rows row0 .. row0 + rows - 1 of a scalar member whose nodes all have 4 entries,
+// two nodes per thread and pass (i and i + kBatchThreads), the loads of both issued
+// before either is computed: a scalar node's few loads leave the memory idle at the
+// batch kernel's occupancy (the single-condensate gather kernel runs scalars at 48
+// warps per SM, the batch kernel at 32).  Per node the arithmetic and its order are
+// parabolic_node_t's (D = 4) and node_finish's.
+template <typename R, typename MK>
+__device__ __forceinline__ void batch_rows_c1x2(const MK& M, const SmemTables<R>& st, const PhysR<R>& P,
+                                                const PhysR<R>* F, const char* prev, char* next, uint32_t row0,
+                                                uint32_t rows) {
+    constexpr uint32_t node_bytes = 2 * sizeof(R);
+    const uint32_t n = rows * M.row_items;
+    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 2 * kBatchThreads) {
+        uint32_t x[2], y[2], z[2], l[2];
+        bool ok[2];
+        size_t own[2];
+        Cx<R> prv[2][1], nv[2][1], v[2][4][1];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint32_t i = i0 + q * kBatchThreads;
+            ok[q] = i < n;
+            const uint32_t ii = ok[q] ? i : i0;   // a valid node either way; its results are not stored
+            const uint32_t rr = fdiv(ii, M.divRow);
+            const uint32_t within = ii - rr * M.row_items;
+            x[q] = fdiv(within, M.divV);
+            l[q] = within - x[q] * M.g.V;
+            const uint32_t row = row0 + rr;
+            z[q] = fdiv(row, M.divY);
+            y[q] = row - z[q] * M.g.Y;
+            const size_t cell_off = (size_t)z[q] * M.g.slice + (size_t)y[q] * M.g.pitch + (size_t)x[q] * M.g.cell_bytes;
+            own[q] = cell_off + l[q] * node_bytes;
+            const int4 o4 = *reinterpret_cast<const int4*>(st.nb_off + 4 * l[q]);
+            const int32_t off[4] = {o4.x, o4.y, o4.z, o4.w};
+            ld_node<R, 1, true>(prev + own[q], prv[q]);
+            ld_node<R, 1, false>(next + own[q], nv[q]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) ld_node<R, 1, true>(prev + cell_off + off[k], v[q][k]);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (!ok[q]) continue;
+            // the node's weights and position, read again from the shared tables
+            const NodeTab<R, 4> t = node_tab<R, 4>(st, l[q]);
+            Cx<R> H[1] = {cx<R>((R)0, (R)0)};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) H[0] += t.w[k] * (v[q][k][0] - prv[q][0]);
+            node_finish<R, 1, GPE_MODE_LEAPFROG>(P, t.pos, x[q], y[q], z[q], prv[q], H, nv[q], next + own[q], nullptr, F);
+        }
+    }
+}
+
 // Rows row0 .. row0 + rows - 1 of a member in the interleaved layout (FP32).
 // Warp task t = u V + l within the item: node l of the item's u-th group
 // (il_lane_group, counted row after row): the 8 warps of a block take
@@ -257,7 +308,7 @@ __device__ __forceinline__ void batch_item(const BatchMember& M, const MK& K, co
     }
     const bool d4 = M.tab.uniform_deg == 4, quad = M.tab.quad_rows != 0;
     if ((CMASK & 1) && M.C == 1) {
-        if (d4) batch_rows<R, 1, 4>(K, st, P, F, prev, next, row0, rows);
+        if (d4) batch_rows_c1x2<R>(K, st, P, F, prev, next, row0, rows);
         else if (quad) batch_rows<R, 1, 4, 4, true>(K, st, P, F, prev, next, row0, rows);
         else batch_rows<R, 1, 0>(K, st, P, F, prev, next, row0, rows);
     } else if ((CMASK & 2) && M.C == 3) {
@@ -481,11 +532,14 @@ std::vector<int32_t> il_offsets(const gpe_handle* h) {
 }
 
 // The layout member m is stepped in: the interleaved one for FP32 spin-1 members on
-// lattices with rows of 4 (or of 4 and 8) entries when GPE_BATCH_LAYOUT is 1 (the
-// default), the handle's own otherwise.  (Spin-2 members keep the handle's layout:
+// lattices of at most 64 nodes a cell with rows of 4 (or of 4 and 8) entries (BCC,
+// FCC, A15, Z) when GPE_BATCH_LAYOUT is 1 (the default), the handle's own otherwise.  (Spin-2 members keep the handle's layout:
 // their interleaved path does not fit the batch kernel's registers.)
 int member_il_deg(const gpe_batch* b, const gpe_handle* h) {
     if (!b->layout || b->precision != GPE_FP32 || h->g.C != 3) return 0;
+    // C15 (136 nodes a cell) measured faster in the handle's layout inside the batch
+    // (the ensemble's 25 C15 spin-1 members: 7.22 against 7.52 ms per step)
+    if (h->g.V > 64) return 0;
     return il_stencil_deg(h);
 }
 
