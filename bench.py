@@ -7,9 +7,10 @@ Bz 0.5 -> -0.5 over 4000 steps plus quadrupole gradient Bq = 0.2, dt = 5e-5.
 Each psi buffer is 255 MB (FP32), larger than the 129 MB L2, so no L2 flush is
 needed between iterations.
 
-One bench "step" = 100 leapfrog steps (one fused kernel each) + one observables
-pass (norm, energy, magnetisation; FP32 node terms, FP64 sums).  value = sites *
-100 * K / time.
+One bench "step" = one gpe_step_observe(100) call: 100 leapfrog steps (one fused
+kernel each, in the cell-interleaved layout the call changes the state into and
+back out of), the observables (norm, energy, magnetisation; FP32 node terms, FP64
+sums) summed inside the last one.  value = sites * 100 * K / time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
