@@ -525,8 +525,10 @@ __device__ __forceinline__ void il_hyper_body(const StepArgs& a, const ILGrid& G
     }
 }
 
-// Register caps: spin-2 at 5 blocks of 128 threads (94 registers, no spills),
-// spin-1 72 registers (7 blocks).
+// Register caps: spin-2 at 5 blocks of 128 threads (96 registers, no spills),
+// spin-1 at 6 (80 registers).  Measured against 6 blocks (80 registers) for
+// spin-2: BCC 96^3 0.98 / 1.03, C15 48^3 0.93 / 0.97, but C15 128^3 (285 M sites)
+// 0.87 / 0.73 of peak; spin-1 at 8 blocks (64 registers) within 1 %.
 template <int C>
 struct IlHyperBounds {
     static constexpr int kMin = C == 5 ? 5 : (C == 3 ? 6 : 8);
