@@ -305,3 +305,26 @@ def test_interleaved_hyperbolic_automatic_choice(gpu, C, want):
         s.start()
         s.step(16)
         assert s.step_timing()["interleaved_calls"] == want
+
+
+@pytest.mark.parametrize("name,C,dims", [("bcc", 3, (40, 3, 2)), ("fcc", 5, (9, 2, 2))])
+def test_interleaved_with_expansion_and_trap_switch(gpu, name, C, dims):
+    """Condensate expansion (the block scale growing from the 5th step on, weights h
+    / bs(t)^2 and positions bs(t)) and the trap switched off mid-call: the
+    interleaved kernel's states equal the gather kernel's bit for bit."""
+    lat = capi.Lattice(name)
+    p = _params(lat, C, dims, flags=capi.FLAG_TRAP_OFF_AFTER, trap_off_time=7.5 * 2e-4)
+    psi = _state(lat, p, 37)
+    with Stepper(lat, p) as a, Stepper(lat, p) as b:
+        a.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_GATHER)
+        b.set_tuning(capi.TUNE_KERNEL, capi.KERNEL_INTERLEAVED)
+        b.set_tuning(capi.TUNE_TIMING, 1)
+        for s in (a, b):
+            s.upload(capi.PSI_ODD, psi)
+            s.set_ramp(_ramp(p.dt), 0.0)
+            s.set_expansion(4 * p.dt, 30.0)
+            s.start()
+            s.step(20)
+        assert b.step_timing()["interleaved_calls"] == 1
+        for slot in (capi.PSI_EVEN, capi.PSI_ODD):
+            np.testing.assert_array_equal(a.download(slot), b.download(slot), err_msg="slot %d" % slot)
