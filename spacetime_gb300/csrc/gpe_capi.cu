@@ -1214,6 +1214,7 @@ constexpr int32_t kIlMinSteps = 16;
 // 0 otherwise.
 namespace gpe {
 int il_stencil_deg(const gpe_handle* h) {
+    if (!il_offsets_fit(make_il_grid(h->g))) return 0;
     for (const gpe_stencil_entry& e : h->lat.stencil)
         if (e.dx < -1 || e.dx > 1 || e.dy < -1 || e.dy > 1 || e.dz < -1 || e.dz > 1) return 0;
     if (h->tab.uniform_deg == 4) return 4;
@@ -1268,6 +1269,7 @@ static bool il_hyper_applies(const gpe_handle* h) {
     if (h->p.scheme != GPE_SCHEME_HYPERBOLIC || h->real_bytes != 4 || h->lat.F != 4 || g.E != 2 * g.V) return false;
     if ((g.V * g.C) % 2 || (g.E * g.C) % 2) return false;
     if (g.cell_bytes != g.V * g.C * 8 || g.qcell_bytes != g.E * g.C * 8) return false;
+    if (!il_offsets_fit(make_il_grid(g)) || !il_offsets_fit(make_il_grid(q_grid(h)))) return false;
     auto adj = [](int dx, int dy, int dz) { return dx >= -1 && dx <= 1 && dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1; };
     for (const gpe_edge& e : h->lat.edges)
         if (!adj(e.dx, e.dy, e.dz)) return false;

@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstddef>
+#include <climits>
 #include <cstdint>
 #include <string>
 #include <cuda_runtime.h>
@@ -103,6 +104,12 @@ struct ILGrid {
 inline uint32_t il_group_cells(uint32_t X) {
     const uint32_t g32 = (X + 31) / 32, g16 = (X + 15) / 16;
     return 32 * g32 <= 16 * g16 ? 32 : 16;
+}
+
+// The interleaved kernels keep a neighbour's offset from its group's base in 32
+// bits: a plane of rows and two groups more must stay below 2^31 bytes.
+inline bool il_offsets_fit(const ILGrid& G) {
+    return (uint64_t)(G.Y + 3) * G.row + 2 * (uint64_t)G.gb < (uint64_t)INT32_MAX;
 }
 
 inline ILGrid make_il_grid(const Grid& g) {
