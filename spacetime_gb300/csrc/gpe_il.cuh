@@ -257,9 +257,6 @@ __host__ __device__ inline uint32_t il_warp_tasks(const ILGrid& G) {
 template <int C, int D, int CELLS, bool OBS>
 __device__ __forceinline__ void il_step_body(const StepArgs& a, const ILGrid& G, uint32_t tasks, FastDiv dGX) {
     static_assert(D == 4 || D == 8, "rows of 4, or of 4 and 8 entries");
-    __shared__ SmemTables<float> st;
-    load_tables<float>(st, a);
-    __syncthreads();
     const PhysR<float>& P = make_phys<float>(a);
     using OA = typename ObsOf<OBS, float>::type;
     __shared__ double obs_sums[OBS ? kObsSums * 256 : 1];
@@ -269,12 +266,18 @@ __device__ __forceinline__ void il_step_body(const StepArgs& a, const ILGrid& G,
     const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
     const uint32_t l = warp - fdiv(warp, a.divV) * G.V;
     const uint32_t nq = G.Y * G.Z * G.GX;
-    const int f0 = st.row_ptr[l];
-    const int nd = D == 4 ? 4 : st.row_ptr[l + 1] - f0;   // 4 or 8, the same in the whole warp
+    // the warp's node's table, read once from global memory (no shared tables: the
+    // block then needs no shared memory, which left the plain kernel at 7 blocks per
+    // SM); weights h / bs^2 of the step's block scale, as load_tables scales them
+    const int f0 = a.tab.row_ptr[l];
+    const int nd = D == 4 ? 4 : a.tab.row_ptr[l + 1] - f0;   // 4 or 8, the same in the whole warp
+    float wt[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) wt[k] = k < nd ? a.tab.w32[f0 + k] * P.ks : 0.f;
     int32_t off[D];
     float w[D];
-    il_node_stencil<D, CELLS>(G, a.tab.ent4 + f0, st.w + f0, nd, sub, off, w);
-    const float pos[3] = {st.pos[3 * l], st.pos[3 * l + 1], st.pos[3 * l + 2]};
+    il_node_stencil<D, CELLS>(G, a.tab.ent4 + f0, wt, nd, sub, off, w);
+    const float pos[3] = {a.tab.pos32[3 * l], a.tab.pos32[3 * l + 1], a.tab.pos32[3 * l + 2]};
     for (uint32_t t = warp; t < tasks; t += nwarps) {
         const uint32_t u = fdiv(t, a.divV);
         uint32_t gx, y, z;
@@ -334,7 +337,7 @@ unsigned il_blocks_d(const ILGrid& G, bool obs, size_t max_blocks) {
     int& o = occ[obs ? 1 : 0];
     if (o == 0) {
         auto k = obs ? il_step_obs_kernel<C, D, CELLS> : il_step_kernel<C, D, CELLS>;
-        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, obs ? 50 : 25);
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, obs ? 50 : 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, k, (int)threads, 0);
         if (o < 1) o = 1;
     }
