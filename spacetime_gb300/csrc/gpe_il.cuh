@@ -296,21 +296,16 @@ __device__ __forceinline__ void il_step_body(const StepArgs& a, const ILGrid& G,
 // shared memory per thread).
 constexpr unsigned kIlPlainThreads = 128;
 constexpr unsigned kIlObsThreads = 256;
-#ifndef IL_B81
-#define IL_B81 8
-#endif
-#ifndef IL_B83
-#define IL_B83 5
-#endif
-#ifndef IL_B85
-#define IL_B85 4
-#endif
 template <int C, int D>
 struct IlBounds {
-    // D = 4: spin-1 BCC 96^3: 7 blocks (72 registers) 0.131 ms per step, 8 (64)
-    // 0.147, 9 (56) 0.145; spin-2 BCC 96^3: 4 blocks (105) 0.222 ms, 5 (96) 0.211,
-    // 6 (80) 0.218.  D = 8 keeps 12 more registers for the second group of entries.
-    static constexpr int kMin = D == 8 ? (C == 5 ? IL_B85 : (C == 3 ? IL_B83 : IL_B81)) : (C == 5 ? 5 : (C == 3 ? 7 : 8));
+    // D = 4: spin-1 BCC 96^3 (the cap 7 blocks lets it use 64 registers, 8 blocks):
+    // 0.130 ms per step; capped at 72 registers before the offsets carried dx, 7
+    // blocks 0.131, 8 (64) 0.147, 9 (56) 0.145; spin-2 BCC 96^3: 4 blocks (105)
+    // 0.222 ms, 5 (96) 0.211, 6 (80) 0.218.  D = 8 keeps 12 more registers for the
+    // second group of entries (FCC 96^3, fraction of the copy peak): spin-1 at 5
+    // blocks (95 registers) 0.58, at 6 (80, 16 bytes of spills) 0.58, at 4 0.52;
+    // spin-2 at 4 blocks (128) 0.58, at 3 0.52, at 5 0.49.
+    static constexpr int kMin = D == 8 ? (C == 5 ? 4 : (C == 3 ? 5 : 8)) : (C == 5 ? 5 : (C == 3 ? 7 : 8));
     static constexpr int kMinObs = (C == 5 || (C == 3 && D == 8)) ? 2 : 3;
 };
 
