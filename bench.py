@@ -105,9 +105,9 @@ def leg_init(w):
 
 def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
     """A configuration on the device: seeded device-side initial state, start,
-    `steps` x `inner` steps timed with CUDA events on the launching stream (each
-    bench step's launches bracketed by events for the step kernel's mean
-    duration), FP64 observables after each bench step outside the kernel timing."""
+    `steps` x `inner` steps timed with CUDA events on the launching stream (the
+    library's events give the step kernel's mean duration), and the observables
+    (FP32 node terms, FP64 sums) after each bench step, inside the timed region."""
     import ctypes as C
 
     import torch
@@ -119,6 +119,8 @@ def time_leg(w, steps, inner, warmup, kernel=0, dims=None):
     stream = torch.cuda.Stream()
     s = Stepper(lat, p)
     s.stream = C.c_void_p(stream.cuda_stream)
+    # the per-bench-step observables as the headline's: FP32 node terms, FP64 sums
+    s.set_tuning(capi.TUNE_OBSERVE_ARITH, 1)
     if kernel:
         s.set_tuning(capi.TUNE_KERNEL, kernel)
     with torch.cuda.stream(stream):
