@@ -146,3 +146,33 @@ def test_noalloc_rejects_bad_tables_and_alignment_on_host(lib):
         assert b"multiples" in lib.gpe_last_error()
     p64 = capi.make_params(components=3, precision=capi.FP64, dims=(4, 4, 4), lattice=lat)
     assert call(lat.desc, (1 << 20) + 8, 2 * pitch, 2 * slice_pitch, p64) == 1
+
+
+def test_python_constants_match_header_enums():
+    """Every GPE_* enumerator of include/gpe.h that the Python front end names
+    (tuning keys, batch keys, kernels, slots, flags) has the header's value."""
+    import os
+    import re
+
+    hdr = open(os.path.join(os.path.dirname(capi.__file__), "..", "include", "gpe.h")).read()
+    values = {}
+    for body in re.findall(r"enum\s*\{([^}]*)\}", hdr):
+        nxt = 0
+        for item in re.sub(r"/\*.*?\*/", "", body, flags=re.S).split(","):
+            item = item.strip()
+            if not item:
+                continue
+            if "=" in item:
+                name, val = (x.strip() for x in item.split("="))
+                nxt = int(val, 0)
+            else:
+                name = item
+            values[name] = nxt
+            nxt += 1
+    pairs = {"GPE_TUNE_KERNEL": capi.TUNE_KERNEL, "GPE_TUNE_TIMING": capi.TUNE_TIMING,
+             "GPE_TUNE_TRANSFER": capi.TUNE_TRANSFER, "GPE_TUNE_OBSERVE_ARITH": capi.TUNE_OBSERVE_ARITH,
+             "GPE_BATCH_ITEM_NODES": capi.BATCH_ITEM_NODES, "GPE_BATCH_STEPS_PER_LAUNCH": capi.BATCH_STEPS_PER_LAUNCH,
+             "GPE_BATCH_BLOCKS_PER_SM": capi.BATCH_BLOCKS_PER_SM, "GPE_BATCH_LAYOUT": capi.BATCH_LAYOUT,
+             "GPE_BATCH_BARRIER_TIMEOUT_MS": capi.BATCH_BARRIER_TIMEOUT_MS}
+    for name, v in pairs.items():
+        assert values.get(name) == v, name
