@@ -675,15 +675,28 @@ extern "C" gpe_status gpe_adjoint_forward(gpe_handle* h, int32_t n_steps, const 
         return st;
     if ((st = copy_state(h, A.ckpt[0], h->alloc[GPE_PSI_ODD], s))) return st;
     if ((st = copy_state(h, A.ckpt[1], h->alloc[GPE_PSI_EVEN], s))) return st;
-    for (int j = 1; j < n_steps; ++j) {
-        const int prev = slot_of(j), next = slot_of(j + 1);
-        if ((st = step_buffers(h, h->interior[next], h->interior[prev], fields[j], A.t0 + j * dt, GPE_MODE_LEAPFROG, s)))
-            return st;
-        if (j % stride == 0) {
-            const int k = j / stride;
-            if ((st = copy_state(h, A.ckpt[2 * k], h->alloc[prev], s))) return st;
-            if ((st = copy_state(h, A.ckpt[2 * k + 1], h->alloc[next], s))) return st;
+    // steps j .. je up to the next checkpoint (after a step j that is a multiple of
+    // the stride), in the interleaved layout where that is the handle's kernel for a
+    // call of that length (the same states as step_buffers', bit for bit, so the
+    // recomputation in the handle's layout reproduces them)
+    for (int j = 1; j < n_steps;) {
+        int je = (j + stride - 1) / stride * stride;
+        if (je > n_steps - 1) je = n_steps - 1;
+        const int32_t cnt = je - j + 1;
+        if (il_leapfrog_applies(h, cnt)) {
+            if ((st = il_leapfrog_explicit(h, slot_of(j), cnt, fields + j, A.t0 + j * dt, dt, s))) return st;
+        } else {
+            for (int jj = j; jj <= je; ++jj)
+                if ((st = step_buffers(h, h->interior[slot_of(jj + 1)], h->interior[slot_of(jj)], fields[jj],
+                                       A.t0 + jj * dt, GPE_MODE_LEAPFROG, s)))
+                    return st;
         }
+        if (je % stride == 0) {
+            const int k = je / stride;
+            if ((st = copy_state(h, A.ckpt[2 * k], h->alloc[slot_of(je)], s))) return st;
+            if ((st = copy_state(h, A.ckpt[2 * k + 1], h->alloc[slot_of(je + 1)], s))) return st;
+        }
+        j = je + 1;
     }
     h->cur = slot_of(n_steps);
     h->nstep = (uint64_t)(n_steps - 1);

@@ -925,7 +925,10 @@ static cudaError_t dispatch_rows(const gpe_handle* h, const StepArgs& a, const R
 // automatic choice is the grid-stride gather kernel: on GB300 (FP32, 10^6-10^7
 // sites) it is as fast as the row tile or faster on every lattice and spin.
 static uint32_t tile_cells(const gpe_handle* h) {
-    if (h->tune_kernel == 0 || h->tune_kernel == 1 || h->tune_kernel == 3 || h->tune_kernel == 5) return 0;
+    // only on request (2) or for the multi-row tile (4); the interleaved choice (6)
+    // steps single steps and explicit-field steps with the gather kernel, whose
+    // states its own equal bit for bit
+    if (h->tune_kernel != 2 && h->tune_kernel != 4) return 0;
     if (h->g.cell_bytes % 16 != 0) return 0;
     const uint32_t V = h->g.V, X = h->g.X;
     uint32_t tmax = 256 / V;
@@ -1397,6 +1400,38 @@ static cudaError_t dispatch_il_step(const gpe_handle* h, const StepArgs& a, bool
 }
 
 static gpe_status fill_observables(const gpe_handle* h, const double* r, gpe_observables* out);
+
+namespace gpe {
+// n parabolic leapfrog steps through the interleaved layout with the fields of
+// every step given: step k reads slot `first_prev` (k even) or the other slot (k
+// odd), at time t_first + k dt with fields[k], as step_buffers does in the
+// handle's layout -- the same states, bit for bit.  False (nothing run) where the
+// interleaved kernel is not the handle's choice for a call of n steps.
+bool il_leapfrog_applies(const gpe_handle* h, int32_t n) {
+    return h->p.scheme == GPE_SCHEME_PARABOLIC && use_interleaved(h, n);
+}
+
+gpe_status il_leapfrog_explicit(gpe_handle* h, int first_prev, int32_t n, const gpe_fields* fields, double t_first,
+                                double dt, cudaStream_t s) {
+    if (!il_leapfrog_applies(h, n)) return fail(GPE_ERR_UNSUPPORTED, "the interleaved kernel does not apply");
+    gpe_status st = ensure_il(h, s);
+    if (st) return st;
+    if ((st = il_convert_all(h, true, s))) return st;
+    int prev = first_prev;
+    for (int32_t k = 0; k < n; ++k) {
+        const int next = prev == GPE_PSI_EVEN ? GPE_PSI_ODD : GPE_PSI_EVEN;
+        StepArgs a = make_args(h, fields[k], t_first + k * dt);
+        a.prev = h->il[prev];
+        a.next = h->il[next];
+        cudaError_t e = dispatch_il_step(h, a, false, s);
+        if (e != cudaSuccess) return cuda_fail(e, "interleaved step launch");
+        h->launches += 1;
+        h->epoch += 1;
+        prev = next;
+    }
+    return il_convert_all(h, false, s);
+}
+}  // namespace gpe
 
 // n leapfrog steps through the interleaved layout: both psi slots changed in,
 // the steps (the observables of the state the last one reads summed inside it when

@@ -126,4 +126,11 @@ void adjoint_release(gpe_handle* h);
 // and the handle's two interleaved psi copies, allocated (zeroed) on first use.
 int il_stencil_deg(const gpe_handle* h);
 gpe_status il_ensure(gpe_handle* h, cudaStream_t s);
+// n parabolic leapfrog steps with explicit fields in the interleaved layout (both
+// psi slots changed in and back), where the handle's kernel choice for a call of n
+// steps is the interleaved kernel (il_leapfrog_applies); the states step_buffers
+// would leave, bit for bit.
+bool il_leapfrog_applies(const gpe_handle* h, int32_t n);
+gpe_status il_leapfrog_explicit(gpe_handle* h, int first_prev, int32_t n, const gpe_fields* fields, double t_first,
+                                double dt, cudaStream_t s);
 }  // namespace gpe

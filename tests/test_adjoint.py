@@ -229,12 +229,15 @@ def test_adjoint_stride_invariance(gpu):
 
 
 @pytest.mark.parametrize("prec,kernel", [(capi.FP32, capi.KERNEL_GATHER), (capi.FP64, capi.KERNEL_TILE),
-                                         (capi.FP32, capi.KERNEL_TILE)])
+                                         (capi.FP32, capi.KERNEL_TILE), (capi.FP32, capi.KERNEL_AUTO),
+                                         (capi.FP32, capi.KERNEL_INTERLEAVED)])
 def test_adjoint_stride_invariance_kernels(gpu, prec, kernel):
     """The recomputation reproduces the forward run's states exactly with either
     step kernel: out of place for the gather kernel, a state copy and an in-place
-    step for the row tile.  Gradients for strides 1 (no recomputation), 4 and N
-    are bit-identical."""
+    step for the row tile; forward segments run by the interleaved kernel (the
+    automatic choice for the 16 steps of stride N, every segment when it is
+    forced) are recomputed by the gather kernel.  Gradients for strides 1 (no
+    recomputation), 4 and N are bit-identical."""
     lat = capi.Lattice("bcc")
     p = _params(lat, 3, prec, (6, 5, 4))
     fields = _fields(17, seed=48)
