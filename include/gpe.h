@@ -387,20 +387,24 @@ gpe_status gpe_node_fields_reduce(gpe_handle* h, int32_t slot, int32_t kind, dou
  *                      4 entries per node and 16-byte cells; ZCHUNK, if set, is the
  *                      number of slabs),
  *                  6 = interleaved kernel for every gpe_step / gpe_step_observe
- *                      call (FP32, parabolic scheme, lattices with 4 entries per
- *                      node: BCC, A15, C15, Z).  The call changes the two psi
- *                      slots into a cell-interleaved layout (node l, component s of
- *                      32 cells along x contiguous), steps there and changes them
- *                      back; the states are those of the gather kernel.
+ *                      call (FP32; the parabolic scheme on lattices with rows of 4
+ *                      entries -- BCC, A15, C15, Z -- or of 4 and 8 -- FCC; the
+ *                      hyperbolic scheme with 4 edges per node and 2 edges per
+ *                      node of a cell -- BCC, C15).  The call changes the two psi
+ *                      slots (and q) into a cell-interleaved layout (node l,
+ *                      component s of 32 or 16 cells along x contiguous), steps
+ *                      there and changes them back; the states are those of the
+ *                      gather kernel, bit for bit.  Single explicit steps
+ *                      (gpe_step_explicit, imaginary time) take the gather kernel.
  *                  The automatic choice (0) is the interleaved kernel for calls of
- *                  16 or more steps on the spinor handles it applies to (faster
- *                  there by 12-50 %; not for scalars, whose 8-byte records
- *                  already load as coalesced runs; the layout changes cost a few
- *                  steps per call), else 1
- *                  (grid-stride gather, whole-record loads) -- which
- *                  gpe_get_tuning reports; 2-5 on
- *                  request, and gpe_autotune may pick any of 1-4 (it times single
- *                  steps; its gather candidate is recorded as 0).
+ *                  16 or more steps on the parabolic spinor handles and the
+ *                  hyperbolic handles it applies to (faster there by 12-50 %; not
+ *                  for parabolic scalars, whose 8-byte records already load as
+ *                  coalesced runs; the layout changes cost a few steps per
+ *                  call), else 1 (grid-stride gather, whole-record loads) -- which
+ *                  gpe_get_tuning reports; 2-5 on request, and gpe_autotune may
+ *                  pick any of 1-4 (it times single steps; its gather candidate is
+ *                  recorded as 0).
  * GPE_TUNE_TILE_CELLS: cells per tile row (0 = automatic).
  * GPE_TUNE_TILE_ROWS: rows per tile along y (z-march TY, row-block RY; 0 = automatic).
  * GPE_TUNE_ZCHUNK: z-march planes per block, or row-block RZ (0 = automatic).
